@@ -1,0 +1,371 @@
+"""Benchmark: electrostatic PIC step, 2D XY plasma slab (512x512 nodes, 4M e- + 4M Ar+).
+
+One step = the loop body of ParticleInCell.solve on the device: advance both
+species (CIC gather + Boris push + discard!/wrap! + CIC deposit), ρ, FP64
+Poisson solve to relative residual 1e-8, E = -∇ϕ.  Metric: particle-steps/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the FP64 CPU restatement of the reference's step
+(oracle/, OpenMP on all host cores) on the same workload.  Under torchrun each
+rank runs an independent replica (the path does not shard: replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+QE = 1.602176634e-19
+ME = 9.1093837015e-31
+AMU = 1.66053906660e-27
+KB = 1.380649e-23
+EPS0 = 8.8541878128e-12
+
+# 2D XY plasma slab on a 512x512 grid
+NX = NY = 512
+DX = 1e-4
+NP = 4_000_000          # per species
+DENSITY = 1e15
+TE_EV, TI_EV = 2.0, 0.03
+M_AR = 39.948 * AMU
+DT = 1e-11
+V_RIGHT = 100.0
+RTOL = 1e-8
+SORT_EVERY = 16
+WORKLOAD = "2D XY slab 512x512, dx=1e-4 m, 4M e- (2 eV) + 4M Ar+ (0.03 eV), x Dirichlet 0/100 V absorbing, y periodic, dt=1e-11 s"
+
+
+def thermal_speed(T_ev, m):
+    # thermal_speed(T, m) = sqrt(2 kB T / m) (problem/configuration.jl), T in K
+    return np.sqrt(2 * KB * (T_ev * QE / KB) / m)
+
+
+def make_state(seed=2):
+    rng = np.random.default_rng(seed)
+    L = (NX - 1) * DX
+    w = DENSITY * L * L * 1.0 / NP
+
+    def species(T_ev, m):
+        x = np.empty((NP, 2), order="F")
+        x[:, 0] = rng.uniform(0, L, NP)
+        x[:, 1] = rng.uniform(0, L, NP)
+        v = np.asfortranarray(rng.standard_normal((NP, 3)) * thermal_speed(T_ev, m))
+        return x, v
+
+    xe, ve = species(TE_EV, ME)
+    xi, vi = species(TI_EV, M_AR)
+    return w, (xe, ve), (xi, vi)
+
+
+def electrode_masks():
+    left = np.zeros((NX, NY), bool)
+    left[0, :] = True
+    right = np.zeros((NX, NY), bool)
+    right[-1, :] = True
+    return left, right
+
+
+def setup_context(w, e, i, stream=0):
+    from iskra_gb300 import _lib
+    from iskra_gb300.device import Context
+    ctx = Context(NX, NY, DX, DX, (0, 0, 0, 0), stream)
+    se = ctx.species_create(-QE, ME, w, NP)
+    si = ctx.species_create(QE, M_AR, w, NP)
+    for s in (se, si):
+        ctx.set_boundary(s, _lib.BND_DISCARD, _lib.BND_WRAP)
+    ctx.upload(se, *e)
+    ctx.upload(si, *i)
+    ctx.poisson_create(EPS0)
+    ctx.apply_periodic(1)
+    left, right = electrode_masks()
+    ctx.apply_dirichlet(left, 0.0)
+    ctx.apply_dirichlet(right, V_RIGHT)
+    ctx.set_sort_every(SORT_EVERY)
+    return ctx, se, si
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+            if self.gpu_id is not None:
+                cmd.insert(1, f"--id={self.gpu_id}")
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([s.strip() for s in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """dram bytes per k_push launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "push_deposit_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("bytes_per_launch_full_size")
+    return None
+
+
+# ----------------------------------------------------------------------------
+# CPU arm: the FP64 oracle (the reference's step restated), all host threads
+# ----------------------------------------------------------------------------
+def cpu_run(w, e, i, max_seconds=20.0, max_steps=None):
+    from oracle import oracle as orc
+    L = orc.lib()
+    threads = L.orc_num_threads()
+    xe, ve = e[0].copy(order="F"), e[1].copy(order="F")
+    xi, vi = i[0].copy(order="F"), i[1].copy(order="F")
+    ps = orc.PoissonOracle(NX, NY, DX, DX, EPS0)
+    ps.apply_periodic(1)
+    left, right = electrode_masks()
+    ps.apply_dirichlet(left, 0.0)
+    ps.apply_dirichlet(right, V_RIGHT)
+    t0 = time.perf_counter()
+    ps.factorize()
+    t_factor = time.perf_counter() - t0
+    V = orc.cell_volume(NX, NY, DX, DX)
+    E = np.zeros((NX, NY, 3), order="F")
+    sp = [[xe, ve, -QE, ME], [xi, vi, QE, M_AR]]
+    steps, psteps = 0, 0
+    t0 = time.perf_counter()
+    while True:
+        rho = np.zeros((NX, NY), order="F")
+        for s in sp:
+            x, v, q, m = s
+            n = x.shape[0]
+            psteps += n
+            pu = orc.grid_to_particle(E, DX, DX, x)
+            orc.push_cartesian(x, v, pu, None, q / m, DT)
+            wg = np.full(n, w)
+            npn, _, _ = orc.discard(x, v, wg, None, w, 0, NX, DX)
+            x, v = np.asfortranarray(x[:npn]), np.asfortranarray(v[:npn])
+            orc.wrap(x, 1, NY, DX)
+            s[0], s[1] = x, v
+            u = orc.particle_to_grid_omp(NX, NY, DX, DX, x, w, threads)
+            rho += q * (u / V)
+        phi = ps.solve(-rho)
+        E = orc.electric_field(phi, DX, DX)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= max_seconds or (max_steps is not None and steps >= max_steps):
+            break
+    return {"psteps": psteps, "seconds": el, "steps": steps, "threads": threads, "factor_s": t_factor}
+
+
+# ----------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        w, e, i = make_state()
+        r = cpu_run(w, e, i, max_seconds=60.0, max_steps=max(args.steps, 1))
+        val = r["psteps"] / r["seconds"]
+        sample = (f"full workload for {r['steps']} step(s) ({r['seconds']:.1f} s of CPU time, "
+                  f"sparse-LU factorisation {r['factor_s']:.1f} s excluded), FP64, "
+                  f"{r['threads']} OpenMP threads")
+        print(json.dumps({
+            "impl": "reference", "metric": "particle-steps/s", "value": val, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": r["steps"], "warmup": 0, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": [NX, NY], "particles": 2 * NP, "parallelism": "replicas"},
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": r["threads"], "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    import torch
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    w, e, i = make_state(seed=2 + rank)
+    ctx, se, si = setup_context(w, e, i)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    # warm-up (also captures the step graph)
+    ctx.step(DT, args.warmup, seed=1, rtol=RTOL)
+    ctx.sync()
+    np_before = ctx.count(se) + ctx.count(si)
+    launches0 = ctx.kernel_launches()
+    gpu_id = None
+    try:
+        gpu_id = str(torch.cuda.get_device_properties(local_rank).uuid)
+        if not gpu_id.startswith("GPU-"):
+            gpu_id = "GPU-" + gpu_id
+    except Exception:
+        gpu_id = None
+    clk = ClockSampler(gpu_id)
+    clk.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    ctx.step(DT, args.steps, seed=1, rtol=RTOL)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ctx.sync()
+    if dist:
+        dist.barrier()
+    clocks = clk.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = ctx.kernel_launches() - launches0
+    np_after = ctx.count(se) + ctx.count(si)
+    it, relres = ctx.solve_info()
+    psteps = 0.5 * (np_before + np_after) * args.steps
+    t = torch.tensor([ms], device="cuda") if dist else None
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        pt = torch.tensor([psteps], device="cuda", dtype=torch.float64)
+        dist.all_reduce(pt)
+        psteps = float(pt.item())
+    value = psteps / (ms * 1e-3)
+
+    # roofline of the dominant kernel (fused gather+push+boundary+deposit), timed
+    # live with CUDA events on the library stream, one launch per event pair
+    durs = []
+    for rep in range(20):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        n_e = ctx.count(se)
+        a.record(stream)
+        ctx.advance(se, DT)
+        b.record(stream)
+        ctx.finalize(se)
+        torch.cuda.synchronize()
+        durs.append((a.elapsed_time(b) * 1e-3, n_e))
+    durs = durs[3:]
+    t_push = statistics.median(d for d, _ in durs)
+    n_push = statistics.median(n for _, n in durs)
+    bytes_launch = 48.0 * n_push + 16.0 * NX * NY
+    peak, peak_kind = peaks()
+    achieved = bytes_launch / t_push / 1e9
+    traffic = committed_traffic()
+
+    # end-to-end through the public API with host buffers: upload the initial
+    # particle arrays (Julia layout, FP64), K steps each reading ϕ back (the
+    # per-step "phi" field record), final particle download
+    ctx.close()
+    w2, e2, i2 = w, e, i
+    phi_host = np.zeros((NX, NY), order="F")
+    k_e2e = min(args.steps, 200)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx2, se2, si2 = setup_context(w2, e2, i2)
+    for k in range(k_e2e):
+        ctx2.step(DT, 1, seed=1, rtol=RTOL)
+        phi_host[...] = ctx2.field(1)
+    xe_o, ve_o, _ = ctx2.download(se2)
+    xi_o, vi_o, _ = ctx2.download(si2)
+    t_e2e = time.perf_counter() - t0
+    np_e2e = 0.5 * (2 * NP + xe_o.shape[0] + xi_o.shape[0])
+    e2e_value = np_e2e * k_e2e / t_e2e
+    h2d = 2 * NP * 5 * 8 / k_e2e
+    d2h = NX * NY * 8 + (xe_o.shape[0] + xi_o.shape[0]) * 5 * 8 / k_e2e
+    ctx2.close()
+
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 push / i64 deposit / f64 Poisson", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [NX, NY], "particles": 2 * NP * world,
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (224 MB particle store)",
+                   "poisson": f"FP64 FFT(y)/tridiagonal(x) to relres {RTOL:g}; last relres {relres:.2e} in {it} sweep(s)",
+                   "sort_every": SORT_EVERY},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_push (gather+push+discard/wrap+deposit)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": t_push * 1e3},
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": k_e2e,
+                "note": "C-ABI from host FP64 arrays: upload, per-step step+phi readback, final download"},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        r = cpu_run(w, e, i, max_seconds=20.0)
+        line["cpu_baseline"] = {
+            "value": r["psteps"] / r["seconds"], "unit": "particle-steps/s", "cores": r["threads"], "kind": "port",
+            "sample": f"full workload, {r['steps']} step(s) in {r['seconds']:.1f} s, FP64 oracle, OpenMP"}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,234 @@
+/*
+ * iskra_gpu.h -- C ABI of libiskra_gpu.so, the GB300 (sm_103a) implementation
+ * of iskra's electrostatic particle-in-cell step.
+ *
+ * Each entry point replaces one call of the Julia reference (bchaber/iskra);
+ * the cited reference function is the one a ccall-based Julia shim would route
+ * to it (paths relative to the reference project root).
+ *
+ * Conventions
+ *   - Every call returns an int status: ISKRA_OK (0) or one of ISKRA_E*.
+ *     iskra_last_error(ctx) gives the message of the last failure on ctx.
+ *     No call aborts the process or traps the GPU.
+ *   - Host arrays use Julia's layout: column-major Float64, node (i,j) of an
+ *     (nx,ny) grid at offset (i-1) + nx*(j-1); particle matrices are
+ *     (ld x D) with the first np rows live (KineticSpecies.x/.v).  Host
+ *     pointers are borrowed for the duration of the call only.
+ *   - The library owns all device memory behind iskra_ctx.  One context is
+ *     one CUDA stream; calls on a context are not re-entrant.  Asynchronous
+ *     calls (marked "async") return once work is queued on the stream; device
+ *     error flags raised by that work are reported by the next synchronising
+ *     call (iskra_sync, any download, or iskra_status).
+ */
+#ifndef ISKRA_GPU_H
+#define ISKRA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define ISKRA_OK 0
+#define ISKRA_EINVAL 1     /* bad argument or unsupported configuration      */
+#define ISKRA_ENOMEM 2     /* device or host allocation failed               */
+#define ISKRA_ECAPACITY 3  /* species capacity exceeded (particles dropped)  */
+#define ISKRA_EDOMAIN 4    /* particle left the grid on an axis without
+                              wrap!/discard! (Julia raises BoundsError)       */
+#define ISKRA_EPROB 5      /* MCC probability bound violated
+                              (Chemistry/src/mcc.jl:244-246,272-279)          */
+#define ISKRA_ENAN 6       /* non-finite value in particle or field data     */
+#define ISKRA_ETIMEDOUT 7  /* a bounded device wait gave up                  */
+#define ISKRA_ECUDA 8      /* CUDA runtime error                             */
+#define ISKRA_ENOTCONV 9   /* Poisson iteration did not reach the tolerance  */
+
+/* after_push boundary mode per axis (ParticleInCell/src/pic/surfaces/wrap.jl) */
+#define ISKRA_BND_NONE 0
+#define ISKRA_BND_WRAP 1    /* wrap!    wrap.jl:20-33 */
+#define ISKRA_BND_DISCARD 2 /* discard! wrap.jl:1-18  */
+
+/* MCC process types (Chemistry/src/mcc.jl:4-8) */
+#define ISKRA_MCC_ELASTIC_ISOTROPIC 0
+#define ISKRA_MCC_ELASTIC_BACKWARD 1
+#define ISKRA_MCC_INELASTIC_BACKWARD 2
+#define ISKRA_MCC_EXCITATION 3
+#define ISKRA_MCC_IONIZATION 4
+
+/* Field selectors for iskra_field_download */
+#define ISKRA_FIELD_RHO 0 /* ρ (nx,ny)             ParticleInCell.jl:118-122  */
+#define ISKRA_FIELD_PHI 1 /* ϕ (nx,ny)             generalized_poisson.jl:377 */
+#define ISKRA_FIELD_E 2   /* E (nx,ny,3) FP64      generalized_poisson.jl:398 */
+
+typedef struct iskra_ctx iskra_ctx;
+
+/* Uniform Cartesian grid: RegularGrids.create_uniform_grid(xs, ys; left,
+ * right, bottom, top) (RegularGrids/src/RegularGrids.jl:55-69).  bc[k] != 0
+ * marks side k (left,right,bottom,top) :periodic; only cell_volume reads it
+ * (RegularGrids.jl:26-38).  The origin must be (0,0): particle_cell ignores it
+ * (ParticleInCell.jl:28-35) while wrap!/discard! use it, so other origins
+ * are inconsistent in the reference itself. */
+typedef struct {
+  int32_t nx, ny;   /* nodes; 2 <= nx,ny <= 65535 */
+  double dx, dy;    /* node spacing (Δh) */
+  double ox, oy;    /* origin, must be 0 */
+  int32_t bc[4];
+} iskra_grid_t;
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates the device context for one grid on the current CUDA device.
+ * stream: a cudaStream_t to run on, or 0 for a library-owned stream. */
+int iskra_ctx_create(const iskra_grid_t *grid, uint64_t stream, iskra_ctx **out);
+int iskra_ctx_destroy(iskra_ctx *ctx);
+const char *iskra_last_error(const iskra_ctx *ctx);
+/* Waits for queued work, then reports device error flags (clearing them). */
+int iskra_sync(iskra_ctx *ctx);
+/* The cudaStream_t (as an integer) all work of ctx is queued on. */
+int iskra_stream(iskra_ctx *ctx, uint64_t *stream);
+
+/* ---- kinetic species (ParticleInCell/src/pic/kinetic.jl:1-18) ----------- */
+/* KineticSpecies{2,3}(name, capacity) with charge q, mass m, default weight
+ * w0 (create_kinetic_species, problem/configuration.jl:141-148).  Particles
+ * are stored on the device as a cell index plus FP32 in-cell offsets and FP32
+ * velocities; every macroparticle carries the weight w0. */
+int iskra_species_create(iskra_ctx *ctx, double q, double m, double w0,
+                         int64_t capacity, int *sid);
+/* Copies np particles in: x (ld x 2) and v (ld x 3) column-major Float64,
+ * wg (np, may be NULL; every entry must equal w0), id (np, may be NULL ->
+ * 1..np).  Replaces the previous content.  Particles are cell-sorted. */
+int iskra_species_upload(iskra_ctx *ctx, int sid, const double *x,
+                         const double *v, const double *wg, const uint32_t *id,
+                         int64_t np, int64_t ld);
+/* Copies the live particles out (compacting first); *np receives the count.
+ * Fails with ISKRA_ECAPACITY if ld is too small (nothing written then). */
+int iskra_species_download(iskra_ctx *ctx, int sid, double *x, double *v,
+                           double *wg, uint32_t *id, int64_t ld, int64_t *np);
+/* Live particle count (synchronises). */
+int iskra_species_count(iskra_ctx *ctx, int sid, int64_t *np);
+/* after_push(part, grid) for this species: per-axis wrap!/discard!/none. */
+int iskra_species_set_boundary(iskra_ctx *ctx, int sid, int mode_x, int mode_y);
+/* Particles removed by discard! since the last call, per wall
+ * {x-low, x-high, y-low, y-high}; the counter is reset. */
+int iskra_species_absorbed(iskra_ctx *ctx, int sid, int64_t counts[4]);
+/* Counting sort by cell + compaction of discarded particles (async). */
+int iskra_species_sort(iskra_ctx *ctx, int sid);
+
+/* ---- fields -------------------------------------------------------------- */
+/* Replaces the device E field used by the gather with a host (nx,ny,3) array
+ * (the E argument of advance!, ParticleInCell.jl:51-57).  E_z is ignored: the
+ * 2D xy push never reads a nonzero E_z from the reference's solver. */
+int iskra_field_upload_E(iskra_ctx *ctx, const double *E);
+/* Copies ρ, ϕ or E (FP64) to the host (synchronises). */
+int iskra_field_download(iskra_ctx *ctx, int which, double *out);
+
+/* ---- ParticleInCell.advance!(::KineticSpecies, E, B, Δt, config) --------
+ * ParticleInCell.jl:51-72: grid_to_particle (cloud_in_cell.jl:20-36), Boris
+ * push with B = 0 (pushers.jl:37-50, calculate_magnetic_field
+ * generalized_poisson.jl:412-419), after_push (wrap.jl).  The same kernel
+ * deposits the pushed particles (cloud_in_cell.jl:1-18) into the species'
+ * int64 fixed-point density accumulator, consumed by iskra_density. (async) */
+int iskra_advance(iskra_ctx *ctx, int sid, double dt);
+
+/* ---- density(species, grid) = particle_to_grid(wg) ./ cell_volume -------
+ * kinetic.jl:53, cloud_in_cell.jl:1-18, RegularGrids.jl:26-38.  Writes the
+ * (nx,ny) density to n_out when non-NULL (synchronises then). */
+int iskra_density(iskra_ctx *ctx, int sid, double *n_out);
+/* ρ = Σ_s q_s n_s over all kinetic species plus an optional fixed background
+ * set by iskra_set_background (ParticleInCell.jl:118-122). (async) */
+int iskra_charge_density(iskra_ctx *ctx);
+/* Fixed (nx,ny) charge density added to ρ (a neutralising fluid species with
+ * constant n, fluid.jl:1-11); NULL clears it. */
+int iskra_set_background(iskra_ctx *ctx, const double *rho_bg);
+
+/* ---- Poisson solver (FiniteDifferenceMethod/src/generalized_poisson.jl) -- */
+/* create_poisson_solver(grid, ε0) (:27-30,34-68). */
+int iskra_poisson_create(iskra_ctx *ctx, double eps0);
+/* apply_dirichlet(ps, nodes, ϕ0) (:205-215); nodes: (nx,ny) uint8 mask. */
+int iskra_poisson_apply_dirichlet(iskra_ctx *ctx, const uint8_t *nodes,
+                                  double phi0);
+/* apply_periodic(ps, axis) (:286-324), axis 1 or 2 in the reference's naming. */
+int iskra_poisson_apply_periodic(iskra_ctx *ctx, int axis);
+/* add_new_dof(ps, :σ) (:217-230); *dof receives the 1-based σ index. */
+int iskra_poisson_add_dof(iskra_ctx *ctx, int *dof);
+/* apply_neumann(ps, nodes, dof) (:235-269). */
+int iskra_poisson_apply_neumann(iskra_ctx *ctx, const uint8_t *nodes, int dof);
+/* get_rhs(ps, :σ, dof) read / write (:367-370). */
+int iskra_poisson_set_sigma(iskra_ctx *ctx, int dof, double value);
+int iskra_poisson_get_sigma(iskra_ctx *ctx, int dof, double *value);
+/* Time-dependent Dirichlet group for the graph-captured step: nodes get
+ * ϕ0(t) = amp*sin(2π f t + phase) + dc at t = (step-1)*Δt, i.e. the
+ * `apply_dirichlet(solver, nodes, V(t))` call of a problem's iteration hook
+ * (problem/11_rf_discharge.jl:93). */
+int iskra_poisson_drive_dirichlet(iskra_ctx *ctx, const uint8_t *nodes,
+                                  double amp, double freq, double phase,
+                                  double dc);
+/* calculate_electric_potential(ps, -ρ) (:372-378) with the device ρ, iterated
+ * to relative residual rtol (FP64), followed by calculate_electric_field
+ * (:398-410).  iters/relres may be NULL; non-NULL makes the call synchronous. */
+int iskra_poisson_solve(iskra_ctx *ctx, double rtol, int maxit, int *iters,
+                        double *relres);
+/* Same with a host right-hand side f (the argument of
+ * calculate_electric_potential) and the potential written to phi_out. */
+int iskra_poisson_solve_host(iskra_ctx *ctx, const double *f, double rtol,
+                             int maxit, double *phi_out, int *iters,
+                             double *relres);
+/* Solver method: 0 = automatic (the exact FFT(y)/tridiagonal(x) solve when
+ * the assembled operator is separable, else CG), 1 = CG with Jacobi scaling
+ * only.  Returns the method in effect through *active when non-NULL. */
+int iskra_poisson_set_method(iskra_ctx *ctx, int method, int *active);
+
+/* ---- Monte Carlo collisions (Chemistry/src/mcc.jl) ----------------------- */
+/* mcc(@reactions ...) -> MonteCarloCollisions (:27-51,291-320) for one source
+ * species against a fluid target.  Process k has type types[k], energy
+ * energies[k] (threshold for excitation/ionisation) and the cross-section
+ * table eps[off[k]..off[k+1]), sigma[...] (CrossSection, cross_section.jl).
+ * gas_n: (nx,ny) target density (FluidSpecies.n).  product_sid: species that
+ * receives ionisation ions (-1 none).  max_sigma_g (may be NULL) receives the
+ * constructor's max Σσ_k g. */
+int iskra_mcc_create(iskra_ctx *ctx, int source_sid, int nproc,
+                     const int *types, const double *energies,
+                     const int32_t *off, const double *eps,
+                     const double *sigma, double gas_mass, double gas_T,
+                     double gas_q, const double *gas_n, int product_sid,
+                     double *max_sigma_g, int *mid);
+/* PIC.perform!(::MonteCarloCollisions, E, Δt, config) (:231-289): the
+ * null-collision step on the current E with a counter-based RNG keyed by
+ * (seed, step, particle id). (async) */
+int iskra_mcc_perform(iskra_ctx *ctx, int mid, double dt, uint64_t seed,
+                      uint64_t step);
+/* Accepted collisions per process since the last call (reset after). */
+int iskra_mcc_counts(iskra_ctx *ctx, int mid, int64_t *counts);
+
+/* ---- RLC circuit (Circuit/src/Circuit.jl, circuit_coupling.jl) ---------- */
+/* rlc(@netlist ...) with V(t) = amp*sin(2π f t) + dc, coupled to the σ dof
+ * of a floating electrode (positive) and a grounded node set (negative), as a
+ * PlasmaDevice (circuit_coupling.jl:18-33).  area: electrode area.
+ * sigma_scale multiplies dσ before it enters the σ row (1 = the reference). */
+int iskra_circuit_create(iskra_ctx *ctx, double R, double L, double C,
+                         double amp, double freq, double dc, int sigma_dof,
+                         const uint8_t *pos_nodes, const uint8_t *neg_nodes,
+                         double area, double sigma_scale);
+/* advance!(circuit, ϕ, Δt, config) (circuit_coupling.jl:35-43 ->
+ * Circuit.jl:117-136), FP64, one device thread. (async) */
+int iskra_circuit_advance(iskra_ctx *ctx, double dt);
+/* {t, i, q, σ, V_ext} */
+int iskra_circuit_state(iskra_ctx *ctx, double state[5]);
+
+/* ---- whole step: the loop body of ParticleInCell.solve (:102-135) -------
+ * MCC sets (in creation order) -> advance! every species -> circuit ->
+ * density/ρ -> Poisson -> E, nsteps times, replayed as one CUDA graph.
+ * seed keys the MCC RNG; the step counter continues across calls. (async) */
+int iskra_step(iskra_ctx *ctx, double dt, int nsteps, uint64_t seed,
+               double rtol);
+/* Cell-sort cadence for iskra_step (0 = never). */
+int iskra_set_sort_every(iskra_ctx *ctx, int every);
+/* Last Poisson solve: iterations and relative residual (synchronises). */
+int iskra_solve_info(iskra_ctx *ctx, int *iters, double *relres);
+/* Diagnostic with no reference counterpart: number of kernels iskra_step has
+ * launched on this context (graph replays x kernel nodes). */
+int iskra_kernel_launches(iskra_ctx *ctx, uint64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISKRA_GPU_H */

@@ -1,0 +1,450 @@
+// ctx.cu -- context, species store, host<->device conversion, error plumbing.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "internal.cuh"
+
+namespace iskra {
+
+int set_err(Ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_check(Ctx *c, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return ISKRA_OK;
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return set_err(c, ISKRA_ENOMEM, m);
+  return set_err(c, ISKRA_ECUDA, m);
+}
+
+int grid_blocks(Ctx *c, int threads, int per_sm) {
+  (void)threads;
+  return c->num_sms * per_sm;
+}
+
+void invalidate_graphs(Ctx *c) {
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->sort_graph) cudaGraphExecDestroy(c->sort_graph);
+  c->graph = nullptr;
+  c->sort_graph = nullptr;
+}
+
+int collect_device_errors(Ctx *c) {
+  ISKRA_CUDA(c, cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  int f = *c->h_err;
+  if (!f) return ISKRA_OK;
+  ISKRA_CUDA(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (f & DERR_NAN) return set_err(c, ISKRA_ENAN, "non-finite particle or field value");
+  if (f & DERR_PROB)
+    return set_err(c, ISKRA_EPROB, "MCC collision probability above its bound (mcc.jl:244-246,272-279)");
+  if (f & DERR_CAPACITY) return set_err(c, ISKRA_ECAPACITY, "species capacity exceeded; particles dropped");
+  if (f & DERR_DOMAIN)
+    return set_err(c, ISKRA_EDOMAIN, "particle outside the grid on an axis without wrap!/discard!");
+  if (f & DERR_TIMEOUT) return set_err(c, ISKRA_ETIMEDOUT, "bounded device wait gave up");
+  if (f & DERR_NOTCONV) return set_err(c, ISKRA_ENOTCONV, "Poisson solve did not reach the tolerance");
+  return set_err(c, ISKRA_ECUDA, "unknown device error flag");
+}
+
+// ---------------------------------------------------------------------------
+// upload / download conversion kernels
+// ---------------------------------------------------------------------------
+// particle_cell (ParticleInCell.jl:28-35) on the upload side: f = 1 + x/Δh,
+// i = floor(f), h = f - i; see k_upload for the quantisation onto the 2^-24 grid.
+__global__ void k_upload(const double *__restrict__ st, long long np, double dx, double dy,
+                         int nx, int ny, const uint32_t *__restrict__ ids, float4 *xv,
+                         float2 *zc, uint32_t *id, int *err) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  double X = st[p], Y = st[p + np];
+  double vx = st[p + 2 * np], vy = st[p + 3 * np], vz = st[p + 4 * np];
+  // i0 = floor(x/Δh) (particle_cell's i - 1, formed without the 1 + ... that
+  // can round x just below the far wall onto node nx), offset rounded to the
+  // nearest point of the 2^-24 grid; a carry into the next cell is taken
+  // unless that cell does not exist (then the offset stays at 1 - 2^-24), so
+  // a download/upload round trip reproduces the state exactly.
+  const double fx = X / dx, fy = Y / dy;
+  const double ix = floor(fx), jy = floor(fy);
+  long long i0 = (long long)ix, j0 = (long long)jy;
+  long long ux = llrint((fx - ix) * 16777216.0), uy = llrint((fy - jy) * 16777216.0);
+  if (ux >= 16777216LL) {
+    if (i0 + 1 <= nx - 2) { i0 += 1; ux = 0; } else { ux = 16777215LL; }
+  }
+  if (uy >= 16777216LL) {
+    if (j0 + 1 <= ny - 2) { j0 += 1; uy = 0; } else { uy = 16777215LL; }
+  }
+  int cell = -1;
+  bool finite = isfinite(X) && isfinite(Y) && isfinite(vx) && isfinite(vy) && isfinite(vz);
+  if (!finite) {
+    atomicOr(err, DERR_NAN);
+  } else if (i0 < 0 || j0 < 0 || i0 > nx - 2 || j0 > ny - 2) {
+    atomicOr(err, DERR_DOMAIN);
+  } else {
+    cell = (int)(i0 | (j0 << 16));
+  }
+  xv[p] = make_float4((float)ux * kOffInv, (float)uy * kOffInv, (float)vx, (float)vy);
+  zc[p] = make_float2((float)vz, __int_as_float(cell));
+  id[p] = ids ? ids[p] : (uint32_t)(p + 1);
+}
+
+__global__ void k_download(double *__restrict__ st, long long np, double dx, double dy,
+                           const float4 *__restrict__ xv, const float2 *__restrict__ zc) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  float4 a = xv[p];
+  float2 b = zc[p];
+  int cell = __float_as_int(b.y);
+  int i0 = cell & 0xffff, j0 = cell >> 16;
+  st[p] = ((double)i0 + (double)a.x) * dx;
+  st[p + np] = ((double)j0 + (double)a.y) * dy;
+  st[p + 2 * np] = a.z;
+  st[p + 3 * np] = a.w;
+  st[p + 4 * np] = b.x;
+}
+
+__global__ void k_upload_E(const double *__restrict__ E, int nn, float2 *E32, double *E64) {
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nn) return;
+  double ex = E[n], ey = E[n + nn], ez = E[n + 2 * nn];
+  E32[n] = make_float2((float)ex, (float)ey);
+  E64[n] = ex;
+  E64[n + nn] = ey;
+  E64[n + 2 * nn] = ez;
+}
+
+static int ensure_stage(Ctx *c, size_t bytes) {
+  if (c->stage_bytes >= bytes) return ISKRA_OK;
+  if (c->stage) cudaFree(c->stage);
+  c->stage = nullptr;
+  c->stage_bytes = 0;
+  ISKRA_CUDA(c, cudaMalloc(&c->stage, bytes));
+  c->stage_bytes = bytes;
+  return ISKRA_OK;
+}
+
+static int check_sid(Ctx *c, int sid) {
+  if (sid < 0 || sid >= (int)c->species.size()) return set_err(c, ISKRA_EINVAL, "bad species id");
+  return ISKRA_OK;
+}
+
+}  // namespace iskra
+
+using namespace iskra;
+
+extern "C" {
+
+int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
+  if (!g || !out) return ISKRA_EINVAL;
+  *out = nullptr;
+  if (g->nx < 2 || g->ny < 2 || g->nx > 65535 || g->ny > 65535 || !(g->dx > 0) || !(g->dy > 0))
+    return ISKRA_EINVAL;
+  if (g->ox != 0.0 || g->oy != 0.0) return ISKRA_EINVAL;
+  iskra_ctx *h = new (std::nothrow) iskra_ctx();
+  if (!h) return ISKRA_ENOMEM;
+  Ctx *c = &h->c;
+  c->g = *g;
+  c->nx = g->nx;
+  c->ny = g->ny;
+  c->nn = g->nx * g->ny;
+  auto fail = [&](int rc) {
+    iskra_ctx_destroy(h);
+    return rc;
+  };
+  if (cudaGetDevice(&c->device) != cudaSuccess) return fail(ISKRA_ECUDA);
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
+    return fail(ISKRA_ECUDA);
+  if (stream) {
+    c->stream = (cudaStream_t)(uintptr_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(ISKRA_ECUDA);
+    c->own_stream = true;
+  }
+  size_t nn = (size_t)c->nn;
+  bool ok = cudaMalloc(&c->E32, nn * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&c->E64, nn * 3 * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&c->rho, nn * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&c->vol_inv, nn * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&c->d_err, sizeof(int)) == cudaSuccess &&
+            cudaMallocHost(&c->h_err, sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->cell_count, (nn + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->cell_cursor, (nn + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->scan_tmp, 4096 * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->d_step, sizeof(unsigned long long)) == cudaSuccess;
+  if (!ok) return fail(ISKRA_ENOMEM);
+  cudaMemsetAsync(c->E32, 0, nn * sizeof(float2), c->stream);
+  cudaMemsetAsync(c->E64, 0, nn * 3 * sizeof(double), c->stream);
+  cudaMemsetAsync(c->rho, 0, nn * sizeof(double), c->stream);
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  cudaMemsetAsync(c->d_step, 0, sizeof(unsigned long long), c->stream);
+  // 1/cell_volume (RegularGrids.jl:26-38)
+  std::vector<double> vinv(nn);
+  double V0 = g->dx * g->dy;
+  for (int j = 0; j < c->ny; j++)
+    for (int i = 0; i < c->nx; i++) {
+      double V = 0.0 + V0;
+      if (i == 0 && !g->bc[0]) V *= 0.5;
+      if (i == c->nx - 1 && !g->bc[1]) V *= 0.5;
+      if (j == 0 && !g->bc[2]) V *= 0.5;
+      if (j == c->ny - 1 && !g->bc[3]) V *= 0.5;
+      vinv[(size_t)i + (size_t)c->nx * j] = 1.0 / V;
+    }
+  if (cudaMemcpyAsync(c->vol_inv, vinv.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->stream) !=
+      cudaSuccess)
+    return fail(ISKRA_ECUDA);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(ISKRA_ECUDA);
+  *out = h;
+  return ISKRA_OK;
+}
+
+int iskra_ctx_destroy(iskra_ctx *h) {
+  if (!h) return ISKRA_OK;
+  Ctx *c = &h->c;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  invalidate_graphs(c);
+  for (auto &s : c->species) {
+    for (int b = 0; b < 2; b++) {
+      cudaFree(s.dev.xv[b]);
+      cudaFree(s.dev.zc[b]);
+      cudaFree(s.dev.id[b]);
+    }
+    cudaFree(s.dev.st);
+    cudaFree(s.dev.acc);
+    cudaFree(s.n);
+  }
+  for (auto *m : c->mccs) mcc_destroy(m);
+  if (c->ps) poisson_destroy(c->ps);
+  cudaFree(c->cir_d);
+  cudaFree(c->cir_seen);
+  cudaFree(c->E32);
+  cudaFree(c->E64);
+  cudaFree(c->rho);
+  cudaFree(c->rho_bg);
+  cudaFree(c->vol_inv);
+  cudaFree(c->d_err);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  cudaFree(c->cell_count);
+  cudaFree(c->cell_cursor);
+  cudaFree(c->scan_tmp);
+  cudaFree(c->stage);
+  cudaFree(c->d_step);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete h;
+  return ISKRA_OK;
+}
+
+const char *iskra_last_error(const iskra_ctx *h) { return h ? h->c.err.c_str() : "null context"; }
+
+int iskra_sync(iskra_ctx *h) {
+  if (!h) return ISKRA_EINVAL;
+  return collect_device_errors(&h->c);
+}
+
+int iskra_stream(iskra_ctx *h, uint64_t *s) {
+  if (!h || !s) return ISKRA_EINVAL;
+  *s = (uint64_t)(uintptr_t)h->c.stream;
+  return ISKRA_OK;
+}
+
+int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t cap, int *sid) {
+  if (!h || !sid) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if ((int)c->species.size() >= kMaxSpecies) return set_err(c, ISKRA_EINVAL, "too many species");
+  if (cap < 1 || cap > (1LL << 31) - 1) return set_err(c, ISKRA_EINVAL, "capacity out of range");
+  if (!(m > 0) || !(w0 > 0) || !std::isfinite(q)) return set_err(c, ISKRA_EINVAL, "bad q/m/w0");
+  Species s;
+  s.q = q;
+  s.m = m;
+  s.w0 = w0;
+  s.cap = cap;
+  // weight W48 = (2^24-u)(2^24-v) etc. < 2^48; a node sums at most cap of them.
+  int bits = 0;
+  while ((1LL << bits) < cap + 1) bits++;
+  s.dev.shift = 48 + bits > 63 ? 48 + bits - 63 : 0;
+  s.dev.cap = cap;
+  size_t nn = (size_t)c->nn;
+  for (int b = 0; b < 2; b++) {
+    ISKRA_CUDA(c, cudaMalloc(&s.dev.xv[b], cap * sizeof(float4)));
+    ISKRA_CUDA(c, cudaMalloc(&s.dev.zc[b], cap * sizeof(float2)));
+    ISKRA_CUDA(c, cudaMalloc(&s.dev.id[b], cap * sizeof(uint32_t)));
+  }
+  ISKRA_CUDA(c, cudaMalloc(&s.dev.st, sizeof(SpeciesState)));
+  ISKRA_CUDA(c, cudaMalloc(&s.dev.acc, nn * sizeof(unsigned long long)));
+  ISKRA_CUDA(c, cudaMalloc(&s.n, nn * sizeof(double)));
+  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.st, 0, sizeof(SpeciesState), c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, nn * sizeof(unsigned long long), c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(s.n, 0, nn * sizeof(double), c->stream));
+  s.acc_valid = false;
+  s.acc_zero = true;
+  s.n_valid = true;  // empty species: zero density is current
+  c->species.push_back(s);
+  *sid = (int)c->species.size() - 1;
+  invalidate_graphs(c);
+  return ISKRA_OK;
+}
+
+int iskra_species_set_boundary(iskra_ctx *h, int sid, int mx, int my) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (check_sid(c, sid)) return ISKRA_EINVAL;
+  if (mx < 0 || mx > 2 || my < 0 || my > 2) return set_err(c, ISKRA_EINVAL, "bad boundary mode");
+  c->species[sid].bnd[0] = mx;
+  c->species[sid].bnd[1] = my;
+  invalidate_graphs(c);
+  return ISKRA_OK;
+}
+
+int iskra_species_upload(iskra_ctx *h, int sid, const double *x, const double *v, const double *wg,
+                         const uint32_t *id, int64_t np, int64_t ld) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (check_sid(c, sid)) return ISKRA_EINVAL;
+  Species &s = c->species[sid];
+  if (np < 0 || np > s.cap) return set_err(c, ISKRA_ECAPACITY, "np exceeds species capacity");
+  if (np > 0 && (!x || !v || ld < np)) return set_err(c, ISKRA_EINVAL, "bad particle arrays");
+  if (wg) {
+    for (int64_t p = 0; p < np; p++)
+      if (wg[p] != s.w0)
+        return set_err(c, ISKRA_EINVAL, "per-particle weights must all equal w0 on the device store");
+  }
+  int rc = ensure_stage(c, (size_t)(np > 0 ? np : 1) * (5 * sizeof(double) + sizeof(uint32_t)));
+  if (rc) return rc;
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  double *st = c->stage;
+  uint32_t *ids = id ? (uint32_t *)(st + 5 * np) : nullptr;
+  for (int k = 0; k < 2 && np > 0; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(st + k * np, x + k * ld, np * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  for (int k = 0; k < 3 && np > 0; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(st + (2 + k) * np, v + k * ld, np * sizeof(double), cudaMemcpyHostToDevice,
+                                  c->stream));
+  if (ids && np > 0)
+    ISKRA_CUDA(c, cudaMemcpyAsync(ids, id, np * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+  SpeciesState st0{};
+  st0.np = np;
+  st0.cur = 0;
+  uint32_t maxid = (uint32_t)np;
+  if (id)
+    for (int64_t p = 0; p < np; p++) maxid = id[p] > maxid ? id[p] : maxid;
+  st0.next_id = maxid + 1;
+  ISKRA_CUDA(c, cudaMemcpyAsync(s.dev.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, c->stream));
+  if (np > 0) {
+    int T = 256;
+    long long B = (np + T - 1) / T;
+    k_upload<<<(unsigned)B, T, 0, c->stream>>>(st, np, c->g.dx, c->g.dy, c->nx, c->ny, ids, s.dev.xv[0],
+                                               s.dev.zc[0], s.dev.id[0], c->d_err);
+    ISKRA_CUDA(c, cudaGetLastError());
+  }
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));  // staging + host buffers done
+  rc = collect_device_errors(c);
+  if (rc) return rc;
+  rc = launch_sort(c, sid);
+  if (rc) return rc;
+  if (s.acc_valid) s.acc_zero = false;
+  s.acc_valid = false;
+  s.n_valid = false;
+  return ISKRA_OK;
+}
+
+int iskra_species_download(iskra_ctx *h, int sid, double *x, double *v, double *wg, uint32_t *id, int64_t ld,
+                           int64_t *np_out) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (check_sid(c, sid)) return ISKRA_EINVAL;
+  Species &s = c->species[sid];
+  int rc = launch_sort(c, sid);  // compacts discarded particles
+  if (rc) return rc;
+  SpeciesState st{};
+  ISKRA_CUDA(c, cudaMemcpyAsync(&st, s.dev.st, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  rc = collect_device_errors(c);
+  if (rc) return rc;
+  long long np = st.np;
+  if (np_out) *np_out = np;
+  if (np > ld) return set_err(c, ISKRA_ECAPACITY, "host arrays too small for the live particles");
+  if (np == 0) return ISKRA_OK;
+  rc = ensure_stage(c, (size_t)np * 5 * sizeof(double));
+  if (rc) return rc;
+  int T = 256;
+  long long B = (np + T - 1) / T;
+  k_download<<<(unsigned)B, T, 0, c->stream>>>(c->stage, np, c->g.dx, c->g.dy, s.dev.xv[st.cur], s.dev.zc[st.cur]);
+  ISKRA_CUDA(c, cudaGetLastError());
+  for (int k = 0; k < 2 && x; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(x + k * ld, c->stage + k * np, np * sizeof(double), cudaMemcpyDeviceToHost,
+                                  c->stream));
+  for (int k = 0; k < 3 && v; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(v + k * ld, c->stage + (2 + k) * np, np * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+  if (id)
+    ISKRA_CUDA(c, cudaMemcpyAsync(id, s.dev.id[st.cur], np * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (wg)
+    for (long long p = 0; p < np; p++) wg[p] = s.w0;
+  return ISKRA_OK;
+}
+
+int iskra_species_count(iskra_ctx *h, int sid, int64_t *np) {
+  if (!h || !np) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (check_sid(c, sid)) return ISKRA_EINVAL;
+  int rc = launch_sort(c, sid);
+  if (rc) return rc;
+  SpeciesState st{};
+  ISKRA_CUDA(c, cudaMemcpyAsync(&st, c->species[sid].dev.st, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  *np = st.np;
+  return collect_device_errors(c);
+}
+
+int iskra_species_absorbed(iskra_ctx *h, int sid, int64_t counts[4]) {
+  if (!h || !counts) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (check_sid(c, sid)) return ISKRA_EINVAL;
+  SpeciesState st{};
+  SpeciesState *d = c->species[sid].dev.st;
+  ISKRA_CUDA(c, cudaMemcpyAsync(&st, d, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(&d->absorbed[0], 0, sizeof(st.absorbed), c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 4; k++) counts[k] = (int64_t)st.absorbed[k];
+  return collect_device_errors(c);
+}
+
+int iskra_species_sort(iskra_ctx *h, int sid) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (check_sid(c, sid)) return ISKRA_EINVAL;
+  return launch_sort(c, sid);
+}
+
+int iskra_field_upload_E(iskra_ctx *h, const double *E) {
+  if (!h || !E) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  int rc = ensure_stage(c, (size_t)c->nn * 3 * sizeof(double));
+  if (rc) return rc;
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  ISKRA_CUDA(c, cudaMemcpyAsync(c->stage, E, (size_t)c->nn * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  k_upload_E<<<(c->nn + 255) / 256, 256, 0, c->stream>>>(c->stage, c->nn, c->E32, c->E64);
+  ISKRA_CUDA(c, cudaGetLastError());
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ISKRA_OK;
+}
+
+int iskra_set_background(iskra_ctx *h, const double *rho_bg) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!rho_bg) {
+    cudaFree(c->rho_bg);
+    c->rho_bg = nullptr;
+  } else {
+    if (!c->rho_bg) ISKRA_CUDA(c, cudaMalloc(&c->rho_bg, (size_t)c->nn * sizeof(double)));
+    ISKRA_CUDA(c, cudaMemcpyAsync(c->rho_bg, rho_bg, (size_t)c->nn * sizeof(double), cudaMemcpyHostToDevice,
+                                  c->stream));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  invalidate_graphs(c);
+  return ISKRA_OK;
+}
+
+}  // extern "C"

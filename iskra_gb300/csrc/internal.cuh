@@ -1,0 +1,165 @@
+// internal.cuh -- device data structures shared by the libiskra_gpu.so sources.
+//
+// Particle store (per species, structure of arrays, double-buffered for the
+// counting sort):
+//   xv[b][p] : float4 {hx, hy, vx, vy}   in-cell offsets and velocity x/y
+//   zc[b][p] : float2 {vz, cell}         cell = (i0 | j0 << 16) as int bits,
+//                                        -1 marks a discarded particle
+//   id[b][p] : uint32 particle identifier (KineticSpecies.id)
+// i0, j0 are the 0-based lower-left node of the particle's cell; the
+// reference's particle_cell gives i = i0 + 1, hx = x/Δx - i0
+// (ParticleInCell.jl:28-35).  Offsets are kept on the 2^-24 grid so that the
+// CIC weights are exact 48-bit integer products (deposit is then exact,
+// deterministic and order-independent without FP64 arithmetic).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/iskra_gpu.h"
+
+namespace iskra {
+
+constexpr float kOffScale = 16777216.0f;  // 2^24
+constexpr float kOffInv = 5.9604644775390625e-08f;  // 2^-24
+constexpr int kMaxSpecies = 8;
+constexpr int kMaxMcc = 8;
+
+// device error flags (bitmask in Ctx::d_err)
+enum : int {
+  DERR_CAPACITY = 1,
+  DERR_DOMAIN = 2,
+  DERR_PROB = 4,
+  DERR_NAN = 8,
+  DERR_TIMEOUT = 16,
+  DERR_NOTCONV = 32,
+};
+
+struct SpeciesState {          // device-resident, written by kernels
+  long long np;                // slots in use (live + discarded holes)
+  int cur;                     // active buffer of the double-buffered store
+  int pad;
+  unsigned long long absorbed[4];  // discard! counts per wall
+  unsigned int next_id;        // identifier for appended particles
+  unsigned int pad2;
+  long long np_new;            // append cursor used while a kernel appends
+};
+
+struct SpeciesDev {            // kernel view of one species (by value)
+  float4 *xv[2];
+  float2 *zc[2];
+  uint32_t *id[2];
+  SpeciesState *st;
+  unsigned long long *acc;     // (nx*ny) fixed-point deposit accumulator
+  long long cap;
+  int shift;                   // weight = W48 >> shift
+  int pad;
+};
+
+// Buffer of a double-buffered array without dynamic indexing of a kernel
+// parameter (which would place the parameter struct in local memory).
+template <class T>
+__device__ __forceinline__ T *pick(T *a, T *b, int cur) {
+  return cur ? b : a;
+}
+
+struct Species {
+  double q = 0, m = 0, w0 = 0;
+  long long cap = 0;
+  int bnd[2] = {ISKRA_BND_NONE, ISKRA_BND_NONE};
+  SpeciesDev dev{};
+  double *n = nullptr;         // FP64 density (nx*ny)
+  // accumulator / density bookkeeping (host side):
+  bool acc_valid = false;      // acc holds the unconsumed deposit of the current positions
+  bool acc_zero = true;        // acc is all zero
+  bool n_valid = true;         // n matches the current positions
+};
+
+struct Poisson;                // poisson.cu
+struct Mcc;                    // mcc.cu
+struct CircuitDev {            // device-resident circuit state (FP64)
+  double R, L, C, amp, freq, dc, area, scale;
+  double t, i, q, vext;
+  int sigma_dof;               // 0-based index into Poisson sigma
+  int pad;
+};
+
+struct Ctx {
+  iskra_grid_t g{};
+  int nx = 0, ny = 0, nn = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int device = 0, num_sms = 0;
+  std::string err;
+  std::vector<Species> species;
+  // fields
+  float2 *E32 = nullptr;       // (nx*ny) {Ex, Ey} for the gather
+  double *E64 = nullptr;       // (nx*ny*3) download scratch
+  double *rho = nullptr;       // (nx*ny)
+  double *rho_bg = nullptr;    // optional background charge density
+  double *vol_inv = nullptr;   // 1 / cell_volume
+  int *d_err = nullptr;        // device error flags
+  int *h_err = nullptr;        // pinned mirror
+  // scratch for scans / sort
+  int *cell_count = nullptr;   // (nx*ny + 1)
+  int *cell_cursor = nullptr;  // (nx*ny + 1)
+  int *scan_tmp = nullptr;
+  double *stage = nullptr;     // upload/download staging (device)
+  size_t stage_bytes = 0;
+  Poisson *ps = nullptr;
+  std::vector<Mcc *> mccs;
+  CircuitDev *cir_d = nullptr;
+  CircuitDev cir_h{};
+  bool has_circuit = false;
+  int cir_pos_ref = -1, cir_neg_ref = -1;  // reference nodes of the electrodes
+  int cir_wall = -1;                       // discard wall feeding the floating electrode
+  unsigned long long *cir_seen = nullptr;  // absorbed counts already credited
+
+  // step state
+  unsigned long long step = 0;  // steps completed by iskra_step
+  int sort_every = 16;
+  cudaGraphExec_t graph = nullptr;       // one PIC step
+  cudaGraphExec_t sort_graph = nullptr;  // cell sort of every species
+  unsigned long long graph_kernels = 0, sort_graph_kernels = 0;
+  unsigned long long launches = 0;       // kernels launched by iskra_step
+  double graph_dt = 0;
+  double graph_rtol = 0;
+  uint64_t graph_seed = 0;
+  unsigned long long *d_step = nullptr;  // device step counter (graph reads it)
+  unsigned long long d_step_known = ~0ull;  // value d_step holds, when known on the host
+  unsigned long long d_step_host = 0;       // source of the d_step upload
+};
+
+// ---- helpers (ctx.cu) ----
+int set_err(Ctx *c, int code, const std::string &msg);
+int cuda_check(Ctx *c, cudaError_t e, const char *what);
+int grid_blocks(Ctx *c, int threads, int per_sm);
+int collect_device_errors(Ctx *c);   // synchronises
+void invalidate_graphs(Ctx *c);      // the captured step no longer matches the setup
+
+#define ISKRA_CUDA(c, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_check((c), e_, #call); \
+  } while (0)
+
+// ---- kernels / launchers shared across files ----
+int launch_advance(Ctx *c, int sid, float dt);
+int launch_deposit(Ctx *c, int sid);
+int launch_charge_density(Ctx *c);
+int launch_efield_from(Ctx *c, const double *phi);
+int launch_sort(Ctx *c, int sid);
+int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host);
+int launch_circuit(Ctx *c, double dt);
+int poisson_solve_async(Ctx *c, double rtol, int max_sweeps);
+int poisson_prepare(Ctx *c);
+void poisson_destroy(Poisson *p);
+void mcc_destroy(Mcc *m);
+
+}  // namespace iskra
+
+struct iskra_ctx {
+  iskra::Ctx c;
+};

@@ -1,0 +1,579 @@
+// mcc.cu -- null-collision Monte Carlo collisions (Chemistry/src/mcc.jl).
+//
+// Reference algorithm (PIC.perform!, mcc.jl:231-289): per step draw
+// Nc = floor(N*maxPt*np + remainder) particles uniformly WITH replacement; for
+// each draw pick process k = floor(N*U)+1 with one uniform U, evaluate
+// P_k = (1-exp(-n σ_k(ε) g Δt)) / (N*maxPt) and accept when U > k/N - P_k.
+//
+// Device algorithm: every live particle is selected c ~ Poisson(N*maxPt)
+// times (the per-particle law of drawing Nc times with replacement, whose
+// mean is N*maxPt per step including the carried remainder), and each
+// selection runs the reference's k-choice, acceptance test and kinematics on
+// that particle in order.  Randomness comes from Philox4x32-10 (Salmon,
+// Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11)
+// keyed by (seed, set) with counter (particle id, step, selection, draw), so
+// the result does not depend on the particle order in memory.  Differences
+// from the reference, both statistical only: particles created by ionisation
+// in this step are not selected again in the same step (the reference re-reads
+// np after each draw), and the number of draws per step is Poisson instead of
+// the deterministic Nc.  Kinematics (mcc.jl:53-229) run in FP32 on the FP32
+// particle velocities.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace iskra {
+
+constexpr int kMaxProc = 8;
+constexpr int kMaxTable = 8192;  // total table nodes of one set
+
+struct MccDev {
+  int N;
+  int types[kMaxProc];
+  float energy[kMaxProc];
+  int off[kMaxProc + 1];
+  const float *eps;      // table energies (eV)
+  const float *sig;      // cross sections (m^2)
+  const float *gas_n;    // (nx*ny) target density
+  float m_ev;            // source mass in eV units (mcc.jl:26)
+  float mr1, mr2;        // m_s/(m_s+m_t), m_t/(m_s+m_t)
+  float vth_t;           // sqrt(2 kB T_t / m_t) (mcc.jl:74-77)
+  float qmt_dt;          // (q_t/m_t) Δt for the target velocity term
+  float lam;             // N*maxPt: mean selections per particle and step
+  float inv_nmaxpt;      // 1/(N*maxPt)
+  float dt;
+  int mp;                // ions appended per ionisation (round(w0_s/w0_p))
+  unsigned long long *counts;  // N
+  unsigned int *nu;      // (nx*ny*N) accepted collisions per node and process
+  uint32_t key0, key1;
+};
+
+struct Mcc {
+  int src = -1, prod = -1;
+  int N = 0;
+  std::vector<int> types;
+  std::vector<double> energies;
+  std::vector<double> eps_h, sig_h;
+  std::vector<int> off;
+  double max_sigma_g = 0;
+  double max_n = 0;
+  double gas_mass = 0, gas_T = 0, gas_q = 0;
+  float *eps = nullptr, *sig = nullptr, *gas_n = nullptr;
+  unsigned long long *counts = nullptr;
+  unsigned int *nu = nullptr;
+  int set_index = 0;
+};
+
+void mcc_destroy(Mcc *m) {
+  if (!m) return;
+  cudaFree(m->eps);
+  cudaFree(m->sig);
+  cudaFree(m->gas_n);
+  cudaFree(m->counts);
+  cudaFree(m->nu);
+  delete m;
+}
+
+// ---- Philox4x32-10 ----------------------------------------------------------
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// uniform in [0,1) with 24 random bits
+__device__ __forceinline__ float u01(uint32_t v) { return (float)(v >> 8) * 5.9604644775390625e-08f; }
+
+struct Stream {
+  U4 ctr;
+  uint32_t k0, k1;
+  U4 buf;
+  int left;
+  __device__ float next() {
+    if (left == 0) {
+      buf = philox4x32_10(ctr, k0, k1);
+      ctr.w += 1;
+      left = 4;
+    }
+    uint32_t v = left == 4 ? buf.x : left == 3 ? buf.y : left == 2 ? buf.z : buf.w;
+    left--;
+    return u01(v);
+  }
+  __device__ float normal() {  // Box-Muller (one of the pair)
+    float a = next();
+    float b = next();
+    a = fmaxf(a, 1.0e-12f);
+    float rad = sqrtf(-2.0f * logf(a));
+    return rad * cospif(2.0f * b);
+  }
+};
+
+// ---- kinematics (mcc.jl:53-229) -------------------------------------------
+// euler_angles (mcc.jl:89-106): cosθ = v_z/|v|, sinθ = sqrt(1 - cos²θ),
+// cosϕ = v_x/|v|/sinθ, sinϕ = v_y/|v|/sinθ.  The same angles are formed here
+// from the transverse speed ρ = sqrt(v_x² + v_y²) (sinθ = ρ/|v|, cosϕ = v_x/ρ),
+// which keeps sin²+cos² = 1 to FP32 rounding when θ is small; sinθ = 0 takes
+// the reference's sinθ ≈ 0 branch.
+__device__ __forceinline__ void euler_angles(const float v[3], float &sth, float &cth, float &sph, float &cph) {
+  const float rho = sqrtf(v[0] * v[0] + v[1] * v[1]);
+  const float nv = sqrtf(rho * rho + v[2] * v[2]);
+  if (!(nv > 0.0f)) {  // zero speed: unrotated frame (the reference yields NaN)
+    sth = 0.0f;
+    cth = 1.0f;
+    sph = 0.0f;
+    cph = 1.0f;
+    return;
+  }
+  cth = v[2] / nv;
+  sth = rho / nv;
+  if (rho == 0.0f) {
+    cph = 1.0f;
+    sph = 0.0f;
+  } else {
+    cph = v[0] / rho;
+    sph = v[1] / rho;
+  }
+}
+
+// [sinχcosη sinχsinη cosχ] * unrotated(θ, ϕ)  (mcc.jl:83-87)
+__device__ __forceinline__ void rotate(float sth, float cth, float sph, float cph, float sch, float cch, float seta,
+                                       float ceta, float out[3]) {
+  const float a0 = sch * ceta, a1 = sch * seta, a2 = cch;
+  out[0] = a0 * (cph * cth) - a1 * sph + a2 * (cph * sth);
+  out[1] = -a0 * (sph * cth) + a1 * cph + a2 * (sph * sth);
+  out[2] = -a0 * sth + a2 * cth;
+}
+
+__device__ __forceinline__ void isotropic_scattering(const float v[3], float u1, float u2, float out[3]) {
+  float sth, cth, sph, cph, sch, cch, seta, ceta;
+  euler_angles(v, sth, cth, sph, cph);
+  sincospif(2.0f * u1, &sch, &cch);  // χ = 2π u1 (mcc.jl:54)
+  sincospif(2.0f * u2, &seta, &ceta);
+  rotate(sth, cth, sph, cph, sch, cch, seta, ceta, out);
+}
+
+__device__ __forceinline__ void diffuse_reflection(const float v[3], float u1, float u2, float out[3]) {
+  float sth, cth, sph, cph, seta, ceta;
+  euler_angles(v, sth, cth, sph, cph);
+  const float sch = sqrtf(u1);
+  const float cch = -sqrtf(fmaxf(1.0f - sch * sch, 0.0f));
+  sincospif(2.0f * u2, &seta, &ceta);
+  rotate(sth, cth, sph, cph, sch, cch, seta, ceta, out);
+}
+
+// CrossSection: linear interpolation, flat extrapolation (cross_section.jl:8-14)
+__device__ __forceinline__ float sigma_at(const float *e, const float *s, int n, float x) {
+  if (x <= e[0]) return s[0];
+  if (x >= e[n - 1]) return s[n - 1];
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (e[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  const float t = (x - e[lo]) / (e[hi] - e[lo]);
+  return (1.0f - t) * s[lo] + t * s[hi];
+}
+
+// warp-aggregated slot reservation: every lane with want=true gets a slot
+__device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsigned int *next_id, uint32_t &nid) {
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(FULL, want);
+  long long base = 0;
+  uint32_t idb = 0;
+  const int leader = m ? __ffs(m) - 1 : 0;
+  if (m && lane == (unsigned)leader) {
+    base = atomicAdd((unsigned long long *)np, (unsigned long long)__popc(m));
+    idb = atomicAdd(next_id, (unsigned)__popc(m));
+  }
+  base = __shfl_sync(FULL, base, leader);
+  idb = __shfl_sync(FULL, idb, leader);
+  const int rank = __popc(m & ((1u << lane) - 1u));
+  nid = idb + rank;
+  return base + rank;
+}
+
+__global__ void __launch_bounds__(256) k_mcc(SpeciesDev s, SpeciesDev prod, int has_prod, MccDev M,
+                                             const float2 *__restrict__ E, int nx,
+                                             const unsigned long long *__restrict__ d_step, int *err) {
+  extern __shared__ float tab[];
+  const unsigned FULL = 0xffffffffu;
+  const int ntab = M.off[M.N];
+  for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
+    tab[t] = M.eps[t];
+    tab[ntab + t] = M.sig[t];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long long np = s.st->np;
+  const int cur = s.st->cur;
+  float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
+  float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
+  uint32_t *__restrict__ ids = pick(s.id[0], s.id[1], cur);
+  const unsigned long long step = *d_step;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned cnt[kMaxProc];
+#pragma unroll
+  for (int k = 0; k < kMaxProc; k++) cnt[k] = 0;
+  int flags = 0;
+  const float expl = __expf(-M.lam);
+  for (long long base = warp * 32; base < np; base += nwarps * 32) {
+    const long long p = base + lane;
+    int cell = -1;
+    float4 a = make_float4(0, 0, 0, 0);
+    float2 b = make_float2(0, 0);
+    uint32_t pid = 0;
+    if (p < np) {
+      b = zc[p];
+      cell = __float_as_int(b.y);
+    }
+    Stream R;
+    int nsel = 0;
+    if (cell >= 0) {
+      pid = ids[p];
+      R.ctr = U4{pid, (uint32_t)step, (uint32_t)(step >> 32), 0u};
+      R.k0 = M.key0;
+      R.k1 = M.key1;
+      R.left = 0;
+      // selections ~ Poisson(lam) by inversion (bounded)
+      float u = R.next();
+      float pk = expl, cdf = expl;
+      while (u > cdf && nsel < 16) {
+        nsel++;
+        pk *= M.lam / nsel;
+        cdf += pk;
+      }
+    }
+    bool any_sel = __any_sync(FULL, nsel > 0);
+    if (!any_sel) continue;
+    bool ion_child = false;
+    float cv[3] = {0, 0, 0};
+    float tv_ion[3] = {0, 0, 0};
+    bool changed = false;
+    float v[3] = {0, 0, 0};
+    int node = 0;
+    if (nsel > 0) {
+      a = xv[p];
+      v[0] = a.z;
+      v[1] = a.w;
+      v[2] = b.x;
+      const int i0 = cell & 0xffff, j0 = cell >> 16;
+      node = i0 + nx * j0;
+      const float n = __ldg(M.gas_n + node);
+      const float2 e = __ldg(E + node);
+      const float tvx = M.qmt_dt * e.x, tvy = M.qmt_dt * e.y;
+      for (int sidx = 0; sidx < nsel && n >= 0.0f; sidx++) {
+        const float U = R.next();
+        int k = (int)floorf(M.N * U);
+        if (k >= M.N) k = M.N - 1;
+        const float gx = tvx - v[0], gy = tvy - v[1], gz = -v[2];
+        const float g = sqrtf(gx * gx + gy * gy + gz * gz);
+        const float eps = 0.5f * M.m_ev * g * g;
+        const float sg = sigma_at(tab + M.off[k], tab + ntab + M.off[k], M.off[k + 1] - M.off[k], eps) * g;
+        float Pk = -expm1f(-n * sg * M.dt);
+        Pk *= M.inv_nmaxpt;
+        if (Pk > 1.0f) {
+          flags |= DERR_PROB;
+          break;
+        }
+        if (!(U > (float)(k + 1) / M.N - Pk)) continue;
+        cnt[k]++;
+        if (M.nu) atomicAdd(M.nu + (size_t)node * M.N + k, 1u);
+        const int type = M.types[k];
+        if (type <= ISKRA_MCC_INELASTIC_BACKWARD) {
+          float tv[3] = {R.normal() * M.vth_t, R.normal() * M.vth_t, R.normal() * M.vth_t};
+          float vr[3], w[3], dir[3];
+          for (int c = 0; c < 3; c++) {
+            vr[c] = v[c] - tv[c];
+            w[c] = M.mr1 * v[c] + M.mr2 * tv[c];
+          }
+          const float nvr = sqrtf(vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2]);
+          float scale = nvr;
+          if (type == ISKRA_MCC_INELASTIC_BACKWARD) scale = R.next() * nvr;
+          const float u1 = R.next(), u2 = R.next();
+          if (type == ISKRA_MCC_ELASTIC_ISOTROPIC) isotropic_scattering(vr, u1, u2, dir);
+          else diffuse_reflection(vr, u1, u2, dir);
+          for (int c = 0; c < 3; c++) v[c] = w[c] + M.mr2 * (scale * dir[c]);
+          changed = true;
+          continue;
+        }
+        const float sE = 0.5f * M.m_ev * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) - M.energy[k];
+        if (sE < 0.0f) continue;  // not enough energy (mcc.jl:179-182,220-223)
+        const float al = sqrtf(2.0f / M.m_ev);
+        if (type == ISKRA_MCC_EXCITATION) {
+          const float ev = al * sqrtf(sE);
+          float dir[3];
+          const float u1 = R.next(), u2 = R.next();
+          isotropic_scattering(v, u1, u2, dir);
+          for (int c = 0; c < 3; c++) v[c] = ev * dir[c];
+          changed = true;
+          continue;
+        }
+        // ionisation (mcc.jl:174-213); one child electron per particle and step
+        const float e1 = sE * R.next(), e2 = sE - e1;
+        const float v1 = al * sqrtf(e1), v2 = al * sqrtf(e2);
+        float dir[3];
+        float u1 = R.next(), u2 = R.next();
+        diffuse_reflection(v, u1, u2, dir);
+        for (int c = 0; c < 3; c++) v[c] = v1 * dir[c];
+        changed = true;
+        if (!ion_child) {
+          u1 = R.next();
+          u2 = R.next();
+          diffuse_reflection(v, u1, u2, dir);
+          for (int c = 0; c < 3; c++) cv[c] = v2 * dir[c];
+          for (int c = 0; c < 3; c++) tv_ion[c] = R.normal() * M.vth_t;
+          ion_child = true;
+        }
+      }
+      if (changed) {
+        if (!isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2])) {
+          flags |= DERR_NAN;
+        }
+        xv[p] = make_float4(a.x, a.y, v[0], v[1]);
+        zc[p] = make_float2(v[2], b.y);
+      }
+    }
+    // appends: child electron into the source species, ions into the product
+    if (__any_sync(FULL, ion_child)) {
+      uint32_t nid;
+      long long slot = warp_reserve(ion_child, &s.st->np_new, &s.st->next_id, nid);
+      if (ion_child) {
+        if (slot < s.cap) {
+          const int cb = s.st->cur;  // unchanged during the kernel
+          pick(s.xv[0], s.xv[1], cb)[slot] = make_float4(a.x, a.y, cv[0], cv[1]);
+          pick(s.zc[0], s.zc[1], cb)[slot] = make_float2(cv[2], __int_as_float(cell));
+          pick(s.id[0], s.id[1], cb)[slot] = nid;
+        } else {
+          flags |= DERR_CAPACITY;
+        }
+      }
+      if (has_prod) {
+        for (int m = 0; m < M.mp; m++) {
+          uint32_t pid2;
+          long long ps = warp_reserve(ion_child, &prod.st->np_new, &prod.st->next_id, pid2);
+          if (ion_child) {
+            if (ps < prod.cap) {
+              const int pb = prod.st->cur;
+              pick(prod.xv[0], prod.xv[1], pb)[ps] = make_float4(a.x, a.y, tv_ion[0], tv_ion[1]);
+              pick(prod.zc[0], prod.zc[1], pb)[ps] = make_float2(tv_ion[2], __int_as_float(cell));
+              pick(prod.id[0], prod.id[1], pb)[ps] = pid2;
+            } else {
+              flags |= DERR_CAPACITY;
+            }
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kMaxProc; k++) {
+    if (k >= M.N) break;
+    unsigned t = __reduce_add_sync(FULL, cnt[k]);
+    if (lane == 0 && t) atomicAdd(M.counts + k, (unsigned long long)t);
+  }
+  int f = __reduce_or_sync(FULL, flags);
+  if (lane == 0 && f) atomicOr(err, f);
+}
+
+// Appends reserve slots from np_new so that np (the loop bound of the running
+// kernel) stays fixed during the launch; np takes the new extent afterwards,
+// clamped to the capacity (failed appends already raised DERR_CAPACITY).
+__global__ void k_append_begin(SpeciesState *a, SpeciesState *b) {
+  a->np_new = a->np;
+  if (b) b->np_new = b->np;
+}
+__global__ void k_append_end(SpeciesState *st, long long cap) {
+  st->np = st->np_new > cap ? cap : st->np_new;
+}
+
+int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host) {
+  (void)step_host;
+  Mcc *m = c->mccs[mid];
+  Species &s = c->species[m->src];
+  const double maxPt = 1.0 - std::exp(-m->max_n * m->max_sigma_g * dt);
+  if (maxPt > 1.0 / m->N)
+    return set_err(c, ISKRA_EPROB, "maximum collision probability above 1/N (mcc.jl:244-246)");
+  MccDev M{};
+  M.N = m->N;
+  for (int k = 0; k < m->N; k++) {
+    M.types[k] = m->types[k];
+    M.energy[k] = (float)m->energies[k];
+  }
+  for (int k = 0; k <= m->N; k++) M.off[k] = m->off[k];
+  M.eps = m->eps;
+  M.sig = m->sig;
+  M.gas_n = m->gas_n;
+  const double m_ev = s.m / 1.60217646e-19;
+  M.m_ev = (float)m_ev;
+  M.mr1 = (float)(s.m / (s.m + m->gas_mass));
+  M.mr2 = (float)(m->gas_mass / (s.m + m->gas_mass));
+  M.vth_t = (float)std::sqrt(2 * 1.3806503e-23 * m->gas_T / m->gas_mass);
+  M.qmt_dt = (float)(m->gas_q / m->gas_mass * dt);
+  M.lam = (float)(m->N * maxPt);
+  M.inv_nmaxpt = maxPt > 0 ? (float)(1.0 / (m->N * maxPt)) : 0.0f;
+  M.dt = (float)dt;
+  M.mp = 0;
+  if (m->prod >= 0) M.mp = (int)std::llround(s.w0 / c->species[m->prod].w0);
+  M.counts = m->counts;
+  M.nu = m->nu;
+  M.key0 = (uint32_t)seed;
+  M.key1 = (uint32_t)(seed >> 32) ^ (0x632BE5ABu * (uint32_t)(m->set_index + 1));
+  const int ntab = m->off[m->N];
+  const size_t smem = (size_t)2 * ntab * sizeof(float);
+  long long want = (s.cap + 255) / 256;
+  long long maxb = (long long)c->num_sms * 8;
+  int blocks = (int)(want < maxb ? (want < 1 ? 1 : want) : maxb);
+  SpeciesDev pd = m->prod >= 0 ? c->species[m->prod].dev : s.dev;
+  k_append_begin<<<1, 1, 0, c->stream>>>(s.dev.st, m->prod >= 0 ? c->species[m->prod].dev.st : nullptr);
+  k_mcc<<<blocks, 256, smem, c->stream>>>(s.dev, pd, m->prod >= 0, M, c->E32, c->nx, d_step, c->d_err);
+  ISKRA_CUDA(c, cudaGetLastError());
+  k_append_end<<<1, 1, 0, c->stream>>>(s.dev.st, s.cap);
+  if (m->prod >= 0) k_append_end<<<1, 1, 0, c->stream>>>(c->species[m->prod].dev.st, c->species[m->prod].cap);
+  ISKRA_CUDA(c, cudaGetLastError());
+  // appended particles are not in the deposit accumulators
+  for (int sid : {m->src, m->prod}) {
+    if (sid < 0) continue;
+    Species &sp = c->species[sid];
+    if (sp.acc_valid) sp.acc_zero = false;
+    sp.acc_valid = false;
+    sp.n_valid = false;
+  }
+  return ISKRA_OK;
+}
+
+}  // namespace iskra
+
+using namespace iskra;
+
+extern "C" {
+
+int iskra_mcc_create(iskra_ctx *h, int src, int nproc, const int *types, const double *energies, const int32_t *off,
+                     const double *eps, const double *sigma, double gas_mass, double gas_T, double gas_q,
+                     const double *gas_n, int prod, double *max_sigma_g, int *mid) {
+  if (!h || !types || !energies || !off || !eps || !sigma || !gas_n || !mid) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (src < 0 || src >= (int)c->species.size()) return set_err(c, ISKRA_EINVAL, "bad source species");
+  if (prod >= (int)c->species.size()) return set_err(c, ISKRA_EINVAL, "bad product species");
+  if (nproc < 1 || nproc > kMaxProc) return set_err(c, ISKRA_EINVAL, "1..8 processes per set");
+  if ((int)c->mccs.size() >= kMaxMcc) return set_err(c, ISKRA_EINVAL, "too many MCC sets");
+  if (!(gas_mass > 0) || !(gas_T >= 0)) return set_err(c, ISKRA_EINVAL, "bad gas mass / temperature");
+  if (off[0] != 0 || off[nproc] > kMaxTable) return set_err(c, ISKRA_EINVAL, "bad table offsets");
+  for (int k = 0; k < nproc; k++) {
+    if (types[k] < 0 || types[k] > 4) return set_err(c, ISKRA_EINVAL, "bad process type");
+    if (off[k + 1] - off[k] < 1) return set_err(c, ISKRA_EINVAL, "empty cross-section table");
+    for (int t = off[k] + 1; t < off[k + 1]; t++)
+      if (!(eps[t] > eps[t - 1])) return set_err(c, ISKRA_EINVAL, "table energies must increase");
+  }
+  Mcc *m = new Mcc();
+  m->src = src;
+  m->prod = prod;
+  m->N = nproc;
+  m->types.assign(types, types + nproc);
+  m->energies.assign(energies, energies + nproc);
+  m->off.assign(off, off + nproc + 1);
+  m->eps_h.assign(eps, eps + off[nproc]);
+  m->sig_h.assign(sigma, sigma + off[nproc]);
+  m->gas_mass = gas_mass;
+  m->gas_T = gas_T;
+  m->gas_q = gas_q;
+  m->set_index = (int)c->mccs.size();
+  // MonteCarloCollisions constructor (mcc.jl:27-51): max over the union of
+  // table energies (plus 0) of Σ_k σ_k(ε) v(ε), v = sqrt(2ε/m_eV)
+  std::vector<double> e = {0.0};
+  e.insert(e.end(), eps, eps + off[nproc]);
+  std::sort(e.begin(), e.end());
+  e.erase(std::unique(e.begin(), e.end()), e.end());
+  const double ms = c->species[src].m / 1.60217646e-19;
+  const double alpha = std::sqrt(2.0 / ms);
+  double best = 0;
+  for (size_t a = 0; a < e.size(); a++) {
+    const double v = alpha * std::sqrt(e[a]);
+    double s = 0;
+    for (int k = 0; k < nproc; k++) {
+      const double *E = eps + off[k], *S = sigma + off[k];
+      const int n = off[k + 1] - off[k];
+      double sg;
+      if (e[a] <= E[0]) sg = S[0];
+      else if (e[a] >= E[n - 1]) sg = S[n - 1];
+      else {
+        int lo = 0, hi = n - 1;
+        while (hi - lo > 1) {
+          int mid2 = (lo + hi) >> 1;
+          if (E[mid2] <= e[a]) lo = mid2; else hi = mid2;
+        }
+        const double t = (e[a] - E[lo]) / (E[hi] - E[lo]);
+        sg = (1.0 - t) * S[lo] + t * S[hi];
+      }
+      s += sg * v;
+    }
+    if (a == 0 || s > best) best = s;
+  }
+  m->max_sigma_g = best;
+  double mx = gas_n[0];
+  for (int k = 1; k < c->nn; k++) mx = gas_n[k] > mx ? gas_n[k] : mx;
+  m->max_n = mx;
+  std::vector<float> ef(eps, eps + off[nproc]), sf(sigma, sigma + off[nproc]), nf(gas_n, gas_n + c->nn);
+  bool ok = cudaMalloc(&m->eps, ef.size() * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->sig, sf.size() * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->gas_n, nf.size() * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->counts, kMaxProc * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMalloc(&m->nu, (size_t)c->nn * nproc * sizeof(unsigned int)) == cudaSuccess;
+  if (!ok) {
+    mcc_destroy(m);
+    return set_err(c, ISKRA_ENOMEM, "MCC tables");
+  }
+  cudaMemcpy(m->eps, ef.data(), ef.size() * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(m->sig, sf.data(), sf.size() * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(m->gas_n, nf.data(), nf.size() * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemset(m->counts, 0, kMaxProc * sizeof(unsigned long long));
+  cudaMemset(m->nu, 0, (size_t)c->nn * nproc * sizeof(unsigned int));
+  c->mccs.push_back(m);
+  *mid = (int)c->mccs.size() - 1;
+  if (max_sigma_g) *max_sigma_g = best;
+  invalidate_graphs(c);
+  return ISKRA_OK;
+}
+
+int iskra_mcc_perform(iskra_ctx *h, int mid, double dt, uint64_t seed, uint64_t step) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (mid < 0 || mid >= (int)c->mccs.size()) return set_err(c, ISKRA_EINVAL, "bad MCC id");
+  if (!(dt > 0)) return set_err(c, ISKRA_EINVAL, "dt must be positive");
+  unsigned long long st = step;
+  ISKRA_CUDA(c, cudaMemcpyAsync(c->d_step, &st, sizeof(st), cudaMemcpyHostToDevice, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->d_step_known = ~0ull;
+  return launch_mcc(c, mid, dt, seed, c->d_step, step);
+}
+
+int iskra_mcc_counts(iskra_ctx *h, int mid, int64_t *counts) {
+  if (!h || !counts) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (mid < 0 || mid >= (int)c->mccs.size()) return set_err(c, ISKRA_EINVAL, "bad MCC id");
+  Mcc *m = c->mccs[mid];
+  unsigned long long tmp[kMaxProc];
+  ISKRA_CUDA(c, cudaMemcpyAsync(tmp, m->counts, sizeof(tmp), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(m->counts, 0, sizeof(tmp), c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < m->N; k++) counts[k] = (int64_t)tmp[k];
+  return collect_device_errors(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,563 @@
+// particles.cu -- the per-particle hot path:
+//   k_push    : CIC gather (cloud_in_cell.jl:20-36) + Boris push with B = 0
+//               (pushers.jl:37-50) + after_push wrap!/discard! (wrap.jl) +
+//               CIC deposit (cloud_in_cell.jl:1-18) of the pushed particle,
+//               fused in one pass over the particle store.
+//   k_finalize: density = deposit ./ cell_volume (kinetic.jl:53,
+//               RegularGrids.jl:26-38) and ρ = Σ q n (ParticleInCell.jl:118-122).
+//   k_efield  : E = -∇ϕ (generalized_poisson.jl:398-410), FP32 copy for the
+//               gather and FP64 copy for download.
+//   sort      : counting sort by cell + compaction of discarded particles.
+//
+// Deposit arithmetic: offsets are multiples of 2^-24, u = hx*2^24 is an exact
+// integer, so the CIC weights (2^24-u)(2^24-v), u(2^24-v), ... are exact 48-bit
+// integers.  They are shifted right by `shift` (0 unless a node could exceed
+// 2^63) and summed with 64-bit integer atomics after a warp-level reduction
+// over lanes that share a cell.  Integer addition is associative, so the
+// density is bit-identical for any particle order or launch shape.
+#include <cmath>
+
+#include "internal.cuh"
+
+namespace iskra {
+
+struct PushParams {
+  float h;          // 0.5 * Δt * q/m
+  float dtdx, dtdy; // Δt/Δx, Δt/Δy
+  int nx, ny;
+  int mode_x, mode_y;
+};
+
+// Reduce four u64 values over the lanes of the warp that share `key`; the
+// lowest lane of each group returns true holding the group sums.
+__device__ __forceinline__ bool reduce_peers(int key, unsigned long long (&w)[4]) {
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(FULL, key);
+  const unsigned lt = (1u << lane) - 1u;
+  const bool leader = (peers & lt) == 0;
+  unsigned above = peers & ~(lt | (1u << lane));
+  int rel = __popc(peers & lt);
+  bool active = true;
+  // at most log2(32) = 5 rounds: each removes half of the active lanes
+  for (int round = 0; round < 6; round++) {
+    if (!__any_sync(FULL, active && above != 0)) break;
+    int src = above ? (__ffs(above) - 1) : (int)lane;
+    unsigned long long t0 = __shfl_sync(FULL, w[0], src);
+    unsigned long long t1 = __shfl_sync(FULL, w[1], src);
+    unsigned long long t2 = __shfl_sync(FULL, w[2], src);
+    unsigned long long t3 = __shfl_sync(FULL, w[3], src);
+    if (active && (rel & 1) == 0 && above) {
+      w[0] += t0;
+      w[1] += t1;
+      w[2] += t2;
+      w[3] += t3;
+    }
+    bool leaving = active && (rel & 1);
+    unsigned leave = __ballot_sync(FULL, leaving);
+    above &= ~leave;
+    if (leaving) active = false;
+    rel >>= 1;
+  }
+  return leader;
+}
+
+// Move by d cells along one axis in FP32: offset h in [0,1) on the 2^-24 grid,
+// cell index i (int).  Returns the new offset; i is updated in place.
+__device__ __forceinline__ float move_axis(float h, float d, int &i) {
+  d = fminf(fmaxf(d, -1.0e9f), 1.0e9f);
+  float fd = floorf(d);
+  float fr = d - fd;           // [0,1)
+  float t = h + fr;            // [0,2)
+  int carry = 0;
+  if (t >= 1.0f) {
+    t -= 1.0f;
+    carry = 1;
+  }
+  int u = __float2int_rn(t * kOffScale);
+  if (u >= (1 << 24)) {
+    u -= (1 << 24);
+    carry += 1;
+  }
+  i += (int)fd + carry;
+  return (float)u * kOffInv;
+}
+
+// after_push along one axis with P = n-1 cells (wrap period (n-1)Δh,
+// wrap.jl:20-33; discard! removes α ≠ 0, wrap.jl:1-18).  Returns 0 = keep,
+// 1 = absorbed at the low wall, 2 = absorbed at the high wall,
+// 3 = out of the grid without a boundary rule.
+template <int MODE>
+__device__ __forceinline__ int apply_boundary(int &i, int P) {
+  if (i >= 0 && i < P) return 0;
+  if (MODE == ISKRA_BND_WRAP) {
+    i %= P;
+    if (i < 0) i += P;
+    return 0;
+  }
+  if (MODE == ISKRA_BND_DISCARD) return i < 0 ? 1 : 2;
+  return 3;
+}
+
+template <bool PUSH, int MX, int MY>
+__global__ void __launch_bounds__(256) k_push(SpeciesDev s, const float2 *__restrict__ E, PushParams P,
+                                               int *err) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long np = s.st->np;
+  const int cur = s.st->cur;
+  float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
+  float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned ab[4] = {0, 0, 0, 0};
+  int flags = 0;
+  const int nx = P.nx;
+  for (long long base = warp * 32; base < np; base += nwarps * 32) {
+    const long long p = base + lane;
+    int key = -1;
+    unsigned long long w[4] = {0, 0, 0, 0};
+    if (p < np) {
+      float4 a = xv[p];
+      float2 b = zc[p];
+      int cell = __float_as_int(b.y);
+      if (cell >= 0) {
+        int i0 = cell & 0xffff, j0 = cell >> 16;
+        float hx = a.x, hy = a.y;
+        if (PUSH) {
+          const int n0 = i0 + nx * j0;
+          const float gx = 1.0f - hx, gy = 1.0f - hy;
+          const float2 e00 = __ldg(E + n0), e10 = __ldg(E + n0 + 1);
+          const float2 e01 = __ldg(E + n0 + nx), e11 = __ldg(E + n0 + nx + 1);
+          const float ex = gx * gy * e00.x + hx * gy * e10.x + gx * hy * e01.x + hx * hy * e11.x;
+          const float ey = gx * gy * e00.y + hx * gy * e10.y + gx * hy * e01.y + hx * hy * e11.y;
+          // Boris with B = 0: v- = v + hE ; v = hE + v+ (v+ = v-)
+          float vx = fmaf(P.h, ex, a.z);
+          float vy = fmaf(P.h, ey, a.w);
+          vx = fmaf(P.h, ex, vx);
+          vy = fmaf(P.h, ey, vy);
+          if (!isfinite(vx) || !isfinite(vy)) {
+            flags |= DERR_NAN;
+            cell = -1;
+          } else {
+            hx = move_axis(hx, vx * P.dtdx, i0);
+            hy = move_axis(hy, vy * P.dtdy, j0);
+            int rx = apply_boundary<MX>(i0, nx - 1);
+            int ry = rx ? 0 : apply_boundary<MY>(j0, P.ny - 1);
+            if (rx == 3 || ry == 3) {
+              flags |= DERR_DOMAIN;
+              cell = -1;
+            } else if (rx) {
+              ab[rx - 1]++;
+              cell = -1;
+            } else if (ry) {
+              ab[ry + 1]++;
+              cell = -1;
+            } else {
+              cell = i0 | (j0 << 16);
+            }
+          }
+          xv[p] = make_float4(hx, hy, vx, vy);
+          zc[p] = make_float2(b.x, __int_as_float(cell));
+        }
+        if (cell >= 0) {
+          key = i0 + nx * j0;
+          const unsigned long long ux = (unsigned long long)__float2uint_rn(hx * kOffScale);
+          const unsigned long long uy = (unsigned long long)__float2uint_rn(hy * kOffScale);
+          const unsigned long long gx = (1ull << 24) - ux, gy = (1ull << 24) - uy;
+          w[0] = gx * gy;
+          w[1] = ux * gy;
+          w[2] = gx * uy;
+          w[3] = ux * uy;
+          if (s.shift) {
+            const unsigned long long half = 1ull << (s.shift - 1);
+#pragma unroll
+            for (int k = 0; k < 4; k++) w[k] = (w[k] + half) >> s.shift;
+          }
+        }
+      }
+    }
+    if (reduce_peers(key, w) && key >= 0) {
+      atomicAdd(s.acc + key, w[0]);
+      atomicAdd(s.acc + key + 1, w[1]);
+      atomicAdd(s.acc + key + nx, w[2]);
+      atomicAdd(s.acc + key + nx + 1, w[3]);
+    }
+  }
+  if (PUSH) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      unsigned t = __reduce_add_sync(FULL, ab[k]);
+      if (lane == 0 && t) atomicAdd(&s.st->absorbed[k], (unsigned long long)t);
+    }
+    int f = __reduce_or_sync(FULL, flags);
+    if (lane == 0 && f) atomicOr(err, f);
+  }
+}
+
+template <bool PUSH>
+static void launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
+  const int T = 256;
+#define ISKRA_PUSH_CASE(MX, MY)                                                     \
+  if (P.mode_x == MX && P.mode_y == MY) {                                           \
+    k_push<PUSH, MX, MY><<<blocks, T, 0, c->stream>>>(s.dev, c->E32, P, c->d_err); \
+    return;                                                                         \
+  }
+  ISKRA_PUSH_CASE(0, 0) ISKRA_PUSH_CASE(0, 1) ISKRA_PUSH_CASE(0, 2)
+  ISKRA_PUSH_CASE(1, 0) ISKRA_PUSH_CASE(1, 1) ISKRA_PUSH_CASE(1, 2)
+  ISKRA_PUSH_CASE(2, 0) ISKRA_PUSH_CASE(2, 1) ISKRA_PUSH_CASE(2, 2)
+#undef ISKRA_PUSH_CASE
+}
+
+static int push_blocks(Ctx *c, Species &s) {
+  long long want = (s.cap + 255) / 256;
+  long long maxb = (long long)c->num_sms * 8;
+  if (want < 1) want = 1;
+  return (int)(want < maxb ? want : maxb);
+}
+
+int launch_advance(Ctx *c, int sid, float dt) {
+  Species &s = c->species[sid];
+  if (!s.acc_zero) {
+    // accumulator holds an old deposit: clear it first
+    ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, (size_t)c->nn * sizeof(unsigned long long), c->stream));
+  }
+  PushParams P;
+  P.h = (float)(0.5 * (double)dt * (s.q / s.m));
+  P.dtdx = (float)((double)dt / c->g.dx);
+  P.dtdy = (float)((double)dt / c->g.dy);
+  P.nx = c->nx;
+  P.ny = c->ny;
+  P.mode_x = s.bnd[0];
+  P.mode_y = s.bnd[1];
+  launch_push_modes<true>(c, s, P, push_blocks(c, s));
+  ISKRA_CUDA(c, cudaGetLastError());
+  s.acc_valid = true;  // accumulator = deposit of the pushed positions (unconsumed)
+  s.acc_zero = false;
+  s.n_valid = false;
+  return ISKRA_OK;
+}
+
+int launch_deposit(Ctx *c, int sid) {
+  Species &s = c->species[sid];
+  if (!s.acc_zero)
+    ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, (size_t)c->nn * sizeof(unsigned long long), c->stream));
+  PushParams P{};
+  P.nx = c->nx;
+  P.ny = c->ny;
+  k_push<false, 0, 0><<<push_blocks(c, s), 256, 0, c->stream>>>(s.dev, c->E32, P, c->d_err);
+  ISKRA_CUDA(c, cudaGetLastError());
+  s.acc_valid = true;
+  s.acc_zero = false;
+  return ISKRA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// density + charge density
+// ---------------------------------------------------------------------------
+struct FinalizeArgs {
+  int ns;
+  unsigned long long *acc[kMaxSpecies];
+  double *n[kMaxSpecies];
+  double scale[kMaxSpecies];  // w0 * 2^(shift-48)
+  double q[kMaxSpecies];
+  int consume[kMaxSpecies];
+};
+
+__global__ void k_finalize(FinalizeArgs A, const double *__restrict__ vol_inv, const double *__restrict__ bg,
+                           double *__restrict__ rho, int nn) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    double r = 0.0;
+    const double vi = vol_inv[k];
+    for (int s = 0; s < A.ns; s++) {
+      double n;
+      if (A.consume[s]) {
+        unsigned long long a = A.acc[s][k];
+        A.acc[s][k] = 0ull;
+        n = (double)a * A.scale[s] * vi;
+        A.n[s][k] = n;
+      } else {
+        n = A.n[s][k];
+      }
+      r += n * A.q[s];
+    }
+    if (bg) r += bg[k];
+    if (rho) rho[k] = r;
+  }
+}
+
+// Brings every species' density up to date (depositing species whose
+// positions changed without a deposit, consuming unconsumed accumulators) and,
+// when with_rho, forms ρ.
+static int finalize(Ctx *c, bool with_rho) {
+  FinalizeArgs A{};
+  A.ns = (int)c->species.size();
+  bool any = false;
+  for (int s = 0; s < A.ns; s++) {
+    Species &sp = c->species[s];
+    if (!sp.acc_valid && !sp.n_valid) {
+      int rc = launch_deposit(c, s);
+      if (rc) return rc;
+    }
+    A.acc[s] = sp.dev.acc;
+    A.n[s] = sp.n;
+    A.scale[s] = sp.w0 * ldexp(1.0, sp.dev.shift - 48);
+    A.q[s] = sp.q;
+    A.consume[s] = sp.acc_valid ? 1 : 0;
+    any |= sp.acc_valid;
+  }
+  if (!any && !with_rho) return ISKRA_OK;
+  int blocks = c->num_sms * 4;
+  int need = (c->nn + 255) / 256;
+  if (need < blocks) blocks = need;
+  k_finalize<<<blocks, 256, 0, c->stream>>>(A, c->vol_inv, c->rho_bg, with_rho ? c->rho : nullptr, c->nn);
+  ISKRA_CUDA(c, cudaGetLastError());
+  for (int s = 0; s < A.ns; s++) {
+    Species &sp = c->species[s];
+    if (sp.acc_valid) {
+      sp.acc_valid = false;
+      sp.acc_zero = true;
+    }
+    sp.n_valid = true;
+  }
+  return ISKRA_OK;
+}
+
+int launch_charge_density(Ctx *c) { return finalize(c, true); }
+
+// ---------------------------------------------------------------------------
+// E = -∇ϕ  (generalized_poisson.jl:398-410)
+// ---------------------------------------------------------------------------
+__global__ void k_efield(const double *__restrict__ phi, int nx, int ny, double idx2, double idx1, double idy2,
+                         double idy1, float2 *__restrict__ E32, double *__restrict__ E64) {
+  const int nn = nx * ny;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const int i = k % nx, j = k / nx;
+    double ex, ey;
+    if (i == 0) ex = (phi[k] - phi[k + 1]) * idx1;
+    else if (i == nx - 1) ex = (phi[k - 1] - phi[k]) * idx1;
+    else ex = (phi[k - 1] - phi[k + 1]) * idx2;
+    if (j == 0) ey = (phi[k] - phi[k + nx]) * idy1;
+    else if (j == ny - 1) ey = (phi[k - nx] - phi[k]) * idy1;
+    else ey = (phi[k - nx] - phi[k + nx]) * idy2;
+    E32[k] = make_float2((float)ex, (float)ey);
+    E64[k] = ex;
+    E64[k + nn] = ey;
+    E64[k + 2 * nn] = 0.0;
+  }
+}
+
+int launch_efield_from(Ctx *c, const double *phi) {
+  int blocks = c->num_sms * 4;
+  int need = (c->nn + 255) / 256;
+  if (need < blocks) blocks = need;
+  k_efield<<<blocks, 256, 0, c->stream>>>(phi, c->nx, c->ny, 1.0 / (2 * c->g.dx), 1.0 / c->g.dx,
+                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, c->E32, c->E64);
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// counting sort by cell (histogram -> exclusive scan -> scatter), dropping
+// discarded particles
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_hist(SpeciesDev s, int nx, int *__restrict__ count) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long np = s.st->np;
+  const int cur = s.st->cur;
+  const float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = warp * 32; base < np; base += nwarps * 32) {
+    const long long p = base + lane;
+    int key = -1;
+    if (p < np) {
+      int cell = __float_as_int(zc[p].y);
+      if (cell >= 0) key = (cell & 0xffff) + nx * (cell >> 16);
+    }
+    unsigned peers = __match_any_sync(FULL, key);
+    if (key >= 0 && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(count + key, __popc(peers));
+  }
+}
+
+// exclusive scan in three phases; block = 1024 threads x 4 items
+constexpr int kScanItems = 4096;
+
+__device__ __forceinline__ int block_scan_excl(int v, int *sh, int &total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
+  }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int y = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += t;
+    }
+    sh[lane] = y;  // inclusive warp prefix
+  }
+  __syncthreads();
+  int off = wid ? sh[wid - 1] : 0;
+  total = sh[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return off + x - v;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_reduce(const int *__restrict__ in, int n, int *__restrict__ part) {
+  __shared__ int sh[32];
+  long long b0 = (long long)blockIdx.x * kScanItems;
+  int v = 0;
+  for (int k = 0; k < 4; k++) {
+    long long idx = b0 + threadIdx.x * 4 + k;
+    if (idx < n) v += in[idx];
+  }
+  int tot;
+  block_scan_excl(v, sh, tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(int *__restrict__ part, int nb) {
+  __shared__ int sh[32];
+  int carry = 0;
+  for (int b = 0; b < nb; b += 1024) {
+    int idx = b + threadIdx.x;
+    int v = idx < nb ? part[idx] : 0;
+    int tot;
+    int e = block_scan_excl(v, sh, tot);
+    if (idx < nb) part[idx] = e + carry;
+    carry += tot;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_down(const int *__restrict__ in, int n, const int *__restrict__ part,
+                                                    int *__restrict__ out) {
+  __shared__ int sh[32];
+  long long b0 = (long long)blockIdx.x * kScanItems;
+  int v[4];
+  int sum = 0;
+  for (int k = 0; k < 4; k++) {
+    long long idx = b0 + threadIdx.x * 4 + k;
+    v[k] = idx < n ? in[idx] : 0;
+    sum += v[k];
+  }
+  int tot;
+  int e = block_scan_excl(sum, sh, tot) + part[blockIdx.x];
+  for (int k = 0; k < 4; k++) {
+    long long idx = b0 + threadIdx.x * 4 + k;
+    if (idx < n) out[idx] = e;
+    e += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = e;  // grand total
+}
+
+__global__ void __launch_bounds__(256) k_scatter(SpeciesDev s, int nx, int *__restrict__ cursor) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long np = s.st->np;
+  const int cur = s.st->cur;
+  const float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
+  const float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
+  const uint32_t *__restrict__ id = pick(s.id[0], s.id[1], cur);
+  float4 *__restrict__ xo = pick(s.xv[0], s.xv[1], cur ^ 1);
+  float2 *__restrict__ zo = pick(s.zc[0], s.zc[1], cur ^ 1);
+  uint32_t *__restrict__ io = pick(s.id[0], s.id[1], cur ^ 1);
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = warp * 32; base < np; base += nwarps * 32) {
+    const long long p = base + lane;
+    int key = -1;
+    float4 a;
+    float2 b;
+    uint32_t pid = 0;
+    if (p < np) {
+      a = xv[p];
+      b = zc[p];
+      pid = id[p];
+      int cell = __float_as_int(b.y);
+      if (cell >= 0) key = (cell & 0xffff) + nx * (cell >> 16);
+    }
+    unsigned peers = __match_any_sync(FULL, key);
+    int leader = __ffs(peers) - 1;
+    int rank = __popc(peers & ((1u << lane) - 1u));
+    int pos = 0;
+    if (key >= 0 && lane == leader) pos = atomicAdd(cursor + key, __popc(peers));
+    pos = __shfl_sync(FULL, pos, leader) + rank;
+    if (key >= 0) {
+      xo[pos] = a;
+      zo[pos] = b;
+      io[pos] = pid;
+    }
+  }
+}
+
+__global__ void k_sort_finish(SpeciesState *st, const int *__restrict__ total) {
+  st->np = *total;
+  st->cur ^= 1;
+}
+
+int launch_sort(Ctx *c, int sid) {
+  Species &s = c->species[sid];
+  const int nn = c->nn;
+  ISKRA_CUDA(c, cudaMemsetAsync(c->cell_count, 0, (size_t)(nn + 1) * sizeof(int), c->stream));
+  int blocks = push_blocks(c, s);
+  k_hist<<<blocks, 256, 0, c->stream>>>(s.dev, c->nx, c->cell_count);
+  ISKRA_CUDA(c, cudaGetLastError());
+  int nb = (nn + kScanItems - 1) / kScanItems;
+  k_scan_reduce<<<nb, 1024, 0, c->stream>>>(c->cell_count, nn, c->scan_tmp);
+  k_scan_top<<<1, 1024, 0, c->stream>>>(c->scan_tmp, nb);
+  k_scan_down<<<nb, 1024, 0, c->stream>>>(c->cell_count, nn, c->scan_tmp, c->cell_cursor);
+  ISKRA_CUDA(c, cudaGetLastError());
+  // cell_count is free again: keep the grand total there for k_sort_finish
+  ISKRA_CUDA(c, cudaMemcpyAsync(c->cell_count + nn, c->cell_cursor + nn, sizeof(int), cudaMemcpyDeviceToDevice,
+                                c->stream));
+  k_scatter<<<blocks, 256, 0, c->stream>>>(s.dev, c->nx, c->cell_cursor);
+  k_sort_finish<<<1, 1, 0, c->stream>>>(s.dev.st, c->cell_count + nn);
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
+}  // namespace iskra
+
+using namespace iskra;
+
+extern "C" {
+
+int iskra_advance(iskra_ctx *h, int sid, double dt) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (sid < 0 || sid >= (int)c->species.size()) return set_err(c, ISKRA_EINVAL, "bad species id");
+  if (!(dt > 0)) return set_err(c, ISKRA_EINVAL, "dt must be positive");
+  return launch_advance(c, sid, (float)dt);
+}
+
+int iskra_density(iskra_ctx *h, int sid, double *n_out) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (sid < 0 || sid >= (int)c->species.size()) return set_err(c, ISKRA_EINVAL, "bad species id");
+  Species &s = c->species[sid];
+  if (!s.n_valid || s.acc_valid) {
+    int rc = finalize(c, false);
+    if (rc) return rc;
+  }
+  if (n_out) {
+    ISKRA_CUDA(c, cudaMemcpyAsync(n_out, s.n, (size_t)c->nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+    return collect_device_errors(c);
+  }
+  return ISKRA_OK;
+}
+
+int iskra_charge_density(iskra_ctx *h) {
+  if (!h) return ISKRA_EINVAL;
+  return launch_charge_density(&h->c);
+}
+
+}  // extern "C"

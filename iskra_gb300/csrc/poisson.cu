@@ -1,0 +1,1367 @@
+// poisson.cu -- FP64 Poisson solve on the reference's assembled operator.
+//
+// Host side: the operator is assembled row by row exactly as
+// FiniteDifferenceMethod/src/generalized_poisson.jl does it
+// (create_generalized_poisson_solver :34-68, apply_dirichlet :205-215,
+// add_new_dof :217-230, apply_neumann :235-269, apply_periodic :286-324),
+// kept in a 7-slot row form per node: self, (i-1,j), (i+1,j), (i,j-1),
+// (i,j+1), x-periodic partner, y-periodic partner; plus σ columns.
+//
+// Device side, per solve of A ϕ = b (b[ρ] = -ρ/ε0, b[Dirichlet] = ϕ0):
+//   * rows that are identity (Dirichlet, σ) are fixed values;
+//   * the remaining rows are scaled by D so that S = -D A_ff is symmetric
+//     positive (semi)definite (Neumann rows of apply_neumann have a different
+//     scale than stencil rows);
+//   * when S separates into (tridiagonal in x) + (periodic ring in y) -- true
+//     for every problem of the reference that uses apply_periodic(solver, 1)
+//     with column electrodes -- it is solved exactly by a real FFT along y, one
+//     tridiagonal (Thomas / Sherman-Morrison for x-periodic) solve per Fourier
+//     mode along x, and an inverse FFT; the residual is then re-evaluated in
+//     FP64 and the correction repeated until ||res|| <= rtol ||rhs||;
+//   * otherwise Jacobi-preconditioned CG iterates to the same tolerance.
+// All-periodic / all-open operators are singular; the solve then uses the
+// mean-zero gauge with the right-hand side projected onto the range (the
+// reference's dense A\b has no defined answer there; E = -∇ϕ is unaffected).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace iskra {
+
+int launch_efield_from(Ctx *c, const double *phi);
+
+struct RowClass {
+  double c0, cW, cE, cS, cN;  // original (unscaled) coefficients
+  double d;                   // symmetrising row scale
+  double sig_coef;            // coefficient of the σ column
+  int sig_dof;                // -1: none
+  int fixed;                  // identity row
+  int rho;                    // b = -ρ/ε0 (ρ dof) else b = bfix
+  int pad;
+};
+
+struct DriveGroup {
+  std::vector<int> nodes;
+  double amp, freq, phase, dc;
+};
+
+struct PoissonScal {           // device-resident solver scalars
+  double lambda;               // singular case: range projection shift
+  double relres;
+  double rhs2, res2;
+  int iters;
+  int done;
+  int sweeps;
+  int pad;
+  double rz, rz_new, pap;
+};
+
+struct Poisson {
+  // ---- host assembly (generalized_poisson.jl) ----
+  int nx = 0, ny = 0, nn = 0;
+  double dx = 0, dy = 0, eps0 = 0;
+  std::vector<double> C;        // nn*7
+  std::vector<double> bfix;     // b for non-ρ rows
+  std::vector<uint8_t> rho_dof;
+  std::vector<std::vector<double>> sig_cols;  // per σ dof: nn column
+  std::vector<double> sig_b;
+  std::vector<DriveGroup> drives;
+  std::vector<double> er;       // (nx+1)*(ny+1) ones
+  bool dirty = true;
+  int method = 0;               // 0 auto, 1 CG
+  // ---- device representation ----
+  bool separable = false, singular = false, cyclic = false;
+  int nclass = 0;
+  uint16_t *cls = nullptr;      // nn
+  RowClass *classes = nullptr;
+  double *bfix_d = nullptr;     // nn
+  double *sigma_d = nullptr;    // nsig
+  int nsig = 0;
+  double *x = nullptr;          // ϕ (nn)
+  double *r = nullptr, *z = nullptr, *p = nullptr, *ap = nullptr;  // nn
+  double *part = nullptr;       // reduction partials (kPartials * 4)
+  PoissonScal *scal = nullptr;
+  PoissonScal *scal_h = nullptr;  // pinned
+  double dsum = 0;              // Σ d over free rows (singular projection)
+  // separable solver
+  int N = 0, K = 0, logN = 0;   // N = ny, K = N/2+1
+  double2 *spec = nullptr;      // nx*K
+  double2 *tw = nullptr;        // N/2 twiddles exp(-2πi m/N)
+  double *low = nullptr, *up = nullptr;        // nx
+  double *inv = nullptr, *cp = nullptr, *q = nullptr;  // nx*K
+  double *gk = nullptr;         // 2K: 1/(1+v.q) and β/γ per mode (x-periodic)
+  int pin_k0 = -1;              // pinned column of mode 0 (singular)
+  // drives on device
+  int ndrive_nodes = 0;
+  int *drive_node = nullptr;
+  int *drive_group = nullptr;
+  double *drive_par = nullptr;  // 4 per group
+  int ndrive = 0;
+  int blocks = 0;
+  int last_iters = 0;
+  double last_relres = 0;
+};
+
+constexpr int kPartials = 1024;
+
+void poisson_destroy(Poisson *p) {
+  if (!p) return;
+  cudaFree(p->cls);
+  cudaFree(p->classes);
+  cudaFree(p->bfix_d);
+  cudaFree(p->sigma_d);
+  cudaFree(p->x);
+  cudaFree(p->r);
+  cudaFree(p->z);
+  cudaFree(p->p);
+  cudaFree(p->ap);
+  cudaFree(p->part);
+  cudaFree(p->scal);
+  if (p->scal_h) cudaFreeHost(p->scal_h);
+  cudaFree(p->spec);
+  cudaFree(p->tw);
+  cudaFree(p->low);
+  cudaFree(p->up);
+  cudaFree(p->inv);
+  cudaFree(p->cp);
+  cudaFree(p->q);
+  cudaFree(p->gk);
+  cudaFree(p->drive_node);
+  cudaFree(p->drive_group);
+  cudaFree(p->drive_par);
+  delete p;
+}
+
+// ===========================================================================
+// device kernels
+// ===========================================================================
+struct OpView {
+  const uint16_t *cls;
+  const RowClass *classes;
+  const double *bfix;
+  const double *sigma;
+  int nx, ny;
+};
+
+__device__ __forceinline__ void nbr(int k, int nx, int ny, int &w, int &e, int &s, int &n) {
+  const int i = k % nx, j = k / nx;
+  w = i > 0 ? k - 1 : k + nx - 1;
+  e = i < nx - 1 ? k + 1 : k - nx + 1;
+  s = j > 0 ? k - nx : k + nx * (ny - 1);
+  n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
+}
+
+__device__ __forceinline__ double drive_value(const double *par, double t) {
+  return par[0] * sin(2.0 * M_PI * par[1] * t + par[2]) + par[3];
+}
+
+// fixed-row values: Dirichlet / driven
+__global__ void k_set_fixed(OpView op, const int *__restrict__ dnode, const int *__restrict__ dgroup,
+                            const double *__restrict__ dpar, int ndn, const unsigned long long *__restrict__ step,
+                            double dt, double *__restrict__ bfix_mut, double *__restrict__ x,
+                            const double *__restrict__ rho, double eps0, int nn) {
+  // driven groups update bfix (solve of step n uses V((n-2)Δt), n >= 2)
+  const unsigned long long n_step = step ? *step : 0ull;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ndn; t += gridDim.x * blockDim.x) {
+    if (n_step >= 2) {
+      double tt = (double)(n_step - 2) * dt;
+      bfix_mut[dnode[t]] = drive_value(dpar + 4 * dgroup[t], tt);
+    }
+  }
+}
+
+__global__ void k_fixed_to_x(OpView op, double *__restrict__ x, const double *__restrict__ rho, double neg_inv_eps0,
+                             int nn) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k]];
+    if (C.fixed) x[k] = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+  }
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double t = 0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// deterministic sum of partials (every block computes the same value)
+__device__ double sum_partials(const double *__restrict__ part, int n, double *sh) {
+  double v = 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) v += part[k];
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) sh[32] = t;
+  __syncthreads();
+  double r = sh[32];
+  __syncthreads();
+  return r;
+}
+
+// Σ d_k b_k over free rows (singular case only: no fixed rows exist)
+__global__ void k_sum_db(OpView op, const double *__restrict__ rho, double neg_inv_eps0, int nn,
+                         double *__restrict__ part) {
+  __shared__ double sh[40];
+  double v = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k]];
+    if (!C.fixed) {
+      double b = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+      if (C.sig_dof >= 0) b -= C.sig_coef * op.sigma[C.sig_dof];
+      v += C.d * b;
+    }
+  }
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_lambda(const double *__restrict__ part, int nparts, double dsum, PoissonScal *sc) {
+  __shared__ double sh[40];
+  double s = sum_partials(part, nparts, sh);
+  if (threadIdx.x == 0) sc->lambda = dsum > 0 ? s / dsum : 0.0;
+}
+
+// res = b - λ - A x over free rows; r = -d * res (scaled residual);
+// partials: ||res||², ||rhs_eff||² where rhs_eff = b - λ - A_fixed x_fixed.
+// When `skip_if_done`, the kernel returns immediately once sc->done is set.
+__global__ void k_residual(OpView op, const double *__restrict__ x, const double *__restrict__ rho,
+                           double neg_inv_eps0, const PoissonScal *__restrict__ sc, double *__restrict__ r,
+                           double *__restrict__ part, int nparts_stride, int nn, int singular, int skip_if_done) {
+  __shared__ double sh[40];
+  if (skip_if_done && sc->done) return;
+  const double lam = singular ? sc->lambda : 0.0;
+  double a2 = 0, b2 = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k]];
+    if (C.fixed) {
+      r[k] = 0.0;
+      continue;
+    }
+    int w, e, s, n;
+    nbr(k, op.nx, op.ny, w, e, s, n);
+    double b = (C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k]) - lam;
+    if (C.sig_dof >= 0) b -= C.sig_coef * op.sigma[C.sig_dof];
+    const RowClass &CW = op.classes[op.cls[w]], &CE = op.classes[op.cls[e]];
+    const RowClass &CS = op.classes[op.cls[s]], &CN = op.classes[op.cls[n]];
+    double afix = 0, afree = C.c0 * x[k];
+    double t;
+    t = C.cW * x[w];
+    if (CW.fixed) afix += t; else afree += t;
+    t = C.cE * x[e];
+    if (CE.fixed) afix += t; else afree += t;
+    t = C.cS * x[s];
+    if (CS.fixed) afix += t; else afree += t;
+    t = C.cN * x[n];
+    if (CN.fixed) afix += t; else afree += t;
+    double rhs = b - afix;
+    double res = rhs - afree;
+    r[k] = -C.d * res;
+    a2 += res * res;
+    b2 += rhs * rhs;
+  }
+  double ta = block_sum(a2, sh);
+  double tb = block_sum(b2, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = ta;
+    part[nparts_stride + blockIdx.x] = tb;
+  }
+}
+
+// convergence check after a residual evaluation
+__global__ void k_check(const double *__restrict__ part, int nparts, int stride, PoissonScal *sc, double rtol2,
+                        int count_sweep) {
+  __shared__ double sh[40];
+  if (sc->done) return;
+  double a = sum_partials(part, nparts, sh);
+  double b = sum_partials(part + stride, nparts, sh);
+  if (threadIdx.x == 0) {
+    sc->res2 = a;
+    sc->rhs2 = b;
+    sc->relres = b > 0 ? sqrt(a / b) : sqrt(a);
+    if (count_sweep) sc->iters += 1;
+    if ((b > 0 && a <= rtol2 * b) || a == 0.0) sc->done = 1;
+  }
+}
+
+// ---------------- separable solver: FFT(y) x tridiagonal(x) ----------------
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ unsigned bitrev(unsigned v, int bits) { return __brev(v) >> (32 - bits); }
+
+// in-place radix-2 DIT FFT of TI columns of length N held in shared memory
+// (input already in bit-reversed order); sign = -1 forward, +1 inverse
+__device__ void fft_columns(double2 *buf, int TI, int N, int logN, const double2 *__restrict__ tw, bool inverse) {
+  const int half_total = TI * (N >> 1);
+  for (int s = 1; s <= logN; s++) {
+    const int half = 1 << (s - 1);
+    const int stride = N >> s;  // twiddle stride
+    for (int b = threadIdx.x; b < half_total; b += blockDim.x) {
+      const int col = b / (N >> 1);
+      const int kk = b - col * (N >> 1);
+      const int grp = kk >> (s - 1);
+      const int pos = kk & (half - 1);
+      const int i1 = grp * (half << 1) + pos, i2 = i1 + half;
+      double2 w = tw[pos * stride];
+      if (inverse) w.y = -w.y;
+      double2 *c = buf + col * N;
+      double2 t = cmul(w, c[i2]);
+      double2 u = c[i1];
+      c[i1] = make_double2(u.x + t.x, u.y + t.y);
+      c[i2] = make_double2(u.x - t.x, u.y - t.y);
+    }
+    __syncthreads();
+  }
+}
+
+// r (nx,ny) -> spec[i][k], k = 0..N/2 (real input, forward FFT along y)
+__global__ void k_fft_fwd(const double *__restrict__ r, int nx, int N, int logN, int TI, const double2 *__restrict__ tw,
+                          double2 *__restrict__ spec, const PoissonScal *__restrict__ sc) {
+  extern __shared__ double2 buf[];
+  if (sc->done) return;
+  const int i0 = blockIdx.x * TI;
+  for (int t = threadIdx.x; t < TI * N; t += blockDim.x) {
+    const int col = t % TI, j = t / TI;
+    const int i = i0 + col;
+    double v = i < nx ? r[i + (size_t)nx * j] : 0.0;
+    buf[col * N + bitrev(j, logN)] = make_double2(v, 0.0);
+  }
+  __syncthreads();
+  fft_columns(buf, TI, N, logN, tw, false);
+  const int K = (N >> 1) + 1;
+  for (int t = threadIdx.x; t < TI * K; t += blockDim.x) {
+    const int col = t / K, k = t - col * K;
+    const int i = i0 + col;
+    if (i < nx) spec[(size_t)i * K + k] = buf[col * N + k];
+  }
+}
+
+// per Fourier mode: tridiagonal solve along x (in place in spec)
+__global__ void k_tridiag(double2 *__restrict__ spec, int nx, int K, const double *__restrict__ low,
+                          const double *__restrict__ up, const double *__restrict__ inv, const double *__restrict__ cp,
+                          const double *__restrict__ q, const double *__restrict__ gk, int cyclic, int pin0,
+                          const PoissonScal *__restrict__ sc) {
+  if (sc->done) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  // forward elimination
+  double2 y = make_double2(0, 0);
+  for (int i = 0; i < nx; i++) {
+    const size_t o = (size_t)i * K + k;
+    double2 rv = spec[o];
+    const double a = i > 0 ? low[i] : 0.0;
+    const double iv = inv[o];
+    y = make_double2((rv.x - a * y.x) * iv, (rv.y - a * y.y) * iv);
+    spec[o] = y;
+  }
+  // back substitution
+  double2 xn = y;
+  for (int i = nx - 2; i >= 0; i--) {
+    const size_t o = (size_t)i * K + k;
+    double2 yv = spec[o];
+    const double c = cp[o];
+    xn = make_double2(yv.x - c * xn.x, yv.y - c * xn.y);
+    spec[o] = xn;
+  }
+  if (cyclic && !(k == 0 && pin0 >= 0)) {
+    const double2 x0 = spec[k], xl = spec[(size_t)(nx - 1) * K + k];
+    const double g = gk[k], vfac = gk[K + k];
+    const double2 f = make_double2((x0.x + vfac * xl.x) * g, (x0.y + vfac * xl.y) * g);
+    for (int i = 0; i < nx; i++) {
+      const size_t o = (size_t)i * K + k;
+      const double qq = q[o];
+      double2 v = spec[o];
+      spec[o] = make_double2(v.x - f.x * qq, v.y - f.y * qq);
+    }
+  }
+}
+
+// spec -> z (nx,ny) via inverse real FFT; x += z on free rows
+__global__ void k_fft_inv_update(const double2 *__restrict__ spec, int nx, int N, int logN, int TI,
+                                 const double2 *__restrict__ tw, OpView op, double *__restrict__ x,
+                                 const PoissonScal *__restrict__ sc) {
+  extern __shared__ double2 buf[];
+  if (sc->done) return;
+  const int i0 = blockIdx.x * TI;
+  const int K = (N >> 1) + 1;
+  for (int t = threadIdx.x; t < TI * N; t += blockDim.x) {
+    const int col = t / N, k = t - col * N;
+    const int i = i0 + col;
+    double2 v = make_double2(0, 0);
+    if (i < nx) {
+      if (k < K) {
+        v = spec[(size_t)i * K + k];
+      } else {
+        v = spec[(size_t)i * K + (N - k)];
+        v.y = -v.y;
+      }
+    }
+    buf[col * N + bitrev(k, logN)] = v;
+  }
+  __syncthreads();
+  fft_columns(buf, TI, N, logN, tw, true);
+  const double invN = 1.0 / N;
+  for (int t = threadIdx.x; t < TI * N; t += blockDim.x) {
+    const int col = t % TI, j = t / TI;
+    const int i = i0 + col;
+    if (i < nx) {
+      const size_t kk = i + (size_t)nx * j;
+      const RowClass &C = op.classes[op.cls[kk]];
+      if (!C.fixed) x[kk] += buf[col * N + j].x * invN;
+    }
+  }
+}
+
+// mean-zero projection of x over nodes (singular case)
+__global__ void k_sum_x(const double *__restrict__ x, int nn, double *__restrict__ part) {
+  __shared__ double sh[40];
+  double v = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) v += x[k];
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+__global__ void k_shift_x(double *__restrict__ x, int nn, const double *__restrict__ part, int nparts) {
+  __shared__ double sh[40];
+  double s = sum_partials(part, nparts, sh);
+  const double m = s / nn;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) x[k] -= m;
+}
+
+// ---------------- Jacobi-preconditioned CG ----------------
+// S p on free rows (p = 0 on fixed rows)
+__device__ __forceinline__ double apply_S(const OpView &op, const RowClass &C, const double *__restrict__ v, int k) {
+  int w, e, s, n;
+  nbr(k, op.nx, op.ny, w, e, s, n);
+  double a = C.c0 * v[k] + C.cW * v[w] + C.cE * v[e] + C.cS * v[s] + C.cN * v[n];
+  return -C.d * a;
+}
+
+__global__ void k_cg_init(OpView op, const double *__restrict__ r, double *__restrict__ z, double *__restrict__ p,
+                          double *__restrict__ part, int nn) {
+  __shared__ double sh[40];
+  double v = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k]];
+    double zz = C.fixed ? 0.0 : r[k] / (-C.d * C.c0);
+    z[k] = zz;
+    p[k] = zz;
+    v += r[k] * zz;
+  }
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_cg_ap(OpView op, const double *__restrict__ p, double *__restrict__ ap, double *__restrict__ part,
+                        int nn, const PoissonScal *__restrict__ sc) {
+  __shared__ double sh[40];
+  if (sc->done) return;
+  double v = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k]];
+    double a = C.fixed ? 0.0 : apply_S(op, C, p, k);
+    ap[k] = a;
+    v += p[k] * a;
+  }
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[kPartials + blockIdx.x] = t;
+}
+
+// α = rz/pAp; x += αp; r -= αAp; z = r/diag; partial rz_new and ||res||²
+__global__ void k_cg_update(OpView op, double *__restrict__ x, double *__restrict__ r, double *__restrict__ z,
+                            const double *__restrict__ p, const double *__restrict__ ap, double *__restrict__ part,
+                            int nparts, int nn, const PoissonScal *__restrict__ sc) {
+  __shared__ double sh[40];
+  if (sc->done) return;
+  const double rz = sum_partials(part, nparts, sh);
+  const double pap = sum_partials(part + kPartials, nparts, sh);
+  const double alpha = pap != 0 ? rz / pap : 0.0;
+  double v = 0, w2 = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k]];
+    if (C.fixed) {
+      z[k] = 0.0;
+      continue;
+    }
+    x[k] += alpha * p[k];
+    double rr = r[k] - alpha * ap[k];
+    r[k] = rr;
+    double zz = rr / (-C.d * C.c0);
+    z[k] = zz;
+    v += rr * zz;
+    double res = rr / C.d;
+    w2 += res * res;
+  }
+  double t = block_sum(v, sh);
+  double t2 = block_sum(w2, sh);
+  if (threadIdx.x == 0) {
+    part[2 * kPartials + blockIdx.x] = t;
+    part[3 * kPartials + blockIdx.x] = t2;
+  }
+}
+
+// β = rz_new/rz; p = z + βp; convergence on the unscaled residual
+__global__ void k_cg_dir(OpView op, const double *__restrict__ z, double *__restrict__ p, double *__restrict__ part,
+                         int nparts, int nn, PoissonScal *sc, double rtol2) {
+  __shared__ double sh[40];
+  if (sc->done) return;
+  const double rz = sum_partials(part, nparts, sh);
+  const double rzn = sum_partials(part + 2 * kPartials, nparts, sh);
+  const double res2 = sum_partials(part + 3 * kPartials, nparts, sh);
+  const double beta = rz != 0 ? rzn / rz : 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) p[k] = z[k] + beta * p[k];
+  // next iteration's rz lives in part[0..nparts): copy rz_new there
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) part[k] = part[2 * kPartials + k];
+    if (threadIdx.x == 0) {
+      sc->res2 = res2;
+      sc->relres = sc->rhs2 > 0 ? sqrt(res2 / sc->rhs2) : sqrt(res2);
+      sc->iters += 1;
+      if ((sc->rhs2 > 0 && res2 <= rtol2 * sc->rhs2) || res2 == 0.0) sc->done = 1;
+    }
+  }
+}
+
+// ===========================================================================
+// host: assembly
+// ===========================================================================
+static inline int slot_col(const Poisson *P, int r, int s) {
+  const int nx = P->nx, ny = P->ny, i = r % nx, j = r / nx;
+  switch (s) {
+    case 0: return r;
+    case 1: return i > 0 ? r - 1 : -1;
+    case 2: return i < nx - 1 ? r + 1 : -1;
+    case 3: return j > 0 ? r - nx : -1;
+    case 4: return j < ny - 1 ? r + nx : -1;
+    case 5: return i == 0 ? (nx - 1) + nx * j : (i == nx - 1 ? nx * j : -1);
+    case 6: return j == 0 ? i + nx * (ny - 1) : (j == ny - 1 ? i : -1);
+  }
+  return -1;
+}
+
+static Poisson *poisson_new(Ctx *c, double eps0) {
+  Poisson *P = new Poisson();
+  P->nx = c->nx;
+  P->ny = c->ny;
+  P->nn = c->nn;
+  P->dx = c->g.dx;
+  P->dy = c->g.dy;
+  P->eps0 = eps0;
+  const int nx = P->nx, ny = P->ny;
+  P->C.assign((size_t)P->nn * 7, 0.0);
+  P->bfix.assign(P->nn, 0.0);
+  P->rho_dof.assign(P->nn, 1);
+  P->er.assign((size_t)(nx + 1) * (ny + 1), 1.0);
+  // create_generalized_poisson_solver (:42-61)
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      double *R = &P->C[(size_t)(i + nx * j) * 7];
+      if (i < nx - 1) { R[0] -= 1.0; R[2] += 1.0; }
+      if (i > 0) { R[0] -= 1.0; R[1] += 1.0; }
+      if (j < ny - 1) { R[0] -= 1.0; R[4] += 1.0; }
+      if (j > 0) { R[0] -= 1.0; R[3] += 1.0; }
+    }
+  const double h2 = P->dx * P->dx;  // A ./= grid.Δh[1]^2 (:65)
+  for (auto &v : P->C) v /= h2;
+  return P;
+}
+
+static double ER(const Poisson *P, int i1, int j1) {  // εr[i,j] with 1-based indices
+  return P->er[(size_t)(i1 - 1) + (size_t)(P->nx + 1) * (j1 - 1)];
+}
+
+static void assemble_periodic(Poisson *P, int axis) {
+  const int nx = P->nx, ny = P->ny;
+  if (axis == 1) {
+    const int js[2] = {1, ny};  // Julia iterates the tuple (1, ny)
+    for (int t = 0; t < 2; t++) {
+      const int j = js[t];
+      for (int i = 1; i <= nx; i++) {
+        double *R = &P->C[(size_t)((i - 1) + nx * (j - 1)) * 7];
+        if (j == ny) {
+          double cc = (0.5 * ER(P, i + 1, j + 1) + 0.5 * ER(P, i, j + 1)) / (P->dx * P->dx);
+          R[0] -= cc;
+          R[6] += cc;
+        }
+        if (j == 1) {
+          double cc = (0.5 * ER(P, i + 1, j) + 0.5 * ER(P, i, j)) / (P->dx * P->dx);
+          R[0] -= cc;
+          R[6] += cc;
+        }
+      }
+    }
+  } else {
+    for (int j = 1; j <= ny; j++) {
+      const int is[2] = {1, nx};
+      for (int t = 0; t < 2; t++) {
+        const int i = is[t];
+        double *R = &P->C[(size_t)((i - 1) + nx * (j - 1)) * 7];
+        if (i == nx) {
+          double cc = (0.5 * ER(P, i + 1, j + 1) + 0.5 * ER(P, i + 1, j)) / (P->dy * P->dy);
+          R[0] -= cc;
+          R[5] += cc;
+        }
+        if (i == 1) {
+          double cc = (0.5 * ER(P, i, j) + 0.5 * ER(P, i, j + 1)) / (P->dy * P->dy);
+          R[0] -= cc;
+          R[5] += cc;
+        }
+      }
+    }
+  }
+}
+
+static void assemble_dirichlet(Poisson *P, const uint8_t *nodes, double phi0) {
+  for (int r = 0; r < P->nn; r++) {
+    if (!nodes[r]) continue;
+    double *R = &P->C[(size_t)r * 7];
+    for (int s = 0; s < 7; s++) R[s] = 0.0;
+    for (auto &col : P->sig_cols) col[r] = 0.0;
+    R[0] = 1.0;
+    P->bfix[r] = phi0;
+    P->rho_dof[r] = 0;
+  }
+}
+
+static void assemble_neumann(Poisson *P, const uint8_t *nodes, int dof) {
+  const int nx = P->nx, ny = P->ny;
+  const double dx = P->dx, dy = P->dy;
+  auto N = [&](int i, int j) { return nodes[i + nx * j] != 0; };  // 0-based
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      if (!N(i, j)) continue;
+      const bool a = i > 0 ? N(i - 1, j) : false;
+      const bool b = i < nx - 1 ? N(i + 1, j) : false;
+      const bool cc = j > 0 ? N(i, j - 1) : true;
+      const bool d = j < ny - 1 ? N(i, j + 1) : true;
+      const int r = i + nx * j;
+      double *R = &P->C[(size_t)r * 7];
+      std::vector<double> &S = P->sig_cols[dof - 1];
+      if (cc == d && d == true && a == b && b == false) {
+        const int ip = i == 0 ? i + 1 : i - 1;
+        for (int s = 0; s < 7; s++) R[s] = 0.0;
+        for (auto &col : P->sig_cols) col[r] = 0.0;
+        R[0] -= 2 * ER(P, i + 1, j + 1) / dx;
+        R[ip == i + 1 ? 2 : 1] += 2 * ER(P, ip + 1, j + 1) / dx;
+        S[r] += 2;
+      }
+      if (cc != d) {
+        const int ip = i == 0 ? i + 1 : i - 1;
+        const int jp = cc ? j + 1 : j - 1;
+        for (int s = 0; s < 7; s++) R[s] = 0.0;
+        for (auto &col : P->sig_cols) col[r] = 0.0;
+        const double e = ER(P, i + 1, j + 1);
+        R[0] -= 4 * e / (3 * dx * dx);
+        R[0] -= 4 * e / (3 * dy * dy);
+        R[ip == i + 1 ? 2 : 1] += 4 * e / (3 * dx * dx);
+        R[jp == j + 1 ? 4 : 3] += 4 * e / (3 * dy * dy);
+        S[r] += (2.0 / 3.0) * (dx + dy) / (dx * dy);
+      }
+    }
+}
+
+// ===========================================================================
+// host: device representation, symmetrisation, separable factorisation
+// ===========================================================================
+struct RowEff {
+  double c0, cW, cE, cS, cN;
+  int sig_dof;
+  double sig_coef;
+  bool fixed, rho;
+};
+
+static RowEff effective_row(const Poisson *P, int r) {
+  const int nx = P->nx, ny = P->ny, i = r % nx, j = r / nx;
+  const double *R = &P->C[(size_t)r * 7];
+  RowEff e{};
+  e.c0 = R[0];
+  e.cW = R[1] + (i == 0 ? R[5] : 0.0);
+  e.cE = R[2] + (i == nx - 1 ? R[5] : 0.0);
+  e.cS = R[3] + (j == 0 ? R[6] : 0.0);
+  e.cN = R[4] + (j == ny - 1 ? R[6] : 0.0);
+  // nx == 1 / ny == 1 cannot occur (nx, ny >= 2)
+  e.sig_dof = -1;
+  e.sig_coef = 0;
+  int nsig_here = 0;
+  for (size_t k = 0; k < P->sig_cols.size(); k++)
+    if (P->sig_cols[k][r] != 0.0) {
+      e.sig_dof = (int)k;
+      e.sig_coef = P->sig_cols[k][r];
+      nsig_here++;
+    }
+  if (nsig_here > 1) e.sig_dof = -2;  // unsupported: flagged by the caller
+  e.fixed = e.c0 == 1.0 && e.cW == 0 && e.cE == 0 && e.cS == 0 && e.cN == 0 && e.sig_dof == -1;
+  e.rho = P->rho_dof[r] != 0;
+  return e;
+}
+
+static int fft_smem_attr(Ctx *c, int N);
+
+static int build_device(Ctx *c, Poisson *P) {
+  const int nx = P->nx, ny = P->ny, nn = P->nn;
+  std::vector<RowEff> rows(nn);
+  for (int r = 0; r < nn; r++) {
+    rows[r] = effective_row(P, r);
+    if (rows[r].sig_dof == -2) return set_err(c, ISKRA_EINVAL, "a row couples to more than one σ dof");
+  }
+  // neighbor indices (wrapped) for the effective coefficients
+  auto nb = [&](int r, int which) {
+    const int i = r % nx, j = r / nx;
+    switch (which) {
+      case 0: return i > 0 ? r - 1 : r + nx - 1;
+      case 1: return i < nx - 1 ? r + 1 : r - nx + 1;
+      case 2: return j > 0 ? r - nx : r + nx * (ny - 1);
+      default: return j < ny - 1 ? r + nx : r - nx * (ny - 1);
+    }
+  };
+  auto coef_to = [&](int r, int col) {  // A[r, col] for a neighbor column
+    const RowEff &e = rows[r];
+    double a = 0;
+    if (nb(r, 0) == col) a += e.cW;
+    if (nb(r, 1) == col) a += e.cE;
+    if (nb(r, 2) == col) a += e.cS;
+    if (nb(r, 3) == col) a += e.cN;
+    return a;
+  };
+  // symmetrising scale by breadth-first propagation over free rows
+  std::vector<double> d(nn, 0.0);
+  std::vector<int> queue;
+  queue.reserve(nn);
+  bool any_fixed = false;
+  for (int r = 0; r < nn; r++) any_fixed |= rows[r].fixed;
+  for (int r0 = 0; r0 < nn; r0++) {
+    if (rows[r0].fixed || d[r0] != 0.0) continue;
+    d[r0] = 1.0;
+    queue.clear();
+    queue.push_back(r0);
+    for (size_t h = 0; h < queue.size(); h++) {
+      const int r = queue[h];
+      for (int w = 0; w < 4; w++) {
+        const int cidx = nb(r, w);
+        if (cidx == r || rows[cidx].fixed) continue;
+        const double arc = coef_to(r, cidx), acr = coef_to(cidx, r);
+        if (arc == 0.0 && acr == 0.0) continue;
+        if (arc == 0.0 || acr == 0.0)
+          return set_err(c, ISKRA_EINVAL, "boundary setup gives a non-symmetrizable operator");
+        const double want = d[r] * arc / acr;
+        if (d[cidx] == 0.0) {
+          d[cidx] = want;
+          queue.push_back(cidx);
+        } else if (std::fabs(d[cidx] - want) > 1e-9 * std::fabs(want)) {
+          return set_err(c, ISKRA_EINVAL, "boundary setup gives a non-symmetrizable operator");
+        }
+      }
+    }
+  }
+  for (int r = 0; r < nn; r++)
+    if (!rows[r].fixed && (!(d[r] > 0) || !(-d[r] * rows[r].c0 > 0)))
+      return set_err(c, ISKRA_EINVAL, "assembled operator is not definite on its free rows");
+  // singular: no fixed row and every free row sums to zero
+  bool singular = !any_fixed;
+  if (singular) {
+    double mx = 0;
+    for (int r = 0; r < nn; r++) mx = std::max(mx, std::fabs(rows[r].c0));
+    for (int r = 0; r < nn && singular; r++) {
+      const RowEff &e = rows[r];
+      if (std::fabs(e.c0 + e.cW + e.cE + e.cS + e.cN) > 1e-12 * mx) singular = false;
+    }
+  }
+  P->singular = singular;
+  P->dsum = 0;
+  for (int r = 0; r < nn; r++)
+    if (!rows[r].fixed) P->dsum += d[r];
+  // classes
+  std::map<std::vector<double>, int> cmap;
+  std::vector<RowClass> classes;
+  std::vector<uint16_t> cls(nn);
+  for (int r = 0; r < nn; r++) {
+    const RowEff &e = rows[r];
+    std::vector<double> key = {e.c0, e.cW, e.cE, e.cS, e.cN, e.fixed ? 1.0 : 0.0, e.rho ? 1.0 : 0.0,
+                               (double)e.sig_dof, e.sig_coef, e.fixed ? 0.0 : d[r]};
+    auto it = cmap.find(key);
+    int id;
+    if (it == cmap.end()) {
+      id = (int)classes.size();
+      if (id >= 65535) return set_err(c, ISKRA_EINVAL, "too many distinct operator rows");
+      cmap[key] = id;
+      RowClass rc{};
+      rc.c0 = e.c0;
+      rc.cW = e.cW;
+      rc.cE = e.cE;
+      rc.cS = e.cS;
+      rc.cN = e.cN;
+      rc.d = e.fixed ? 1.0 : d[r];
+      rc.sig_coef = e.sig_coef;
+      rc.sig_dof = e.sig_dof;
+      rc.fixed = e.fixed;
+      rc.rho = e.rho;
+      classes.push_back(rc);
+    } else {
+      id = it->second;
+    }
+    cls[r] = (uint16_t)id;
+  }
+  P->nclass = (int)classes.size();
+  // ---- separability: per column i, every j gives the same scaled row ----
+  bool sep = P->method == 0 && ny >= 2 && (ny & (ny - 1)) == 0 && ny <= 4096;
+  std::vector<double> s0(nx), sW(nx), sE(nx), ey(nx);
+  std::vector<int> colfixed(nx);
+  for (int i = 0; i < nx && sep; i++) {
+    const RowEff &e0 = rows[i];
+    colfixed[i] = e0.fixed;
+    for (int j = 1; j < ny && sep; j++) {
+      const RowEff &e = rows[i + nx * j];
+      if (e.fixed != e0.fixed) sep = false;
+      if (!e.fixed && (e.c0 != e0.c0 || e.cW != e0.cW || e.cE != e0.cE || e.cS != e0.cS || e.cN != e0.cN ||
+                       d[i + nx * j] != d[i]))
+        sep = false;
+    }
+    if (!sep) break;
+    if (!e0.fixed) {
+      if (e0.cS != e0.cN) sep = false;
+      s0[i] = -d[i] * e0.c0;
+      sW[i] = -d[i] * e0.cW;
+      sE[i] = -d[i] * e0.cE;
+      ey[i] = -d[i] * e0.cS;
+    }
+  }
+  P->separable = sep;
+  // ---- device upload ----
+  cudaStream_t st = c->stream;
+  ISKRA_CUDA(c, cudaStreamSynchronize(st));
+  cudaFree(P->cls);
+  cudaFree(P->classes);
+  P->cls = nullptr;
+  P->classes = nullptr;
+  ISKRA_CUDA(c, cudaMalloc(&P->cls, nn * sizeof(uint16_t)));
+  ISKRA_CUDA(c, cudaMalloc(&P->classes, classes.size() * sizeof(RowClass)));
+  ISKRA_CUDA(c, cudaMemcpy(P->cls, cls.data(), nn * sizeof(uint16_t), cudaMemcpyHostToDevice));
+  ISKRA_CUDA(c, cudaMemcpy(P->classes, classes.data(), classes.size() * sizeof(RowClass), cudaMemcpyHostToDevice));
+  if (!P->bfix_d) ISKRA_CUDA(c, cudaMalloc(&P->bfix_d, nn * sizeof(double)));
+  ISKRA_CUDA(c, cudaMemcpy(P->bfix_d, P->bfix.data(), nn * sizeof(double), cudaMemcpyHostToDevice));
+  const int nsig = (int)P->sig_b.size();
+  if (P->sigma_d && P->nsig > 0) {
+    // the device σ values are authoritative (the circuit kernel updates them)
+    ISKRA_CUDA(c, cudaMemcpy(P->sig_b.data(), P->sigma_d, std::min(nsig, P->nsig) * sizeof(double),
+                             cudaMemcpyDeviceToHost));
+  }
+  if (nsig != P->nsig) {
+    cudaFree(P->sigma_d);
+    P->sigma_d = nullptr;
+    P->nsig = nsig;
+  }
+  if (!P->sigma_d) ISKRA_CUDA(c, cudaMalloc(&P->sigma_d, (nsig > 0 ? nsig : 1) * sizeof(double)));
+  if (nsig) ISKRA_CUDA(c, cudaMemcpy(P->sigma_d, P->sig_b.data(), nsig * sizeof(double), cudaMemcpyHostToDevice));
+  if (!P->x) {
+    ISKRA_CUDA(c, cudaMalloc(&P->x, nn * sizeof(double)));
+    ISKRA_CUDA(c, cudaMemset(P->x, 0, nn * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->r, nn * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->z, nn * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->p, nn * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->ap, nn * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->part, 4 * kPartials * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->scal, sizeof(PoissonScal)));
+    ISKRA_CUDA(c, cudaMallocHost(&P->scal_h, sizeof(PoissonScal)));
+    ISKRA_CUDA(c, cudaMemset(P->scal, 0, sizeof(PoissonScal)));
+  }
+  // drives
+  cudaFree(P->drive_node);
+  cudaFree(P->drive_group);
+  cudaFree(P->drive_par);
+  P->drive_node = nullptr;
+  P->drive_group = nullptr;
+  P->drive_par = nullptr;
+  {
+    std::vector<int> dn, dg;
+    std::vector<double> dp;
+    for (size_t g = 0; g < P->drives.size(); g++) {
+      for (int n : P->drives[g].nodes) {
+        dn.push_back(n);
+        dg.push_back((int)g);
+      }
+      dp.insert(dp.end(), {P->drives[g].amp, P->drives[g].freq, P->drives[g].phase, P->drives[g].dc});
+    }
+    P->ndrive_nodes = (int)dn.size();
+    P->ndrive = (int)P->drives.size();
+    if (!dn.empty()) {
+      ISKRA_CUDA(c, cudaMalloc(&P->drive_node, dn.size() * sizeof(int)));
+      ISKRA_CUDA(c, cudaMalloc(&P->drive_group, dg.size() * sizeof(int)));
+      ISKRA_CUDA(c, cudaMalloc(&P->drive_par, dp.size() * sizeof(double)));
+      ISKRA_CUDA(c, cudaMemcpy(P->drive_node, dn.data(), dn.size() * sizeof(int), cudaMemcpyHostToDevice));
+      ISKRA_CUDA(c, cudaMemcpy(P->drive_group, dg.data(), dg.size() * sizeof(int), cudaMemcpyHostToDevice));
+      ISKRA_CUDA(c, cudaMemcpy(P->drive_par, dp.data(), dp.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+  }
+  P->blocks = std::min(kPartials, std::max(1, std::min(c->num_sms * 2, (nn + 255) / 256)));
+  // ---- separable factorisation ----
+  cudaFree(P->spec);
+  cudaFree(P->tw);
+  cudaFree(P->low);
+  cudaFree(P->up);
+  cudaFree(P->inv);
+  cudaFree(P->cp);
+  cudaFree(P->q);
+  cudaFree(P->gk);
+  P->spec = nullptr;
+  P->tw = nullptr;
+  P->low = P->up = P->inv = P->cp = P->q = P->gk = nullptr;
+  if (sep) {
+    const int N = ny, K = N / 2 + 1;
+    int logN = 0;
+    while ((1 << logN) < N) logN++;
+    P->N = N;
+    P->K = K;
+    P->logN = logN;
+    // tridiagonal couplings per column (k-independent); fixed columns decouple
+    std::vector<double> lo(nx, 0.0), upv(nx, 0.0);
+    double corner_lo = 0.0, corner_up = 0.0;  // T[0][nx-1], T[nx-1][0]
+    for (int i = 0; i < nx; i++) {
+      if (colfixed[i]) continue;
+      const int iw = i > 0 ? i - 1 : nx - 1, ie = i < nx - 1 ? i + 1 : 0;
+      double w = colfixed[iw] ? 0.0 : sW[i];
+      double e = colfixed[ie] ? 0.0 : sE[i];
+      if (i == 0) {
+        if (iw == ie) { e += w; w = 0; }  // nx == 2: wrap partner is the east neighbour
+        corner_lo = w;
+      } else {
+        lo[i] = w;
+      }
+      if (i == nx - 1) {
+        if (iw == ie) { lo[i] += e; e = 0; }
+        corner_up = e;
+      } else {
+        upv[i] = e;
+      }
+    }
+    const bool cyclic = corner_lo != 0.0 || corner_up != 0.0;
+    P->cyclic = cyclic;
+    const int pin = singular ? 0 : -1;  // singular => no fixed column, pin column 0 of mode 0
+    P->pin_k0 = pin;
+    std::vector<double> inv((size_t)nx * K), cpv((size_t)nx * K), qv(cyclic ? (size_t)nx * K : 1), gkv(2 * K, 0.0);
+    for (int k = 0; k < K; k++) {
+      double vfac = 0;
+      const double ck = std::cos(2.0 * M_PI * k / N);
+      std::vector<double> diag(nx), lk(lo), uk(upv);
+      for (int i = 0; i < nx; i++) diag[i] = colfixed[i] ? 1.0 : s0[i] + 2.0 * ey[i] * ck;
+      const bool pinned = (k == 0 && pin >= 0);
+      const bool cyc = cyclic && !pinned;
+      double gamma = 0;
+      if (cyc) {
+        gamma = -diag[0];
+        vfac = corner_lo / gamma;  // v = [1, 0, ..., 0, β/γ], β = T[0][nx-1]
+        gkv[K + k] = vfac;
+        diag[0] -= gamma;
+        diag[nx - 1] -= corner_up * corner_lo / gamma;
+      }
+      // Thomas factors
+      double cprev = 0;
+      for (int i = 0; i < nx; i++) {
+        const size_t o = (size_t)i * K + k;
+        if (pinned && i == pin) {
+          inv[o] = 0.0;  // y_pin = 0
+          cpv[o] = 0.0;
+          cprev = 0.0;
+          continue;
+        }
+        const double a = i > 0 ? lk[i] : 0.0;
+        const double den = diag[i] - a * cprev;
+        if (den == 0.0) return set_err(c, ISKRA_EINVAL, "singular tridiagonal mode in the Poisson factorisation");
+        inv[o] = 1.0 / den;
+        cprev = (i < nx - 1 ? uk[i] : 0.0) / den;
+        cpv[o] = cprev;
+      }
+      if (cyc) {
+        // q = T'^{-1} u, u = [γ, 0, ..., 0, α], α = T[nx-1][0]
+        std::vector<double> y(nx), u(nx, 0.0);
+        u[0] = gamma;
+        u[nx - 1] += corner_up;
+        for (int i = 0; i < nx; i++) {
+          const size_t o = (size_t)i * K + k;
+          const double a = i > 0 ? lk[i] : 0.0;
+          y[i] = (u[i] - a * (i > 0 ? y[i - 1] : 0.0)) * inv[o];
+        }
+        for (int i = nx - 2; i >= 0; i--) y[i] -= cpv[(size_t)i * K + k] * y[i + 1];
+        for (int i = 0; i < nx; i++) qv[(size_t)i * K + k] = y[i];
+        gkv[k] = 1.0 / (1.0 + y[0] + vfac * y[nx - 1]);
+      }
+    }
+    std::vector<double2> tw(N / 2 > 0 ? N / 2 : 1);
+    for (int m = 0; m < N / 2; m++) {
+      const double ang = -2.0 * M_PI * m / N;
+      tw[m] = make_double2(std::cos(ang), std::sin(ang));
+    }
+    ISKRA_CUDA(c, cudaMalloc(&P->spec, (size_t)nx * K * sizeof(double2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->tw, tw.size() * sizeof(double2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->low, nx * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->up, nx * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->inv, (size_t)nx * K * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cp, (size_t)nx * K * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->gk, 2 * K * sizeof(double)));
+    ISKRA_CUDA(c, cudaMemcpy(P->tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->low, lo.data(), nx * sizeof(double), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->up, upv.data(), nx * sizeof(double), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->inv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->cp, cpv.data(), cpv.size() * sizeof(double), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->gk, gkv.data(), 2 * K * sizeof(double), cudaMemcpyHostToDevice));
+    if (cyclic) {
+      ISKRA_CUDA(c, cudaMalloc(&P->q, qv.size() * sizeof(double)));
+      ISKRA_CUDA(c, cudaMemcpy(P->q, qv.data(), qv.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+  }
+  if (sep) {
+    int rc = fft_smem_attr(c, P->N);
+    if (rc) return rc;
+  }
+  P->dirty = false;
+  return ISKRA_OK;
+}
+
+int poisson_prepare(Ctx *c) {
+  Poisson *P = c->ps;
+  if (!P) return set_err(c, ISKRA_EINVAL, "no Poisson solver: call iskra_poisson_create");
+  if (!P->dirty) return ISKRA_OK;
+  invalidate_graphs(c);
+  return build_device(c, P);
+}
+
+static OpView opview(Poisson *P) {
+  OpView o;
+  o.cls = P->cls;
+  o.classes = P->classes;
+  o.bfix = P->bfix_d;
+  o.sigma = P->sigma_d;
+  o.nx = P->nx;
+  o.ny = P->ny;
+  return o;
+}
+
+// columns per FFT block: up to 64 KB of double2 per block (two blocks per SM)
+static int fft_ti(int N) {
+  int ti = 4096 / N;
+  if (ti < 1) ti = 1;
+  if (ti > 16) ti = 16;
+  return ti;
+}
+
+static int fft_smem_attr(Ctx *c, int N) {
+  const int smem = fft_ti(N) * N * (int)sizeof(double2);
+  if (smem > 48 * 1024) {
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  }
+  return ISKRA_OK;
+}
+
+// One solve queued on the stream (no host synchronisation).  Separable
+// operators: up to max_sweeps FFT/tridiagonal corrections, each skipped on the
+// device once the residual meets rtol.  Other operators: max_sweeps CG
+// iterations (the caller loops for more).
+static int solve_queue(Ctx *c, double rtol, int max_sweeps, double dt_for_drive, bool reset) {
+  Poisson *P = c->ps;
+  const int nn = P->nn, B = P->blocks, T = 256;
+  OpView op = opview(P);
+  const double nie = -1.0 / P->eps0;
+  const double rtol2 = rtol * rtol;
+  cudaStream_t st = c->stream;
+  if (reset) {
+    ISKRA_CUDA(c, cudaMemsetAsync(P->scal, 0, sizeof(PoissonScal), st));
+    if (P->ndrive_nodes)
+      k_set_fixed<<<(P->ndrive_nodes + 255) / 256, 256, 0, st>>>(op, P->drive_node, P->drive_group, P->drive_par,
+                                                               P->ndrive_nodes, c->d_step, dt_for_drive,
+                                                               P->bfix_d, P->x, c->rho, P->eps0, nn);
+    k_fixed_to_x<<<B, T, 0, st>>>(op, P->x, c->rho, nie, nn);
+    if (P->singular) {
+      k_sum_db<<<B, T, 0, st>>>(op, c->rho, nie, nn, P->part);
+      k_lambda<<<1, T, 0, st>>>(P->part, B, P->dsum, P->scal);
+    }
+    k_residual<<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, P->part, kPartials, nn, P->singular, 0);
+    k_check<<<1, T, 0, st>>>(P->part, B, kPartials, P->scal, rtol2, 0);
+  }
+  if (P->separable) {
+    const int N = P->N, K = P->K, TI = fft_ti(N);
+    const int fb = (P->nx + TI - 1) / TI;
+    const size_t smem = (size_t)TI * N * sizeof(double2);
+    for (int s = 0; s < max_sweeps; s++) {
+      k_fft_fwd<<<fb, 256, smem, st>>>(P->r, P->nx, N, P->logN, TI, P->tw, P->spec, P->scal);
+      k_tridiag<<<(K + 63) / 64, 64, 0, st>>>(P->spec, P->nx, K, P->low, P->up, P->inv, P->cp, P->q, P->gk,
+                                              P->cyclic, P->pin_k0, P->scal);
+      k_fft_inv_update<<<fb, 256, smem, st>>>(P->spec, P->nx, N, P->logN, TI, P->tw, op, P->x, P->scal);
+      k_residual<<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, P->part, kPartials, nn, P->singular, 1);
+      k_check<<<1, T, 0, st>>>(P->part, B, kPartials, P->scal, rtol2, 1);
+    }
+  } else {
+    if (reset) {
+      k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);
+      // rhs2 from the residual check is already in scal
+    }
+    for (int s = 0; s < max_sweeps; s++) {
+      k_cg_ap<<<B, T, 0, st>>>(op, P->p, P->ap, P->part, nn, P->scal);
+      k_cg_update<<<B, T, 0, st>>>(op, P->x, P->r, P->z, P->p, P->ap, P->part, B, nn, P->scal);
+      k_cg_dir<<<B, T, 0, st>>>(op, P->z, P->p, P->part, B, nn, P->scal, rtol2);
+    }
+  }
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
+static int finish_solve(Ctx *c) {
+  Poisson *P = c->ps;
+  if (P->singular) {
+    k_sum_x<<<P->blocks, 256, 0, c->stream>>>(P->x, P->nn, P->part);
+    k_shift_x<<<P->blocks, 256, 0, c->stream>>>(P->x, P->nn, P->part, P->blocks);
+  }
+  return launch_efield_from(c, P->x);
+}
+
+// Graph-capturable solve (separable operators): fixed number of sweeps.
+int poisson_solve_async(Ctx *c, double rtol, int max_sweeps) {
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  Poisson *P = c->ps;
+  if (!P->separable) return set_err(c, ISKRA_EINVAL, "asynchronous solve needs a separable operator");
+  rc = solve_queue(c, rtol, max_sweeps, c->graph_dt, true);
+  if (rc) return rc;
+  return finish_solve(c);
+}
+
+static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres) {
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  Poisson *P = c->ps;
+  const int chunk = P->separable ? 2 : 32;
+  bool first = true;
+  int done_it = 0;
+  for (;;) {
+    rc = solve_queue(c, rtol, chunk, c->graph_dt, first);
+    if (rc) return rc;
+    first = false;
+    ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost, c->stream));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+    done_it = P->scal_h->iters;
+    if (P->scal_h->done || done_it >= maxit) break;
+  }
+  rc = finish_solve(c);
+  if (rc) return rc;
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  P->last_iters = P->scal_h->iters;
+  P->last_relres = P->scal_h->relres;
+  if (iters) *iters = P->scal_h->iters;
+  if (relres) *relres = P->scal_h->relres;
+  if (!P->scal_h->done) return set_err(c, ISKRA_ENOTCONV, "Poisson solve did not reach the tolerance");
+  return collect_device_errors(c);
+}
+
+double *poisson_sigma_ptr(Ctx *c) { return c->ps ? c->ps->sigma_d : nullptr; }
+const double *poisson_x_ptr(Ctx *c) { return c->ps ? c->ps->x : nullptr; }
+bool poisson_separable(Ctx *c) { return c->ps && c->ps->separable; }
+int poisson_solve_blocking(Ctx *c, double rtol, int maxit) { return solve_sync(c, rtol, maxit, nullptr, nullptr); }
+
+}  // namespace iskra
+
+using namespace iskra;
+
+extern "C" {
+
+int iskra_poisson_create(iskra_ctx *h, double eps0) {
+  if (!h || !(eps0 > 0)) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (c->ps) poisson_destroy(c->ps);
+  c->ps = poisson_new(c, eps0);
+  return ISKRA_OK;
+}
+
+int iskra_poisson_apply_dirichlet(iskra_ctx *h, const uint8_t *nodes, double phi0) {
+  if (!h || !nodes) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  Poisson *P = c->ps;
+  // value-only update of rows that are already identity rows: no rebuild
+  bool structural = false;
+  for (int r = 0; r < P->nn && !structural; r++) {
+    if (!nodes[r]) continue;
+    const double *R = &P->C[(size_t)r * 7];
+    bool ident = R[0] == 1.0;
+    for (int s = 1; s < 7; s++) ident &= R[s] == 0.0;
+    for (auto &col : P->sig_cols) ident &= col[r] == 0.0;
+    if (!ident || P->rho_dof[r]) structural = true;
+  }
+  assemble_dirichlet(P, nodes, phi0);
+  if (structural || P->dirty) {
+    P->dirty = true;
+    return ISKRA_OK;
+  }
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  ISKRA_CUDA(c, cudaMemcpy(P->bfix_d, P->bfix.data(), P->nn * sizeof(double), cudaMemcpyHostToDevice));
+  return ISKRA_OK;
+}
+
+int iskra_poisson_apply_periodic(iskra_ctx *h, int axis) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  if (axis != 1 && axis != 2) return set_err(c, ISKRA_EINVAL, "axis must be 1 or 2");
+  assemble_periodic(c->ps, axis);
+  c->ps->dirty = true;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_add_dof(iskra_ctx *h, int *dof) {
+  if (!h || !dof) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  c->ps->sig_cols.emplace_back(c->ps->nn, 0.0);
+  c->ps->sig_b.push_back(0.0);
+  *dof = (int)c->ps->sig_b.size();
+  c->ps->dirty = true;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_apply_neumann(iskra_ctx *h, const uint8_t *nodes, int dof) {
+  if (!h || !nodes) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  if (dof < 1 || dof > (int)c->ps->sig_b.size()) return set_err(c, ISKRA_EINVAL, "bad σ dof");
+  assemble_neumann(c->ps, nodes, dof);
+  c->ps->dirty = true;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_set_sigma(iskra_ctx *h, int dof, double value) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps || dof < 1 || dof > (int)c->ps->sig_b.size()) return set_err(c, ISKRA_EINVAL, "bad σ dof");
+  c->ps->sig_b[dof - 1] = value;
+  if (c->ps->sigma_d && dof <= c->ps->nsig) {
+    ISKRA_CUDA(c, cudaMemcpyAsync(c->ps->sigma_d + (dof - 1), &c->ps->sig_b[dof - 1], sizeof(double),
+                                  cudaMemcpyHostToDevice, c->stream));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return ISKRA_OK;
+}
+
+int iskra_poisson_get_sigma(iskra_ctx *h, int dof, double *value) {
+  if (!h || !value) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps || dof < 1 || dof > (int)c->ps->sig_b.size()) return set_err(c, ISKRA_EINVAL, "bad σ dof");
+  if (c->ps->sigma_d && dof <= c->ps->nsig) {
+    ISKRA_CUDA(c, cudaMemcpyAsync(&c->ps->sig_b[dof - 1], c->ps->sigma_d + (dof - 1), sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  *value = c->ps->sig_b[dof - 1];
+  return ISKRA_OK;
+}
+
+int iskra_poisson_drive_dirichlet(iskra_ctx *h, const uint8_t *nodes, double amp, double freq, double phase,
+                                  double dc) {
+  if (!h || !nodes) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  DriveGroup g;
+  for (int r = 0; r < c->ps->nn; r++) {
+    if (!nodes[r]) continue;
+    const double *R = &c->ps->C[(size_t)r * 7];
+    bool ident = R[0] == 1.0 && !c->ps->rho_dof[r];
+    for (int s = 1; s < 7; s++) ident &= R[s] == 0.0;
+    if (!ident) return set_err(c, ISKRA_EINVAL, "driven nodes must be Dirichlet rows (apply_dirichlet first)");
+    g.nodes.push_back(r);
+  }
+  g.amp = amp;
+  g.freq = freq;
+  g.phase = phase;
+  g.dc = dc;
+  c->ps->drives.push_back(g);
+  c->ps->dirty = true;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_set_method(iskra_ctx *h, int method, int *active) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  if (method != 0 && method != 1) return set_err(c, ISKRA_EINVAL, "method must be 0 or 1");
+  if (c->ps->method != method) {
+    c->ps->method = method;
+    c->ps->dirty = true;
+  }
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  if (active) *active = c->ps->separable ? 0 : 1;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_solve(iskra_ctx *h, double rtol, int maxit, int *iters, double *relres) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!(rtol > 0) || maxit < 1) return set_err(c, ISKRA_EINVAL, "bad tolerance / iteration limit");
+  int rc = launch_charge_density(c);
+  if (rc) return rc;
+  return solve_sync(c, rtol, maxit, iters, relres);
+}
+
+int iskra_poisson_solve_host(iskra_ctx *h, const double *f, double rtol, int maxit, double *phi_out, int *iters,
+                             double *relres) {
+  if (!h || !f) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!(rtol > 0) || maxit < 1) return set_err(c, ISKRA_EINVAL, "bad tolerance / iteration limit");
+  // the device ρ holds -f: b[ρ] = f/ε0 = -ρ/ε0
+  std::vector<double> negf(c->nn);
+  for (int k = 0; k < c->nn; k++) negf[k] = -f[k];
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  ISKRA_CUDA(c, cudaMemcpy(c->rho, negf.data(), c->nn * sizeof(double), cudaMemcpyHostToDevice));
+  int rc = solve_sync(c, rtol, maxit, iters, relres);
+  if (rc && rc != ISKRA_ENOTCONV) return rc;
+  if (phi_out) {
+    ISKRA_CUDA(c, cudaMemcpyAsync(phi_out, c->ps->x, c->nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return rc;
+}
+
+int iskra_solve_info(iskra_ctx *h, int *iters, double *relres) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps || !c->ps->scal) return set_err(c, ISKRA_EINVAL, "no solve yet");
+  ISKRA_CUDA(c, cudaMemcpyAsync(c->ps->scal_h, c->ps->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (iters) *iters = c->ps->scal_h->iters;
+  if (relres) *relres = c->ps->scal_h->relres;
+  return ISKRA_OK;
+}
+
+int iskra_field_download(iskra_ctx *h, int which, double *out) {
+  if (!h || !out) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  const double *src = nullptr;
+  size_t n = (size_t)c->nn;
+  if (which == ISKRA_FIELD_RHO) {
+    src = c->rho;
+  } else if (which == ISKRA_FIELD_PHI) {
+    if (!c->ps || !c->ps->x) return set_err(c, ISKRA_EINVAL, "no potential yet");
+    src = c->ps->x;
+  } else if (which == ISKRA_FIELD_E) {
+    src = c->E64;
+    n *= 3;
+  } else {
+    return set_err(c, ISKRA_EINVAL, "bad field selector");
+  }
+  ISKRA_CUDA(c, cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  return collect_device_errors(c);
+}
+
+}  // extern "C"

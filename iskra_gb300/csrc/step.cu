@@ -1,0 +1,305 @@
+// step.cu -- the RLC circuit (Circuit/src/Circuit.jl, circuit_coupling.jl) and
+// the whole PIC step (the loop body of ParticleInCell.solve,
+// ParticleInCell/src/ParticleInCell.jl:102-135) replayed as a CUDA graph.
+#include <cmath>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace iskra {
+
+double *poisson_sigma_ptr(Ctx *c);
+const double *poisson_x_ptr(Ctx *c);
+bool poisson_separable(Ctx *c);
+int poisson_solve_blocking(Ctx *c, double rtol, int maxit);
+
+struct CircuitArgs {
+  CircuitDev *cd;
+  const double *phi;
+  double *sigma;
+  int pos_ref, neg_ref;
+  int wall;                    // discard wall feeding the floating electrode, -1 none
+  int ns;
+  SpeciesState *st[kMaxSpecies];
+  double qw[kMaxSpecies];      // q * w0 per species
+};
+
+// advance!(circuit, ϕ, Δt, config) (circuit_coupling.jl:35-43) with
+// advance_circuit! (Circuit.jl:117-136); V_ext = ϕ(positive) - ϕ(negative)
+// of the PlasmaDevice (circuit_coupling.jl:18-29); wall-absorbed charge enters
+// σ as hit! does (circuit_coupling.jl:45-55).  One thread, FP64.
+__global__ void k_circuit(CircuitArgs A, double dt, unsigned long long *seen) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  CircuitDev &c = *A.cd;
+  const double vext = A.phi[A.pos_ref] - A.phi[A.neg_ref];
+  const double i = c.i, q = c.q, t = c.t;
+  const double vsrc = c.amp * sin(2.0 * M_PI * c.freq * t) + c.dc;
+  double in = (c.L / dt - c.R / 2) * i + vext - vsrc;
+  if (c.C > 0.0) {
+    in -= q / c.C;
+    in /= (c.L / dt + c.R / 2);
+    c.q = q + dt * i;
+  } else {
+    in /= (c.L / dt + c.R / 2);
+  }
+  c.i = in;
+  c.t = t + dt;
+  c.vext = vext;
+  double ds = -dt * in / c.area * c.scale;
+  if (A.wall >= 0) {
+    for (int s = 0; s < A.ns; s++) {
+      const unsigned long long now = A.st[s]->absorbed[A.wall];
+      const unsigned long long d = now - seen[s];
+      seen[s] = now;
+      ds += A.qw[s] * (double)d / c.area;
+    }
+  }
+  A.sigma[c.sigma_dof] += ds;
+}
+
+__global__ void k_step_begin(unsigned long long *d_step) { *d_step += 1ull; }
+
+int launch_circuit(Ctx *c, double dt) {
+  if (!c->cir_d) return set_err(c, ISKRA_EINVAL, "no circuit");
+  CircuitArgs A{};
+  A.cd = c->cir_d;
+  A.phi = poisson_x_ptr(c);
+  A.sigma = poisson_sigma_ptr(c);
+  A.pos_ref = c->cir_pos_ref;
+  A.neg_ref = c->cir_neg_ref;
+  A.wall = c->cir_wall;
+  A.ns = (int)c->species.size();
+  for (int s = 0; s < A.ns; s++) {
+    A.st[s] = c->species[s].dev.st;
+    A.qw[s] = c->species[s].q * c->species[s].w0;
+  }
+  k_circuit<<<1, 32, 0, c->stream>>>(A, dt, c->cir_seen);
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
+// queue one PIC step (async; separable Poisson)
+static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocking_solve) {
+  k_step_begin<<<1, 1, 0, c->stream>>>(c->d_step);
+  ISKRA_CUDA(c, cudaGetLastError());
+  int rc;
+  for (int m = 0; m < (int)c->mccs.size(); m++) {
+    rc = launch_mcc(c, m, dt, seed, c->d_step, 0);
+    if (rc) return rc;
+  }
+  for (int s = 0; s < (int)c->species.size(); s++) {
+    rc = launch_advance(c, s, (float)dt);
+    if (rc) return rc;
+  }
+  if (c->cir_d) {
+    rc = launch_circuit(c, dt);
+    if (rc) return rc;
+  }
+  rc = launch_charge_density(c);
+  if (rc) return rc;
+  if (blocking_solve) return poisson_solve_blocking(c, rtol, 10000);
+  return poisson_solve_async(c, rtol, 2);
+}
+
+static int queue_sorts(Ctx *c) {
+  for (int s = 0; s < (int)c->species.size(); s++) {
+    int rc = launch_sort(c, s);
+    if (rc) return rc;
+  }
+  return ISKRA_OK;
+}
+
+// Captures the work queued by fn() on the context stream into an executable
+// graph and counts its kernel nodes.
+template <class F>
+static int capture(Ctx *c, cudaGraphExec_t *out, unsigned long long *kernels, F fn) {
+  cudaGraph_t g;
+  ISKRA_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int crc = fn();
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (crc) {
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    return crc;
+  }
+  ISKRA_CUDA(c, e);
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+  unsigned long long k = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+  }
+  cudaError_t ei = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  ISKRA_CUDA(c, ei);
+  *kernels = k;
+  return ISKRA_OK;
+}
+
+}  // namespace iskra
+
+using namespace iskra;
+
+extern "C" {
+
+int iskra_circuit_create(iskra_ctx *h, double R, double L, double C, double amp, double freq, double dc,
+                         int sigma_dof, const uint8_t *pos_nodes, const uint8_t *neg_nodes, double area,
+                         double sigma_scale) {
+  if (!h || !pos_nodes || !neg_nodes) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "create the Poisson solver first");
+  double sv = 0;
+  if (iskra_poisson_get_sigma(h, sigma_dof, &sv)) return set_err(c, ISKRA_EINVAL, "bad σ dof");
+  if (!(area > 0) || !(L / 1.0 >= 0) || !(R >= 0)) return set_err(c, ISKRA_EINVAL, "bad circuit values");
+  int pos_ref = -1, neg_ref = -1, wall = -1;
+  for (int r = 0; r < c->nn && pos_ref < 0; r++)
+    if (pos_nodes[r]) pos_ref = r;  // find_reference_node (configuration.jl:59-62)
+  for (int r = 0; r < c->nn && neg_ref < 0; r++)
+    if (neg_nodes[r]) neg_ref = r;
+  if (pos_ref < 0 || neg_ref < 0) return set_err(c, ISKRA_EINVAL, "empty electrode");
+  // the wall whose discarded particles land on the floating electrode:
+  // 0 x-low (column i=1), 1 x-high (i=nx), 2 y-low (row j=1), 3 y-high (j=ny)
+  for (int w = 0; w < 4 && wall < 0; w++) {
+    bool all = true;
+    const int len = w < 2 ? c->ny : c->nx;
+    for (int k = 0; k < len && all; k++) {
+      const int i = w == 0 ? 0 : w == 1 ? c->nx - 1 : k;
+      const int j = w == 2 ? 0 : w == 3 ? c->ny - 1 : k;
+      all = pos_nodes[i + c->nx * j] != 0;
+    }
+    if (all) wall = w;
+  }
+  CircuitDev d{};
+  d.R = R;
+  d.L = L;
+  d.C = C;
+  d.amp = amp;
+  d.freq = freq;
+  d.dc = dc;
+  d.area = area;
+  d.scale = sigma_scale;
+  d.sigma_dof = sigma_dof - 1;
+  if (!c->cir_d) ISKRA_CUDA(c, cudaMalloc(&c->cir_d, sizeof(CircuitDev)));
+  ISKRA_CUDA(c, cudaMemcpy(c->cir_d, &d, sizeof(d), cudaMemcpyHostToDevice));
+  c->cir_h = d;
+  c->cir_pos_ref = pos_ref;
+  c->cir_neg_ref = neg_ref;
+  c->cir_wall = wall;
+  if (!c->cir_seen) ISKRA_CUDA(c, cudaMalloc(&c->cir_seen, kMaxSpecies * sizeof(unsigned long long)));
+  std::vector<unsigned long long> seen(kMaxSpecies, 0);
+  for (int s = 0; s < (int)c->species.size(); s++) {
+    SpeciesState st{};
+    ISKRA_CUDA(c, cudaMemcpy(&st, c->species[s].dev.st, sizeof(st), cudaMemcpyDeviceToHost));
+    if (wall >= 0) seen[s] = st.absorbed[wall];
+  }
+  ISKRA_CUDA(c, cudaMemcpy(c->cir_seen, seen.data(), kMaxSpecies * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+  c->has_circuit = true;
+  invalidate_graphs(c);
+  return ISKRA_OK;
+}
+
+int iskra_circuit_advance(iskra_ctx *h, double dt) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!(dt > 0)) return set_err(c, ISKRA_EINVAL, "dt must be positive");
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  return launch_circuit(c, dt);
+}
+
+int iskra_circuit_state(iskra_ctx *h, double state[5]) {
+  if (!h || !state) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->cir_d) return set_err(c, ISKRA_EINVAL, "no circuit");
+  CircuitDev d{};
+  ISKRA_CUDA(c, cudaMemcpyAsync(&d, c->cir_d, sizeof(d), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  double sv = 0;
+  int rc = iskra_poisson_get_sigma(h, d.sigma_dof + 1, &sv);
+  if (rc) return rc;
+  state[0] = d.t;
+  state[1] = d.i;
+  state[2] = d.q;
+  state[3] = sv;
+  state[4] = d.vext;
+  return collect_device_errors(c);
+}
+
+int iskra_set_sort_every(iskra_ctx *h, int every) {
+  if (!h || every < 0) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  c->sort_every = every;
+  return ISKRA_OK;
+}
+
+int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!(dt > 0) || nsteps < 0 || !(rtol > 0)) return set_err(c, ISKRA_EINVAL, "bad dt / nsteps / rtol");
+  if (nsteps == 0) return ISKRA_OK;
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  // bring every accumulator to the consumed state the captured step expects
+  bool stale = false;
+  for (auto &s : c->species) stale |= s.acc_valid || !s.n_valid;
+  if (stale) {
+    rc = launch_charge_density(c);
+    if (rc) return rc;
+  }
+  if (c->d_step_known != c->step) {
+    c->d_step_host = c->step;
+    ISKRA_CUDA(c, cudaMemcpyAsync(c->d_step, &c->d_step_host, sizeof(c->d_step_host), cudaMemcpyHostToDevice,
+                                  c->stream));
+  }
+  c->graph_dt = dt;
+  if (!poisson_separable(c)) {
+    // eager path: CG needs host-side convergence checks
+    for (int n = 0; n < nsteps; n++) {
+      rc = queue_step(c, dt, seed, rtol, true);
+      if (rc) return rc;
+      c->step++;
+      c->d_step_known = c->step;
+      if (c->sort_every && c->step % c->sort_every == 0) {
+        rc = queue_sorts(c);
+        if (rc) return rc;
+      }
+    }
+    return collect_device_errors(c);
+  }
+  if (c->graph && (c->graph_rtol != rtol || c->graph_seed != seed || c->graph_dt != dt)) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  if (!c->graph) {
+    rc = capture(c, &c->graph, &c->graph_kernels, [&]() { return queue_step(c, dt, seed, rtol, false); });
+    if (rc) return rc;
+    c->graph_rtol = rtol;
+    c->graph_seed = seed;
+    c->graph_dt = dt;
+  }
+  if (!c->sort_graph && c->sort_every > 0) {
+    rc = capture(c, &c->sort_graph, &c->sort_graph_kernels, [&]() { return queue_sorts(c); });
+    if (rc) return rc;
+  }
+  for (int n = 0; n < nsteps; n++) {
+    ISKRA_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
+    c->launches += c->graph_kernels;
+    c->step++;
+    c->d_step_known = c->step;
+    if (c->sort_every > 0 && c->step % c->sort_every == 0) {
+      ISKRA_CUDA(c, cudaGraphLaunch(c->sort_graph, c->stream));
+      c->launches += c->sort_graph_kernels;
+    }
+  }
+  return ISKRA_OK;
+}
+
+int iskra_kernel_launches(iskra_ctx *h, uint64_t *count) {
+  if (!h || !count) return ISKRA_EINVAL;
+  *count = h->c.launches;
+  return ISKRA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,255 @@
+"""Device context: one grid, its species, fields, Poisson solver, MCC sets and
+circuit on one GB300, driven through the C ABI of libiskra_gpu.so.
+
+Arrays crossing this boundary use the reference's (Julia) layout: column-major
+float64 node arrays (nx, ny), particle matrices (np, 2) / (np, 3).
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_double, c_int, c_int64, c_uint64, c_void_p
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+
+def _f64(a, shape=None):
+    a = np.asarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape, order="F")
+    return np.asfortranarray(a)
+
+
+def _ptr(a, t=_lib.dp):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def _mask(nodes, nx, ny):
+    m = np.asarray(nodes, dtype=bool).reshape((nx, ny), order="F")
+    return np.asfortranarray(m.astype(np.uint8))
+
+
+class Context:
+    """Owns an iskra_ctx (one CUDA stream)."""
+
+    def __init__(self, nx, ny, dx, dy, bcs=(0, 0, 0, 0), stream: int = 0):
+        self.lib = _lib.load()
+        g = _lib.Grid(nx, ny, dx, dy, 0.0, 0.0, (ctypes.c_int32 * 4)(*[int(bool(b)) for b in bcs]))
+        h = c_void_p()
+        rc = self.lib.iskra_ctx_create(byref(g), stream, byref(h))
+        if rc != 0:
+            raise _lib.IskraError(rc, "iskra_ctx_create failed (is a CUDA device visible?)")
+        self.h = h
+        self.nx, self.ny, self.dx, self.dy = nx, ny, dx, dy
+        self.bcs = tuple(bcs)
+        self.species = []
+
+    # -- plumbing --
+    def _c(self, rc):
+        return check(self.lib, self.h, rc)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.iskra_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        self._c(self.lib.iskra_sync(self.h))
+
+    @property
+    def stream(self) -> int:
+        s = c_uint64()
+        self._c(self.lib.iskra_stream(self.h, byref(s)))
+        return s.value
+
+    # -- species --
+    def species_create(self, q, m, w0, capacity):
+        sid = c_int()
+        self._c(self.lib.iskra_species_create(self.h, q, m, w0, capacity, byref(sid)))
+        self.species.append(sid.value)
+        return sid.value
+
+    def upload(self, sid, x, v, wg=None, ids=None):
+        x = _f64(x)
+        v = _f64(v)
+        n = x.shape[0]
+        wg = None if wg is None else _f64(wg)
+        ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+        self._c(self.lib.iskra_species_upload(self.h, sid, _ptr(x), _ptr(v), _ptr(wg), _ptr(ids, _lib.u32p), n, n))
+
+    def count(self, sid):
+        n = c_int64()
+        self._c(self.lib.iskra_species_count(self.h, sid, byref(n)))
+        return n.value
+
+    def download(self, sid):
+        n = self.count(sid)
+        cap = max(n, 1)
+        x = np.zeros((cap, 2), order="F")
+        v = np.zeros((cap, 3), order="F")
+        ids = np.zeros(cap, dtype=np.uint32)
+        got = c_int64()
+        self._c(self.lib.iskra_species_download(self.h, sid, _ptr(x), _ptr(v), None, _ptr(ids, _lib.u32p), cap,
+                                                byref(got)))
+        n = got.value
+        return np.asfortranarray(x[:n]), np.asfortranarray(v[:n]), ids[:n].copy()
+
+    def set_boundary(self, sid, mode_x, mode_y):
+        self._c(self.lib.iskra_species_set_boundary(self.h, sid, mode_x, mode_y))
+
+    def absorbed(self, sid):
+        a = (c_int64 * 4)()
+        self._c(self.lib.iskra_species_absorbed(self.h, sid, a))
+        return list(a)
+
+    def sort(self, sid):
+        self._c(self.lib.iskra_species_sort(self.h, sid))
+
+    # -- fields --
+    def upload_E(self, E):
+        E = _f64(E, (self.nx, self.ny, 3))
+        self._c(self.lib.iskra_field_upload_E(self.h, _ptr(E)))
+
+    def field(self, which):
+        shape = (self.nx, self.ny, 3) if which == _lib.FIELD_E else (self.nx, self.ny)
+        out = np.zeros(shape, order="F")
+        self._c(self.lib.iskra_field_download(self.h, which, _ptr(out)))
+        return out
+
+    def advance(self, sid, dt):
+        self._c(self.lib.iskra_advance(self.h, sid, dt))
+
+    def density(self, sid):
+        out = np.zeros((self.nx, self.ny), order="F")
+        self._c(self.lib.iskra_density(self.h, sid, _ptr(out)))
+        return out
+
+    def finalize(self, sid):
+        """density(species) kept on the device (consumes the deposit accumulator)."""
+        self._c(self.lib.iskra_density(self.h, sid, None))
+
+    def charge_density(self):
+        self._c(self.lib.iskra_charge_density(self.h))
+        return self.field(_lib.FIELD_RHO)
+
+    def set_background(self, rho_bg):
+        if rho_bg is None:
+            self._c(self.lib.iskra_set_background(self.h, None))
+        else:
+            a = _f64(rho_bg, (self.nx, self.ny))
+            self._c(self.lib.iskra_set_background(self.h, _ptr(a)))
+
+    # -- Poisson --
+    def poisson_create(self, eps0):
+        self._c(self.lib.iskra_poisson_create(self.h, eps0))
+
+    def apply_dirichlet(self, nodes, phi0):
+        m = _mask(nodes, self.nx, self.ny)
+        self._c(self.lib.iskra_poisson_apply_dirichlet(self.h, _ptr(m, _lib.u8p), phi0))
+
+    def apply_periodic(self, axis):
+        self._c(self.lib.iskra_poisson_apply_periodic(self.h, axis))
+
+    def add_dof(self):
+        d = c_int()
+        self._c(self.lib.iskra_poisson_add_dof(self.h, byref(d)))
+        return d.value
+
+    def apply_neumann(self, nodes, dof):
+        m = _mask(nodes, self.nx, self.ny)
+        self._c(self.lib.iskra_poisson_apply_neumann(self.h, _ptr(m, _lib.u8p), dof))
+
+    def set_sigma(self, dof, value):
+        self._c(self.lib.iskra_poisson_set_sigma(self.h, dof, value))
+
+    def get_sigma(self, dof):
+        v = c_double()
+        self._c(self.lib.iskra_poisson_get_sigma(self.h, dof, byref(v)))
+        return v.value
+
+    def drive_dirichlet(self, nodes, amp, freq, phase=0.0, dc=0.0):
+        m = _mask(nodes, self.nx, self.ny)
+        self._c(self.lib.iskra_poisson_drive_dirichlet(self.h, _ptr(m, _lib.u8p), amp, freq, phase, dc))
+
+    def set_method(self, method):
+        a = c_int()
+        self._c(self.lib.iskra_poisson_set_method(self.h, method, byref(a)))
+        return a.value
+
+    def solve(self, rtol=1e-8, maxit=10000):
+        it, rr = c_int(), c_double()
+        self._c(self.lib.iskra_poisson_solve(self.h, rtol, maxit, byref(it), byref(rr)))
+        return it.value, rr.value
+
+    def solve_host(self, f, rtol=1e-8, maxit=10000):
+        f = _f64(f, (self.nx, self.ny))
+        phi = np.zeros((self.nx, self.ny), order="F")
+        it, rr = c_int(), c_double()
+        self._c(self.lib.iskra_poisson_solve_host(self.h, _ptr(f), rtol, maxit, _ptr(phi), byref(it), byref(rr)))
+        return phi, it.value, rr.value
+
+    def solve_info(self):
+        it, rr = c_int(), c_double()
+        self._c(self.lib.iskra_solve_info(self.h, byref(it), byref(rr)))
+        return it.value, rr.value
+
+    # -- MCC --
+    def mcc_create(self, src, processes, gas_mass, gas_T, gas_n, gas_q=0.0, product=-1):
+        """processes: list of (type, energy, eps_nodes, sigma_nodes)."""
+        N = len(processes)
+        types = (c_int * N)(*[int(p[0]) for p in processes])
+        energies = (c_double * N)(*[float(p[1]) for p in processes])
+        off = np.zeros(N + 1, dtype=np.int32)
+        for k, p in enumerate(processes):
+            off[k + 1] = off[k] + len(p[2])
+        eps = np.ascontiguousarray(np.concatenate([np.asarray(p[2], float) for p in processes]))
+        sig = np.ascontiguousarray(np.concatenate([np.asarray(p[3], float) for p in processes]))
+        gn = _f64(gas_n, (self.nx, self.ny))
+        msg = c_double()
+        mid = c_int()
+        self._c(self.lib.iskra_mcc_create(self.h, src, N, types, energies, _ptr(off, _lib.i32p), _ptr(eps), _ptr(sig),
+                                          gas_mass, gas_T, gas_q, _ptr(gn), product, byref(msg), byref(mid)))
+        return mid.value, msg.value
+
+    def mcc_perform(self, mid, dt, seed, step):
+        self._c(self.lib.iskra_mcc_perform(self.h, mid, dt, seed, step))
+
+    def mcc_counts(self, mid, nproc):
+        a = (c_int64 * nproc)()
+        self._c(self.lib.iskra_mcc_counts(self.h, mid, a))
+        return list(a)
+
+    # -- circuit --
+    def circuit_create(self, R, L, C, amp, freq, dc, sigma_dof, pos_nodes, neg_nodes, area, sigma_scale=1.0):
+        pm = _mask(pos_nodes, self.nx, self.ny)
+        nm = _mask(neg_nodes, self.nx, self.ny)
+        self._c(self.lib.iskra_circuit_create(self.h, R, L, C, amp, freq, dc, sigma_dof, _ptr(pm, _lib.u8p),
+                                              _ptr(nm, _lib.u8p), area, sigma_scale))
+
+    def circuit_advance(self, dt):
+        self._c(self.lib.iskra_circuit_advance(self.h, dt))
+
+    def circuit_state(self):
+        s = (c_double * 5)()
+        self._c(self.lib.iskra_circuit_state(self.h, s))
+        return dict(zip(("t", "i", "q", "sigma", "vext"), list(s)))
+
+    # -- whole step --
+    def step(self, dt, nsteps=1, seed=0, rtol=1e-8):
+        self._c(self.lib.iskra_step(self.h, dt, nsteps, seed, rtol))
+
+    def kernel_launches(self):
+        n = c_uint64()
+        self._c(self.lib.iskra_kernel_launches(self.h, byref(n)))
+        return n.value
+
+    def set_sort_every(self, every):
+        self._c(self.lib.iskra_set_sort_every(self.h, every))

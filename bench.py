@@ -216,7 +216,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle leg (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -320,23 +321,25 @@ def main():
     # particle arrays (Julia layout, FP64), K steps each reading ϕ back (the
     # per-step "phi" field record), final particle download
     ctx.close()
-    w2, e2, i2 = w, e, i
-    phi_host = np.zeros((NX, NY), order="F")
-    k_e2e = min(args.steps, 200)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ctx2, se2, si2 = setup_context(w2, e2, i2)
-    for k in range(k_e2e):
-        ctx2.step(DT, 1, seed=1, rtol=RTOL)
-        phi_host[...] = ctx2.field(1)
-    xe_o, ve_o, _ = ctx2.download(se2)
-    xi_o, vi_o, _ = ctx2.download(si2)
-    t_e2e = time.perf_counter() - t0
-    np_e2e = 0.5 * (2 * NP + xe_o.shape[0] + xi_o.shape[0])
-    e2e_value = np_e2e * k_e2e / t_e2e
-    h2d = 2 * NP * 5 * 8 / k_e2e
-    d2h = NX * NY * 8 + (xe_o.shape[0] + xi_o.shape[0]) * 5 * 8 / k_e2e
-    ctx2.close()
+    e2e = None
+    if not args.no_e2e:
+        phi_host = np.zeros((NX, NY), order="F")
+        k_e2e = min(args.steps, 200)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx2, se2, si2 = setup_context(w, e, i)
+        for k in range(k_e2e):
+            ctx2.step(DT, 1, seed=1, rtol=RTOL)
+            phi_host[...] = ctx2.field(1)
+        xe_o, ve_o, _ = ctx2.download(se2)
+        xi_o, vi_o, _ = ctx2.download(si2)
+        t_e2e = time.perf_counter() - t0
+        np_e2e = 0.5 * (2 * NP + xe_o.shape[0] + xi_o.shape[0])
+        e2e = {"value": np_e2e * k_e2e / t_e2e, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 2 * NP * 5 * 8 / k_e2e,
+               "d2h_bytes_per_step": NX * NY * 8 + (xe_o.shape[0] + xi_o.shape[0]) * 5 * 8 / k_e2e, "steps": k_e2e,
+               "note": "C-ABI from host FP64 arrays: upload, per-step step+phi readback, final download"}
+        ctx2.close()
 
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -352,9 +355,7 @@ def main():
                      "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": t_push * 1e3},
         "clocks": clocks,
-        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": k_e2e,
-                "note": "C-ABI from host FP64 arrays: upload, per-step step+phi readback, final download"},
+        "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:
         r = cpu_run(w, e, i, max_seconds=20.0)

@@ -228,6 +228,25 @@ int iskra_solve_info(iskra_ctx *ctx, int *iters, double *relres);
  * launched on this context (graph replays x kernel nodes). */
 int iskra_kernel_launches(iskra_ctx *ctx, uint64_t *count);
 
+/* ---- density without device allocation -----------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: a host framework that reserves the GPU's memory up front and
+ * forbids later cudaMalloc, or code running while another library holds the
+ * stream in capture.  Same result as iskra_density (CIC deposit ./
+ * cell_volume, exact int64 fixed-point sums) for the np particles whose
+ * positions x (ld x 2, column-major FP64) are in DEVICE memory; the (nx,ny)
+ * density goes to n_out (device memory); *flag (device int) is set to 1 when
+ * a position lies outside the grid (that particle is skipped), else 0.
+ * Allocates nothing: the accumulator is a library-static device array of
+ * 2^20 nodes (8 MiB, held on every GPU that loads the library until exit);
+ * larger grids return ISKRA_EINVAL.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress): make that first call before any
+ * stream capture.  Each call clears the array it shares with every other
+ * call; calls that overlap on the GPU race.  Asynchronous on `stream`. */
+int iskra_density_noalloc(const iskra_grid_t *grid, const double *x,
+                          int64_t np, int64_t ld, double w0, double *n_out,
+                          int *flag, uint64_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,6 +84,8 @@ SIGNATURES = [
     ("iskra_set_sort_every", c_int, [CTX, c_int]),
     ("iskra_solve_info", c_int, [CTX, ip, dp]),
     ("iskra_kernel_launches", c_int, [CTX, POINTER(c_uint64)]),
+    ("iskra_density_noalloc", c_int, [POINTER(Grid), c_void_p, c_int64, c_int64, c_double, c_void_p, c_void_p,
+                                      c_uint64]),
 ]
 
 _LIB = None

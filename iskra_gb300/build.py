@@ -18,6 +18,8 @@ LIB = os.path.join(OUT_DIR, "libiskra_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xptxas", "-v" if os.environ.get("ISKRA_PTXAS_V") else "-O3"]
+# extra nvcc flags for tuning builds, e.g. ISKRA_NVCC_FLAGS="-DISKRA_PUSH_MIN_BLOCKS=6"
+FLAGS += os.environ.get("ISKRA_NVCC_FLAGS", "").split()
 
 
 def nvcc():

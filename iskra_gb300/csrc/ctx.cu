@@ -47,6 +47,8 @@ int collect_device_errors(Ctx *c) {
     return set_err(c, ISKRA_EDOMAIN, "particle outside the grid on an axis without wrap!/discard!");
   if (f & DERR_TIMEOUT) return set_err(c, ISKRA_ETIMEDOUT, "bounded device wait gave up");
   if (f & DERR_NOTCONV) return set_err(c, ISKRA_ENOTCONV, "Poisson solve did not reach the tolerance");
+  if (f & DERR_OVERFLOW)
+    return set_err(c, ISKRA_ECAPACITY, "deposit: more than 16383 macroparticles in one cell (int64 node sums could wrap)");
   return set_err(c, ISKRA_ECUDA, "unknown device error flag");
 }
 
@@ -106,11 +108,13 @@ __global__ void k_download(double *__restrict__ st, long long np, double dx, dou
   st[p + 4 * np] = b.x;
 }
 
-__global__ void k_upload_E(const double *__restrict__ E, int nn, float2 *E32, double *E64) {
+__global__ void k_upload_E(const double *__restrict__ E, int nx, int ny, float2 *E32, float4 *E4, double *E64) {
+  const int nn = nx * ny;
   int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nn) return;
   double ex = E[n], ey = E[n + nn], ez = E[n + 2 * nn];
   E32[n] = make_float2((float)ex, (float)ey);
+  store_corners(E4, nx, ny, n % nx, n / nx, make_float2((float)ex, (float)ey));
   E64[n] = ex;
   E64[n + nn] = ey;
   E64[n + 2 * nn] = ez;
@@ -165,6 +169,7 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
   }
   size_t nn = (size_t)c->nn;
   bool ok = cudaMalloc(&c->E32, nn * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&c->E4, nn * 2 * sizeof(float4)) == cudaSuccess &&
             cudaMalloc(&c->E64, nn * 3 * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&c->rho, nn * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&c->vol_inv, nn * sizeof(double)) == cudaSuccess &&
@@ -176,6 +181,7 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
             cudaMalloc(&c->d_step, sizeof(unsigned long long)) == cudaSuccess;
   if (!ok) return fail(ISKRA_ENOMEM);
   cudaMemsetAsync(c->E32, 0, nn * sizeof(float2), c->stream);
+  cudaMemsetAsync(c->E4, 0, nn * 2 * sizeof(float4), c->stream);
   cudaMemsetAsync(c->E64, 0, nn * 3 * sizeof(double), c->stream);
   cudaMemsetAsync(c->rho, 0, nn * sizeof(double), c->stream);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
@@ -213,6 +219,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
     }
     cudaFree(s.dev.st);
     cudaFree(s.dev.acc);
+    cudaFree(s.dev.cnt);
     cudaFree(s.n);
   }
   for (auto *m : c->mccs) mcc_destroy(m);
@@ -220,6 +227,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   cudaFree(c->cir_d);
   cudaFree(c->cir_seen);
   cudaFree(c->E32);
+  cudaFree(c->E4);
   cudaFree(c->E64);
   cudaFree(c->rho);
   cudaFree(c->rho_bg);
@@ -260,10 +268,6 @@ int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t ca
   s.m = m;
   s.w0 = w0;
   s.cap = cap;
-  // weight W48 = (2^24-u)(2^24-v) etc. < 2^48; a node sums at most cap of them.
-  int bits = 0;
-  while ((1LL << bits) < cap + 1) bits++;
-  s.dev.shift = 48 + bits > 63 ? 48 + bits - 63 : 0;
   s.dev.cap = cap;
   size_t nn = (size_t)c->nn;
   for (int b = 0; b < 2; b++) {
@@ -273,9 +277,11 @@ int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t ca
   }
   ISKRA_CUDA(c, cudaMalloc(&s.dev.st, sizeof(SpeciesState)));
   ISKRA_CUDA(c, cudaMalloc(&s.dev.acc, nn * sizeof(unsigned long long)));
+  ISKRA_CUDA(c, cudaMalloc(&s.dev.cnt, nn * sizeof(unsigned)));
   ISKRA_CUDA(c, cudaMalloc(&s.n, nn * sizeof(double)));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.st, 0, sizeof(SpeciesState), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, nn * sizeof(unsigned long long), c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, nn * sizeof(unsigned), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.n, 0, nn * sizeof(double), c->stream));
   s.acc_valid = false;
   s.acc_zero = true;
@@ -425,7 +431,7 @@ int iskra_field_upload_E(iskra_ctx *h, const double *E) {
   if (rc) return rc;
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   ISKRA_CUDA(c, cudaMemcpyAsync(c->stage, E, (size_t)c->nn * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  k_upload_E<<<(c->nn + 255) / 256, 256, 0, c->stream>>>(c->stage, c->nn, c->E32, c->E64);
+  k_upload_E<<<(c->nn + 255) / 256, 256, 0, c->stream>>>(c->stage, c->nx, c->ny, c->E32, c->E4, c->E64);
   ISKRA_CUDA(c, cudaGetLastError());
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   return ISKRA_OK;

@@ -35,6 +35,7 @@ enum : int {
   DERR_NAN = 8,
   DERR_TIMEOUT = 16,
   DERR_NOTCONV = 32,
+  DERR_OVERFLOW = 64,
 };
 
 struct SpeciesState {          // device-resident, written by kernels
@@ -54,8 +55,7 @@ struct SpeciesDev {            // kernel view of one species (by value)
   SpeciesState *st;
   unsigned long long *acc;     // (nx*ny) fixed-point deposit accumulator
   long long cap;
-  int shift;                   // weight = W48 >> shift
-  int pad;
+  unsigned *cnt;               // (nx*ny) particles deposited per cell (overflow guard)
 };
 
 // Buffer of a double-buffered array without dynamic indexing of a kernel
@@ -63,6 +63,19 @@ struct SpeciesDev {            // kernel view of one species (by value)
 template <class T>
 __device__ __forceinline__ T *pick(T *a, T *b, int cur) {
   return cur ? b : a;
+}
+
+// Per-cell E record of cell (ci, cj) (index ci + nx cj): float4 {E(ci,cj),
+// E(ci+1,cj)} then float4 {E(ci,cj+1), E(ci+1,cj+1)}, so the CIC gather of a
+// particle reads one 32-byte record.  Node (i, j) is a corner of up to four
+// cells; this writes its value into each of them.
+__device__ __forceinline__ void store_corners(float4 *E4, int nx, int ny, int i, int j, float2 e) {
+  float2 *r = reinterpret_cast<float2 *>(E4);
+  const int k = i + nx * j;
+  if (i <= nx - 2 && j <= ny - 2) r[4 * k + 0] = e;
+  if (i >= 1 && j <= ny - 2) r[4 * (k - 1) + 1] = e;
+  if (i <= nx - 2 && j >= 1) r[4 * (k - nx) + 2] = e;
+  if (i >= 1 && j >= 1) r[4 * (k - nx - 1) + 3] = e;
 }
 
 struct Species {
@@ -95,7 +108,8 @@ struct Ctx {
   std::string err;
   std::vector<Species> species;
   // fields
-  float2 *E32 = nullptr;       // (nx*ny) {Ex, Ey} for the gather
+  float2 *E32 = nullptr;       // (nx*ny) {Ex, Ey} at the nodes (MCC target term)
+  float4 *E4 = nullptr;        // (nx*ny*2) per cell: the 4 corner fields, gather input
   double *E64 = nullptr;       // (nx*ny*3) download scratch
   double *rho = nullptr;       // (nx*ny)
   double *rho_bg = nullptr;    // optional background charge density

@@ -10,11 +10,16 @@
 //   sort      : counting sort by cell + compaction of discarded particles.
 //
 // Deposit arithmetic: offsets are multiples of 2^-24, u = hx*2^24 is an exact
-// integer, so the CIC weights (2^24-u)(2^24-v), u(2^24-v), ... are exact 48-bit
-// integers.  They are shifted right by `shift` (0 unless a node could exceed
-// 2^63) and summed with 64-bit integer atomics after a warp-level reduction
-// over lanes that share a cell.  Integer addition is associative, so the
-// density is bit-identical for any particle order or launch shape.
+// integer, so the CIC weights (2^24-u)(2^24-v), u(2^24-v), (2^24-u)v, uv are
+// exact 48-bit integers.  Over the particles of one cell they sum to
+//   W11 = Σuv,  W10 = 2^24 Σu - Σuv,  W01 = 2^24 Σv - Σuv,
+//   W00 = 2^48 n - 2^24 Σu - 2^24 Σv + Σuv,
+// so a warp reduces the moments (n, Σu, Σv: 32-bit; Σuv: 64-bit) over each run
+// of lanes in the same cell and the run's last lane adds the four node sums
+// with 64-bit integer atomics.  Integer addition is associative: the density
+// is bit-identical for any particle order or launch shape.  A node's sum
+// stays below 2^64 while each of its four cells holds at most 16383
+// particles; the per-cell counts are kept alongside and checked by k_finalize.
 #include <cmath>
 
 #include "internal.cuh"
@@ -28,38 +33,44 @@ struct PushParams {
   int mode_x, mode_y;
 };
 
-// Reduce four u64 values over the lanes of the warp that share `key`; the
-// lowest lane of each group returns true holding the group sums.
-__device__ __forceinline__ bool reduce_peers(int key, unsigned long long (&w)[4]) {
+// Moments of one particle: u, v < 2^24 and uv = hi 2^24 + lo with hi, lo < 2^24,
+// so every sum over at most 32 lanes fits in 32 bits.
+struct Moments {
+  unsigned su, sv, hi, lo;
+};
+
+// Inclusive segmented sum of the moments over runs of lanes holding the same
+// key (any particle order is correct; cell-sorted particles give long runs):
+// five shuffle rounds with a run-start guard.  Returns true on the last lane
+// of each run, which then holds the run's sums; *n receives the run length.
+// (A per-run __reduce_add_sync over the run's lane mask measured 2x slower on
+// GB300 once the runs shorten between sorts.)
+__device__ __forceinline__ bool reduce_runs(int key, Moments &m, unsigned &n) {
   const unsigned FULL = 0xffffffffu;
-  const unsigned lane = threadIdx.x & 31;
-  const unsigned peers = __match_any_sync(FULL, key);
-  const unsigned lt = (1u << lane) - 1u;
-  const bool leader = (peers & lt) == 0;
-  unsigned above = peers & ~(lt | (1u << lane));
-  int rel = __popc(peers & lt);
-  bool active = true;
-  // at most log2(32) = 5 rounds: each removes half of the active lanes
-  for (int round = 0; round < 6; round++) {
-    if (!__any_sync(FULL, active && above != 0)) break;
-    int src = above ? (__ffs(above) - 1) : (int)lane;
-    unsigned long long t0 = __shfl_sync(FULL, w[0], src);
-    unsigned long long t1 = __shfl_sync(FULL, w[1], src);
-    unsigned long long t2 = __shfl_sync(FULL, w[2], src);
-    unsigned long long t3 = __shfl_sync(FULL, w[3], src);
-    if (active && (rel & 1) == 0 && above) {
-      w[0] += t0;
-      w[1] += t1;
-      w[2] += t2;
-      w[3] += t3;
+  const int lane = threadIdx.x & 31;
+  const int prev = __shfl_up_sync(FULL, key, 1);
+  const int next = __shfl_down_sync(FULL, key, 1);
+  const bool head = lane == 0 || prev != key;
+  const bool tail = lane == 31 || next != key;
+  const unsigned heads = __ballot_sync(FULL, head);
+  const int start = 31 - __clz(heads & ((2u << lane) - 1u));  // first lane of my run
+  if (heads != FULL) {  // warp-uniform: some run is longer than one lane
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned su = __shfl_up_sync(FULL, m.su, d);
+      const unsigned sv = __shfl_up_sync(FULL, m.sv, d);
+      const unsigned hi = __shfl_up_sync(FULL, m.hi, d);
+      const unsigned lo = __shfl_up_sync(FULL, m.lo, d);
+      if (lane - d >= start) {
+        m.su += su;
+        m.sv += sv;
+        m.hi += hi;
+        m.lo += lo;
+      }
     }
-    bool leaving = active && (rel & 1);
-    unsigned leave = __ballot_sync(FULL, leaving);
-    above &= ~leave;
-    if (leaving) active = false;
-    rel >>= 1;
   }
-  return leader;
+  n = (unsigned)(lane - start + 1);
+  return tail;
 }
 
 // Move by d cells along one axis in FP32: offset h in [0,1) on the 2^-24 grid,
@@ -99,9 +110,15 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
   return 3;
 }
 
+// Minimum resident blocks per SM requested from the register allocator
+// (256-thread blocks); tuned on GB300.
+#ifndef ISKRA_PUSH_MIN_BLOCKS
+#define ISKRA_PUSH_MIN_BLOCKS 1
+#endif
+
 template <bool PUSH, int MX, int MY>
-__global__ void __launch_bounds__(256) k_push(SpeciesDev s, const float2 *__restrict__ E, PushParams P,
-                                               int *err) {
+__global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev s, const float4 *__restrict__ E4,
+                                                                     PushParams P, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const long long np = s.st->np;
@@ -116,10 +133,10 @@ __global__ void __launch_bounds__(256) k_push(SpeciesDev s, const float2 *__rest
   for (long long base = warp * 32; base < np; base += nwarps * 32) {
     const long long p = base + lane;
     int key = -1;
-    unsigned long long w[4] = {0, 0, 0, 0};
+    Moments m = {0u, 0u, 0u, 0u};
     if (p < np) {
-      float4 a = xv[p];
-      float2 b = zc[p];
+      float4 a = __ldcs(xv + p);
+      float2 b = __ldcs(zc + p);
       int cell = __float_as_int(b.y);
       if (cell >= 0) {
         int i0 = cell & 0xffff, j0 = cell >> 16;
@@ -127,8 +144,9 @@ __global__ void __launch_bounds__(256) k_push(SpeciesDev s, const float2 *__rest
         if (PUSH) {
           const int n0 = i0 + nx * j0;
           const float gx = 1.0f - hx, gy = 1.0f - hy;
-          const float2 e00 = __ldg(E + n0), e10 = __ldg(E + n0 + 1);
-          const float2 e01 = __ldg(E + n0 + nx), e11 = __ldg(E + n0 + nx + 1);
+          const float4 r0 = __ldg(E4 + 2 * n0), r1 = __ldg(E4 + 2 * n0 + 1);  // the cell's corner fields
+          const float2 e00 = make_float2(r0.x, r0.y), e10 = make_float2(r0.z, r0.w);
+          const float2 e01 = make_float2(r1.x, r1.y), e11 = make_float2(r1.z, r1.w);
           const float ex = gx * gy * e00.x + hx * gy * e10.x + gx * hy * e01.x + hx * hy * e11.x;
           const float ey = gx * gy * e00.y + hx * gy * e10.y + gx * hy * e01.y + hx * hy * e11.y;
           // Boris with B = 0: v- = v + hE ; v = hE + v+ (v+ = v-)
@@ -157,31 +175,30 @@ __global__ void __launch_bounds__(256) k_push(SpeciesDev s, const float2 *__rest
               cell = i0 | (j0 << 16);
             }
           }
-          xv[p] = make_float4(hx, hy, vx, vy);
-          zc[p] = make_float2(b.x, __int_as_float(cell));
+          __stcs(xv + p, make_float4(hx, hy, vx, vy));
+          __stcs(zc + p, make_float2(b.x, __int_as_float(cell)));
         }
         if (cell >= 0) {
           key = i0 + nx * j0;
-          const unsigned long long ux = (unsigned long long)__float2uint_rn(hx * kOffScale);
-          const unsigned long long uy = (unsigned long long)__float2uint_rn(hy * kOffScale);
-          const unsigned long long gx = (1ull << 24) - ux, gy = (1ull << 24) - uy;
-          w[0] = gx * gy;
-          w[1] = ux * gy;
-          w[2] = gx * uy;
-          w[3] = ux * uy;
-          if (s.shift) {
-            const unsigned long long half = 1ull << (s.shift - 1);
-#pragma unroll
-            for (int k = 0; k < 4; k++) w[k] = (w[k] + half) >> s.shift;
-          }
+          const unsigned ux = __float2uint_rn(hx * kOffScale);
+          const unsigned uy = __float2uint_rn(hy * kOffScale);
+          const unsigned long long uv = (unsigned long long)ux * uy;
+          m.su = ux;
+          m.sv = uy;
+          m.hi = (unsigned)(uv >> 24);
+          m.lo = (unsigned)uv & 0xffffffu;
         }
       }
     }
-    if (reduce_peers(key, w) && key >= 0) {
-      atomicAdd(s.acc + key, w[0]);
-      atomicAdd(s.acc + key + 1, w[1]);
-      atomicAdd(s.acc + key + nx, w[2]);
-      atomicAdd(s.acc + key + nx + 1, w[3]);
+    unsigned n;
+    if (reduce_runs(key, m, n) && key >= 0) {
+      const unsigned long long U = (unsigned long long)m.su << 24, V = (unsigned long long)m.sv << 24;
+      const unsigned long long UV = ((unsigned long long)m.hi << 24) + m.lo;
+      atomicAdd(s.acc + key, ((unsigned long long)n << 48) - U - V + UV);
+      atomicAdd(s.acc + key + 1, U - UV);
+      atomicAdd(s.acc + key + nx, V - UV);
+      atomicAdd(s.acc + key + nx + 1, UV);
+      atomicAdd(s.cnt + key, n);
     }
   }
   if (PUSH) {
@@ -200,7 +217,7 @@ static void launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
   const int T = 256;
 #define ISKRA_PUSH_CASE(MX, MY)                                                     \
   if (P.mode_x == MX && P.mode_y == MY) {                                           \
-    k_push<PUSH, MX, MY><<<blocks, T, 0, c->stream>>>(s.dev, c->E32, P, c->d_err); \
+    k_push<PUSH, MX, MY><<<blocks, T, 0, c->stream>>>(s.dev, c->E4, P, c->d_err);  \
     return;                                                                         \
   }
   ISKRA_PUSH_CASE(0, 0) ISKRA_PUSH_CASE(0, 1) ISKRA_PUSH_CASE(0, 2)
@@ -221,6 +238,7 @@ int launch_advance(Ctx *c, int sid, float dt) {
   if (!s.acc_zero) {
     // accumulator holds an old deposit: clear it first
     ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, (size_t)c->nn * sizeof(unsigned long long), c->stream));
+    ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, (size_t)c->nn * sizeof(unsigned), c->stream));
   }
   PushParams P;
   P.h = (float)(0.5 * (double)dt * (s.q / s.m));
@@ -242,10 +260,11 @@ int launch_deposit(Ctx *c, int sid) {
   Species &s = c->species[sid];
   if (!s.acc_zero)
     ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, (size_t)c->nn * sizeof(unsigned long long), c->stream));
+    ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, (size_t)c->nn * sizeof(unsigned), c->stream));
   PushParams P{};
   P.nx = c->nx;
   P.ny = c->ny;
-  k_push<false, 0, 0><<<push_blocks(c, s), 256, 0, c->stream>>>(s.dev, c->E32, P, c->d_err);
+  k_push<false, 0, 0><<<push_blocks(c, s), 256, 0, c->stream>>>(s.dev, c->E4, P, c->d_err);
   ISKRA_CUDA(c, cudaGetLastError());
   s.acc_valid = true;
   s.acc_zero = false;
@@ -258,32 +277,57 @@ int launch_deposit(Ctx *c, int sid) {
 struct FinalizeArgs {
   int ns;
   unsigned long long *acc[kMaxSpecies];
+  unsigned *cnt[kMaxSpecies];
   double *n[kMaxSpecies];
-  double scale[kMaxSpecies];  // w0 * 2^(shift-48)
+  double scale[kMaxSpecies];  // w0 * 2^-48
   double q[kMaxSpecies];
   int consume[kMaxSpecies];
 };
 
+// A node sums the weights of the particles in its four cells; with at most
+// kMaxCell particles per cell the sum stays below 4 * 16383 * 2^48 < 2^64.
+constexpr unsigned kMaxCell = 16383;
+
 __global__ void k_finalize(FinalizeArgs A, const double *__restrict__ vol_inv, const double *__restrict__ bg,
-                           double *__restrict__ rho, int nn) {
+                           double *__restrict__ rho, int nn, int *err) {
+  int flags = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    double r = 0.0;
+    // all loads of the node first (independent, in flight together), then the
+    // arithmetic and the stores
     const double vi = vol_inv[k];
-    for (int s = 0; s < A.ns; s++) {
+    const double b = bg ? bg[k] : 0.0;
+    unsigned long long a[kMaxSpecies];
+    unsigned cn[kMaxSpecies];
+    double nold[kMaxSpecies];
+#pragma unroll
+    for (int s = 0; s < kMaxSpecies; s++) {
+      if (s >= A.ns) break;
+      if (A.consume[s]) {
+        a[s] = A.acc[s][k];
+        cn[s] = A.cnt[s][k];
+      } else {
+        nold[s] = A.n[s][k];
+      }
+    }
+    double r = 0.0;
+#pragma unroll
+    for (int s = 0; s < kMaxSpecies; s++) {
+      if (s >= A.ns) break;
       double n;
       if (A.consume[s]) {
-        unsigned long long a = A.acc[s][k];
-        A.acc[s][k] = 0ull;
-        n = (double)a * A.scale[s] * vi;
+        if (cn[s] > kMaxCell) flags |= DERR_OVERFLOW;
+        n = (double)a[s] * A.scale[s] * vi;
         A.n[s][k] = n;
+        A.acc[s][k] = 0ull;
+        A.cnt[s][k] = 0u;
       } else {
-        n = A.n[s][k];
+        n = nold[s];
       }
       r += n * A.q[s];
     }
-    if (bg) r += bg[k];
-    if (rho) rho[k] = r;
+    if (rho) rho[k] = r + b;
   }
+  if (flags) atomicOr(err, flags);
 }
 
 // Brings every species' density up to date (depositing species whose
@@ -300,8 +344,9 @@ static int finalize(Ctx *c, bool with_rho) {
       if (rc) return rc;
     }
     A.acc[s] = sp.dev.acc;
+    A.cnt[s] = sp.dev.cnt;
     A.n[s] = sp.n;
-    A.scale[s] = sp.w0 * ldexp(1.0, sp.dev.shift - 48);
+    A.scale[s] = sp.w0 * ldexp(1.0, -48);
     A.q[s] = sp.q;
     A.consume[s] = sp.acc_valid ? 1 : 0;
     any |= sp.acc_valid;
@@ -310,7 +355,8 @@ static int finalize(Ctx *c, bool with_rho) {
   int blocks = c->num_sms * 4;
   int need = (c->nn + 255) / 256;
   if (need < blocks) blocks = need;
-  k_finalize<<<blocks, 256, 0, c->stream>>>(A, c->vol_inv, c->rho_bg, with_rho ? c->rho : nullptr, c->nn);
+  k_finalize<<<blocks, 256, 0, c->stream>>>(A, c->vol_inv, c->rho_bg, with_rho ? c->rho : nullptr, c->nn,
+                                            c->d_err);
   ISKRA_CUDA(c, cudaGetLastError());
   for (int s = 0; s < A.ns; s++) {
     Species &sp = c->species[s];
@@ -329,7 +375,7 @@ int launch_charge_density(Ctx *c) { return finalize(c, true); }
 // E = -∇ϕ  (generalized_poisson.jl:398-410)
 // ---------------------------------------------------------------------------
 __global__ void k_efield(const double *__restrict__ phi, int nx, int ny, double idx2, double idx1, double idy2,
-                         double idy1, float2 *__restrict__ E32, double *__restrict__ E64) {
+                         double idy1, float2 *__restrict__ E32, float4 *__restrict__ E4, double *__restrict__ E64) {
   const int nn = nx * ny;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const int i = k % nx, j = k / nx;
@@ -341,6 +387,7 @@ __global__ void k_efield(const double *__restrict__ phi, int nx, int ny, double 
     else if (j == ny - 1) ey = (phi[k - nx] - phi[k]) * idy1;
     else ey = (phi[k - nx] - phi[k + nx]) * idy2;
     E32[k] = make_float2((float)ex, (float)ey);
+    store_corners(E4, nx, ny, i, j, make_float2((float)ex, (float)ey));
     E64[k] = ex;
     E64[k + nn] = ey;
     E64[k + 2 * nn] = 0.0;
@@ -352,7 +399,7 @@ int launch_efield_from(Ctx *c, const double *phi) {
   int need = (c->nn + 255) / 256;
   if (need < blocks) blocks = need;
   k_efield<<<blocks, 256, 0, c->stream>>>(phi, c->nx, c->ny, 1.0 / (2 * c->g.dx), 1.0 / c->g.dx,
-                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, c->E32, c->E64);
+                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, c->E32, c->E4, c->E64);
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }

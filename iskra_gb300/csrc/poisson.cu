@@ -95,6 +95,11 @@ struct Poisson {
   double *low = nullptr, *up = nullptr;        // nx
   double *inv = nullptr, *cp = nullptr, *q = nullptr;  // nx*K
   double *gk = nullptr;         // 2K: 1/(1+v.q) and β/γ per mode (x-periodic)
+  int cr_levels = 0;            // cyclic reduction: L = floor(log2 nx)
+  double2 *cr_fwd = nullptr;    // (α, γ) per updated row and mode
+  double2 *cr_back = nullptr;   // (a/b, c/b) per eliminated row and mode
+  double *cr_backb = nullptr;   // 1/b per eliminated row and mode
+  double *cr_top = nullptr;     // 1/b of the last row per mode
   int pin_k0 = -1;              // pinned column of mode 0 (singular)
   // drives on device
   int ndrive_nodes = 0;
@@ -131,6 +136,10 @@ void poisson_destroy(Poisson *p) {
   cudaFree(p->cp);
   cudaFree(p->q);
   cudaFree(p->gk);
+  cudaFree(p->cr_fwd);
+  cudaFree(p->cr_back);
+  cudaFree(p->cr_backb);
+  cudaFree(p->cr_top);
   cudaFree(p->drive_node);
   cudaFree(p->drive_group);
   cudaFree(p->drive_par);
@@ -350,43 +359,140 @@ __global__ void k_fft_fwd(const double *__restrict__ r, int nx, int N, int logN,
   }
 }
 
-// per Fourier mode: tridiagonal solve along x (in place in spec)
-__global__ void k_tridiag(double2 *__restrict__ spec, int nx, int K, const double *__restrict__ low,
-                          const double *__restrict__ up, const double *__restrict__ inv, const double *__restrict__ cp,
-                          const double *__restrict__ q, const double *__restrict__ gk, int cyclic, int pin0,
-                          const PoissonScal *__restrict__ sc) {
+// Per Fourier mode and per real/imaginary part (one thread each): Thomas
+// forward elimination and back substitution along x with the precomputed
+// factors, in place in spec; Sherman-Morrison correction for x-periodic
+// operators.  Rows are fetched in chunks of kTriChunk so that the chunk's
+// loads are in flight together instead of one L2 round trip per row of the
+// dependent recurrence.
+constexpr int kTriChunk = 16;
+
+__global__ void __launch_bounds__(64) k_tridiag(double *__restrict__ spec, int nx, int K,
+                                                const double *__restrict__ low, const double *__restrict__ inv,
+                                                const double *__restrict__ cp, const double *__restrict__ q,
+                                                const double *__restrict__ gk, int cyclic, int pin0,
+                                                const PoissonScal *__restrict__ sc) {
   if (sc->done) return;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = t >> 1, part = t & 1;
   if (k >= K) return;
-  // forward elimination
-  double2 y = make_double2(0, 0);
-  for (int i = 0; i < nx; i++) {
-    const size_t o = (size_t)i * K + k;
-    double2 rv = spec[o];
-    const double a = i > 0 ? low[i] : 0.0;
-    const double iv = inv[o];
-    y = make_double2((rv.x - a * y.x) * iv, (rv.y - a * y.y) * iv);
-    spec[o] = y;
+  const size_t K2 = 2 * (size_t)K;
+  double *__restrict__ col = spec + 2 * (size_t)k + part;  // row i at col[i * K2]
+  double y = 0.0;
+  for (int i0 = 0; i0 < nx; i0 += kTriChunk) {
+    double r[kTriChunk], iv[kTriChunk], a[kTriChunk];
+#pragma unroll
+    for (int c = 0; c < kTriChunk; c++) {
+      const int i = i0 + c;
+      if (i < nx) {
+        r[c] = col[i * K2];
+        iv[c] = inv[(size_t)i * K + k];
+        a[c] = i > 0 ? __ldg(low + i) : 0.0;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < kTriChunk; c++) {
+      const int i = i0 + c;
+      if (i < nx) {
+        y = (r[c] - a[c] * y) * iv[c];
+        col[i * K2] = y;
+      }
+    }
   }
-  // back substitution
-  double2 xn = y;
-  for (int i = nx - 2; i >= 0; i--) {
-    const size_t o = (size_t)i * K + k;
-    double2 yv = spec[o];
-    const double c = cp[o];
-    xn = make_double2(yv.x - c * xn.x, yv.y - c * xn.y);
-    spec[o] = xn;
+  double xn = y;
+  for (int i1 = nx - 2; i1 >= 0; i1 -= kTriChunk) {
+    double yv[kTriChunk], cv[kTriChunk];
+#pragma unroll
+    for (int c = 0; c < kTriChunk; c++) {
+      const int i = i1 - c;
+      if (i >= 0) {
+        yv[c] = col[i * K2];
+        cv[c] = cp[(size_t)i * K + k];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < kTriChunk; c++) {
+      const int i = i1 - c;
+      if (i >= 0) {
+        xn = yv[c] - cv[c] * xn;
+        col[i * K2] = xn;
+      }
+    }
   }
   if (cyclic && !(k == 0 && pin0 >= 0)) {
-    const double2 x0 = spec[k], xl = spec[(size_t)(nx - 1) * K + k];
-    const double g = gk[k], vfac = gk[K + k];
-    const double2 f = make_double2((x0.x + vfac * xl.x) * g, (x0.y + vfac * xl.y) * g);
-    for (int i = 0; i < nx; i++) {
-      const size_t o = (size_t)i * K + k;
-      const double qq = q[o];
-      double2 v = spec[o];
-      spec[o] = make_double2(v.x - f.x * qq, v.y - f.y * qq);
+    const double x0 = col[0], xl = col[(size_t)(nx - 1) * K2];
+    const double f = (x0 + gk[K + k] * xl) * gk[k];
+    for (int i = 0; i < nx; i++) col[i * K2] -= f * q[(size_t)i * K + k];
+  }
+}
+
+// The same per-mode solve as k_tridiag by cyclic reduction in shared memory:
+// a block holds G consecutive Fourier modes (real and imaginary parts, 2G
+// columns of nx rows); level l of the forward pass updates rows (m+1)2^(l+1)-1
+// from rows at distance 2^l, the back substitution recovers the rows
+// eliminated at each level.  The coefficients of every level are precomputed
+// per mode on the host, so the device work is one FMA pair per row and level.
+__global__ void __launch_bounds__(256) k_tridiag_cr(double *__restrict__ spec, int nx, int K, int G, int L,
+                                                    const double2 *__restrict__ fwd, const double2 *__restrict__ back,
+                                                    const double *__restrict__ backb, const double *__restrict__ top,
+                                                    const double *__restrict__ q, const double *__restrict__ gk,
+                                                    int cyclic, int pin0, const PoissonScal *__restrict__ sc) {
+  extern __shared__ double dsh[];  // [col][nx], col = 2 (k - k0) + part
+  if (sc->done) return;
+  const int k0 = blockIdx.x * G;
+  const int ncol = 2 * min(G, K - k0);
+  for (int t = threadIdx.x; t < nx * ncol; t += blockDim.x) {
+    const int i = t / ncol, col = t - i * ncol;
+    const int k = k0 + (col >> 1);
+    double v = spec[((size_t)i * K + k) * 2 + (col & 1)];
+    if (pin0 >= 0 && k == 0 && i == pin0) v = 0.0;  // pinned row of the singular mode
+    dsh[col * nx + i] = v;
+  }
+  __syncthreads();
+  size_t F = 0, B = 0;
+  for (int l = 0; l < L; l++) {
+    const int s = 1 << l, cnt = nx >> (l + 1);
+    for (int t = threadIdx.x; t < cnt * ncol; t += blockDim.x) {
+      const int m = t / ncol, col = t - m * ncol;
+      const int k = k0 + (col >> 1);
+      const int i = (m + 1) * 2 * s - 1;
+      const double2 ag = fwd[(F + m) * K + k];
+      double *dc = dsh + col * nx;
+      double v = dc[i] - ag.x * dc[i - s];
+      if (i + s < nx) v -= ag.y * dc[i + s];
+      dc[i] = v;
     }
+    F += cnt;
+    B += ((nx >> l) + 1) >> 1;
+    __syncthreads();
+  }
+  const int topr = (1 << L) - 1;
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) dsh[col * nx + topr] *= top[k0 + (col >> 1)];
+  __syncthreads();
+  for (int l = L - 1; l >= 0; l--) {
+    const int s = 1 << l, ecnt = ((nx >> l) + 1) >> 1;
+    B -= ecnt;
+    for (int t = threadIdx.x; t < ecnt * ncol; t += blockDim.x) {
+      const int m = t / ncol, col = t - m * ncol;
+      const int k = k0 + (col >> 1);
+      const int j = (2 * m + 1) * s - 1;
+      const size_t o = (B + m) * K + k;
+      const double2 r = back[o];
+      double *dc = dsh + col * nx;
+      double x = backb[o] * dc[j];
+      if (j - s >= 0) x -= r.x * dc[j - s];
+      if (j + s < nx) x -= r.y * dc[j + s];
+      dc[j] = x;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < nx * ncol; t += blockDim.x) {
+    const int i = t / ncol, col = t - i * ncol;
+    const int k = k0 + (col >> 1);
+    const double *dc = dsh + col * nx;
+    double v = dc[i];
+    if (cyclic && !(k == 0 && pin0 >= 0)) v -= (dc[0] + gk[K + k] * dc[nx - 1]) * gk[k] * q[(size_t)i * K + k];
+    spec[((size_t)i * K + k) * 2 + (col & 1)] = v;
   }
 }
 
@@ -916,6 +1022,12 @@ static int build_device(Ctx *c, Poisson *P) {
   cudaFree(P->cp);
   cudaFree(P->q);
   cudaFree(P->gk);
+  cudaFree(P->cr_fwd);
+  cudaFree(P->cr_back);
+  cudaFree(P->cr_backb);
+  cudaFree(P->cr_top);
+  P->cr_fwd = P->cr_back = nullptr;
+  P->cr_backb = P->cr_top = nullptr;
   P->spec = nullptr;
   P->tw = nullptr;
   P->low = P->up = P->inv = P->cp = P->q = P->gk = nullptr;
@@ -952,6 +1064,15 @@ static int build_device(Ctx *c, Poisson *P) {
     const int pin = singular ? 0 : -1;  // singular => no fixed column, pin column 0 of mode 0
     P->pin_k0 = pin;
     std::vector<double> inv((size_t)nx * K), cpv((size_t)nx * K), qv(cyclic ? (size_t)nx * K : 1), gkv(2 * K, 0.0);
+    int cr_levels = 0;
+    while ((2 << cr_levels) <= nx) cr_levels++;  // L = floor(log2 nx)
+    size_t cr_nf = 0, cr_nb = 0;
+    for (int l = 0; l < cr_levels; l++) {
+      cr_nf += nx >> (l + 1);
+      cr_nb += ((nx >> l) + 1) >> 1;
+    }
+    std::vector<double2> cr_fwd(cr_nf * K), cr_back(cr_nb * K);
+    std::vector<double> cr_backb(cr_nb * K), cr_top(K);
     for (int k = 0; k < K; k++) {
       double vfac = 0;
       const double ck = std::cos(2.0 * M_PI * k / N);
@@ -967,7 +1088,7 @@ static int build_device(Ctx *c, Poisson *P) {
         diag[0] -= gamma;
         diag[nx - 1] -= corner_up * corner_lo / gamma;
       }
-      // Thomas factors
+      // Thomas factors (host: the Sherman-Morrison vector q below)
       double cprev = 0;
       for (int i = 0; i < nx; i++) {
         const size_t o = (size_t)i * K + k;
@@ -983,6 +1104,48 @@ static int build_device(Ctx *c, Poisson *P) {
         inv[o] = 1.0 / den;
         cprev = (i < nx - 1 ? uk[i] : 0.0) / den;
         cpv[o] = cprev;
+      }
+      // cyclic-reduction coefficients of T' (device solve).  Level l (stride
+      // s = 2^l) updates rows i = (m+1)2s-1 from rows i-s, i+s and eliminates
+      // rows j = (2m+1)s-1, which the back substitution recovers from rows j-s,
+      // j+s; the last row left is 2^L-1, L = floor(log2 nx).
+      {
+        std::vector<double> a(nx), b(diag), cc(nx);
+        for (int i = 0; i < nx; i++) {
+          a[i] = i > 0 ? lk[i] : 0.0;
+          cc[i] = i < nx - 1 ? uk[i] : 0.0;
+        }
+        if (pinned) {  // identity row; the kernel zeroes its right-hand side
+          a[pin] = 0.0;
+          cc[pin] = 0.0;
+          b[pin] = 1.0;
+        }
+        size_t F = 0, B = 0;
+        for (int l = 0; l < cr_levels; l++) {
+          const int s = 1 << l;
+          const int ecnt = ((nx >> l) + 1) >> 1, cnt = nx >> (l + 1);
+          for (int m = 0; m < ecnt; m++) {
+            const int j = (2 * m + 1) * s - 1;
+            if (b[j] == 0.0) return set_err(c, ISKRA_EINVAL, "singular tridiagonal mode in the Poisson factorisation");
+            const size_t o = (B + m) * K + k;
+            cr_back[o] = make_double2(a[j] / b[j], cc[j] / b[j]);
+            cr_backb[o] = 1.0 / b[j];
+          }
+          for (int m = 0; m < cnt; m++) {
+            const int i = (m + 1) * 2 * s - 1, im = i - s, ip = i + s;
+            const double al = a[i] / b[im];
+            const double ga = ip < nx ? cc[i] / b[ip] : 0.0;
+            cr_fwd[(F + m) * K + k] = make_double2(al, ga);
+            b[i] = b[i] - al * cc[im] - (ip < nx ? ga * a[ip] : 0.0);
+            a[i] = -al * a[im];
+            cc[i] = ip < nx ? -ga * cc[ip] : 0.0;
+          }
+          F += cnt;
+          B += ecnt;
+        }
+        const int top = (1 << cr_levels) - 1;
+        if (b[top] == 0.0) return set_err(c, ISKRA_EINVAL, "singular tridiagonal mode in the Poisson factorisation");
+        cr_top[k] = 1.0 / b[top];
       }
       if (cyc) {
         // q = T'^{-1} u, u = [γ, 0, ..., 0, α], α = T[nx-1][0]
@@ -1017,6 +1180,18 @@ static int build_device(Ctx *c, Poisson *P) {
     ISKRA_CUDA(c, cudaMemcpy(P->inv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice));
     ISKRA_CUDA(c, cudaMemcpy(P->cp, cpv.data(), cpv.size() * sizeof(double), cudaMemcpyHostToDevice));
     ISKRA_CUDA(c, cudaMemcpy(P->gk, gkv.data(), 2 * K * sizeof(double), cudaMemcpyHostToDevice));
+    P->cr_levels = cr_levels;
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_fwd, std::max<size_t>(1, cr_fwd.size()) * sizeof(double2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_back, std::max<size_t>(1, cr_back.size()) * sizeof(double2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_backb, std::max<size_t>(1, cr_backb.size()) * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_top, K * sizeof(double)));
+    if (!cr_fwd.empty())
+      ISKRA_CUDA(c, cudaMemcpy(P->cr_fwd, cr_fwd.data(), cr_fwd.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    if (!cr_back.empty()) {
+      ISKRA_CUDA(c, cudaMemcpy(P->cr_back, cr_back.data(), cr_back.size() * sizeof(double2), cudaMemcpyHostToDevice));
+      ISKRA_CUDA(c, cudaMemcpy(P->cr_backb, cr_backb.data(), cr_backb.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    ISKRA_CUDA(c, cudaMemcpy(P->cr_top, cr_top.data(), K * sizeof(double), cudaMemcpyHostToDevice));
     if (cyclic) {
       ISKRA_CUDA(c, cudaMalloc(&P->q, qv.size() * sizeof(double)));
       ISKRA_CUDA(c, cudaMemcpy(P->q, qv.data(), qv.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -1049,20 +1224,34 @@ static OpView opview(Poisson *P) {
   return o;
 }
 
-// columns per FFT block: up to 64 KB of double2 per block (two blocks per SM)
-static int fft_ti(int N) {
-  int ti = 4096 / N;
+// Columns per FFT block: enough blocks to cover every SM twice, at most 64 KB
+// of double2 per block.
+static int fft_ti(int N, int nx, int sms) {
+  int ti = nx / (2 * sms);
+  const int cap = 4096 / N < 16 ? 4096 / N : 16;
+  if (ti > cap) ti = cap;
   if (ti < 1) ti = 1;
-  if (ti > 16) ti = 16;
   return ti;
 }
 
+// Fourier modes per cyclic-reduction block (2G columns of nx doubles); 0 when
+// nx is too large for shared memory (the chunked Thomas kernel is used then).
+static int cr_modes_per_block(int nx) {
+  if (2 * (size_t)nx * sizeof(double) > 96 * 1024) return 0;
+  int g = 1024 / nx;
+  return g < 1 ? 1 : (g > 8 ? 8 : g);
+}
+
 static int fft_smem_attr(Ctx *c, int N) {
-  const int smem = fft_ti(N) * N * (int)sizeof(double2);
+  const int smem = fft_ti(N, c->ps->nx, c->num_sms) * N * (int)sizeof(double2);
   if (smem > 48 * 1024) {
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   }
+  const int G = cr_modes_per_block(c->ps->nx);
+  const int crsm = 2 * G * c->ps->nx * (int)sizeof(double);
+  if (G && crsm > 48 * 1024)
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_tridiag_cr, cudaFuncAttributeMaxDynamicSharedMemorySize, crsm));
   return ISKRA_OK;
 }
 
@@ -1092,13 +1281,20 @@ static int solve_queue(Ctx *c, double rtol, int max_sweeps, double dt_for_drive,
     k_check<<<1, T, 0, st>>>(P->part, B, kPartials, P->scal, rtol2, 0);
   }
   if (P->separable) {
-    const int N = P->N, K = P->K, TI = fft_ti(N);
+    const int N = P->N, K = P->K, TI = fft_ti(N, P->nx, c->num_sms);
     const int fb = (P->nx + TI - 1) / TI;
     const size_t smem = (size_t)TI * N * sizeof(double2);
     for (int s = 0; s < max_sweeps; s++) {
       k_fft_fwd<<<fb, 256, smem, st>>>(P->r, P->nx, N, P->logN, TI, P->tw, P->spec, P->scal);
-      k_tridiag<<<(K + 63) / 64, 64, 0, st>>>(P->spec, P->nx, K, P->low, P->up, P->inv, P->cp, P->q, P->gk,
-                                              P->cyclic, P->pin_k0, P->scal);
+      const int G = cr_modes_per_block(P->nx);
+      if (G) {
+        k_tridiag_cr<<<(K + G - 1) / G, 256, (size_t)2 * G * P->nx * sizeof(double), st>>>(
+            (double *)P->spec, P->nx, K, G, P->cr_levels, P->cr_fwd, P->cr_back, P->cr_backb, P->cr_top, P->q, P->gk,
+            P->cyclic, P->pin_k0, P->scal);
+      } else {
+        k_tridiag<<<(2 * K + 63) / 64, 64, 0, st>>>((double *)P->spec, P->nx, K, P->low, P->inv, P->cp, P->q, P->gk,
+                                                    P->cyclic, P->pin_k0, P->scal);
+      }
       k_fft_inv_update<<<fb, 256, smem, st>>>(P->spec, P->nx, N, P->logN, TI, P->tw, op, P->x, P->scal);
       k_residual<<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, P->part, kPartials, nn, P->singular, 1);
       k_check<<<1, T, 0, st>>>(P->part, B, kPartials, P->scal, rtol2, 1);

@@ -510,3 +510,122 @@ class PoissonOracle:
         b = self.rhs(f)
         r = b - self.A @ x
         return np.linalg.norm(r) / max(np.linalg.norm(b), 1e-300)
+
+
+# ----------------------------------------------------------------------------
+# The time loop body of ParticleInCell.solve (ParticleInCell.jl:102-135)
+# ----------------------------------------------------------------------------
+
+class SpeciesStore:
+    """KineticSpecies{2,3} host store (pic/kinetic.jl:1-18): (cap,2)/(cap,3) F-order."""
+
+    def __init__(self, q, m, w0, cap, x, v):
+        self.q, self.m, self.w0, self.cap = q, m, w0, cap
+        self.x = np.zeros((cap, 2), order="F")
+        self.v = np.zeros((cap, 3), order="F")
+        n = len(x)
+        self.x[:n] = x
+        self.v[:n] = v
+        self.np = n
+        self.bnd = (0, 0)       # after_push per axis: 0 none, 1 wrap!, 2 discard!
+        self.absorbed = [0, 0, 0, 0]
+
+
+class PicOracle:
+    """MCC sets -> advance! every species -> circuit -> density/ρ -> ϕ -> E,
+    each stage by the restatements above."""
+
+    def __init__(self, nx, ny, dx, dy, eps0, bcs=(0, 0, 0, 0)):
+        self.nx, self.ny, self.dx, self.dy, self.bcs = nx, ny, dx, dy, bcs
+        self.ps = PoissonOracle(nx, ny, dx, dy, eps0)
+        self.species = []
+        self.mccs = []          # (MCCOracle, source index, product index or None, gas density)
+        self.circuit = None
+        self.E = np.zeros((nx, ny, 3), order="F")
+        self.phi = np.zeros((nx, ny), order="F")
+        self.rho = np.zeros((nx, ny), order="F")
+        self.background = None
+        self.counts = []
+
+    def add_species(self, q, m, w0, cap, x, v, bnd=(0, 0)):
+        s = SpeciesStore(q, m, w0, cap, x, v)
+        s.bnd = bnd
+        self.species.append(s)
+        return len(self.species) - 1
+
+    def add_mcc(self, mcc, src, prod, gas_n):
+        self.mccs.append((mcc, src, prod, np.asfortranarray(gas_n, dtype=float)))
+        self.counts.append(np.zeros(mcc.N, dtype=np.int64))
+
+    def drive_dirichlet(self, nodes, amp, freq, phase=0.0, dc=0.0):
+        """A problem's iteration hook calling apply_dirichlet(solver, nodes, V(t))
+        after step n-1 (problem/11_rf_discharge.jl:93): the solve of step n
+        (n >= 2) uses V((n-2)Δt)."""
+        self.drives = getattr(self, "drives", []) + [(np.asarray(nodes, bool), amp, freq, phase, dc)]
+        self.nstep = getattr(self, "nstep", 0)
+
+    def set_circuit(self, R, L, C, amp, freq, dc, dof, pos_ref, neg_ref, area, scale=1.0, wall=0):
+        """advance!(::CircuitRLC) (circuit_coupling.jl:35-43, Circuit.jl:117-136);
+        pos_ref/neg_ref: (i, j) 0-based reference nodes; wall: discard! wall whose
+        absorbed charge lands on the floating electrode (0 = x-low)."""
+        self.circuit = dict(R=R, L=L, C=C, amp=amp, freq=freq, dc=dc, dof=dof, pos=pos_ref, neg=neg_ref,
+                            area=area, scale=scale, wall=wall, state=np.zeros(3), absorbed_seen=None)
+
+    def step(self, dt, seed):
+        nx, ny, dx, dy = self.nx, self.ny, self.dx, self.dy
+        for k, (m, si, pi, gas) in enumerate(self.mccs):
+            S = self.species[si]
+            P = self.species[pi] if pi is not None else None
+            snp, pnp, c = m.perform(self.E, gas, dx, dy, dt, S.x, S.v, S.np, seed + 7919 * k,
+                                    None if P is None else P.x, None if P is None else P.v,
+                                    0 if P is None else P.np)
+            S.np = snp
+            if P is not None:
+                P.np = pnp
+            self.counts[k] += c
+        for S in self.species:
+            n = S.np
+            x = np.asfortranarray(S.x[:n])
+            v = np.asfortranarray(S.v[:n])
+            pu = grid_to_particle(self.E, dx, dy, x)
+            push_cartesian(x, v, pu, None, S.q / S.m, dt)
+            for d, (mode, nn_, h) in enumerate(((S.bnd[0], nx, dx), (S.bnd[1], ny, dy))):
+                if mode == 2:
+                    wg = np.full(len(x), S.w0)
+                    npn, lo, hi = discard(x, v, wg, None, S.w0, d, nn_, h)
+                    x, v = np.asfortranarray(x[:npn]), np.asfortranarray(v[:npn])
+                    S.absorbed[2 * d] += lo
+                    S.absorbed[2 * d + 1] += hi
+            for d, (mode, nn_, h) in enumerate(((S.bnd[0], nx, dx), (S.bnd[1], ny, dy))):
+                if mode == 1:
+                    wrap(x, d, nn_, h)
+            S.np = len(x)
+            S.x[:S.np] = x
+            S.v[:S.np] = v
+        if self.circuit is not None:
+            c = self.circuit
+            vext = self.phi[c["pos"]] - self.phi[c["neg"]]
+            st = c["state"]
+            vsrc = c["amp"] * np.sin(2 * np.pi * c["freq"] * st[2]) + c["dc"]
+            c["state"] = advance_circuit(c["R"], c["L"], c["C"], st, vext, vsrc, dt)
+            ds = -dt * c["state"][0] / c["area"] * c["scale"]
+            seen = c["absorbed_seen"] or [0] * len(self.species)
+            for s, S in enumerate(self.species):
+                ds += S.q * S.w0 * (S.absorbed[c["wall"]] - seen[s]) / c["area"]
+            c["absorbed_seen"] = [S.absorbed[c["wall"]] for S in self.species]
+            self.ps.set_sigma(c["dof"], self.ps.sig_b[c["dof"] - 1] + ds)
+            c["vext"] = vext
+        rho = np.zeros((nx, ny), order="F")
+        V = cell_volume(nx, ny, dx, dy, self.bcs)
+        for S in self.species:
+            u = particle_to_grid(nx, ny, dx, dy, S.x[:S.np], None, S.w0)
+            rho += S.q * (u / V)
+        if self.background is not None:
+            rho += self.background
+        self.rho = rho
+        self.nstep = getattr(self, "nstep", 0) + 1
+        if self.nstep >= 2:
+            for mask, amp, freq, phase, dc in getattr(self, "drives", []):
+                self.ps.apply_dirichlet(mask, amp * np.sin(2 * np.pi * freq * (self.nstep - 2) * dt + phase) + dc)
+        self.phi = self.ps.solve(-rho)
+        self.E = electric_field(self.phi, dx, dy)

@@ -13,6 +13,12 @@ def pytest_configure(config):
 
 
 @pytest.fixture(scope="session")
+def lib():
+    from iskra_gb300 import _lib
+    return _lib
+
+
+@pytest.fixture(scope="session")
 def orc():
     from oracle import oracle
     oracle.lib()

@@ -69,7 +69,7 @@ typedef struct iskra_ctx iskra_ctx;
  * (ParticleInCell.jl:28-35) while wrap!/discard! use it, so other origins
  * are inconsistent in the reference itself. */
 typedef struct {
-  int32_t nx, ny;   /* nodes; 2 <= nx,ny <= 65535 */
+  int32_t nx, ny;   /* nodes; 2 <= nx <= 65535, 2 <= ny <= 32768, nx*ny <= 2^30 */
   double dx, dy;    /* node spacing (Δh) */
   double ox, oy;    /* origin, must be 0 */
   int32_t bc[4];

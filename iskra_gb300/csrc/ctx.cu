@@ -1,4 +1,5 @@
 // ctx.cu -- context, species store, host<->device conversion, error plumbing.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -144,8 +145,10 @@ extern "C" {
 int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
   if (!g || !out) return ISKRA_EINVAL;
   *out = nullptr;
-  if (g->nx < 2 || g->ny < 2 || g->nx > 65535 || g->ny > 65535 || !(g->dx > 0) || !(g->dy > 0))
+  // a particle's cell is packed as i0 | j0 << 16 in a non-negative int
+  if (g->nx < 2 || g->ny < 2 || g->nx > 65535 || g->ny > 32768 || !(g->dx > 0) || !(g->dy > 0))
     return ISKRA_EINVAL;
+  if ((long long)g->nx * g->ny > (1LL << 30)) return ISKRA_EINVAL;
   if (g->ox != 0.0 || g->oy != 0.0) return ISKRA_EINVAL;
   iskra_ctx *h = new (std::nothrow) iskra_ctx();
   if (!h) return ISKRA_ENOMEM;
@@ -154,6 +157,10 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
   c->nx = g->nx;
   c->ny = g->ny;
   c->nn = g->nx * g->ny;
+  c->tiles_x = (std::max(g->nx - 1, 1) + kTile - 1) / kTile;
+  c->tiles_y = (std::max(g->ny - 1, 1) + kTile - 1) / kTile;
+  c->ntiles = c->tiles_x * c->tiles_y;
+  c->nkeys = c->ntiles * kTile * kTile;
   auto fail = [&](int rc) {
     iskra_ctx_destroy(h);
     return rc;
@@ -175,9 +182,9 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
             cudaMalloc(&c->vol_inv, nn * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&c->d_err, sizeof(int)) == cudaSuccess &&
             cudaMallocHost(&c->h_err, sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&c->cell_count, (nn + 1) * sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&c->cell_cursor, (nn + 1) * sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&c->scan_tmp, 4096 * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->cell_count, ((size_t)c->nkeys + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->cell_cursor, ((size_t)c->nkeys + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->scan_tmp, ((size_t)c->nkeys / 4096 + 2) * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&c->d_step, sizeof(unsigned long long)) == cudaSuccess;
   if (!ok) return fail(ISKRA_ENOMEM);
   cudaMemsetAsync(c->E32, 0, nn * sizeof(float2), c->stream);
@@ -220,6 +227,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
     cudaFree(s.dev.st);
     cudaFree(s.dev.acc);
     cudaFree(s.dev.cnt);
+    cudaFree(s.dev.tile_begin);
     cudaFree(s.n);
   }
   for (auto *m : c->mccs) mcc_destroy(m);
@@ -278,6 +286,8 @@ int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t ca
   ISKRA_CUDA(c, cudaMalloc(&s.dev.st, sizeof(SpeciesState)));
   ISKRA_CUDA(c, cudaMalloc(&s.dev.acc, nn * sizeof(unsigned long long)));
   ISKRA_CUDA(c, cudaMalloc(&s.dev.cnt, nn * sizeof(unsigned)));
+  ISKRA_CUDA(c, cudaMalloc(&s.dev.tile_begin, ((size_t)c->ntiles + 1) * sizeof(int)));
+  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.tile_begin, 0, ((size_t)c->ntiles + 1) * sizeof(int), c->stream));
   ISKRA_CUDA(c, cudaMalloc(&s.n, nn * sizeof(double)));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.st, 0, sizeof(SpeciesState), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, nn * sizeof(unsigned long long), c->stream));
@@ -432,6 +442,7 @@ int iskra_field_upload_E(iskra_ctx *h, const double *E) {
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   ISKRA_CUDA(c, cudaMemcpyAsync(c->stage, E, (size_t)c->nn * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   k_upload_E<<<(c->nn + 255) / 256, 256, 0, c->stream>>>(c->stage, c->nx, c->ny, c->E32, c->E4, c->E64);
+  c->e_from_phi = false;
   ISKRA_CUDA(c, cudaGetLastError());
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   return ISKRA_OK;

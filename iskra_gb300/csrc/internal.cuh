@@ -46,6 +46,7 @@ struct SpeciesState {          // device-resident, written by kernels
   unsigned int next_id;        // identifier for appended particles
   unsigned int pad2;
   long long np_new;            // append cursor used while a kernel appends
+  long long sorted_n;          // slots [0, sorted_n) are grouped by tile (last sort); the rest is unsorted
 };
 
 struct SpeciesDev {            // kernel view of one species (by value)
@@ -56,7 +57,21 @@ struct SpeciesDev {            // kernel view of one species (by value)
   unsigned long long *acc;     // (nx*ny) fixed-point deposit accumulator
   long long cap;
   unsigned *cnt;               // (nx*ny) particles deposited per cell (overflow guard)
+  int *tile_begin;             // (ntiles + 1) first slot of each tile after the last sort
 };
+
+// Tiles: the push runs one block per tile of kTile x kTile cells over the
+// particles the last sort grouped there, with the E records and the deposit
+// of the tile and a kHalo-cell margin in shared memory.  The sort key of a
+// cell is tile-major: tile * kTile^2 + the cell's position in the tile.
+constexpr int kTile = 16;
+constexpr int kTileShift = 4;
+constexpr int kHalo = 2;
+
+__device__ __host__ __forceinline__ int cell_key(int i0, int j0, int tiles_x) {
+  const int t = (i0 >> kTileShift) + tiles_x * (j0 >> kTileShift);
+  return (t << (2 * kTileShift)) + (i0 & (kTile - 1)) + ((j0 & (kTile - 1)) << kTileShift);
+}
 
 // Buffer of a double-buffered array without dynamic indexing of a kernel
 // parameter (which would place the parameter struct in local memory).
@@ -102,6 +117,7 @@ struct CircuitDev {            // device-resident circuit state (FP64)
 struct Ctx {
   iskra_grid_t g{};
   int nx = 0, ny = 0, nn = 0;
+  int tiles_x = 0, tiles_y = 0, ntiles = 0, nkeys = 0;  // push tiles; sort keys = ntiles * kTile^2
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int device = 0, num_sms = 0;
@@ -111,14 +127,15 @@ struct Ctx {
   float2 *E32 = nullptr;       // (nx*ny) {Ex, Ey} at the nodes (MCC target term)
   float4 *E4 = nullptr;        // (nx*ny*2) per cell: the 4 corner fields, gather input
   double *E64 = nullptr;       // (nx*ny*3) download scratch
+  bool e_from_phi = false;     // E comes from the last solve (E64 is rebuilt from ϕ on download)
   double *rho = nullptr;       // (nx*ny)
   double *rho_bg = nullptr;    // optional background charge density
   double *vol_inv = nullptr;   // 1 / cell_volume
   int *d_err = nullptr;        // device error flags
   int *h_err = nullptr;        // pinned mirror
   // scratch for scans / sort
-  int *cell_count = nullptr;   // (nx*ny + 1)
-  int *cell_cursor = nullptr;  // (nx*ny + 1)
+  int *cell_count = nullptr;   // (nkeys + 1)
+  int *cell_cursor = nullptr;  // (nkeys + 1)
   int *scan_tmp = nullptr;
   double *stage = nullptr;     // upload/download staging (device)
   size_t stage_bytes = 0;
@@ -164,6 +181,7 @@ int launch_advance(Ctx *c, int sid, float dt);
 int launch_deposit(Ctx *c, int sid);
 int launch_charge_density(Ctx *c);
 int launch_efield_from(Ctx *c, const double *phi);
+int launch_efield64(Ctx *c, const double *phi);
 int launch_sort(Ctx *c, int sid);
 int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host);
 int launch_circuit(Ctx *c, double dt);

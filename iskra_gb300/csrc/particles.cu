@@ -31,6 +31,7 @@ struct PushParams {
   float dtdx, dtdy; // Δt/Δx, Δt/Δy
   int nx, ny;
   int mode_x, mode_y;
+  int tiles_x;      // tiles per row
 };
 
 // Moments of one particle: u, v < 2^24 and uv = hi 2^24 + lo with hi, lo < 2^24,
@@ -113,92 +114,237 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 // Minimum resident blocks per SM requested from the register allocator
 // (256-thread blocks); tuned on GB300.
 #ifndef ISKRA_PUSH_MIN_BLOCKS
-#define ISKRA_PUSH_MIN_BLOCKS 1
+#define ISKRA_PUSH_MIN_BLOCKS 5
 #endif
 
+// Shared-memory window of a tile block: the tile's cells and a kHalo-cell
+// margin (particles drift off their tile between sorts).
+constexpr int kWin = kTile + 2 * kHalo;  // window cells per axis
+constexpr int kWinN = kWin + 1;          // window nodes per axis
+constexpr int kWinCells = kWin * kWin;
+
+// Per window cell, the deposit moments of the run sums added there, in 32-bit
+// limbs that cannot overflow while the cell holds at most kMaxCell particles
+// (shared-memory atomics on 32-bit words run at ~7x the rate of 64-bit ones
+// on GB300): n; Σu as Σ(su >> 12), Σ(su & 0xfff); Σv likewise; Σuv as
+// Σ(hi >> 12), Σ(hi & 0xfff), Σ(lo >> 12), Σ(lo & 0xfff) with
+// uv = hi 2^24 + lo.  Every limb sum stays below 2^26.
+enum { kMomN, kMomUh, kMomUl, kMomVh, kMomVl, kMomHh, kMomHl, kMomLh, kMomLl, kMoms };
+
+struct PushShared {
+  float4 e[2 * kWinCells];        // E records of the window cells
+  unsigned mom[kMoms][kWinCells];  // deposit moments of the window cells
+};
+
+// One warp step over the slots base + lane: gather, Boris push, boundary
+// rules and the deposit of the new positions.  Cells inside the block's
+// window (origin ox, oy) read E from and deposit into shared memory; other
+// cells (particles that drifted off the window, the unsorted tail) use the
+// global records and 64-bit atomics.  The deposit key is the window cell, or
+// kWinCells + the global cell index, so runs never mix the two.
+template <bool PUSH, int MX, int MY, bool WIN>
+__device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
+                                          long long p, bool valid, float4 a, float2 b,
+                                          const float4 *__restrict__ E4, PushShared &sh, int ox, int oy,
+                                          const PushParams &P, unsigned ab[4], int &flags) {
+  const int nx = P.nx;
+  int key = -1;
+  Moments m = {0u, 0u, 0u, 0u};
+  if (valid) {
+    int cell = __float_as_int(b.y);
+    if (cell >= 0) {
+      int i0 = cell & 0xffff, j0 = cell >> 16;
+      float hx = a.x, hy = a.y;
+      if (PUSH) {
+        float4 r0, r1;  // the cell's corner fields
+        const int la = i0 - ox, lb = j0 - oy;
+        if (WIN && (unsigned)la < (unsigned)kWin && (unsigned)lb < (unsigned)kWin) {
+          const int w = la + kWin * lb;
+          r0 = sh.e[2 * w];
+          r1 = sh.e[2 * w + 1];
+        } else {
+          const int n0 = i0 + nx * j0;
+          r0 = __ldg(E4 + 2 * n0);
+          r1 = __ldg(E4 + 2 * n0 + 1);
+        }
+        const float gx = 1.0f - hx, gy = 1.0f - hy;
+        const float2 e00 = make_float2(r0.x, r0.y), e10 = make_float2(r0.z, r0.w);
+        const float2 e01 = make_float2(r1.x, r1.y), e11 = make_float2(r1.z, r1.w);
+        const float ex = gx * gy * e00.x + hx * gy * e10.x + gx * hy * e01.x + hx * hy * e11.x;
+        const float ey = gx * gy * e00.y + hx * gy * e10.y + gx * hy * e01.y + hx * hy * e11.y;
+        // Boris with B = 0: v- = v + hE ; v = hE + v+ (v+ = v-)
+        float vx = fmaf(P.h, ex, a.z);
+        float vy = fmaf(P.h, ey, a.w);
+        vx = fmaf(P.h, ex, vx);
+        vy = fmaf(P.h, ey, vy);
+        if (!isfinite(vx) || !isfinite(vy)) {
+          flags |= DERR_NAN;
+          cell = -1;
+        } else {
+          hx = move_axis(hx, vx * P.dtdx, i0);
+          hy = move_axis(hy, vy * P.dtdy, j0);
+          int rx = apply_boundary<MX>(i0, nx - 1);
+          int ry = rx ? 0 : apply_boundary<MY>(j0, P.ny - 1);
+          if (rx == 3 || ry == 3) {
+            flags |= DERR_DOMAIN;
+            cell = -1;
+          } else if (rx) {
+            ab[rx - 1]++;
+            cell = -1;
+          } else if (ry) {
+            ab[ry + 1]++;
+            cell = -1;
+          } else {
+            cell = i0 | (j0 << 16);
+          }
+        }
+        __stcs(xv + p, make_float4(hx, hy, vx, vy));
+        __stcs(zc + p, make_float2(b.x, __int_as_float(cell)));
+      }
+      if (cell >= 0) {
+        const int la = i0 - ox, lb = j0 - oy;
+        key = (WIN && (unsigned)la < (unsigned)kWin && (unsigned)lb < (unsigned)kWin) ? la + kWin * lb
+                                                                                        : kWinCells + i0 + nx * j0;
+        const unsigned ux = __float2uint_rn(hx * kOffScale);
+        const unsigned uy = __float2uint_rn(hy * kOffScale);
+        const unsigned long long uv = (unsigned long long)ux * uy;
+        m.su = ux;
+        m.sv = uy;
+        m.hi = (unsigned)(uv >> 24);
+        m.lo = (unsigned)uv & 0xffffffu;
+      }
+    }
+  }
+  unsigned n;
+  if (reduce_runs(key, m, n) && key >= 0) {
+    if (WIN && key < kWinCells) {
+      atomicAdd(&sh.mom[kMomN][key], n);
+      atomicAdd(&sh.mom[kMomUh][key], m.su >> 12);
+      atomicAdd(&sh.mom[kMomUl][key], m.su & 0xfffu);
+      atomicAdd(&sh.mom[kMomVh][key], m.sv >> 12);
+      atomicAdd(&sh.mom[kMomVl][key], m.sv & 0xfffu);
+      atomicAdd(&sh.mom[kMomHh][key], m.hi >> 12);
+      atomicAdd(&sh.mom[kMomHl][key], m.hi & 0xfffu);
+      atomicAdd(&sh.mom[kMomLh][key], m.lo >> 12);
+      atomicAdd(&sh.mom[kMomLl][key], m.lo & 0xfffu);
+    } else {
+      const unsigned long long U = (unsigned long long)m.su << 24, V = (unsigned long long)m.sv << 24;
+      const unsigned long long UV = ((unsigned long long)m.hi << 24) + m.lo;
+      const int g = key - kWinCells;
+      atomicAdd(s.acc + g, ((unsigned long long)n << 48) - U - V + UV);
+      atomicAdd(s.acc + g + 1, U - UV);
+      atomicAdd(s.acc + g + nx, V - UV);
+      atomicAdd(s.acc + g + nx + 1, UV);
+      atomicAdd(s.cnt + g, n);
+    }
+  }
+}
+
+// Blocks [0, ntiles) each take the particles the last sort grouped in their
+// tile: stage the window's E records, push, deposit into the window, then add
+// the window's nonzero node sums and cell counts to the global accumulators.
+// Blocks from ntiles on walk the slots appended since that sort.  Integer
+// sums: the density is the same bit for bit whichever block adds what.
 template <bool PUSH, int MX, int MY>
 __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev s, const float4 *__restrict__ E4,
-                                                                     PushParams P, int *err) {
+                                                                     PushParams P, int ntiles, int *err) {
+  __shared__ PushShared sh;
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const long long np = s.st->np;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
   const int cur = s.st->cur;
   float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
   float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   unsigned ab[4] = {0, 0, 0, 0};
   int flags = 0;
   const int nx = P.nx;
-  for (long long base = warp * 32; base < np; base += nwarps * 32) {
-    const long long p = base + lane;
-    int key = -1;
-    Moments m = {0u, 0u, 0u, 0u};
-    if (p < np) {
-      float4 a = __ldcs(xv + p);
-      float2 b = __ldcs(zc + p);
-      int cell = __float_as_int(b.y);
-      if (cell >= 0) {
-        int i0 = cell & 0xffff, j0 = cell >> 16;
-        float hx = a.x, hy = a.y;
+  if ((int)blockIdx.x < ntiles) {
+    const int tile = blockIdx.x;
+    const long long begin = s.tile_begin[tile], end = s.tile_begin[tile + 1];
+    if (begin < end) {  // block-uniform
+      const int ox = (tile % P.tiles_x) * kTile - kHalo, oy = (tile / P.tiles_x) * kTile - kHalo;
+      for (int t = threadIdx.x; t < kWinCells; t += blockDim.x) {
         if (PUSH) {
-          const int n0 = i0 + nx * j0;
-          const float gx = 1.0f - hx, gy = 1.0f - hy;
-          const float4 r0 = __ldg(E4 + 2 * n0), r1 = __ldg(E4 + 2 * n0 + 1);  // the cell's corner fields
-          const float2 e00 = make_float2(r0.x, r0.y), e10 = make_float2(r0.z, r0.w);
-          const float2 e01 = make_float2(r1.x, r1.y), e11 = make_float2(r1.z, r1.w);
-          const float ex = gx * gy * e00.x + hx * gy * e10.x + gx * hy * e01.x + hx * hy * e11.x;
-          const float ey = gx * gy * e00.y + hx * gy * e10.y + gx * hy * e01.y + hx * hy * e11.y;
-          // Boris with B = 0: v- = v + hE ; v = hE + v+ (v+ = v-)
-          float vx = fmaf(P.h, ex, a.z);
-          float vy = fmaf(P.h, ey, a.w);
-          vx = fmaf(P.h, ex, vx);
-          vy = fmaf(P.h, ey, vy);
-          if (!isfinite(vx) || !isfinite(vy)) {
-            flags |= DERR_NAN;
-            cell = -1;
-          } else {
-            hx = move_axis(hx, vx * P.dtdx, i0);
-            hy = move_axis(hy, vy * P.dtdy, j0);
-            int rx = apply_boundary<MX>(i0, nx - 1);
-            int ry = rx ? 0 : apply_boundary<MY>(j0, P.ny - 1);
-            if (rx == 3 || ry == 3) {
-              flags |= DERR_DOMAIN;
-              cell = -1;
-            } else if (rx) {
-              ab[rx - 1]++;
-              cell = -1;
-            } else if (ry) {
-              ab[ry + 1]++;
-              cell = -1;
-            } else {
-              cell = i0 | (j0 << 16);
-            }
+          const int i = ox + t % kWin, j = oy + t / kWin;
+          if (i >= 0 && i < nx - 1 && j >= 0 && j < P.ny - 1) {
+            const int n0 = i + nx * j;
+            sh.e[2 * t] = __ldg(E4 + 2 * n0);
+            sh.e[2 * t + 1] = __ldg(E4 + 2 * n0 + 1);
           }
-          __stcs(xv + p, make_float4(hx, hy, vx, vy));
-          __stcs(zc + p, make_float2(b.x, __int_as_float(cell)));
         }
-        if (cell >= 0) {
-          key = i0 + nx * j0;
-          const unsigned ux = __float2uint_rn(hx * kOffScale);
-          const unsigned uy = __float2uint_rn(hy * kOffScale);
-          const unsigned long long uv = (unsigned long long)ux * uy;
-          m.su = ux;
-          m.sv = uy;
-          m.hi = (unsigned)(uv >> 24);
-          m.lo = (unsigned)uv & 0xffffffu;
+#pragma unroll
+        for (int q = 0; q < kMoms; q++) sh.mom[q][t] = 0u;
+      }
+      __syncthreads();
+      // each warp takes a contiguous slice of the tile's slots (cell-sorted
+      // slices touch few cells in common)
+      const long long len = end - begin;
+      const long long slice = ((len + nwb * 32 - 1) / (nwb * 32)) * 32;
+      const long long w0 = begin + wib * slice, w1 = min(end, w0 + slice);
+      // the next slot's record is loaded while this one is processed
+      bool v = w0 + lane < w1;
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+      float2 b = make_float2(0.f, 0.f);
+      if (v) {
+        a = __ldcs(xv + w0 + lane);
+        b = __ldcs(zc + w0 + lane);
+      }
+      for (long long base = w0; base < w1; base += 32) {
+        const long long nb = base + 32;
+        const bool nv = nb + lane < w1;
+        float4 a2 = a;
+        float2 b2 = b;
+        if (nv) {
+          a2 = __ldcs(xv + nb + lane);
+          b2 = __ldcs(zc + nb + lane);
         }
+        push_warp<PUSH, MX, MY, true>(s, xv, zc, base + lane, v, a, b, E4, sh, ox, oy, P, ab, flags);
+        a = a2;
+        b = b2;
+        v = nv;
+      }
+      __syncthreads();
+      // node sums from the moments of the up to four window cells around each node
+      for (int t = threadIdx.x; t < kWinN * kWinN; t += blockDim.x) {
+        const int a = t % kWinN, b = t / kWinN;
+        unsigned long long v = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int ca = a - (c & 1), cb = b - (c >> 1);  // cell whose corner (c & 1, c >> 1) is this node
+          if (ca < 0 || cb < 0 || ca >= kWin || cb >= kWin) continue;
+          const int w = ca + kWin * cb;
+          const unsigned long long n = sh.mom[kMomN][w];
+          if (!n) continue;
+          const unsigned long long U = (((unsigned long long)sh.mom[kMomUh][w] << 12) + sh.mom[kMomUl][w]) << 24;
+          const unsigned long long V = (((unsigned long long)sh.mom[kMomVh][w] << 12) + sh.mom[kMomVl][w]) << 24;
+          const unsigned long long UV =
+              ((((unsigned long long)sh.mom[kMomHh][w] << 12) + sh.mom[kMomHl][w]) << 24) +
+              (((unsigned long long)sh.mom[kMomLh][w] << 12) + sh.mom[kMomLl][w]);
+          if (c == 0) v += (n << 48) - U - V + UV;
+          else if (c == 1) v += U - UV;
+          else if (c == 2) v += V - UV;
+          else v += UV;
+        }
+        if (v) atomicAdd(s.acc + (ox + a) + nx * (oy + b), v);
+      }
+      for (int t = threadIdx.x; t < kWinCells; t += blockDim.x) {
+        const unsigned v = sh.mom[kMomN][t];
+        if (v) atomicAdd(s.cnt + (ox + t % kWin) + nx * (oy + t / kWin), v);
       }
     }
-    unsigned n;
-    if (reduce_runs(key, m, n) && key >= 0) {
-      const unsigned long long U = (unsigned long long)m.su << 24, V = (unsigned long long)m.sv << 24;
-      const unsigned long long UV = ((unsigned long long)m.hi << 24) + m.lo;
-      atomicAdd(s.acc + key, ((unsigned long long)n << 48) - U - V + UV);
-      atomicAdd(s.acc + key + 1, U - UV);
-      atomicAdd(s.acc + key + nx, V - UV);
-      atomicAdd(s.acc + key + nx + 1, UV);
-      atomicAdd(s.cnt + key, n);
+  } else {
+    const long long np = s.st->np, t0 = s.st->sorted_n;
+    const long long warp = (long long)(blockIdx.x - ntiles) * nwb + wib;
+    const long long nwarps = (long long)(gridDim.x - ntiles) * nwb;
+    for (long long base = t0 + warp * 32; base < np; base += nwarps * 32) {
+      const long long p = base + lane;
+      const bool v = p < np;
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+      float2 b = make_float2(0.f, 0.f);
+      if (v) {
+        a = __ldcs(xv + p);
+        b = __ldcs(zc + p);
+      }
+      push_warp<PUSH, MX, MY, false>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, P, ab, flags);
     }
   }
   if (PUSH) {
@@ -212,13 +358,14 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev 
   }
 }
 
-template <bool PUSH>
 static void launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
   const int T = 256;
-#define ISKRA_PUSH_CASE(MX, MY)                                                     \
-  if (P.mode_x == MX && P.mode_y == MY) {                                           \
-    k_push<PUSH, MX, MY><<<blocks, T, 0, c->stream>>>(s.dev, c->E4, P, c->d_err);  \
-    return;                                                                         \
+#define ISKRA_PUSH_CASE(MX, MY)                                                                 \
+  if (P.mode_x == MX && P.mode_y == MY) {                                                       \
+    cudaFuncSetAttribute(k_push<true, MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,  \
+                         (int)cudaSharedmemCarveoutMaxShared);                                  \
+    k_push<true, MX, MY><<<blocks, T, 0, c->stream>>>(s.dev, c->E4, P, c->ntiles, c->d_err);   \
+    return;                                                                                     \
   }
   ISKRA_PUSH_CASE(0, 0) ISKRA_PUSH_CASE(0, 1) ISKRA_PUSH_CASE(0, 2)
   ISKRA_PUSH_CASE(1, 0) ISKRA_PUSH_CASE(1, 1) ISKRA_PUSH_CASE(1, 2)
@@ -226,7 +373,10 @@ static void launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
 #undef ISKRA_PUSH_CASE
 }
 
-static int push_blocks(Ctx *c, Species &s) {
+// one block per tile plus a grid-stride set for the unsorted tail
+static int push_blocks(Ctx *c) { return c->ntiles + c->num_sms; }
+
+static int sort_blocks(Ctx *c, Species &s) {
   long long want = (s.cap + 255) / 256;
   long long maxb = (long long)c->num_sms * 8;
   if (want < 1) want = 1;
@@ -248,7 +398,8 @@ int launch_advance(Ctx *c, int sid, float dt) {
   P.ny = c->ny;
   P.mode_x = s.bnd[0];
   P.mode_y = s.bnd[1];
-  launch_push_modes<true>(c, s, P, push_blocks(c, s));
+  P.tiles_x = c->tiles_x;
+  launch_push_modes(c, s, P, push_blocks(c));
   ISKRA_CUDA(c, cudaGetLastError());
   s.acc_valid = true;  // accumulator = deposit of the pushed positions (unconsumed)
   s.acc_zero = false;
@@ -258,13 +409,17 @@ int launch_advance(Ctx *c, int sid, float dt) {
 
 int launch_deposit(Ctx *c, int sid) {
   Species &s = c->species[sid];
-  if (!s.acc_zero)
+  if (!s.acc_zero) {
     ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, (size_t)c->nn * sizeof(unsigned long long), c->stream));
     ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, (size_t)c->nn * sizeof(unsigned), c->stream));
+  }
   PushParams P{};
   P.nx = c->nx;
   P.ny = c->ny;
-  k_push<false, 0, 0><<<push_blocks(c, s), 256, 0, c->stream>>>(s.dev, c->E4, P, c->d_err);
+  P.tiles_x = c->tiles_x;
+  cudaFuncSetAttribute(k_push<false, 0, 0>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       (int)cudaSharedmemCarveoutMaxShared);
+  k_push<false, 0, 0><<<push_blocks(c), 256, 0, c->stream>>>(s.dev, c->E4, P, c->ntiles, c->d_err);
   ISKRA_CUDA(c, cudaGetLastError());
   s.acc_valid = true;
   s.acc_zero = false;
@@ -386,8 +541,10 @@ __global__ void k_efield(const double *__restrict__ phi, int nx, int ny, double 
     if (j == 0) ey = (phi[k] - phi[k + nx]) * idy1;
     else if (j == ny - 1) ey = (phi[k - nx] - phi[k]) * idy1;
     else ey = (phi[k - nx] - phi[k + nx]) * idy2;
-    E32[k] = make_float2((float)ex, (float)ey);
-    store_corners(E4, nx, ny, i, j, make_float2((float)ex, (float)ey));
+    if (E32) {
+      E32[k] = make_float2((float)ex, (float)ey);
+      store_corners(E4, nx, ny, i, j, make_float2((float)ex, (float)ey));
+    }
     E64[k] = ex;
     E64[k + nn] = ey;
     E64[k + 2 * nn] = 0.0;
@@ -404,11 +561,22 @@ int launch_efield_from(Ctx *c, const double *phi) {
   return ISKRA_OK;
 }
 
+// FP64 E of ϕ for download only: the FP32 gather fields stay as the solve left them
+int launch_efield64(Ctx *c, const double *phi) {
+  int blocks = c->num_sms * 4;
+  int need = (c->nn + 255) / 256;
+  if (need < blocks) blocks = need;
+  k_efield<<<blocks, 256, 0, c->stream>>>(phi, c->nx, c->ny, 1.0 / (2 * c->g.dx), 1.0 / c->g.dx,
+                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, nullptr, nullptr, c->E64);
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
 // ---------------------------------------------------------------------------
 // counting sort by cell (histogram -> exclusive scan -> scatter), dropping
 // discarded particles
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_hist(SpeciesDev s, int nx, int *__restrict__ count) {
+__global__ void __launch_bounds__(256) k_hist(SpeciesDev s, int tiles_x, int *__restrict__ count) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const long long np = s.st->np;
@@ -421,7 +589,7 @@ __global__ void __launch_bounds__(256) k_hist(SpeciesDev s, int nx, int *__restr
     int key = -1;
     if (p < np) {
       int cell = __float_as_int(zc[p].y);
-      if (cell >= 0) key = (cell & 0xffff) + nx * (cell >> 16);
+      if (cell >= 0) key = cell_key(cell & 0xffff, cell >> 16, tiles_x);
     }
     unsigned peers = __match_any_sync(FULL, key);
     if (key >= 0 && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(count + key, __popc(peers));
@@ -484,8 +652,10 @@ __global__ void __launch_bounds__(1024) k_scan_top(int *__restrict__ part, int n
   }
 }
 
+// out = exclusive scan of in (n + 1 entries, the last the total); tile_begin
+// receives the entries at the multiples of kTile^2 (the first slot of each tile)
 __global__ void __launch_bounds__(1024) k_scan_down(const int *__restrict__ in, int n, const int *__restrict__ part,
-                                                    int *__restrict__ out) {
+                                                    int *__restrict__ out, int *__restrict__ tile_begin) {
   __shared__ int sh[32];
   long long b0 = (long long)blockIdx.x * kScanItems;
   int v[4];
@@ -497,15 +667,22 @@ __global__ void __launch_bounds__(1024) k_scan_down(const int *__restrict__ in, 
   }
   int tot;
   int e = block_scan_excl(sum, sh, tot) + part[blockIdx.x];
+  constexpr int kKeysPerTile = kTile * kTile;
   for (int k = 0; k < 4; k++) {
     long long idx = b0 + threadIdx.x * 4 + k;
-    if (idx < n) out[idx] = e;
+    if (idx < n) {
+      out[idx] = e;
+      if (idx % kKeysPerTile == 0) tile_begin[idx / kKeysPerTile] = e;
+    }
     e += v[k];
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = e;  // grand total
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) {  // grand total
+    out[n] = e;
+    tile_begin[n / kKeysPerTile] = e;
+  }
 }
 
-__global__ void __launch_bounds__(256) k_scatter(SpeciesDev s, int nx, int *__restrict__ cursor) {
+__global__ void __launch_bounds__(256) k_scatter(SpeciesDev s, int tiles_x, int *__restrict__ cursor) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const long long np = s.st->np;
@@ -529,7 +706,7 @@ __global__ void __launch_bounds__(256) k_scatter(SpeciesDev s, int nx, int *__re
       b = zc[p];
       pid = id[p];
       int cell = __float_as_int(b.y);
-      if (cell >= 0) key = (cell & 0xffff) + nx * (cell >> 16);
+      if (cell >= 0) key = cell_key(cell & 0xffff, cell >> 16, tiles_x);
     }
     unsigned peers = __match_any_sync(FULL, key);
     int leader = __ffs(peers) - 1;
@@ -547,26 +724,27 @@ __global__ void __launch_bounds__(256) k_scatter(SpeciesDev s, int nx, int *__re
 
 __global__ void k_sort_finish(SpeciesState *st, const int *__restrict__ total) {
   st->np = *total;
+  st->sorted_n = *total;
   st->cur ^= 1;
 }
 
 int launch_sort(Ctx *c, int sid) {
   Species &s = c->species[sid];
-  const int nn = c->nn;
-  ISKRA_CUDA(c, cudaMemsetAsync(c->cell_count, 0, (size_t)(nn + 1) * sizeof(int), c->stream));
-  int blocks = push_blocks(c, s);
-  k_hist<<<blocks, 256, 0, c->stream>>>(s.dev, c->nx, c->cell_count);
+  const int nk = c->nkeys;
+  ISKRA_CUDA(c, cudaMemsetAsync(c->cell_count, 0, (size_t)(nk + 1) * sizeof(int), c->stream));
+  int blocks = sort_blocks(c, s);
+  k_hist<<<blocks, 256, 0, c->stream>>>(s.dev, c->tiles_x, c->cell_count);
   ISKRA_CUDA(c, cudaGetLastError());
-  int nb = (nn + kScanItems - 1) / kScanItems;
-  k_scan_reduce<<<nb, 1024, 0, c->stream>>>(c->cell_count, nn, c->scan_tmp);
+  int nb = (nk + kScanItems - 1) / kScanItems;
+  k_scan_reduce<<<nb, 1024, 0, c->stream>>>(c->cell_count, nk, c->scan_tmp);
   k_scan_top<<<1, 1024, 0, c->stream>>>(c->scan_tmp, nb);
-  k_scan_down<<<nb, 1024, 0, c->stream>>>(c->cell_count, nn, c->scan_tmp, c->cell_cursor);
+  k_scan_down<<<nb, 1024, 0, c->stream>>>(c->cell_count, nk, c->scan_tmp, c->cell_cursor, s.dev.tile_begin);
   ISKRA_CUDA(c, cudaGetLastError());
   // cell_count is free again: keep the grand total there for k_sort_finish
-  ISKRA_CUDA(c, cudaMemcpyAsync(c->cell_count + nn, c->cell_cursor + nn, sizeof(int), cudaMemcpyDeviceToDevice,
+  ISKRA_CUDA(c, cudaMemcpyAsync(c->cell_count + nk, c->cell_cursor + nk, sizeof(int), cudaMemcpyDeviceToDevice,
                                 c->stream));
-  k_scatter<<<blocks, 256, 0, c->stream>>>(s.dev, c->nx, c->cell_cursor);
-  k_sort_finish<<<1, 1, 0, c->stream>>>(s.dev.st, c->cell_count + nn);
+  k_scatter<<<blocks, 256, 0, c->stream>>>(s.dev, c->tiles_x, c->cell_cursor);
+  k_sort_finish<<<1, 1, 0, c->stream>>>(s.dev.st, c->cell_count + nk);
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }

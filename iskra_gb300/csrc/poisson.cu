@@ -33,8 +33,6 @@
 
 namespace iskra {
 
-int launch_efield_from(Ctx *c, const double *phi);
-
 struct RowClass {
   double c0, cW, cE, cS, cN;  // original (unscaled) coefficients
   double d;                   // symmetrising row scale
@@ -57,7 +55,7 @@ struct PoissonScal {           // device-resident solver scalars
   int iters;
   int done;
   int sweeps;
-  int pad;
+  unsigned ticket;             // blocks of the running k_residual that have finished
   double rz, rz_new, pap;
 };
 
@@ -90,16 +88,19 @@ struct Poisson {
   double dsum = 0;              // Σ d over free rows (singular projection)
   // separable solver
   int N = 0, K = 0, logN = 0;   // N = ny, K = N/2+1
-  double2 *spec = nullptr;      // nx*K
-  double2 *tw = nullptr;        // N/2 twiddles exp(-2πi m/N)
-  double *low = nullptr, *up = nullptr;        // nx
-  double *inv = nullptr, *cp = nullptr, *q = nullptr;  // nx*K
-  double *gk = nullptr;         // 2K: 1/(1+v.q) and β/γ per mode (x-periodic)
+  // (FP32 correction: factors computed in FP64 on the host, stored rounded)
+  float *r32 = nullptr;         // nn scaled residual, input of the correction
+  float2 *spec = nullptr;       // nx*K
+  float2 *tw = nullptr;         // N/2 twiddles exp(-2πi m/N)
+  float *low = nullptr, *up = nullptr;        // nx
+  float *inv = nullptr, *cp = nullptr, *q = nullptr;  // nx*K
+  float *gk = nullptr;          // 2K: 1/(1+v.q) and β/γ per mode (x-periodic)
   int cr_levels = 0;            // cyclic reduction: L = floor(log2 nx)
-  double2 *cr_fwd = nullptr;    // (α, γ) per updated row and mode
-  double2 *cr_back = nullptr;   // (a/b, c/b) per eliminated row and mode
-  double *cr_backb = nullptr;   // 1/b per eliminated row and mode
-  double *cr_top = nullptr;     // 1/b of the last row per mode
+  int cr_nf = 0, cr_nb = 0;     // updated / eliminated rows over all levels
+  float2 *cr_fwd = nullptr;     // (α, γ) per mode and updated row
+  float2 *cr_back = nullptr;    // (a/b, c/b) per mode and eliminated row
+  float *cr_backb = nullptr;    // 1/b per mode and eliminated row
+  float *cr_top = nullptr;      // 1/b of the last row per mode
   int pin_k0 = -1;              // pinned column of mode 0 (singular)
   // drives on device
   int ndrive_nodes = 0;
@@ -108,6 +109,7 @@ struct Poisson {
   double *drive_par = nullptr;  // 4 per group
   int ndrive = 0;
   int blocks = 0;
+  bool rho_fixed = false;       // some identity row takes its value from ρ (rewritten every solve)
   int last_iters = 0;
   double last_relres = 0;
 };
@@ -128,6 +130,7 @@ void poisson_destroy(Poisson *p) {
   cudaFree(p->part);
   cudaFree(p->scal);
   if (p->scal_h) cudaFreeHost(p->scal_h);
+  cudaFree(p->r32);
   cudaFree(p->spec);
   cudaFree(p->tw);
   cudaFree(p->low);
@@ -149,12 +152,17 @@ void poisson_destroy(Poisson *p) {
 // ===========================================================================
 // device kernels
 // ===========================================================================
+// cls[k] = row class id of node k, with kFixedBit set on identity (fixed) rows
+constexpr unsigned kFixedBit = 0x8000u;
+constexpr unsigned kClassMask = 0x7fffu;
+
 struct OpView {
   const uint16_t *cls;
   const RowClass *classes;
   const double *bfix;
   const double *sigma;
   int nx, ny;
+  int nclass;
 };
 
 __device__ __forceinline__ void nbr(int k, int nx, int ny, int &w, int &e, int &s, int &n) {
@@ -177,18 +185,20 @@ __global__ void k_set_fixed(OpView op, const int *__restrict__ dnode, const int 
   // driven groups update bfix (solve of step n uses V((n-2)Δt), n >= 2)
   const unsigned long long n_step = step ? *step : 0ull;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ndn; t += gridDim.x * blockDim.x) {
+    const int k = dnode[t];
     if (n_step >= 2) {
       double tt = (double)(n_step - 2) * dt;
-      bfix_mut[dnode[t]] = drive_value(dpar + 4 * dgroup[t], tt);
+      bfix_mut[k] = drive_value(dpar + 4 * dgroup[t], tt);
     }
+    x[k] = bfix_mut[k];
   }
 }
 
 __global__ void k_fixed_to_x(OpView op, double *__restrict__ x, const double *__restrict__ rho, double neg_inv_eps0,
                              int nn) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const RowClass &C = op.classes[op.cls[k]];
-    if (C.fixed) x[k] = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+    const unsigned ck = op.cls[k];
+    if (ck & kFixedBit) x[k] = op.classes[ck & kClassMask].rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
   }
 }
 
@@ -211,7 +221,7 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // deterministic sum of partials (every block computes the same value)
 __device__ double sum_partials(const double *__restrict__ part, int n, double *sh) {
   double v = 0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) v += part[k];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) v += __ldcg(part + k);  // written by other blocks
   double t = block_sum(v, sh);
   if (threadIdx.x == 0) sh[32] = t;
   __syncthreads();
@@ -226,7 +236,7 @@ __global__ void k_sum_db(OpView op, const double *__restrict__ rho, double neg_i
   __shared__ double sh[40];
   double v = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const RowClass &C = op.classes[op.cls[k]];
+    const RowClass &C = op.classes[op.cls[k] & kClassMask];
     if (!C.fixed) {
       double b = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
       if (C.sig_dof >= 0) b -= C.sig_coef * op.sigma[C.sig_dof];
@@ -243,151 +253,228 @@ __global__ void k_lambda(const double *__restrict__ part, int nparts, double dsu
   if (threadIdx.x == 0) sc->lambda = dsum > 0 ? s / dsum : 0.0;
 }
 
-// res = b - λ - A x over free rows; r = -d * res (scaled residual);
-// partials: ||res||², ||rhs_eff||² where rhs_eff = b - λ - A_fixed x_fixed.
-// When `skip_if_done`, the kernel returns immediately once sc->done is set.
-__global__ void k_residual(OpView op, const double *__restrict__ x, const double *__restrict__ rho,
-                           double neg_inv_eps0, const PoissonScal *__restrict__ sc, double *__restrict__ r,
-                           double *__restrict__ part, int nparts_stride, int nn, int singular, int skip_if_done) {
+// Optional E = -∇ϕ output of k_residual (generalized_poisson.jl:398-410):
+// FP32 node values for the MCC target term and per-cell records for the gather.
+// The node differences are taken in FP64 (ϕ is ~10^2-10^3 V while neighbour
+// differences are ~10^-1 V) and scaled in FP32.
+struct EOut {
+  float2 *E32;
+  float4 *E4;
+  float idx2, idx1, idy2, idy1;  // 1/(2Δx), 1/Δx, 1/(2Δy), 1/Δy
+};
+
+__device__ __forceinline__ void efield_at(const double *__restrict__ x, int k, int i, int j, int nx, int ny,
+                                          const EOut &eo) {
+  float ex, ey;
+  if (i == 0) ex = (float)(x[k] - x[k + 1]) * eo.idx1;
+  else if (i == nx - 1) ex = (float)(x[k - 1] - x[k]) * eo.idx1;
+  else ex = (float)(x[k - 1] - x[k + 1]) * eo.idx2;
+  if (j == 0) ey = (float)(x[k] - x[k + nx]) * eo.idy1;
+  else if (j == ny - 1) ey = (float)(x[k - nx] - x[k]) * eo.idy1;
+  else ey = (float)(x[k - nx] - x[k + nx]) * eo.idy2;
+  const float2 e = make_float2(ex, ey);
+  eo.E32[k] = e;
+  store_corners(eo.E4, nx, ny, i, j, e);
+}
+
+constexpr int kSmemClasses = 128;  // row-class table held in shared memory up to this size
+
+// res = b - λ - A x over free rows, stored scaled as r = -d * res (FP64 in
+// r64 for CG, FP32 in r32 as the input of the FP32 separable correction).
+// Block partials of ||res||² (and, in the FIRST pass of a solve, of
+// ||rhs_eff||², rhs_eff = b - λ - A_fixed x_fixed) are summed by the last
+// block to finish, in block order (deterministic), which updates
+// relres/iters and sets sc->done when ||res|| <= rtol ||rhs_eff||.  With
+// EOUT, E = -∇ϕ of x is written too.  Passes after the first return at once
+// when sc->done is set and count one sweep each.
+//
+// GB300 runs FP64 at ~1/64 of the FP32 rate, so this pass is built to use few
+// FP64 instructions: the sweep form sums the whole stencil in one FMA chain.
+template <bool FIRST, bool EOUT>
+__global__ void __launch_bounds__(256) k_residual(OpView op, const double *__restrict__ x,
+                                                  const double *__restrict__ rho, double neg_inv_eps0,
+                                                  PoissonScal *sc, double *__restrict__ r64, float *__restrict__ r32,
+                                                  double *__restrict__ part, int nn, int singular, double rtol2,
+                                                  EOut eo) {
   __shared__ double sh[40];
-  if (skip_if_done && sc->done) return;
+  __shared__ RowClass cls_sh[kSmemClasses];
+  __shared__ int last;
+  if (!FIRST && sc->done) return;
+  const bool sm = op.nclass <= kSmemClasses;
+  if (sm)
+    for (int t = threadIdx.x; t < op.nclass; t += blockDim.x) cls_sh[t] = op.classes[t];
+  __syncthreads();
+  const RowClass *__restrict__ CT = sm ? cls_sh : op.classes;
   const double lam = singular ? sc->lambda : 0.0;
+  const int nx = op.nx, ny = op.ny;
   double a2 = 0, b2 = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const RowClass &C = op.classes[op.cls[k]];
-    if (C.fixed) {
-      r[k] = 0.0;
+    const int j = k / nx, i = k - j * nx;
+    if (EOUT) efield_at(x, k, i, j, nx, ny, eo);
+    const unsigned ck = op.cls[k];
+    if (ck & kFixedBit) {
+      if (r32) r32[k] = 0.f;
+      else r64[k] = 0.0;
       continue;
     }
-    int w, e, s, n;
-    nbr(k, op.nx, op.ny, w, e, s, n);
-    double b = (C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k]) - lam;
+    const RowClass &C = CT[ck];
+    const int w = i > 0 ? k - 1 : k + nx - 1;
+    const int e = i < nx - 1 ? k + 1 : k - nx + 1;
+    const int s = j > 0 ? k - nx : k + nx * (ny - 1);
+    const int n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
+    double b = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+    if (singular) b -= lam;
     if (C.sig_dof >= 0) b -= C.sig_coef * op.sigma[C.sig_dof];
-    const RowClass &CW = op.classes[op.cls[w]], &CE = op.classes[op.cls[e]];
-    const RowClass &CS = op.classes[op.cls[s]], &CN = op.classes[op.cls[n]];
-    double afix = 0, afree = C.c0 * x[k];
-    double t;
-    t = C.cW * x[w];
-    if (CW.fixed) afix += t; else afree += t;
-    t = C.cE * x[e];
-    if (CE.fixed) afix += t; else afree += t;
-    t = C.cS * x[s];
-    if (CS.fixed) afix += t; else afree += t;
-    t = C.cN * x[n];
-    if (CN.fixed) afix += t; else afree += t;
-    double rhs = b - afix;
-    double res = rhs - afree;
-    r[k] = -C.d * res;
-    a2 += res * res;
-    b2 += rhs * rhs;
+    double res;
+    if (FIRST) {
+      double afix = 0, afree = C.c0 * x[k];
+      double t;
+      t = C.cW * x[w];
+      if (op.cls[w] & kFixedBit) afix += t; else afree += t;
+      t = C.cE * x[e];
+      if (op.cls[e] & kFixedBit) afix += t; else afree += t;
+      t = C.cS * x[s];
+      if (op.cls[s] & kFixedBit) afix += t; else afree += t;
+      t = C.cN * x[n];
+      if (op.cls[n] & kFixedBit) afix += t; else afree += t;
+      const double rhs = b - afix;
+      res = rhs - afree;
+      b2 = fma(rhs, rhs, b2);
+    } else {
+      double ax = C.c0 * x[k];
+      ax = fma(C.cW, x[w], ax);
+      ax = fma(C.cE, x[e], ax);
+      ax = fma(C.cS, x[s], ax);
+      ax = fma(C.cN, x[n], ax);
+      res = b - ax;
+    }
+    const double sr = -C.d * res;
+    if (r32) r32[k] = (float)sr;
+    else r64[k] = sr;
+    a2 = fma(res, res, a2);
   }
-  double ta = block_sum(a2, sh);
-  double tb = block_sum(b2, sh);
+  const double ta = block_sum(a2, sh);
+  const double tb = FIRST ? block_sum(b2, sh) : 0.0;
   if (threadIdx.x == 0) {
     part[blockIdx.x] = ta;
-    part[nparts_stride + blockIdx.x] = tb;
+    if (FIRST) part[kPartials + blockIdx.x] = tb;
+    __threadfence();
+    last = atomicAdd(&sc->ticket, 1u) == gridDim.x - 1;
   }
-}
-
-// convergence check after a residual evaluation
-__global__ void k_check(const double *__restrict__ part, int nparts, int stride, PoissonScal *sc, double rtol2,
-                        int count_sweep) {
-  __shared__ double sh[40];
-  if (sc->done) return;
-  double a = sum_partials(part, nparts, sh);
-  double b = sum_partials(part + stride, nparts, sh);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const double a = sum_partials(part, gridDim.x, sh);
+  const double bb = FIRST ? sum_partials(part + kPartials, gridDim.x, sh) : 0.0;
   if (threadIdx.x == 0) {
+    sc->ticket = 0u;
+    const double rhs2 = FIRST ? bb : sc->rhs2;
+    if (FIRST) sc->rhs2 = bb;
+    else sc->iters += 1;
     sc->res2 = a;
-    sc->rhs2 = b;
-    sc->relres = b > 0 ? sqrt(a / b) : sqrt(a);
-    if (count_sweep) sc->iters += 1;
-    if ((b > 0 && a <= rtol2 * b) || a == 0.0) sc->done = 1;
+    sc->relres = rhs2 > 0 ? sqrt(a / rhs2) : sqrt(a);
+    if ((rhs2 > 0 && a <= rtol2 * rhs2) || a == 0.0) sc->done = 1;
   }
 }
 
-// ---------------- separable solver: FFT(y) x tridiagonal(x) ----------------
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+// ---------------- separable correction: FFT(y) x tridiagonal(x), FP32 ----------------
+// One sweep computes δ ≈ S^-1 r in FP32 and adds it to the FP64 ϕ; the FP64
+// residual pass that follows decides convergence (iterative refinement), so
+// the converged ϕ meets the FP64 tolerance while the transform and the
+// tridiagonal solves run on the FP32 pipes.  Two real columns share one
+// complex FFT: z = a + i b, A_k = (Z_k + conj Z_{N-k})/2,
+// B_k = (Z_k - conj Z_{N-k})/(2i).
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
 __device__ __forceinline__ unsigned bitrev(unsigned v, int bits) { return __brev(v) >> (32 - bits); }
 
-// in-place radix-2 DIT FFT of TI columns of length N held in shared memory
-// (input already in bit-reversed order); sign = -1 forward, +1 inverse
-__device__ void fft_columns(double2 *buf, int TI, int N, int logN, const double2 *__restrict__ tw, bool inverse) {
-  const int half_total = TI * (N >> 1);
+// in-place radix-2 DIT FFT of TP length-N columns held in shared memory with
+// column stride S (input in bit-reversed order), twiddles tw (N/2, shared);
+// the inverse uses conjugate twiddles and leaves the 1/N to the caller
+__device__ void fft_columns(float2 *buf, int TP, int N, int S, int logN, const float2 *tw, bool inverse) {
+  const int hlog = logN - 1, hn = N >> 1;
+  const int total = TP * hn;
   for (int s = 1; s <= logN; s++) {
     const int half = 1 << (s - 1);
-    const int stride = N >> s;  // twiddle stride
-    for (int b = threadIdx.x; b < half_total; b += blockDim.x) {
-      const int col = b / (N >> 1);
-      const int kk = b - col * (N >> 1);
-      const int grp = kk >> (s - 1);
+    const int tws = logN - s;  // twiddle index = pos << tws
+    for (int b = threadIdx.x; b < total; b += blockDim.x) {
+      const int col = b >> hlog;
+      const int kk = b & (hn - 1);
       const int pos = kk & (half - 1);
-      const int i1 = grp * (half << 1) + pos, i2 = i1 + half;
-      double2 w = tw[pos * stride];
+      const int i1 = ((kk >> (s - 1)) << s) + pos, i2 = i1 + half;
+      float2 w = tw[pos << tws];
       if (inverse) w.y = -w.y;
-      double2 *c = buf + col * N;
-      double2 t = cmul(w, c[i2]);
-      double2 u = c[i1];
-      c[i1] = make_double2(u.x + t.x, u.y + t.y);
-      c[i2] = make_double2(u.x - t.x, u.y - t.y);
+      float2 *c = buf + col * S;
+      const float2 t = cmulf(w, c[i2]);
+      const float2 u = c[i1];
+      c[i1] = make_float2(u.x + t.x, u.y + t.y);
+      c[i2] = make_float2(u.x - t.x, u.y - t.y);
     }
     __syncthreads();
   }
 }
 
-// r (nx,ny) -> spec[i][k], k = 0..N/2 (real input, forward FFT along y)
-__global__ void k_fft_fwd(const double *__restrict__ r, int nx, int N, int logN, int TI, const double2 *__restrict__ tw,
-                          double2 *__restrict__ spec, const PoissonScal *__restrict__ sc) {
-  extern __shared__ double2 buf[];
+// r (nx, ny) -> spec[i K + k], k = 0..N/2: forward FFT along y of the 2 TP
+// columns of this block, two per complex transform
+__global__ void __launch_bounds__(256) k_fft_fwd(const float *__restrict__ r, int nx, int N, int logN, int TP,
+                                                 const float2 *__restrict__ tw, float2 *__restrict__ spec,
+                                                 const PoissonScal *__restrict__ sc) {
+  extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
   if (sc->done) return;
-  const int i0 = blockIdx.x * TI;
-  for (int t = threadIdx.x; t < TI * N; t += blockDim.x) {
-    const int col = t % TI, j = t / TI;
-    const int i = i0 + col;
-    double v = i < nx ? r[i + (size_t)nx * j] : 0.0;
-    buf[col * N + bitrev(j, logN)] = make_double2(v, 0.0);
+  const int S = N + 1, W = 2 * TP, K = (N >> 1) + 1;
+  const int i0 = blockIdx.x * W;
+  float2 *tws = fbuf + TP * S;
+  for (int t = threadIdx.x; t < (N >> 1); t += blockDim.x) tws[t] = __ldg(tw + t);
+  for (int t = threadIdx.x; t < W * N; t += blockDim.x) {
+    const int j = t / W, c = t - j * W;
+    const int i = i0 + c;
+    const float v = i < nx ? r[i + (size_t)nx * j] : 0.f;
+    reinterpret_cast<float *>(fbuf + (c >> 1) * S + bitrev(j, logN))[c & 1] = v;
   }
   __syncthreads();
-  fft_columns(buf, TI, N, logN, tw, false);
-  const int K = (N >> 1) + 1;
-  for (int t = threadIdx.x; t < TI * K; t += blockDim.x) {
-    const int col = t / K, k = t - col * K;
-    const int i = i0 + col;
-    if (i < nx) spec[(size_t)i * K + k] = buf[col * N + k];
+  fft_columns(fbuf, TP, N, S, logN, tws, false);
+  for (int t = threadIdx.x; t < TP * K; t += blockDim.x) {
+    const int p = t / K, k = t - p * K;
+    const float2 zk = fbuf[p * S + k];
+    const float2 zm = fbuf[p * S + ((N - k) & (N - 1))];
+    const int ia = i0 + 2 * p;
+    if (ia < nx) spec[(size_t)ia * K + k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+    if (ia + 1 < nx) spec[(size_t)(ia + 1) * K + k] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
   }
 }
 
-// Per Fourier mode and per real/imaginary part (one thread each): Thomas
-// forward elimination and back substitution along x with the precomputed
-// factors, in place in spec; Sherman-Morrison correction for x-periodic
-// operators.  Rows are fetched in chunks of kTriChunk so that the chunk's
-// loads are in flight together instead of one L2 round trip per row of the
-// dependent recurrence.
+// Per Fourier mode and real/imaginary part (one thread each): Thomas forward
+// elimination and back substitution along x with the precomputed factors, in
+// place in spec; Sherman-Morrison correction for x-periodic operators.  Used
+// when a mode's column does not fit in shared memory for cyclic reduction.
+// Rows are fetched in chunks of kTriChunk so that the chunk's loads are in
+// flight together instead of one L2 round trip per row of the recurrence.
 constexpr int kTriChunk = 16;
 
-__global__ void __launch_bounds__(64) k_tridiag(double *__restrict__ spec, int nx, int K,
-                                                const double *__restrict__ low, const double *__restrict__ inv,
-                                                const double *__restrict__ cp, const double *__restrict__ q,
-                                                const double *__restrict__ gk, int cyclic, int pin0,
+__global__ void __launch_bounds__(64) k_tridiag(float *__restrict__ spec, int nx, int K,
+                                                const float *__restrict__ low, const float *__restrict__ inv,
+                                                const float *__restrict__ cp, const float *__restrict__ q,
+                                                const float *__restrict__ gk, int cyclic, int pin0,
                                                 const PoissonScal *__restrict__ sc) {
   if (sc->done) return;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = t >> 1, part = t & 1;
   if (k >= K) return;
   const size_t K2 = 2 * (size_t)K;
-  double *__restrict__ col = spec + 2 * (size_t)k + part;  // row i at col[i * K2]
-  double y = 0.0;
+  float *__restrict__ col = spec + 2 * (size_t)k + part;  // row i at col[i * K2]
+  if (pin0 >= 0 && k == 0) col[(size_t)pin0 * K2] = 0.f;  // pinned row of the singular mode
+  float y = 0.f;
   for (int i0 = 0; i0 < nx; i0 += kTriChunk) {
-    double r[kTriChunk], iv[kTriChunk], a[kTriChunk];
+    float r[kTriChunk], iv[kTriChunk], a[kTriChunk];
 #pragma unroll
     for (int c = 0; c < kTriChunk; c++) {
       const int i = i0 + c;
       if (i < nx) {
         r[c] = col[i * K2];
         iv[c] = inv[(size_t)i * K + k];
-        a[c] = i > 0 ? __ldg(low + i) : 0.0;
+        a[c] = i > 0 ? __ldg(low + i) : 0.f;
       }
     }
 #pragma unroll
@@ -399,9 +486,9 @@ __global__ void __launch_bounds__(64) k_tridiag(double *__restrict__ spec, int n
       }
     }
   }
-  double xn = y;
+  float xn = y;
   for (int i1 = nx - 2; i1 >= 0; i1 -= kTriChunk) {
-    double yv[kTriChunk], cv[kTriChunk];
+    float yv[kTriChunk], cv[kTriChunk];
 #pragma unroll
     for (int c = 0; c < kTriChunk; c++) {
       const int i = i1 - c;
@@ -420,45 +507,53 @@ __global__ void __launch_bounds__(64) k_tridiag(double *__restrict__ spec, int n
     }
   }
   if (cyclic && !(k == 0 && pin0 >= 0)) {
-    const double x0 = col[0], xl = col[(size_t)(nx - 1) * K2];
-    const double f = (x0 + gk[K + k] * xl) * gk[k];
+    const float x0 = col[0], xl = col[(size_t)(nx - 1) * K2];
+    const float f = (x0 + gk[K + k] * xl) * gk[k];
     for (int i = 0; i < nx; i++) col[i * K2] -= f * q[(size_t)i * K + k];
   }
 }
 
-// The same per-mode solve as k_tridiag by cyclic reduction in shared memory:
-// a block holds G consecutive Fourier modes (real and imaginary parts, 2G
-// columns of nx rows); level l of the forward pass updates rows (m+1)2^(l+1)-1
-// from rows at distance 2^l, the back substitution recovers the rows
-// eliminated at each level.  The coefficients of every level are precomputed
-// per mode on the host, so the device work is one FMA pair per row and level.
-__global__ void __launch_bounds__(256) k_tridiag_cr(double *__restrict__ spec, int nx, int K, int G, int L,
-                                                    const double2 *__restrict__ fwd, const double2 *__restrict__ back,
-                                                    const double *__restrict__ backb, const double *__restrict__ top,
-                                                    const double *__restrict__ q, const double *__restrict__ gk,
-                                                    int cyclic, int pin0, const PoissonScal *__restrict__ sc) {
-  extern __shared__ double dsh[];  // [col][nx], col = 2 (k - k0) + part
+// Cyclic reduction along x for G Fourier modes (2G real columns) held in
+// shared memory.  The host factorisation stores each mode's coefficients
+// contiguously (fwd: nf (α, γ) pairs, back: nb (a/b, c/b) pairs, backb: nb
+// 1/b, then 1/b of the last row), and the block stages them in shared memory
+// with the data in one pass, so the 2L dependent levels run on shared memory
+// only.
+__global__ void __launch_bounds__(256) k_tridiag_cr(float *__restrict__ spec, int nx, int K, int G, int L, int nf,
+                                                    int nb, const float2 *__restrict__ fwd,
+                                                    const float2 *__restrict__ back, const float *__restrict__ backb,
+                                                    const float *__restrict__ top, const float *__restrict__ q,
+                                                    const float *__restrict__ gk, int cyclic, int pin0,
+                                                    const PoissonScal *__restrict__ sc) {
+  extern __shared__ float fsh[];  // data [col][nx] (col = 2 (k - k0) + part), then per mode fwd, back, backb
   if (sc->done) return;
   const int k0 = blockIdx.x * G;
-  const int ncol = 2 * min(G, K - k0);
+  const int g = min(G, K - k0), ncol = 2 * g;
+  float2 *cf = reinterpret_cast<float2 *>(fsh + 2 * G * nx);  // [g][nf]
+  float2 *cb = cf + (size_t)G * nf;                            // [g][nb]
+  float *cbb = reinterpret_cast<float *>(cb + (size_t)G * nb);  // [g][nb]
+  for (int t = threadIdx.x; t < g * nf; t += blockDim.x) cf[t] = __ldg(fwd + (size_t)k0 * nf + t);
+  for (int t = threadIdx.x; t < g * nb; t += blockDim.x) {
+    cb[t] = __ldg(back + (size_t)k0 * nb + t);
+    cbb[t] = __ldg(backb + (size_t)k0 * nb + t);
+  }
   for (int t = threadIdx.x; t < nx * ncol; t += blockDim.x) {
     const int i = t / ncol, col = t - i * ncol;
     const int k = k0 + (col >> 1);
-    double v = spec[((size_t)i * K + k) * 2 + (col & 1)];
-    if (pin0 >= 0 && k == 0 && i == pin0) v = 0.0;  // pinned row of the singular mode
-    dsh[col * nx + i] = v;
+    float v = spec[((size_t)i * K + k) * 2 + (col & 1)];
+    if (pin0 >= 0 && k == 0 && i == pin0) v = 0.f;  // pinned row of the singular mode
+    fsh[col * nx + i] = v;
   }
   __syncthreads();
-  size_t F = 0, B = 0;
+  int F = 0, B = 0;
   for (int l = 0; l < L; l++) {
     const int s = 1 << l, cnt = nx >> (l + 1);
     for (int t = threadIdx.x; t < cnt * ncol; t += blockDim.x) {
       const int m = t / ncol, col = t - m * ncol;
-      const int k = k0 + (col >> 1);
       const int i = (m + 1) * 2 * s - 1;
-      const double2 ag = fwd[(F + m) * K + k];
-      double *dc = dsh + col * nx;
-      double v = dc[i] - ag.x * dc[i - s];
+      const float2 ag = cf[(col >> 1) * nf + F + m];
+      float *dc = fsh + col * nx;
+      float v = dc[i] - ag.x * dc[i - s];
       if (i + s < nx) v -= ag.y * dc[i + s];
       dc[i] = v;
     }
@@ -467,19 +562,18 @@ __global__ void __launch_bounds__(256) k_tridiag_cr(double *__restrict__ spec, i
     __syncthreads();
   }
   const int topr = (1 << L) - 1;
-  for (int col = threadIdx.x; col < ncol; col += blockDim.x) dsh[col * nx + topr] *= top[k0 + (col >> 1)];
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) fsh[col * nx + topr] *= __ldg(top + k0 + (col >> 1));
   __syncthreads();
   for (int l = L - 1; l >= 0; l--) {
     const int s = 1 << l, ecnt = ((nx >> l) + 1) >> 1;
     B -= ecnt;
     for (int t = threadIdx.x; t < ecnt * ncol; t += blockDim.x) {
       const int m = t / ncol, col = t - m * ncol;
-      const int k = k0 + (col >> 1);
       const int j = (2 * m + 1) * s - 1;
-      const size_t o = (B + m) * K + k;
-      const double2 r = back[o];
-      double *dc = dsh + col * nx;
-      double x = backb[o] * dc[j];
+      const int o = (col >> 1) * nb + B + m;
+      const float2 r = cb[o];
+      float *dc = fsh + col * nx;
+      float x = cbb[o] * dc[j];
       if (j - s >= 0) x -= r.x * dc[j - s];
       if (j + s < nx) x -= r.y * dc[j + s];
       dc[j] = x;
@@ -489,45 +583,77 @@ __global__ void __launch_bounds__(256) k_tridiag_cr(double *__restrict__ spec, i
   for (int t = threadIdx.x; t < nx * ncol; t += blockDim.x) {
     const int i = t / ncol, col = t - i * ncol;
     const int k = k0 + (col >> 1);
-    const double *dc = dsh + col * nx;
-    double v = dc[i];
+    const float *dc = fsh + col * nx;
+    float v = dc[i];
     if (cyclic && !(k == 0 && pin0 >= 0)) v -= (dc[0] + gk[K + k] * dc[nx - 1]) * gk[k] * q[(size_t)i * K + k];
     spec[((size_t)i * K + k) * 2 + (col & 1)] = v;
   }
 }
 
-// spec -> z (nx,ny) via inverse real FFT; x += z on free rows
-__global__ void k_fft_inv_update(const double2 *__restrict__ spec, int nx, int N, int logN, int TI,
-                                 const double2 *__restrict__ tw, OpView op, double *__restrict__ x,
-                                 const PoissonScal *__restrict__ sc) {
-  extern __shared__ double2 buf[];
+// spec -> δ (nx, ny) by the inverse of k_fft_fwd; x += δ on free rows
+__global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict__ spec, int nx, int N, int logN,
+                                                        int TP, const float2 *__restrict__ tw,
+                                                        const uint16_t *__restrict__ cls, double *__restrict__ x,
+                                                        const PoissonScal *__restrict__ sc) {
+  extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
   if (sc->done) return;
-  const int i0 = blockIdx.x * TI;
-  const int K = (N >> 1) + 1;
-  for (int t = threadIdx.x; t < TI * N; t += blockDim.x) {
-    const int col = t / N, k = t - col * N;
-    const int i = i0 + col;
-    double2 v = make_double2(0, 0);
-    if (i < nx) {
-      if (k < K) {
-        v = spec[(size_t)i * K + k];
-      } else {
-        v = spec[(size_t)i * K + (N - k)];
-        v.y = -v.y;
-      }
+  const int S = N + 1, W = 2 * TP, K = (N >> 1) + 1;
+  const int i0 = blockIdx.x * W;
+  float2 *tws = fbuf + TP * S;
+  for (int t = threadIdx.x; t < (N >> 1); t += blockDim.x) tws[t] = __ldg(tw + t);
+  // the update's ϕ values and row classes, fetched before the transform
+  constexpr int kPre = 8;
+  double xp[kPre];
+  bool freep[kPre];
+#pragma unroll
+  for (int u = 0; u < kPre; u++) {
+    const int t = threadIdx.x + u * blockDim.x;
+    const int j = t / W, c = t - j * W;
+    const int i = i0 + c;
+    freep[u] = false;
+    xp[u] = 0.0;
+    if (t < W * N && i < nx) {
+      const size_t kk = i + (size_t)nx * j;
+      freep[u] = !(cls[kk] & kFixedBit);
+      if (freep[u]) xp[u] = x[kk];
     }
-    buf[col * N + bitrev(k, logN)] = v;
+  }
+  for (int t = threadIdx.x; t < TP * N; t += blockDim.x) {
+    const int p = t >> logN, k = t & (N - 1);
+    const int ia = i0 + 2 * p;
+    const bool hi = k >= K;
+    const int kk = hi ? N - k : k;
+    float2 a = make_float2(0.f, 0.f), b = a;
+    if (ia < nx) a = spec[(size_t)ia * K + kk];
+    if (ia + 1 < nx) b = spec[(size_t)(ia + 1) * K + kk];
+    if (hi) {
+      a.y = -a.y;
+      b.y = -b.y;
+    }
+    fbuf[p * S + bitrev(k, logN)] = make_float2(a.x - b.y, a.y + b.x);
   }
   __syncthreads();
-  fft_columns(buf, TI, N, logN, tw, true);
-  const double invN = 1.0 / N;
-  for (int t = threadIdx.x; t < TI * N; t += blockDim.x) {
-    const int col = t % TI, j = t / TI;
-    const int i = i0 + col;
+  fft_columns(fbuf, TP, N, S, logN, tws, true);
+  const float invN = 1.f / (float)N;  // N is a power of two: exact
+#pragma unroll
+  for (int u = 0; u < kPre; u++) {
+    const int t = threadIdx.x + u * blockDim.x;
+    const int j = t / W, c = t - j * W;
+    const int i = i0 + c;
+    if (freep[u]) {
+      const float2 z = fbuf[(c >> 1) * S + j];
+      x[i + (size_t)nx * j] = xp[u] + (double)((c & 1 ? z.y : z.x) * invN);
+    }
+  }
+  for (int t = threadIdx.x + kPre * blockDim.x; t < W * N; t += blockDim.x) {
+    const int j = t / W, c = t - j * W;
+    const int i = i0 + c;
     if (i < nx) {
       const size_t kk = i + (size_t)nx * j;
-      const RowClass &C = op.classes[op.cls[kk]];
-      if (!C.fixed) x[kk] += buf[col * N + j].x * invN;
+      if (!(cls[kk] & kFixedBit)) {
+        const float2 z = fbuf[(c >> 1) * S + j];
+        x[kk] += (double)((c & 1 ? z.y : z.x) * invN);
+      }
     }
   }
 }
@@ -561,7 +687,7 @@ __global__ void k_cg_init(OpView op, const double *__restrict__ r, double *__res
   __shared__ double sh[40];
   double v = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const RowClass &C = op.classes[op.cls[k]];
+    const RowClass &C = op.classes[op.cls[k] & kClassMask];
     double zz = C.fixed ? 0.0 : r[k] / (-C.d * C.c0);
     z[k] = zz;
     p[k] = zz;
@@ -577,7 +703,7 @@ __global__ void k_cg_ap(OpView op, const double *__restrict__ p, double *__restr
   if (sc->done) return;
   double v = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const RowClass &C = op.classes[op.cls[k]];
+    const RowClass &C = op.classes[op.cls[k] & kClassMask];
     double a = C.fixed ? 0.0 : apply_S(op, C, p, k);
     ap[k] = a;
     v += p[k] * a;
@@ -597,7 +723,7 @@ __global__ void k_cg_update(OpView op, double *__restrict__ x, double *__restric
   const double alpha = pap != 0 ? rz / pap : 0.0;
   double v = 0, w2 = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const RowClass &C = op.classes[op.cls[k]];
+    const RowClass &C = op.classes[op.cls[k] & kClassMask];
     if (C.fixed) {
       z[k] = 0.0;
       continue;
@@ -891,6 +1017,7 @@ static int build_device(Ctx *c, Poisson *P) {
   for (int r = 0; r < nn; r++)
     if (!rows[r].fixed) P->dsum += d[r];
   // classes
+  bool rho_fixed = false;
   std::map<std::vector<double>, int> cmap;
   std::vector<RowClass> classes;
   std::vector<uint16_t> cls(nn);
@@ -902,7 +1029,7 @@ static int build_device(Ctx *c, Poisson *P) {
     int id;
     if (it == cmap.end()) {
       id = (int)classes.size();
-      if (id >= 65535) return set_err(c, ISKRA_EINVAL, "too many distinct operator rows");
+      if (id > (int)kClassMask) return set_err(c, ISKRA_EINVAL, "too many distinct operator rows");
       cmap[key] = id;
       RowClass rc{};
       rc.c0 = e.c0;
@@ -919,9 +1046,11 @@ static int build_device(Ctx *c, Poisson *P) {
     } else {
       id = it->second;
     }
-    cls[r] = (uint16_t)id;
+    cls[r] = (uint16_t)(id | (e.fixed ? kFixedBit : 0u));
+    rho_fixed |= e.fixed && e.rho;
   }
   P->nclass = (int)classes.size();
+  P->rho_fixed = rho_fixed;
   // ---- separability: per column i, every j gives the same scaled row ----
   bool sep = P->method == 0 && ny >= 2 && (ny & (ny - 1)) == 0 && ny <= 4096;
   std::vector<double> s0(nx), sW(nx), sE(nx), ey(nx);
@@ -1014,6 +1143,7 @@ static int build_device(Ctx *c, Poisson *P) {
   }
   P->blocks = std::min(kPartials, std::max(1, std::min(c->num_sms * 2, (nn + 255) / 256)));
   // ---- separable factorisation ----
+  cudaFree(P->r32);
   cudaFree(P->spec);
   cudaFree(P->tw);
   cudaFree(P->low);
@@ -1028,6 +1158,7 @@ static int build_device(Ctx *c, Poisson *P) {
   cudaFree(P->cr_top);
   P->cr_fwd = P->cr_back = nullptr;
   P->cr_backb = P->cr_top = nullptr;
+  P->r32 = nullptr;
   P->spec = nullptr;
   P->tw = nullptr;
   P->low = P->up = P->inv = P->cp = P->q = P->gk = nullptr;
@@ -1127,7 +1258,7 @@ static int build_device(Ctx *c, Poisson *P) {
           for (int m = 0; m < ecnt; m++) {
             const int j = (2 * m + 1) * s - 1;
             if (b[j] == 0.0) return set_err(c, ISKRA_EINVAL, "singular tridiagonal mode in the Poisson factorisation");
-            const size_t o = (B + m) * K + k;
+            const size_t o = (size_t)k * cr_nb + B + m;
             cr_back[o] = make_double2(a[j] / b[j], cc[j] / b[j]);
             cr_backb[o] = 1.0 / b[j];
           }
@@ -1135,7 +1266,7 @@ static int build_device(Ctx *c, Poisson *P) {
             const int i = (m + 1) * 2 * s - 1, im = i - s, ip = i + s;
             const double al = a[i] / b[im];
             const double ga = ip < nx ? cc[i] / b[ip] : 0.0;
-            cr_fwd[(F + m) * K + k] = make_double2(al, ga);
+            cr_fwd[(size_t)k * cr_nf + F + m] = make_double2(al, ga);
             b[i] = b[i] - al * cc[im] - (ip < nx ? ga * a[ip] : 0.0);
             a[i] = -al * a[im];
             cc[i] = ip < nx ? -ga * cc[ip] : 0.0;
@@ -1162,39 +1293,52 @@ static int build_device(Ctx *c, Poisson *P) {
         gkv[k] = 1.0 / (1.0 + y[0] + vfac * y[nx - 1]);
       }
     }
-    std::vector<double2> tw(N / 2 > 0 ? N / 2 : 1);
+    // device tables in FP32 (the correction runs in FP32)
+    auto f32 = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
+    auto f32x2 = [](const std::vector<double2> &v) {
+      std::vector<float2> o(v.size());
+      for (size_t n = 0; n < v.size(); n++) o[n] = make_float2((float)v[n].x, (float)v[n].y);
+      return o;
+    };
+    std::vector<float2> tw(N / 2 > 0 ? N / 2 : 1);
     for (int m = 0; m < N / 2; m++) {
       const double ang = -2.0 * M_PI * m / N;
-      tw[m] = make_double2(std::cos(ang), std::sin(ang));
+      tw[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
-    ISKRA_CUDA(c, cudaMalloc(&P->spec, (size_t)nx * K * sizeof(double2)));
-    ISKRA_CUDA(c, cudaMalloc(&P->tw, tw.size() * sizeof(double2)));
-    ISKRA_CUDA(c, cudaMalloc(&P->low, nx * sizeof(double)));
-    ISKRA_CUDA(c, cudaMalloc(&P->up, nx * sizeof(double)));
-    ISKRA_CUDA(c, cudaMalloc(&P->inv, (size_t)nx * K * sizeof(double)));
-    ISKRA_CUDA(c, cudaMalloc(&P->cp, (size_t)nx * K * sizeof(double)));
-    ISKRA_CUDA(c, cudaMalloc(&P->gk, 2 * K * sizeof(double)));
-    ISKRA_CUDA(c, cudaMemcpy(P->tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
-    ISKRA_CUDA(c, cudaMemcpy(P->low, lo.data(), nx * sizeof(double), cudaMemcpyHostToDevice));
-    ISKRA_CUDA(c, cudaMemcpy(P->up, upv.data(), nx * sizeof(double), cudaMemcpyHostToDevice));
-    ISKRA_CUDA(c, cudaMemcpy(P->inv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice));
-    ISKRA_CUDA(c, cudaMemcpy(P->cp, cpv.data(), cpv.size() * sizeof(double), cudaMemcpyHostToDevice));
-    ISKRA_CUDA(c, cudaMemcpy(P->gk, gkv.data(), 2 * K * sizeof(double), cudaMemcpyHostToDevice));
+    const std::vector<float> lo32 = f32(lo), up32 = f32(upv), inv32 = f32(inv), cp32 = f32(cpv), gk32 = f32(gkv),
+                             q32 = f32(qv), backb32 = f32(cr_backb), top32 = f32(cr_top);
+    const std::vector<float2> fwd32 = f32x2(cr_fwd), back32 = f32x2(cr_back);
+    ISKRA_CUDA(c, cudaMalloc(&P->r32, nn * sizeof(float)));
+    ISKRA_CUDA(c, cudaMalloc(&P->spec, (size_t)nx * K * sizeof(float2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->tw, tw.size() * sizeof(float2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->low, nx * sizeof(float)));
+    ISKRA_CUDA(c, cudaMalloc(&P->up, nx * sizeof(float)));
+    ISKRA_CUDA(c, cudaMalloc(&P->inv, (size_t)nx * K * sizeof(float)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cp, (size_t)nx * K * sizeof(float)));
+    ISKRA_CUDA(c, cudaMalloc(&P->gk, 2 * K * sizeof(float)));
+    ISKRA_CUDA(c, cudaMemcpy(P->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->low, lo32.data(), nx * sizeof(float), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->up, up32.data(), nx * sizeof(float), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->inv, inv32.data(), inv32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->cp, cp32.data(), cp32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->gk, gk32.data(), 2 * K * sizeof(float), cudaMemcpyHostToDevice));
     P->cr_levels = cr_levels;
-    ISKRA_CUDA(c, cudaMalloc(&P->cr_fwd, std::max<size_t>(1, cr_fwd.size()) * sizeof(double2)));
-    ISKRA_CUDA(c, cudaMalloc(&P->cr_back, std::max<size_t>(1, cr_back.size()) * sizeof(double2)));
-    ISKRA_CUDA(c, cudaMalloc(&P->cr_backb, std::max<size_t>(1, cr_backb.size()) * sizeof(double)));
-    ISKRA_CUDA(c, cudaMalloc(&P->cr_top, K * sizeof(double)));
-    if (!cr_fwd.empty())
-      ISKRA_CUDA(c, cudaMemcpy(P->cr_fwd, cr_fwd.data(), cr_fwd.size() * sizeof(double2), cudaMemcpyHostToDevice));
-    if (!cr_back.empty()) {
-      ISKRA_CUDA(c, cudaMemcpy(P->cr_back, cr_back.data(), cr_back.size() * sizeof(double2), cudaMemcpyHostToDevice));
-      ISKRA_CUDA(c, cudaMemcpy(P->cr_backb, cr_backb.data(), cr_backb.size() * sizeof(double), cudaMemcpyHostToDevice));
+    P->cr_nf = (int)cr_nf;
+    P->cr_nb = (int)cr_nb;
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_fwd, std::max<size_t>(1, fwd32.size()) * sizeof(float2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_back, std::max<size_t>(1, back32.size()) * sizeof(float2)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_backb, std::max<size_t>(1, backb32.size()) * sizeof(float)));
+    ISKRA_CUDA(c, cudaMalloc(&P->cr_top, K * sizeof(float)));
+    if (!fwd32.empty())
+      ISKRA_CUDA(c, cudaMemcpy(P->cr_fwd, fwd32.data(), fwd32.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    if (!back32.empty()) {
+      ISKRA_CUDA(c, cudaMemcpy(P->cr_back, back32.data(), back32.size() * sizeof(float2), cudaMemcpyHostToDevice));
+      ISKRA_CUDA(c, cudaMemcpy(P->cr_backb, backb32.data(), backb32.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
-    ISKRA_CUDA(c, cudaMemcpy(P->cr_top, cr_top.data(), K * sizeof(double), cudaMemcpyHostToDevice));
+    ISKRA_CUDA(c, cudaMemcpy(P->cr_top, top32.data(), K * sizeof(float), cudaMemcpyHostToDevice));
     if (cyclic) {
-      ISKRA_CUDA(c, cudaMalloc(&P->q, qv.size() * sizeof(double)));
-      ISKRA_CUDA(c, cudaMemcpy(P->q, qv.data(), qv.size() * sizeof(double), cudaMemcpyHostToDevice));
+      ISKRA_CUDA(c, cudaMalloc(&P->q, q32.size() * sizeof(float)));
+      ISKRA_CUDA(c, cudaMemcpy(P->q, q32.data(), q32.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
   }
   if (sep) {
@@ -1205,12 +1349,16 @@ static int build_device(Ctx *c, Poisson *P) {
   return ISKRA_OK;
 }
 
+static int fixed_to_x_now(Ctx *c);
+
 int poisson_prepare(Ctx *c) {
   Poisson *P = c->ps;
   if (!P) return set_err(c, ISKRA_EINVAL, "no Poisson solver: call iskra_poisson_create");
   if (!P->dirty) return ISKRA_OK;
   invalidate_graphs(c);
-  return build_device(c, P);
+  int rc = build_device(c, P);
+  if (rc) return rc;
+  return fixed_to_x_now(c);
 }
 
 static OpView opview(Poisson *P) {
@@ -1221,35 +1369,73 @@ static OpView opview(Poisson *P) {
   o.sigma = P->sigma_d;
   o.nx = P->nx;
   o.ny = P->ny;
+  o.nclass = P->nclass;
   return o;
 }
 
-// Columns per FFT block: enough blocks to cover every SM twice, at most 64 KB
-// of double2 per block.
-static int fft_ti(int N, int nx, int sms) {
-  int ti = nx / (2 * sms);
-  const int cap = 4096 / N < 16 ? 4096 / N : 16;
-  if (ti > cap) ti = cap;
-  if (ti < 1) ti = 1;
-  return ti;
+static EOut eout(Ctx *c, bool on) {
+  EOut e{};
+  if (!on) return e;
+  e.E32 = c->E32;
+  e.E4 = c->E4;
+  e.idx2 = (float)(1.0 / (2 * c->g.dx));
+  e.idx1 = (float)(1.0 / c->g.dx);
+  e.idy2 = (float)(1.0 / (2 * c->g.dy));
+  e.idy1 = (float)(1.0 / c->g.dy);
+  return e;
 }
 
-// Fourier modes per cyclic-reduction block (2G columns of nx doubles); 0 when
-// nx is too large for shared memory (the chunked Thomas kernel is used then).
-static int cr_modes_per_block(int nx) {
-  if (2 * (size_t)nx * sizeof(double) > 96 * 1024) return 0;
-  int g = 1024 / nx;
-  return g < 1 ? 1 : (g > 8 ? 8 : g);
+// x at the fixed rows from the fixed values.  Solves rewrite only rows whose
+// value can change between solves (driven rows, ρ-valued rows); the others are
+// written here, after an operator build or a host update of Dirichlet values.
+static int fixed_to_x_now(Ctx *c) {
+  Poisson *P = c->ps;
+  k_fixed_to_x<<<P->blocks, 256, 0, c->stream>>>(opview(P), P->x, c->rho, -1.0 / P->eps0, P->nn);
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
+// Column pairs per FFT block: about two blocks per SM (at least one pair),
+// at most 64 KB of float2 per block.
+static int fft_tp(int N, int nx, int sms) {
+  int tp = nx / (4 * sms);
+  const int cap = (65536 / (int)sizeof(float2) - N / 2) / (N + 1);
+  if (tp > cap) tp = cap;
+  if (tp > 16) tp = 16;
+  if (tp < 1) tp = 1;
+  return tp;
+}
+
+static size_t fft_smem(int N, int tp) { return ((size_t)tp * (N + 1) + N / 2) * sizeof(float2); }
+
+// Shared memory of one cyclic-reduction mode: 2 columns of nx floats and its
+// coefficients (nf + nb float2, nb float; nf, nb < nx).
+static size_t cr_mode_bytes(int nx) { return (size_t)nx * (2 * sizeof(float) + 2 * sizeof(float2) + sizeof(float)); }
+
+// Fourier modes per cyclic-reduction block, about one block per mode up to
+// K = 2 x SMs; 0 when one mode does not fit in shared memory (the chunked
+// Thomas kernel is used then).
+static int cr_modes_per_block(int nx, int K, int sms) {
+  if (cr_mode_bytes(nx) > 160 * 1024) return 0;
+  int g = K / (2 * sms);
+  const int cap = (int)(160 * 1024 / cr_mode_bytes(nx));
+  if (g > cap) g = cap;
+  if (g > 8) g = 8;
+  return g < 1 ? 1 : g;
+}
+
+static size_t cr_smem(const Poisson *P, int G) {
+  return (size_t)G * (2 * P->nx * sizeof(float) + (P->cr_nf + P->cr_nb) * sizeof(float2) + P->cr_nb * sizeof(float));
 }
 
 static int fft_smem_attr(Ctx *c, int N) {
-  const int smem = fft_ti(N, c->ps->nx, c->num_sms) * N * (int)sizeof(double2);
+  const int smem = (int)fft_smem(N, fft_tp(N, c->ps->nx, c->num_sms));
   if (smem > 48 * 1024) {
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   }
-  const int G = cr_modes_per_block(c->ps->nx);
-  const int crsm = 2 * G * c->ps->nx * (int)sizeof(double);
+  const int G = cr_modes_per_block(c->ps->nx, c->ps->K, c->num_sms);
+  const int crsm = (int)cr_smem(c->ps, G);
   if (G && crsm > 48 * 1024)
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_tridiag_cr, cudaFuncAttributeMaxDynamicSharedMemorySize, crsm));
   return ISKRA_OK;
@@ -1272,32 +1458,37 @@ static int solve_queue(Ctx *c, double rtol, int max_sweeps, double dt_for_drive,
       k_set_fixed<<<(P->ndrive_nodes + 255) / 256, 256, 0, st>>>(op, P->drive_node, P->drive_group, P->drive_par,
                                                                P->ndrive_nodes, c->d_step, dt_for_drive,
                                                                P->bfix_d, P->x, c->rho, P->eps0, nn);
-    k_fixed_to_x<<<B, T, 0, st>>>(op, P->x, c->rho, nie, nn);
+    // k_set_fixed wrote the driven rows; ρ-valued identity rows follow ρ
+    if (P->rho_fixed) k_fixed_to_x<<<B, T, 0, st>>>(op, P->x, c->rho, nie, nn);
     if (P->singular) {
       k_sum_db<<<B, T, 0, st>>>(op, c->rho, nie, nn, P->part);
       k_lambda<<<1, T, 0, st>>>(P->part, B, P->dsum, P->scal);
     }
-    k_residual<<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, P->part, kPartials, nn, P->singular, 0);
-    k_check<<<1, T, 0, st>>>(P->part, B, kPartials, P->scal, rtol2, 0);
+    if (P->separable)
+      k_residual<true, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
+                                              P->singular, rtol2, eout(c, true));
+    else
+      k_residual<true, false><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, nullptr, P->part, nn,
+                                               P->singular, rtol2, eout(c, false));
   }
   if (P->separable) {
-    const int N = P->N, K = P->K, TI = fft_ti(N, P->nx, c->num_sms);
-    const int fb = (P->nx + TI - 1) / TI;
-    const size_t smem = (size_t)TI * N * sizeof(double2);
+    const int N = P->N, K = P->K, TP = fft_tp(N, P->nx, c->num_sms);
+    const int fb = (P->nx + 2 * TP - 1) / (2 * TP);
+    const size_t smem = fft_smem(N, TP);
+    const int G = cr_modes_per_block(P->nx, K, c->num_sms);
     for (int s = 0; s < max_sweeps; s++) {
-      k_fft_fwd<<<fb, 256, smem, st>>>(P->r, P->nx, N, P->logN, TI, P->tw, P->spec, P->scal);
-      const int G = cr_modes_per_block(P->nx);
+      k_fft_fwd<<<fb, 256, smem, st>>>(P->r32, P->nx, N, P->logN, TP, P->tw, P->spec, P->scal);
       if (G) {
-        k_tridiag_cr<<<(K + G - 1) / G, 256, (size_t)2 * G * P->nx * sizeof(double), st>>>(
-            (double *)P->spec, P->nx, K, G, P->cr_levels, P->cr_fwd, P->cr_back, P->cr_backb, P->cr_top, P->q, P->gk,
-            P->cyclic, P->pin_k0, P->scal);
+        k_tridiag_cr<<<(K + G - 1) / G, 256, cr_smem(P, G), st>>>(
+            (float *)P->spec, P->nx, K, G, P->cr_levels, P->cr_nf, P->cr_nb, P->cr_fwd, P->cr_back, P->cr_backb,
+            P->cr_top, P->q, P->gk, P->cyclic, P->pin_k0, P->scal);
       } else {
-        k_tridiag<<<(2 * K + 63) / 64, 64, 0, st>>>((double *)P->spec, P->nx, K, P->low, P->inv, P->cp, P->q, P->gk,
+        k_tridiag<<<(2 * K + 63) / 64, 64, 0, st>>>((float *)P->spec, P->nx, K, P->low, P->inv, P->cp, P->q, P->gk,
                                                     P->cyclic, P->pin_k0, P->scal);
       }
-      k_fft_inv_update<<<fb, 256, smem, st>>>(P->spec, P->nx, N, P->logN, TI, P->tw, op, P->x, P->scal);
-      k_residual<<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, P->part, kPartials, nn, P->singular, 1);
-      k_check<<<1, T, 0, st>>>(P->part, B, kPartials, P->scal, rtol2, 1);
+      k_fft_inv_update<<<fb, 256, smem, st>>>(P->spec, P->nx, N, P->logN, TP, P->tw, P->cls, P->x, P->scal);
+      k_residual<false, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
+                                               P->singular, rtol2, eout(c, true));
     }
   } else {
     if (reset) {
@@ -1320,6 +1511,10 @@ static int finish_solve(Ctx *c) {
     k_sum_x<<<P->blocks, 256, 0, c->stream>>>(P->x, P->nn, P->part);
     k_shift_x<<<P->blocks, 256, 0, c->stream>>>(P->x, P->nn, P->part, P->blocks);
   }
+  // the separable path wrote E in its residual passes (the mean shift of the
+  // singular case leaves E unchanged); CG computes it here
+  c->e_from_phi = true;
+  if (P->separable) return ISKRA_OK;
   return launch_efield_from(c, P->x);
 }
 
@@ -1338,10 +1533,10 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
   int rc = poisson_prepare(c);
   if (rc) return rc;
   Poisson *P = c->ps;
-  const int chunk = P->separable ? 2 : 32;
   bool first = true;
   int done_it = 0;
   for (;;) {
+    const int chunk = std::min(P->separable ? 2 : 32, maxit - done_it);
     rc = solve_queue(c, rtol, chunk, c->graph_dt, first);
     if (rc) return rc;
     first = false;
@@ -1402,7 +1597,7 @@ int iskra_poisson_apply_dirichlet(iskra_ctx *h, const uint8_t *nodes, double phi
   }
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   ISKRA_CUDA(c, cudaMemcpy(P->bfix_d, P->bfix.data(), P->nn * sizeof(double), cudaMemcpyHostToDevice));
-  return ISKRA_OK;
+  return fixed_to_x_now(c);
 }
 
 int iskra_poisson_apply_periodic(iskra_ctx *h, int axis) {
@@ -1550,6 +1745,10 @@ int iskra_field_download(iskra_ctx *h, int which, double *out) {
     if (!c->ps || !c->ps->x) return set_err(c, ISKRA_EINVAL, "no potential yet");
     src = c->ps->x;
   } else if (which == ISKRA_FIELD_E) {
+    if (c->e_from_phi && c->ps && c->ps->x) {
+      int rc = launch_efield64(c, c->ps->x);
+      if (rc) return rc;
+    }
     src = c->E64;
     n *= 3;
   } else {

@@ -286,6 +286,7 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
   for (int n = 0; n < nsteps; n++) {
     ISKRA_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
     c->launches += c->graph_kernels;
+    c->e_from_phi = true;
     c->step++;
     c->d_step_known = c->step;
     if (c->sort_every > 0 && c->step % c->sort_every == 0) {

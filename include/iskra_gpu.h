@@ -220,7 +220,9 @@ int iskra_circuit_state(iskra_ctx *ctx, double state[5]);
  * seed keys the MCC RNG; the step counter continues across calls. (async) */
 int iskra_step(iskra_ctx *ctx, double dt, int nsteps, uint64_t seed,
                double rtol);
-/* Cell-sort cadence for iskra_step (0 = never). */
+/* Tile-sort cadence for iskra_step: every > 0 sorts every species each
+ * `every` steps, 0 never, < 0 (default) per species from its rms speed.
+ * Sorting only reorders particles in memory; the deposit is order-independent. */
 int iskra_set_sort_every(iskra_ctx *ctx, int every);
 /* Last Poisson solve: iterations and relative residual (synchronises). */
 int iskra_solve_info(iskra_ctx *ctx, int *iters, double *relres);

@@ -28,9 +28,12 @@ int grid_blocks(Ctx *c, int threads, int per_sm) {
 
 void invalidate_graphs(Ctx *c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  if (c->sort_graph) cudaGraphExecDestroy(c->sort_graph);
   c->graph = nullptr;
-  c->sort_graph = nullptr;
+  for (auto &g : c->sort_graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  c->periods_valid = false;
 }
 
 int collect_device_errors(Ctx *c) {
@@ -185,7 +188,8 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
             cudaMalloc(&c->cell_count, ((size_t)c->nkeys + 1) * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&c->cell_cursor, ((size_t)c->nkeys + 1) * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&c->scan_tmp, ((size_t)c->nkeys / 4096 + 2) * sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&c->d_step, sizeof(unsigned long long)) == cudaSuccess;
+            cudaMalloc(&c->d_step, sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMalloc(&c->d_scratch, 16 * sizeof(double)) == cudaSuccess;
   if (!ok) return fail(ISKRA_ENOMEM);
   cudaMemsetAsync(c->E32, 0, nn * sizeof(float2), c->stream);
   cudaMemsetAsync(c->E4, 0, nn * 2 * sizeof(float4), c->stream);
@@ -247,6 +251,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   cudaFree(c->scan_tmp);
   cudaFree(c->stage);
   cudaFree(c->d_step);
+  cudaFree(c->d_scratch);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete h;
   return ISKRA_OK;

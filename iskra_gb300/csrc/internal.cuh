@@ -150,10 +150,14 @@ struct Ctx {
 
   // step state
   unsigned long long step = 0;  // steps completed by iskra_step
-  int sort_every = 16;
+  int sort_every = -1;                   // > 0 fixed period, 0 never, < 0 per species from its speed
+  int sort_period[kMaxSpecies] = {};     // steps between sorts of each species (0 = never)
+  bool periods_valid = false;
+  double periods_dt = 0;
   cudaGraphExec_t graph = nullptr;       // one PIC step
-  cudaGraphExec_t sort_graph = nullptr;  // cell sort of every species
-  unsigned long long graph_kernels = 0, sort_graph_kernels = 0;
+  cudaGraphExec_t sort_graph[kMaxSpecies] = {};  // tile sort of one species
+  unsigned long long graph_kernels = 0, sort_graph_kernels[kMaxSpecies] = {};
+  double *d_scratch = nullptr;           // 16 doubles of reduction scratch
   unsigned long long launches = 0;       // kernels launched by iskra_step
   double graph_dt = 0;
   double graph_rtol = 0;
@@ -183,9 +187,9 @@ int launch_charge_density(Ctx *c);
 int launch_efield_from(Ctx *c, const double *phi);
 int launch_efield64(Ctx *c, const double *phi);
 int launch_sort(Ctx *c, int sid);
+int species_speed2(Ctx *c, int sid, double *mean_v2);  // <vx² + vy²> of the live particles (synchronises)
 int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host);
 int launch_circuit(Ctx *c, double dt);
-int poisson_solve_async(Ctx *c, double rtol, int max_sweeps);
 int poisson_prepare(Ctx *c);
 void poisson_destroy(Poisson *p);
 void mcc_destroy(Mcc *m);

@@ -749,6 +749,52 @@ int launch_sort(Ctx *c, int sid) {
   return ISKRA_OK;
 }
 
+// Σ (vx² + vy²) and the number of live particles (for the sort cadence)
+__global__ void k_speed2(SpeciesDev s, double *__restrict__ out) {
+  __shared__ float sh[2][8];
+  const long long np = s.st->np;
+  const int cur = s.st->cur;
+  const float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
+  const float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
+  float v2 = 0.f, n = 0.f;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < np; p += (long long)gridDim.x * blockDim.x) {
+    if (__float_as_int(zc[p].y) < 0) continue;
+    const float4 a = xv[p];
+    v2 = fmaf(a.z, a.z, fmaf(a.w, a.w, v2));
+    n += 1.f;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    v2 += __shfl_down_sync(0xffffffffu, v2, o);
+    n += __shfl_down_sync(0xffffffffu, n, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = v2;
+    sh[1][threadIdx.x >> 5] = n;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      a += sh[0][w];
+      b += sh[1][w];
+    }
+    atomicAdd(out, a);
+    atomicAdd(out + 1, b);
+  }
+}
+
+int species_speed2(Ctx *c, int sid, double *mean_v2) {
+  Species &s = c->species[sid];
+  ISKRA_CUDA(c, cudaMemsetAsync(c->d_scratch, 0, 2 * sizeof(double), c->stream));
+  k_speed2<<<c->num_sms * 4, 256, 0, c->stream>>>(s.dev, c->d_scratch);
+  ISKRA_CUDA(c, cudaGetLastError());
+  double h[2];
+  ISKRA_CUDA(c, cudaMemcpyAsync(h, c->d_scratch, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  *mean_v2 = h[1] > 0 ? h[0] / h[1] : 0.0;
+  return ISKRA_OK;
+}
+
 }  // namespace iskra
 
 using namespace iskra;

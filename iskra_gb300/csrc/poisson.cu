@@ -290,12 +290,18 @@ constexpr int kSmemClasses = 128;  // row-class table held in shared memory up t
 //
 // GB300 runs FP64 at ~1/64 of the FP32 rate, so this pass is built to use few
 // FP64 instructions: the sweep form sums the whole stencil in one FMA chain.
+// In a step graph the residual of the last sweep flags DERR_NOTCONV (in
+// *notconv) when the solve stops above tolerance.
+struct SweepLoop {
+  int *notconv;
+};
+
 template <bool FIRST, bool EOUT>
 __global__ void __launch_bounds__(256) k_residual(OpView op, const double *__restrict__ x,
                                                   const double *__restrict__ rho, double neg_inv_eps0,
                                                   PoissonScal *sc, double *__restrict__ r64, float *__restrict__ r32,
                                                   double *__restrict__ part, int nn, int singular, double rtol2,
-                                                  EOut eo) {
+                                                  EOut eo, SweepLoop loop) {
   __shared__ double sh[40];
   __shared__ RowClass cls_sh[kSmemClasses];
   __shared__ int last;
@@ -373,7 +379,9 @@ __global__ void __launch_bounds__(256) k_residual(OpView op, const double *__res
     else sc->iters += 1;
     sc->res2 = a;
     sc->relres = rhs2 > 0 ? sqrt(a / rhs2) : sqrt(a);
-    if ((rhs2 > 0 && a <= rtol2 * rhs2) || a == 0.0) sc->done = 1;
+    const int done = (rhs2 > 0 && a <= rtol2 * rhs2) || a == 0.0;
+    if (done) sc->done = 1;
+    if (loop.notconv && !done) atomicOr(loop.notconv, DERR_NOTCONV);
   }
 }
 
@@ -1441,42 +1449,51 @@ static int fft_smem_attr(Ctx *c, int N) {
   return ISKRA_OK;
 }
 
-// One solve queued on the stream (no host synchronisation).  Separable
-// operators: up to max_sweeps FFT/tridiagonal corrections, each skipped on the
-// device once the residual meets rtol.  Other operators: max_sweeps CG
-// iterations (the caller loops for more).
-static int solve_queue(Ctx *c, double rtol, int max_sweeps, double dt_for_drive, bool reset) {
+// First part of a solve: reset the scalars, fixed rows, the singular-case
+// shift and the first residual (with E for separable operators).
+static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop loop) {
+  Poisson *P = c->ps;
+  const int nn = P->nn, B = P->blocks, T = 256;
+  OpView op = opview(P);
+  const double nie = -1.0 / P->eps0;
+  cudaStream_t st = c->stream;
+  ISKRA_CUDA(c, cudaMemsetAsync(P->scal, 0, sizeof(PoissonScal), st));
+  if (P->ndrive_nodes)
+    k_set_fixed<<<(P->ndrive_nodes + 255) / 256, 256, 0, st>>>(op, P->drive_node, P->drive_group, P->drive_par,
+                                                             P->ndrive_nodes, c->d_step, dt_for_drive, P->bfix_d,
+                                                             P->x, c->rho, P->eps0, nn);
+  // k_set_fixed wrote the driven rows; ρ-valued identity rows follow ρ
+  if (P->rho_fixed) k_fixed_to_x<<<B, T, 0, st>>>(op, P->x, c->rho, nie, nn);
+  if (P->singular) {
+    k_sum_db<<<B, T, 0, st>>>(op, c->rho, nie, nn, P->part);
+    k_lambda<<<1, T, 0, st>>>(P->part, B, P->dsum, P->scal);
+  }
+  if (P->separable)
+    k_residual<true, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
+                                            P->singular, rtol * rtol, eout(c, true), loop);
+  else
+    k_residual<true, false><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, nullptr, P->part, nn,
+                                             P->singular, rtol * rtol, eout(c, false), loop);
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
+// `count` corrections: separable operators run the FP32 FFT/tridiagonal
+// sweep and the FP64 residual (skipped on the device once converged); other
+// operators run CG iterations (the caller loops for more).
+static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop loop) {
   Poisson *P = c->ps;
   const int nn = P->nn, B = P->blocks, T = 256;
   OpView op = opview(P);
   const double nie = -1.0 / P->eps0;
   const double rtol2 = rtol * rtol;
   cudaStream_t st = c->stream;
-  if (reset) {
-    ISKRA_CUDA(c, cudaMemsetAsync(P->scal, 0, sizeof(PoissonScal), st));
-    if (P->ndrive_nodes)
-      k_set_fixed<<<(P->ndrive_nodes + 255) / 256, 256, 0, st>>>(op, P->drive_node, P->drive_group, P->drive_par,
-                                                               P->ndrive_nodes, c->d_step, dt_for_drive,
-                                                               P->bfix_d, P->x, c->rho, P->eps0, nn);
-    // k_set_fixed wrote the driven rows; ρ-valued identity rows follow ρ
-    if (P->rho_fixed) k_fixed_to_x<<<B, T, 0, st>>>(op, P->x, c->rho, nie, nn);
-    if (P->singular) {
-      k_sum_db<<<B, T, 0, st>>>(op, c->rho, nie, nn, P->part);
-      k_lambda<<<1, T, 0, st>>>(P->part, B, P->dsum, P->scal);
-    }
-    if (P->separable)
-      k_residual<true, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
-                                              P->singular, rtol2, eout(c, true));
-    else
-      k_residual<true, false><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, nullptr, P->part, nn,
-                                               P->singular, rtol2, eout(c, false));
-  }
   if (P->separable) {
     const int N = P->N, K = P->K, TP = fft_tp(N, P->nx, c->num_sms);
     const int fb = (P->nx + 2 * TP - 1) / (2 * TP);
     const size_t smem = fft_smem(N, TP);
     const int G = cr_modes_per_block(P->nx, K, c->num_sms);
-    for (int s = 0; s < max_sweeps; s++) {
+    for (int s = 0; s < count; s++) {
       k_fft_fwd<<<fb, 256, smem, st>>>(P->r32, P->nx, N, P->logN, TP, P->tw, P->spec, P->scal);
       if (G) {
         k_tridiag_cr<<<(K + G - 1) / G, 256, cr_smem(P, G), st>>>(
@@ -1488,14 +1505,11 @@ static int solve_queue(Ctx *c, double rtol, int max_sweeps, double dt_for_drive,
       }
       k_fft_inv_update<<<fb, 256, smem, st>>>(P->spec, P->nx, N, P->logN, TP, P->tw, P->cls, P->x, P->scal);
       k_residual<false, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
-                                               P->singular, rtol2, eout(c, true));
+                                               P->singular, rtol2, eout(c, true), loop);
     }
   } else {
-    if (reset) {
-      k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);
-      // rhs2 from the residual check is already in scal
-    }
-    for (int s = 0; s < max_sweeps; s++) {
+    if (reset_cg) k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);  // rhs2 is already in scal
+    for (int s = 0; s < count; s++) {
       k_cg_ap<<<B, T, 0, st>>>(op, P->p, P->ap, P->part, nn, P->scal);
       k_cg_update<<<B, T, 0, st>>>(op, P->x, P->r, P->z, P->p, P->ap, P->part, B, nn, P->scal);
       k_cg_dir<<<B, T, 0, st>>>(op, P->z, P->p, P->part, B, nn, P->scal, rtol2);
@@ -1503,6 +1517,14 @@ static int solve_queue(Ctx *c, double rtol, int max_sweeps, double dt_for_drive,
   }
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
+}
+
+// Sweeps a step graph runs per solve (each skipped on the device once the
+// residual meets rtol): one FP32 correction reduces the residual by about
+// 10^-5 (cold start) and the step starts from the previous potential.
+static int graph_sweeps(double rtol) {
+  const int n = (int)std::ceil(std::log(rtol) / std::log(1e-5));
+  return std::max(2, std::min(8, n));
 }
 
 static int finish_solve(Ctx *c) {
@@ -1518,13 +1540,19 @@ static int finish_solve(Ctx *c) {
   return launch_efield_from(c, P->x);
 }
 
-// Graph-capturable solve (separable operators): fixed number of sweeps.
-int poisson_solve_async(Ctx *c, double rtol, int max_sweeps) {
+// Solve queued inside a step capture (separable operators).
+int poisson_solve_graph(Ctx *c, double rtol) {
   int rc = poisson_prepare(c);
   if (rc) return rc;
   Poisson *P = c->ps;
-  if (!P->separable) return set_err(c, ISKRA_EINVAL, "asynchronous solve needs a separable operator");
-  rc = solve_queue(c, rtol, max_sweeps, c->graph_dt, true);
+  if (!P->separable) return set_err(c, ISKRA_EINVAL, "graph solve needs a separable operator");
+  const int n = graph_sweeps(rtol);
+  const SweepLoop none{}, last{c->d_err};
+  rc = queue_prologue(c, rtol, c->graph_dt, none);
+  if (rc) return rc;
+  rc = queue_sweeps(c, rtol, n - 1, false, none);
+  if (rc) return rc;
+  rc = queue_sweeps(c, rtol, 1, false, last);
   if (rc) return rc;
   return finish_solve(c);
 }
@@ -1535,9 +1563,14 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
   Poisson *P = c->ps;
   bool first = true;
   int done_it = 0;
+  const SweepLoop none{};
   for (;;) {
     const int chunk = std::min(P->separable ? 2 : 32, maxit - done_it);
-    rc = solve_queue(c, rtol, chunk, c->graph_dt, first);
+    if (first) {
+      rc = queue_prologue(c, rtol, c->graph_dt, none);
+      if (rc) return rc;
+    }
+    rc = queue_sweeps(c, rtol, chunk, first, none);
     if (rc) return rc;
     first = false;
     ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost, c->stream));

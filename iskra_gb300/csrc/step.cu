@@ -1,6 +1,7 @@
 // step.cu -- the RLC circuit (Circuit/src/Circuit.jl, circuit_coupling.jl) and
 // the whole PIC step (the loop body of ParticleInCell.solve,
 // ParticleInCell/src/ParticleInCell.jl:102-135) replayed as a CUDA graph.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -12,6 +13,7 @@ double *poisson_sigma_ptr(Ctx *c);
 const double *poisson_x_ptr(Ctx *c);
 bool poisson_separable(Ctx *c);
 int poisson_solve_blocking(Ctx *c, double rtol, int maxit);
+int poisson_solve_graph(Ctx *c, double rtol);
 
 struct CircuitArgs {
   CircuitDev *cd;
@@ -98,14 +100,30 @@ static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocki
   rc = launch_charge_density(c);
   if (rc) return rc;
   if (blocking_solve) return poisson_solve_blocking(c, rtol, 10000);
-  return poisson_solve_async(c, rtol, 2);
+  return poisson_solve_graph(c, rtol);
 }
 
-static int queue_sorts(Ctx *c) {
+// Steps between tile sorts of each species.  Between sorts the push reads E
+// from and deposits into its tile's shared-memory window; particles that drift
+// more than the kHalo-cell margin off their tile take the slower global path,
+// and particles appended by MCC wait in the unsorted tail.  The automatic
+// period lets the rms in-plane particle move reach 1.5 kHalo cells, clamped
+// to [4, 64] steps.
+static int update_sort_periods(Ctx *c, double dt) {
+  const double h = std::min(c->g.dx, c->g.dy);
   for (int s = 0; s < (int)c->species.size(); s++) {
-    int rc = launch_sort(c, s);
+    if (c->sort_every >= 0) {
+      c->sort_period[s] = c->sort_every;
+      continue;
+    }
+    double v2 = 0;
+    int rc = species_speed2(c, s, &v2);
     if (rc) return rc;
+    const double cells = std::sqrt(v2) * dt / h;  // rms cells moved per step
+    double p = cells > 0 ? 1.5 * kHalo / cells : 64.0;
+    c->sort_period[s] = (int)std::max(4.0, std::min(64.0, std::floor(p)));
   }
+  c->periods_valid = true;
   return ISKRA_OK;
 }
 
@@ -228,9 +246,10 @@ int iskra_circuit_state(iskra_ctx *h, double state[5]) {
 }
 
 int iskra_set_sort_every(iskra_ctx *h, int every) {
-  if (!h || every < 0) return ISKRA_EINVAL;
+  if (!h) return ISKRA_EINVAL;
   Ctx *c = &h->c;
-  c->sort_every = every;
+  c->sort_every = every < 0 ? -1 : every;
+  c->periods_valid = false;
   return ISKRA_OK;
 }
 
@@ -254,6 +273,11 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
                                   c->stream));
   }
   c->graph_dt = dt;
+  if (!c->periods_valid || c->periods_dt != dt) {
+    rc = update_sort_periods(c, dt);
+    if (rc) return rc;
+    c->periods_dt = dt;
+  }
   if (!poisson_separable(c)) {
     // eager path: CG needs host-side convergence checks
     for (int n = 0; n < nsteps; n++) {
@@ -261,9 +285,11 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
       if (rc) return rc;
       c->step++;
       c->d_step_known = c->step;
-      if (c->sort_every && c->step % c->sort_every == 0) {
-        rc = queue_sorts(c);
-        if (rc) return rc;
+      for (int s = 0; s < (int)c->species.size(); s++) {
+        if (c->sort_period[s] > 0 && c->step % c->sort_period[s] == 0) {
+          rc = launch_sort(c, s);
+          if (rc) return rc;
+        }
       }
     }
     return collect_device_errors(c);
@@ -279,9 +305,11 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
     c->graph_seed = seed;
     c->graph_dt = dt;
   }
-  if (!c->sort_graph && c->sort_every > 0) {
-    rc = capture(c, &c->sort_graph, &c->sort_graph_kernels, [&]() { return queue_sorts(c); });
-    if (rc) return rc;
+  for (int s = 0; s < (int)c->species.size(); s++) {
+    if (!c->sort_graph[s] && c->sort_period[s] > 0) {
+      rc = capture(c, &c->sort_graph[s], &c->sort_graph_kernels[s], [&]() { return launch_sort(c, s); });
+      if (rc) return rc;
+    }
   }
   for (int n = 0; n < nsteps; n++) {
     ISKRA_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
@@ -289,9 +317,11 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
     c->e_from_phi = true;
     c->step++;
     c->d_step_known = c->step;
-    if (c->sort_every > 0 && c->step % c->sort_every == 0) {
-      ISKRA_CUDA(c, cudaGraphLaunch(c->sort_graph, c->stream));
-      c->launches += c->sort_graph_kernels;
+    for (int s = 0; s < (int)c->species.size(); s++) {
+      if (c->sort_period[s] > 0 && c->step % c->sort_period[s] == 0) {
+        ISKRA_CUDA(c, cudaGraphLaunch(c->sort_graph[s], c->stream));
+        c->launches += c->sort_graph_kernels[s];
+      }
     }
   }
   return ISKRA_OK;

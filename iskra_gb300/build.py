@@ -43,7 +43,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     srcs = sources()
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     hdrs.append(os.path.join(os.path.dirname(HERE), "include", "iskra_gpu.h"))
-    if not force and os.path.exists(LIB):
+    stamp = os.path.join(OUT_DIR, ".flags")
+    flags = " ".join(ARCH + FLAGS)
+    old = open(stamp).read() if os.path.exists(stamp) else ""
+    if not force and os.path.exists(LIB) and old == flags:
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(f) < t for f in srcs + hdrs + [__file__]):
             return LIB
@@ -63,6 +66,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    with open(stamp, "w") as f:
+        f.write(flags)
     return LIB
 
 

@@ -42,7 +42,8 @@ struct Moments {
 
 // Inclusive segmented sum of the moments over runs of lanes holding the same
 // key (any particle order is correct; cell-sorted particles give long runs):
-// five shuffle rounds with a run-start guard.  Returns true on the last lane
+// shuffle rounds with a run-start guard, as many as the longest run needs
+// (at most five).  Returns true on the last lane
 // of each run, which then holds the run's sums; *n receives the run length.
 // (A per-run __reduce_add_sync over the run's lane mask measured 2x slower on
 // GB300 once the runs shorten between sorts.)
@@ -56,8 +57,11 @@ __device__ __forceinline__ bool reduce_runs(int key, Moments &m, unsigned &n) {
   const unsigned heads = __ballot_sync(FULL, head);
   const int start = 31 - __clz(heads & ((2u << lane) - 1u));  // first lane of my run
   if (heads != FULL) {  // warp-uniform: some run is longer than one lane
+    // rounds up to the longest run only (d < its length)
+    const int pos = lane - start;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
+      if (!__any_sync(FULL, pos >= d)) break;
       const unsigned su = __shfl_up_sync(FULL, m.su, d);
       const unsigned sv = __shfl_up_sync(FULL, m.sv, d);
       const unsigned hi = __shfl_up_sync(FULL, m.hi, d);

@@ -40,7 +40,7 @@ struct RowClass {
   int sig_dof;                // -1: none
   int fixed;                  // identity row
   int rho;                    // b = -ρ/ε0 (ρ dof) else b = bfix
-  int pad;
+  float nd32;                 // -d in FP32 (scaling of the FP32 residual)
 };
 
 struct DriveGroup {
@@ -296,79 +296,74 @@ struct SweepLoop {
   int *notconv;
 };
 
-template <bool FIRST, bool EOUT>
-__global__ void __launch_bounds__(256) k_residual(OpView op, const double *__restrict__ x,
-                                                  const double *__restrict__ rho, double neg_inv_eps0,
-                                                  PoissonScal *sc, double *__restrict__ r64, float *__restrict__ r32,
-                                                  double *__restrict__ part, int nn, int singular, double rtol2,
-                                                  EOut eo, SweepLoop loop) {
-  __shared__ double sh[40];
-  __shared__ RowClass cls_sh[kSmemClasses];
-  __shared__ int last;
-  if (!FIRST && sc->done) return;
-  const bool sm = op.nclass <= kSmemClasses;
-  if (sm)
-    for (int t = threadIdx.x; t < op.nclass; t += blockDim.x) cls_sh[t] = op.classes[t];
-  __syncthreads();
-  const RowClass *__restrict__ CT = sm ? cls_sh : op.classes;
-  const double lam = singular ? sc->lambda : 0.0;
+// Residual of free row k: res = b - λ - A x, returned scaled as -d res in
+// FP32 (r64 != nullptr also receives it in FP64); 0 on fixed rows.  The
+// FIRST pass of a solve also accumulates ||rhs_eff||² (rhs_eff = b - λ -
+// A_fixed x_fixed).
+template <bool FIRST>
+__device__ __forceinline__ float residual_node(const OpView &op, const RowClass *__restrict__ CT,
+                                               const double *__restrict__ x, const double *__restrict__ rho,
+                                               double neg_inv_eps0, double lam, int singular, int k, int i, int j,
+                                               double *__restrict__ r64, double &a2, double &b2) {
   const int nx = op.nx, ny = op.ny;
-  double a2 = 0, b2 = 0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const int j = k / nx, i = k - j * nx;
-    if (EOUT) efield_at(x, k, i, j, nx, ny, eo);
-    const unsigned ck = op.cls[k];
-    if (ck & kFixedBit) {
-      if (r32) r32[k] = 0.f;
-      else r64[k] = 0.0;
-      continue;
-    }
-    const RowClass &C = CT[ck];
-    const int w = i > 0 ? k - 1 : k + nx - 1;
-    const int e = i < nx - 1 ? k + 1 : k - nx + 1;
-    const int s = j > 0 ? k - nx : k + nx * (ny - 1);
-    const int n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
-    double b = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
-    if (singular) b -= lam;
-    if (C.sig_dof >= 0) b -= C.sig_coef * op.sigma[C.sig_dof];
-    double res;
-    if (FIRST) {
-      double afix = 0, afree = C.c0 * x[k];
-      double t;
-      t = C.cW * x[w];
-      if (op.cls[w] & kFixedBit) afix += t; else afree += t;
-      t = C.cE * x[e];
-      if (op.cls[e] & kFixedBit) afix += t; else afree += t;
-      t = C.cS * x[s];
-      if (op.cls[s] & kFixedBit) afix += t; else afree += t;
-      t = C.cN * x[n];
-      if (op.cls[n] & kFixedBit) afix += t; else afree += t;
-      const double rhs = b - afix;
-      res = rhs - afree;
-      b2 = fma(rhs, rhs, b2);
-    } else {
-      double ax = C.c0 * x[k];
-      ax = fma(C.cW, x[w], ax);
-      ax = fma(C.cE, x[e], ax);
-      ax = fma(C.cS, x[s], ax);
-      ax = fma(C.cN, x[n], ax);
-      res = b - ax;
-    }
-    const double sr = -C.d * res;
-    if (r32) r32[k] = (float)sr;
-    else r64[k] = sr;
-    a2 = fma(res, res, a2);
+  const unsigned ck = op.cls[k];
+  if (ck & kFixedBit) {
+    if (r64) r64[k] = 0.0;
+    return 0.f;
   }
+  const RowClass &C = CT[ck];
+  const int w = i > 0 ? k - 1 : k + nx - 1;
+  const int e = i < nx - 1 ? k + 1 : k - nx + 1;
+  const int s = j > 0 ? k - nx : k + nx * (ny - 1);
+  const int n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
+  double b = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+  if (singular) b -= lam;
+  if (C.sig_dof >= 0) b -= C.sig_coef * op.sigma[C.sig_dof];
+  double res;
+  if (FIRST) {
+    double afix = 0, afree = C.c0 * x[k];
+    double t;
+    t = C.cW * x[w];
+    if (op.cls[w] & kFixedBit) afix += t; else afree += t;
+    t = C.cE * x[e];
+    if (op.cls[e] & kFixedBit) afix += t; else afree += t;
+    t = C.cS * x[s];
+    if (op.cls[s] & kFixedBit) afix += t; else afree += t;
+    t = C.cN * x[n];
+    if (op.cls[n] & kFixedBit) afix += t; else afree += t;
+    const double rhs = b - afix;
+    res = rhs - afree;
+    b2 = fma(rhs, rhs, b2);
+  } else {
+    // GB300 runs FP64 at ~1/64 of the FP32 rate: one FMA chain over the stencil
+    double ax = C.c0 * x[k];
+    ax = fma(C.cW, x[w], ax);
+    ax = fma(C.cE, x[e], ax);
+    ax = fma(C.cS, x[s], ax);
+    ax = fma(C.cN, x[n], ax);
+    res = b - ax;
+  }
+  a2 = fma(res, res, a2);
+  if (r64) r64[k] = -C.d * res;
+  return (float)res * C.nd32;
+}
+
+// Block partials of the norms, then the last block to finish sums them in
+// block order (deterministic), updates relres/iters and sets sc->done when
+// ||res|| <= rtol ||rhs_eff||.  Ends the kernel for every other block.
+template <bool FIRST>
+__device__ __forceinline__ void finish_norms(PoissonScal *sc, double *__restrict__ part, double a2, double b2,
+                                             double rtol2, SweepLoop loop, double *sh, int *last) {
   const double ta = block_sum(a2, sh);
   const double tb = FIRST ? block_sum(b2, sh) : 0.0;
   if (threadIdx.x == 0) {
     part[blockIdx.x] = ta;
     if (FIRST) part[kPartials + blockIdx.x] = tb;
     __threadfence();
-    last = atomicAdd(&sc->ticket, 1u) == gridDim.x - 1;
+    *last = atomicAdd(&sc->ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last) return;
+  if (!*last) return;
   __threadfence();
   const double a = sum_partials(part, gridDim.x, sh);
   const double bb = FIRST ? sum_partials(part + kPartials, gridDim.x, sh) : 0.0;
@@ -383,6 +378,40 @@ __global__ void __launch_bounds__(256) k_residual(OpView op, const double *__res
     if (done) sc->done = 1;
     if (loop.notconv && !done) atomicOr(loop.notconv, DERR_NOTCONV);
   }
+}
+
+__device__ __forceinline__ const RowClass *stage_classes(const OpView &op, RowClass *cls_sh) {
+  const bool sm = op.nclass <= kSmemClasses;
+  if (sm)
+    for (int t = threadIdx.x; t < op.nclass; t += blockDim.x) cls_sh[t] = op.classes[t];
+  __syncthreads();
+  return sm ? cls_sh : op.classes;
+}
+
+// Residual pass over all nodes (scaled residual to r32 or r64), optionally
+// with E = -∇ϕ, and the convergence test.  Passes after the first return at
+// once when sc->done is set and count one sweep each.
+template <bool FIRST, bool EOUT>
+__global__ void __launch_bounds__(256) k_residual(OpView op, const double *__restrict__ x,
+                                                  const double *__restrict__ rho, double neg_inv_eps0,
+                                                  PoissonScal *sc, double *__restrict__ r64, float *__restrict__ r32,
+                                                  double *__restrict__ part, int nn, int singular, double rtol2,
+                                                  EOut eo, SweepLoop loop) {
+  __shared__ double sh[40];
+  __shared__ RowClass cls_sh[kSmemClasses];
+  __shared__ int last;
+  if (!FIRST && sc->done) return;
+  const RowClass *__restrict__ CT = stage_classes(op, cls_sh);
+  const double lam = singular ? sc->lambda : 0.0;
+  const int nx = op.nx, ny = op.ny;
+  double a2 = 0, b2 = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const int j = k / nx, i = k - j * nx;
+    if (EOUT) efield_at(x, k, i, j, nx, ny, eo);
+    const float v = residual_node<FIRST>(op, CT, x, rho, neg_inv_eps0, lam, singular, k, i, j, r64, a2, b2);
+    if (r32) r32[k] = v;
+  }
+  finish_norms<FIRST>(sc, part, a2, b2, rtol2, loop, sh, &last);
 }
 
 // ---------------- separable correction: FFT(y) x tridiagonal(x), FP32 ----------------
@@ -1046,6 +1075,7 @@ static int build_device(Ctx *c, Poisson *P) {
       rc.cS = e.cS;
       rc.cN = e.cN;
       rc.d = e.fixed ? 1.0 : d[r];
+      rc.nd32 = (float)(-rc.d);
       rc.sig_coef = e.sig_coef;
       rc.sig_dof = e.sig_dof;
       rc.fixed = e.fixed;
@@ -1438,15 +1468,29 @@ static size_t cr_smem(const Poisson *P, int G) {
 
 static int fft_smem_attr(Ctx *c, int N) {
   const int smem = (int)fft_smem(N, fft_tp(N, c->ps->nx, c->num_sms));
-  if (smem > 48 * 1024) {
-    ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  }
+  ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   const int G = cr_modes_per_block(c->ps->nx, c->ps->K, c->num_sms);
   const int crsm = (int)cr_smem(c->ps, G);
   if (G && crsm > 48 * 1024)
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_tridiag_cr, cudaFuncAttributeMaxDynamicSharedMemorySize, crsm));
   return ISKRA_OK;
+}
+
+// Launch shape of the separable correction.
+struct SepShape {
+  int TP, fb, G;
+  size_t smem;
+};
+
+static SepShape sep_shape(Ctx *c) {
+  Poisson *P = c->ps;
+  SepShape sh;
+  sh.TP = fft_tp(P->N, P->nx, c->num_sms);
+  sh.fb = (P->nx + 2 * sh.TP - 1) / (2 * sh.TP);
+  sh.smem = fft_smem(P->N, sh.TP);
+  sh.G = cr_modes_per_block(P->nx, P->K, c->num_sms);
+  return sh;
 }
 
 // First part of a solve: reset the scalars, fixed rows, the singular-case
@@ -1468,19 +1512,21 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
     k_sum_db<<<B, T, 0, st>>>(op, c->rho, nie, nn, P->part);
     k_lambda<<<1, T, 0, st>>>(P->part, B, P->dsum, P->scal);
   }
-  if (P->separable)
+  if (P->separable) {
     k_residual<true, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
                                             P->singular, rtol * rtol, eout(c, true), loop);
-  else
+  } else {
     k_residual<true, false><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, nullptr, P->part, nn,
                                              P->singular, rtol * rtol, eout(c, false), loop);
+  }
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }
 
-// `count` corrections: separable operators run the FP32 FFT/tridiagonal
-// sweep and the FP64 residual (skipped on the device once converged); other
-// operators run CG iterations (the caller loops for more).
+// `count` corrections: separable operators run the FP32 FFT, tridiagonal
+// solve and inverse FFT, then the FP64 residual (each skipped on the device
+// once converged); other operators run CG iterations (the caller loops for
+// more).  `loop` applies to the last residual only.
 static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop loop) {
   Poisson *P = c->ps;
   const int nn = P->nn, B = P->blocks, T = 256;
@@ -1488,24 +1534,24 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
   const double nie = -1.0 / P->eps0;
   const double rtol2 = rtol * rtol;
   cudaStream_t st = c->stream;
+  const SweepLoop none{};
   if (P->separable) {
-    const int N = P->N, K = P->K, TP = fft_tp(N, P->nx, c->num_sms);
-    const int fb = (P->nx + 2 * TP - 1) / (2 * TP);
-    const size_t smem = fft_smem(N, TP);
-    const int G = cr_modes_per_block(P->nx, K, c->num_sms);
+    const SepShape sh = sep_shape(c);
+    const int N = P->N, K = P->K;
     for (int s = 0; s < count; s++) {
-      k_fft_fwd<<<fb, 256, smem, st>>>(P->r32, P->nx, N, P->logN, TP, P->tw, P->spec, P->scal);
-      if (G) {
-        k_tridiag_cr<<<(K + G - 1) / G, 256, cr_smem(P, G), st>>>(
-            (float *)P->spec, P->nx, K, G, P->cr_levels, P->cr_nf, P->cr_nb, P->cr_fwd, P->cr_back, P->cr_backb,
+      const bool last = s == count - 1;
+      k_fft_fwd<<<sh.fb, 256, sh.smem, st>>>(P->r32, P->nx, N, P->logN, sh.TP, P->tw, P->spec, P->scal);
+      if (sh.G) {
+        k_tridiag_cr<<<(K + sh.G - 1) / sh.G, 256, cr_smem(P, sh.G), st>>>(
+            (float *)P->spec, P->nx, K, sh.G, P->cr_levels, P->cr_nf, P->cr_nb, P->cr_fwd, P->cr_back, P->cr_backb,
             P->cr_top, P->q, P->gk, P->cyclic, P->pin_k0, P->scal);
       } else {
         k_tridiag<<<(2 * K + 63) / 64, 64, 0, st>>>((float *)P->spec, P->nx, K, P->low, P->inv, P->cp, P->q, P->gk,
                                                     P->cyclic, P->pin_k0, P->scal);
       }
-      k_fft_inv_update<<<fb, 256, smem, st>>>(P->spec, P->nx, N, P->logN, TP, P->tw, P->cls, P->x, P->scal);
+      k_fft_inv_update<<<sh.fb, 256, sh.smem, st>>>(P->spec, P->nx, N, P->logN, sh.TP, P->tw, P->cls, P->x, P->scal);
       k_residual<false, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
-                                               P->singular, rtol2, eout(c, true), loop);
+                                               P->singular, rtol2, eout(c, true), last ? loop : none);
     }
   } else {
     if (reset_cg) k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);  // rhs2 is already in scal
@@ -1550,9 +1596,7 @@ int poisson_solve_graph(Ctx *c, double rtol) {
   const SweepLoop none{}, last{c->d_err};
   rc = queue_prologue(c, rtol, c->graph_dt, none);
   if (rc) return rc;
-  rc = queue_sweeps(c, rtol, n - 1, false, none);
-  if (rc) return rc;
-  rc = queue_sweeps(c, rtol, 1, false, last);
+  rc = queue_sweeps(c, rtol, n, false, last);
   if (rc) return rc;
   return finish_solve(c);
 }

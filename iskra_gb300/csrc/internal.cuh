@@ -167,6 +167,30 @@ struct Ctx {
   unsigned long long d_step_host = 0;       // source of the d_step upload
 };
 
+// ---- programmatic dependent launch ----
+// Step kernels are launched with programmatic stream serialisation: the next
+// kernel is scheduled while the previous one drains, and waits here (before
+// its first access to anything an earlier kernel wrote) until that kernel
+// has completed and its memory is visible.  Outside such a launch the wait
+// returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... K, typename... A>
+inline cudaError_t launch_pdl(void (*kern)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              A &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<A &&>(args)...);
+}
+
 // ---- helpers (ctx.cu) ----
 int set_err(Ctx *c, int code, const std::string &msg);
 int cuda_check(Ctx *c, cudaError_t e, const char *what);

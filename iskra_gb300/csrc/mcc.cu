@@ -211,6 +211,7 @@ __device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsi
 __global__ void __launch_bounds__(256) k_mcc(SpeciesDev s, SpeciesDev prod, int has_prod, MccDev M,
                                              const float2 *__restrict__ E, int nx,
                                              const unsigned long long *__restrict__ d_step, int *err) {
+  pdl_wait();
   extern __shared__ float tab[];
   const unsigned FULL = 0xffffffffu;
   const int ntab = M.off[M.N];
@@ -396,10 +397,12 @@ __global__ void __launch_bounds__(256) k_mcc(SpeciesDev s, SpeciesDev prod, int 
 // kernel) stays fixed during the launch; np takes the new extent afterwards,
 // clamped to the capacity (failed appends already raised DERR_CAPACITY).
 __global__ void k_append_begin(SpeciesState *a, SpeciesState *b) {
+  pdl_wait();
   a->np_new = a->np;
   if (b) b->np_new = b->np;
 }
 __global__ void k_append_end(SpeciesState *st, long long cap) {
+  pdl_wait();
   st->np = st->np_new > cap ? cap : st->np_new;
 }
 
@@ -441,11 +444,13 @@ int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long lo
   long long maxb = (long long)c->num_sms * 8;
   int blocks = (int)(want < maxb ? (want < 1 ? 1 : want) : maxb);
   SpeciesDev pd = m->prod >= 0 ? c->species[m->prod].dev : s.dev;
-  k_append_begin<<<1, 1, 0, c->stream>>>(s.dev.st, m->prod >= 0 ? c->species[m->prod].dev.st : nullptr);
-  k_mcc<<<blocks, 256, smem, c->stream>>>(s.dev, pd, m->prod >= 0, M, c->E32, c->nx, d_step, c->d_err);
-  ISKRA_CUDA(c, cudaGetLastError());
-  k_append_end<<<1, 1, 0, c->stream>>>(s.dev.st, s.cap);
-  if (m->prod >= 0) k_append_end<<<1, 1, 0, c->stream>>>(c->species[m->prod].dev.st, c->species[m->prod].cap);
+  SpeciesState *pst = m->prod >= 0 ? c->species[m->prod].dev.st : nullptr;
+  ISKRA_CUDA(c, launch_pdl(k_append_begin, 1, 1, 0, c->stream, s.dev.st, pst));
+  ISKRA_CUDA(c, launch_pdl(k_mcc, blocks, 256, smem, c->stream, s.dev, pd, (int)(m->prod >= 0), M, c->E32, c->nx,
+                           d_step, c->d_err));
+  ISKRA_CUDA(c, launch_pdl(k_append_end, 1, 1, 0, c->stream, s.dev.st, s.cap));
+  if (m->prod >= 0)
+    ISKRA_CUDA(c, launch_pdl(k_append_end, 1, 1, 0, c->stream, c->species[m->prod].dev.st, c->species[m->prod].cap));
   ISKRA_CUDA(c, cudaGetLastError());
   // appended particles are not in the deposit accumulators
   for (int sid : {m->src, m->prod}) {

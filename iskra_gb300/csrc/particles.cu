@@ -252,6 +252,7 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
 template <bool PUSH, int MX, int MY>
 __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev s, const float4 *__restrict__ E4,
                                                                      PushParams P, int ntiles, int *err) {
+  pdl_wait();
   __shared__ PushShared sh;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
@@ -362,19 +363,20 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev 
   }
 }
 
-static void launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
+static cudaError_t launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
   const int T = 256;
 #define ISKRA_PUSH_CASE(MX, MY)                                                                 \
   if (P.mode_x == MX && P.mode_y == MY) {                                                       \
     cudaFuncSetAttribute(k_push<true, MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,  \
                          (int)cudaSharedmemCarveoutMaxShared);                                  \
-    k_push<true, MX, MY><<<blocks, T, 0, c->stream>>>(s.dev, c->E4, P, c->ntiles, c->d_err);   \
-    return;                                                                                     \
+    return launch_pdl(k_push<true, MX, MY>, blocks, T, 0, c->stream, s.dev, (const float4 *)c->E4, P,  \
+                      c->ntiles, c->d_err);                                                     \
   }
   ISKRA_PUSH_CASE(0, 0) ISKRA_PUSH_CASE(0, 1) ISKRA_PUSH_CASE(0, 2)
   ISKRA_PUSH_CASE(1, 0) ISKRA_PUSH_CASE(1, 1) ISKRA_PUSH_CASE(1, 2)
   ISKRA_PUSH_CASE(2, 0) ISKRA_PUSH_CASE(2, 1) ISKRA_PUSH_CASE(2, 2)
 #undef ISKRA_PUSH_CASE
+  return cudaErrorInvalidValue;
 }
 
 // one block per tile plus a grid-stride set for the unsorted tail
@@ -403,7 +405,7 @@ int launch_advance(Ctx *c, int sid, float dt) {
   P.mode_x = s.bnd[0];
   P.mode_y = s.bnd[1];
   P.tiles_x = c->tiles_x;
-  launch_push_modes(c, s, P, push_blocks(c));
+  ISKRA_CUDA(c, launch_push_modes(c, s, P, push_blocks(c)));
   ISKRA_CUDA(c, cudaGetLastError());
   s.acc_valid = true;  // accumulator = deposit of the pushed positions (unconsumed)
   s.acc_zero = false;
@@ -449,6 +451,7 @@ constexpr unsigned kMaxCell = 16383;
 
 __global__ void k_finalize(FinalizeArgs A, const double *__restrict__ vol_inv, const double *__restrict__ bg,
                            double *__restrict__ rho, int nn, int *err) {
+  pdl_wait();
   int flags = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     // all loads of the node first (independent, in flight together), then the
@@ -514,8 +517,8 @@ static int finalize(Ctx *c, bool with_rho) {
   int blocks = c->num_sms * 4;
   int need = (c->nn + 255) / 256;
   if (need < blocks) blocks = need;
-  k_finalize<<<blocks, 256, 0, c->stream>>>(A, c->vol_inv, c->rho_bg, with_rho ? c->rho : nullptr, c->nn,
-                                            c->d_err);
+  ISKRA_CUDA(c, launch_pdl(k_finalize, blocks, 256, 0, c->stream, A, (const double *)c->vol_inv,
+                           (const double *)c->rho_bg, with_rho ? c->rho : nullptr, c->nn, c->d_err));
   ISKRA_CUDA(c, cudaGetLastError());
   for (int s = 0; s < A.ns; s++) {
     Species &sp = c->species[s];

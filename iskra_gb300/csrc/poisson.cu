@@ -182,6 +182,7 @@ __global__ void k_set_fixed(OpView op, const int *__restrict__ dnode, const int 
                             const double *__restrict__ dpar, int ndn, const unsigned long long *__restrict__ step,
                             double dt, double *__restrict__ bfix_mut, double *__restrict__ x,
                             const double *__restrict__ rho, double eps0, int nn) {
+  pdl_wait();
   // driven groups update bfix (solve of step n uses V((n-2)Δt), n >= 2)
   const unsigned long long n_step = step ? *step : 0ull;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ndn; t += gridDim.x * blockDim.x) {
@@ -196,6 +197,7 @@ __global__ void k_set_fixed(OpView op, const int *__restrict__ dnode, const int 
 
 __global__ void k_fixed_to_x(OpView op, double *__restrict__ x, const double *__restrict__ rho, double neg_inv_eps0,
                              int nn) {
+  pdl_wait();
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const unsigned ck = op.cls[k];
     if (ck & kFixedBit) x[k] = op.classes[ck & kClassMask].rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
@@ -233,6 +235,7 @@ __device__ double sum_partials(const double *__restrict__ part, int n, double *s
 // Σ d_k b_k over free rows (singular case only: no fixed rows exist)
 __global__ void k_sum_db(OpView op, const double *__restrict__ rho, double neg_inv_eps0, int nn,
                          double *__restrict__ part) {
+  pdl_wait();
   __shared__ double sh[40];
   double v = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
@@ -248,6 +251,7 @@ __global__ void k_sum_db(OpView op, const double *__restrict__ rho, double neg_i
 }
 
 __global__ void k_lambda(const double *__restrict__ part, int nparts, double dsum, PoissonScal *sc) {
+  pdl_wait();
   __shared__ double sh[40];
   double s = sum_partials(part, nparts, sh);
   if (threadIdx.x == 0) sc->lambda = dsum > 0 ? s / dsum : 0.0;
@@ -370,12 +374,16 @@ __device__ __forceinline__ void finish_norms(PoissonScal *sc, double *__restrict
   if (threadIdx.x == 0) {
     sc->ticket = 0u;
     const double rhs2 = FIRST ? bb : sc->rhs2;
-    if (FIRST) sc->rhs2 = bb;
-    else sc->iters += 1;
+    if (FIRST) {
+      sc->rhs2 = bb;
+      sc->iters = 0;
+    } else {
+      sc->iters += 1;
+    }
     sc->res2 = a;
     sc->relres = rhs2 > 0 ? sqrt(a / rhs2) : sqrt(a);
     const int done = (rhs2 > 0 && a <= rtol2 * rhs2) || a == 0.0;
-    if (done) sc->done = 1;
+    sc->done = done;
     if (loop.notconv && !done) atomicOr(loop.notconv, DERR_NOTCONV);
   }
 }
@@ -397,6 +405,7 @@ __global__ void __launch_bounds__(256) k_residual(OpView op, const double *__res
                                                   PoissonScal *sc, double *__restrict__ r64, float *__restrict__ r32,
                                                   double *__restrict__ part, int nn, int singular, double rtol2,
                                                   EOut eo, SweepLoop loop) {
+  pdl_wait();
   __shared__ double sh[40];
   __shared__ RowClass cls_sh[kSmemClasses];
   __shared__ int last;
@@ -458,6 +467,7 @@ __device__ void fft_columns(float2 *buf, int TP, int N, int S, int logN, const f
 __global__ void __launch_bounds__(256) k_fft_fwd(const float *__restrict__ r, int nx, int N, int logN, int TP,
                                                  const float2 *__restrict__ tw, float2 *__restrict__ spec,
                                                  const PoissonScal *__restrict__ sc) {
+  pdl_wait();
   extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
   if (sc->done) return;
   const int S = N + 1, W = 2 * TP, K = (N >> 1) + 1;
@@ -495,6 +505,7 @@ __global__ void __launch_bounds__(64) k_tridiag(float *__restrict__ spec, int nx
                                                 const float *__restrict__ cp, const float *__restrict__ q,
                                                 const float *__restrict__ gk, int cyclic, int pin0,
                                                 const PoissonScal *__restrict__ sc) {
+  pdl_wait();
   if (sc->done) return;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = t >> 1, part = t & 1;
@@ -562,6 +573,7 @@ __global__ void __launch_bounds__(256) k_tridiag_cr(float *__restrict__ spec, in
                                                     const float *__restrict__ top, const float *__restrict__ q,
                                                     const float *__restrict__ gk, int cyclic, int pin0,
                                                     const PoissonScal *__restrict__ sc) {
+  pdl_wait();
   extern __shared__ float fsh[];  // data [col][nx] (col = 2 (k - k0) + part), then per mode fwd, back, backb
   if (sc->done) return;
   const int k0 = blockIdx.x * G;
@@ -632,6 +644,7 @@ __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict
                                                         int TP, const float2 *__restrict__ tw,
                                                         const uint16_t *__restrict__ cls, double *__restrict__ x,
                                                         const PoissonScal *__restrict__ sc) {
+  pdl_wait();
   extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
   if (sc->done) return;
   const int S = N + 1, W = 2 * TP, K = (N >> 1) + 1;
@@ -697,6 +710,7 @@ __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict
 
 // mean-zero projection of x over nodes (singular case)
 __global__ void k_sum_x(const double *__restrict__ x, int nn, double *__restrict__ part) {
+  pdl_wait();
   __shared__ double sh[40];
   double v = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) v += x[k];
@@ -704,6 +718,7 @@ __global__ void k_sum_x(const double *__restrict__ x, int nn, double *__restrict
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 __global__ void k_shift_x(double *__restrict__ x, int nn, const double *__restrict__ part, int nparts) {
+  pdl_wait();
   __shared__ double sh[40];
   double s = sum_partials(part, nparts, sh);
   const double m = s / nn;
@@ -1501,23 +1516,26 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
   OpView op = opview(P);
   const double nie = -1.0 / P->eps0;
   cudaStream_t st = c->stream;
-  ISKRA_CUDA(c, cudaMemsetAsync(P->scal, 0, sizeof(PoissonScal), st));
+  // (the first residual pass resets the solver scalars)
   if (P->ndrive_nodes)
-    k_set_fixed<<<(P->ndrive_nodes + 255) / 256, 256, 0, st>>>(op, P->drive_node, P->drive_group, P->drive_par,
-                                                             P->ndrive_nodes, c->d_step, dt_for_drive, P->bfix_d,
-                                                             P->x, c->rho, P->eps0, nn);
+    ISKRA_CUDA(c, launch_pdl(k_set_fixed, (P->ndrive_nodes + 255) / 256, 256, 0, st, op,
+                             (const int *)P->drive_node, (const int *)P->drive_group, (const double *)P->drive_par,
+                             P->ndrive_nodes, (const unsigned long long *)c->d_step, dt_for_drive, P->bfix_d, P->x,
+                             (const double *)c->rho, P->eps0, nn));
   // k_set_fixed wrote the driven rows; ρ-valued identity rows follow ρ
-  if (P->rho_fixed) k_fixed_to_x<<<B, T, 0, st>>>(op, P->x, c->rho, nie, nn);
+  if (P->rho_fixed) ISKRA_CUDA(c, launch_pdl(k_fixed_to_x, B, T, 0, st, op, P->x, (const double *)c->rho, nie, nn));
   if (P->singular) {
-    k_sum_db<<<B, T, 0, st>>>(op, c->rho, nie, nn, P->part);
-    k_lambda<<<1, T, 0, st>>>(P->part, B, P->dsum, P->scal);
+    ISKRA_CUDA(c, launch_pdl(k_sum_db, B, T, 0, st, op, (const double *)c->rho, nie, nn, P->part));
+    ISKRA_CUDA(c, launch_pdl(k_lambda, 1, T, 0, st, (const double *)P->part, B, P->dsum, P->scal));
   }
   if (P->separable) {
-    k_residual<true, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
-                                            P->singular, rtol * rtol, eout(c, true), loop);
+    ISKRA_CUDA(c, launch_pdl(k_residual<true, true>, B, T, 0, st, op, (const double *)P->x, (const double *)c->rho,
+                             nie, P->scal, (double *)nullptr, P->r32, P->part, nn, (int)P->singular, rtol * rtol,
+                             eout(c, true), loop));
   } else {
-    k_residual<true, false><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, P->r, nullptr, P->part, nn,
-                                             P->singular, rtol * rtol, eout(c, false), loop);
+    ISKRA_CUDA(c, launch_pdl(k_residual<true, false>, B, T, 0, st, op, (const double *)P->x, (const double *)c->rho,
+                             nie, P->scal, P->r, (float *)nullptr, P->part, nn, (int)P->singular, rtol * rtol,
+                             eout(c, false), loop));
   }
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
@@ -1540,18 +1558,24 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
     const int N = P->N, K = P->K;
     for (int s = 0; s < count; s++) {
       const bool last = s == count - 1;
-      k_fft_fwd<<<sh.fb, 256, sh.smem, st>>>(P->r32, P->nx, N, P->logN, sh.TP, P->tw, P->spec, P->scal);
+      const PoissonScal *sc = P->scal;
+      ISKRA_CUDA(c, launch_pdl(k_fft_fwd, sh.fb, 256, sh.smem, st, (const float *)P->r32, P->nx, N, P->logN, sh.TP,
+                               (const float2 *)P->tw, P->spec, sc));
       if (sh.G) {
-        k_tridiag_cr<<<(K + sh.G - 1) / sh.G, 256, cr_smem(P, sh.G), st>>>(
-            (float *)P->spec, P->nx, K, sh.G, P->cr_levels, P->cr_nf, P->cr_nb, P->cr_fwd, P->cr_back, P->cr_backb,
-            P->cr_top, P->q, P->gk, P->cyclic, P->pin_k0, P->scal);
+        ISKRA_CUDA(c, launch_pdl(k_tridiag_cr, (K + sh.G - 1) / sh.G, 256, cr_smem(P, sh.G), st, (float *)P->spec,
+                                 P->nx, K, sh.G, P->cr_levels, P->cr_nf, P->cr_nb, (const float2 *)P->cr_fwd,
+                                 (const float2 *)P->cr_back, (const float *)P->cr_backb, (const float *)P->cr_top,
+                                 (const float *)P->q, (const float *)P->gk, (int)P->cyclic, P->pin_k0, sc));
       } else {
-        k_tridiag<<<(2 * K + 63) / 64, 64, 0, st>>>((float *)P->spec, P->nx, K, P->low, P->inv, P->cp, P->q, P->gk,
-                                                    P->cyclic, P->pin_k0, P->scal);
+        ISKRA_CUDA(c, launch_pdl(k_tridiag, (2 * K + 63) / 64, 64, 0, st, (float *)P->spec, P->nx, K,
+                                 (const float *)P->low, (const float *)P->inv, (const float *)P->cp,
+                                 (const float *)P->q, (const float *)P->gk, (int)P->cyclic, P->pin_k0, sc));
       }
-      k_fft_inv_update<<<sh.fb, 256, sh.smem, st>>>(P->spec, P->nx, N, P->logN, sh.TP, P->tw, P->cls, P->x, P->scal);
-      k_residual<false, true><<<B, T, 0, st>>>(op, P->x, c->rho, nie, P->scal, nullptr, P->r32, P->part, nn,
-                                               P->singular, rtol2, eout(c, true), last ? loop : none);
+      ISKRA_CUDA(c, launch_pdl(k_fft_inv_update, sh.fb, 256, sh.smem, st, (const float2 *)P->spec, P->nx, N,
+                               P->logN, sh.TP, (const float2 *)P->tw, (const uint16_t *)P->cls, P->x, sc));
+      ISKRA_CUDA(c, launch_pdl(k_residual<false, true>, B, T, 0, st, op, (const double *)P->x,
+                               (const double *)c->rho, nie, P->scal, (double *)nullptr, P->r32, P->part, nn,
+                               (int)P->singular, rtol2, eout(c, true), last ? loop : none));
     }
   } else {
     if (reset_cg) k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);  // rhs2 is already in scal
@@ -1576,8 +1600,9 @@ static int graph_sweeps(double rtol) {
 static int finish_solve(Ctx *c) {
   Poisson *P = c->ps;
   if (P->singular) {
-    k_sum_x<<<P->blocks, 256, 0, c->stream>>>(P->x, P->nn, P->part);
-    k_shift_x<<<P->blocks, 256, 0, c->stream>>>(P->x, P->nn, P->part, P->blocks);
+    ISKRA_CUDA(c, launch_pdl(k_sum_x, P->blocks, 256, 0, c->stream, (const double *)P->x, P->nn, P->part));
+    ISKRA_CUDA(c, launch_pdl(k_shift_x, P->blocks, 256, 0, c->stream, P->x, P->nn, (const double *)P->part,
+                             P->blocks));
   }
   // the separable path wrote E in its residual passes (the mean shift of the
   // singular case leaves E unchanged); CG computes it here

@@ -31,6 +31,7 @@ struct CircuitArgs {
 // of the PlasmaDevice (circuit_coupling.jl:18-29); wall-absorbed charge enters
 // σ as hit! does (circuit_coupling.jl:45-55).  One thread, FP64.
 __global__ void k_circuit(CircuitArgs A, double dt, unsigned long long *seen) {
+  pdl_wait();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   CircuitDev &c = *A.cd;
   const double vext = A.phi[A.pos_ref] - A.phi[A.neg_ref];
@@ -59,7 +60,7 @@ __global__ void k_circuit(CircuitArgs A, double dt, unsigned long long *seen) {
   A.sigma[c.sigma_dof] += ds;
 }
 
-__global__ void k_step_begin(unsigned long long *d_step) { *d_step += 1ull; }
+__global__ void k_step_begin(unsigned long long *d_step) { pdl_wait(); *d_step += 1ull; }
 
 int launch_circuit(Ctx *c, double dt) {
   if (!c->cir_d) return set_err(c, ISKRA_EINVAL, "no circuit");
@@ -75,14 +76,14 @@ int launch_circuit(Ctx *c, double dt) {
     A.st[s] = c->species[s].dev.st;
     A.qw[s] = c->species[s].q * c->species[s].w0;
   }
-  k_circuit<<<1, 32, 0, c->stream>>>(A, dt, c->cir_seen);
+  ISKRA_CUDA(c, launch_pdl(k_circuit, 1, 32, 0, c->stream, A, dt, c->cir_seen));
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }
 
 // queue one PIC step (async; separable Poisson)
 static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocking_solve) {
-  k_step_begin<<<1, 1, 0, c->stream>>>(c->d_step);
+  ISKRA_CUDA(c, launch_pdl(k_step_begin, 1, 1, 0, c->stream, c->d_step));
   ISKRA_CUDA(c, cudaGetLastError());
   int rc;
   for (int m = 0; m < (int)c->mccs.size(); m++) {

@@ -249,6 +249,48 @@ int iskra_density_noalloc(const iskra_grid_t *grid, const double *x,
                           int64_t np, int64_t ld, double w0, double *n_out,
                           int *flag, uint64_t stream);
 
+/* ---- batched ensembles (config C4: many independent small discharges) ----
+ * No single reference counterpart: the reference runs one problem per
+ * process; this is the GPUEnsemble drop-in of the batched configuration.  An
+ * ensemble copies a configured template context -- species (q, m, w0,
+ * boundary rules), MCC sets (mcc.jl:27-51), the assembled Poisson operator
+ * with its driven electrodes -- and holds nruns independent runs of it, each
+ * with its own particles, fields, MCC seed (default 1000 + run) and drive
+ * amplitudes.  One iskra_ens_step advances every run by the reference's loop
+ * body (ParticleInCell.jl:102-135: MCC, advance!, ρ, ϕ, E) in one CUDA graph.
+ * Runs with the same seed and initial state follow the same algorithm as a
+ * single-run context.  Limits: at most 400 cells per run; separable operator
+ * with ny <= 16, no x-periodic wrap, no σ dof (electrodes are Dirichlet,
+ * possibly driven); no circuit.  The template context must outlive the
+ * ensemble; the ensemble uses the template's stream. */
+typedef struct iskra_ens iskra_ens;
+int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t capacity_per_run,
+                     iskra_ens **out);
+int iskra_ens_destroy(iskra_ens *ens);
+const char *iskra_ens_last_error(const iskra_ens *ens);
+/* seeds[nruns] of the MCC random streams (keys as in iskra_step) */
+int iskra_ens_set_seeds(iskra_ens *ens, const uint64_t *seeds);
+/* amplitude amp[nruns] of driven-electrode group `group` (0-based, creation
+ * order of iskra_poisson_drive_dirichlet) */
+int iskra_ens_set_drive_amplitude(iskra_ens *ens, int group, const double *amp);
+/* particles of one run, layouts as iskra_species_upload / _download */
+int iskra_ens_upload(iskra_ens *ens, int run, int sid, const double *x,
+                     const double *v, const uint32_t *id, int64_t np,
+                     int64_t ld);
+int iskra_ens_download(iskra_ens *ens, int run, int sid, double *x, double *v,
+                       uint32_t *id, int64_t ld, int64_t *np_out);
+int iskra_ens_count(iskra_ens *ens, int run, int sid, int64_t *np);
+/* nsteps steps of every run (async) */
+int iskra_ens_step(iskra_ens *ens, double dt, int nsteps);
+int iskra_ens_sync(iskra_ens *ens);
+/* accepted collisions per process of MCC set mid in one run */
+int iskra_ens_mcc_counts(iskra_ens *ens, int run, int mid, uint64_t *counts);
+/* ρ, ϕ or E of one run (layouts as iskra_field_download) */
+int iskra_ens_field(iskra_ens *ens, int run, int which, double *out);
+/* steps between compactions of discarded particles (0 = only on count /
+ * download) */
+int iskra_ens_set_compact_every(iskra_ens *ens, int every);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,19 @@ SIGNATURES = [
     ("iskra_kernel_launches", c_int, [CTX, POINTER(c_uint64)]),
     ("iskra_density_noalloc", c_int, [POINTER(Grid), c_void_p, c_int64, c_int64, c_double, c_void_p, c_void_p,
                                       c_uint64]),
+    ("iskra_ens_create", c_int, [CTX, c_int, c_int64, POINTER(c_void_p)]),
+    ("iskra_ens_destroy", c_int, [c_void_p]),
+    ("iskra_ens_last_error", c_char_p, [c_void_p]),
+    ("iskra_ens_set_seeds", c_int, [c_void_p, POINTER(c_uint64)]),
+    ("iskra_ens_set_drive_amplitude", c_int, [c_void_p, c_int, dp]),
+    ("iskra_ens_upload", c_int, [c_void_p, c_int, c_int, dp, dp, u32p, c_int64, c_int64]),
+    ("iskra_ens_download", c_int, [c_void_p, c_int, c_int, dp, dp, u32p, c_int64, i64p]),
+    ("iskra_ens_count", c_int, [c_void_p, c_int, c_int, i64p]),
+    ("iskra_ens_step", c_int, [c_void_p, c_double, c_int]),
+    ("iskra_ens_sync", c_int, [c_void_p]),
+    ("iskra_ens_mcc_counts", c_int, [c_void_p, c_int, c_int, POINTER(c_uint64)]),
+    ("iskra_ens_field", c_int, [c_void_p, c_int, c_int, dp]),
+    ("iskra_ens_set_compact_every", c_int, [c_void_p, c_int]),
 ]
 
 _LIB = None

@@ -139,6 +139,51 @@ static int check_sid(Ctx *c, int sid) {
   return ISKRA_OK;
 }
 
+// Host particle arrays (column-major, leading dimension ld) -> one store
+// segment (buffer 0) through the context's staging buffer; synchronous.
+int upload_particles(Ctx *c, const double *x, const double *v, const uint32_t *id, int64_t np, int64_t ld,
+                     float4 *xv, float2 *zc, uint32_t *idd) {
+  int rc = ensure_stage(c, (size_t)(np > 0 ? np : 1) * (5 * sizeof(double) + sizeof(uint32_t)));
+  if (rc) return rc;
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  double *st = c->stage;
+  uint32_t *ids = id ? (uint32_t *)(st + 5 * np) : nullptr;
+  for (int k = 0; k < 2 && np > 0; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(st + k * np, x + k * ld, np * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  for (int k = 0; k < 3 && np > 0; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(st + (2 + k) * np, v + k * ld, np * sizeof(double), cudaMemcpyHostToDevice,
+                                  c->stream));
+  if (ids && np > 0)
+    ISKRA_CUDA(c, cudaMemcpyAsync(ids, id, np * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+  if (np > 0) {
+    const long long B = (np + 255) / 256;
+    k_upload<<<(unsigned)B, 256, 0, c->stream>>>(st, np, c->g.dx, c->g.dy, c->nx, c->ny, ids, xv, zc, idd, c->d_err);
+    ISKRA_CUDA(c, cudaGetLastError());
+  }
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  return collect_device_errors(c);
+}
+
+// One store segment (np live particles, no holes) -> host arrays; synchronous.
+int download_particles(Ctx *c, const float4 *xv, const float2 *zc, const uint32_t *idd, long long np, double *x,
+                       double *v, uint32_t *id, int64_t ld) {
+  if (np == 0) return ISKRA_OK;
+  int rc = ensure_stage(c, (size_t)np * 5 * sizeof(double));
+  if (rc) return rc;
+  const long long B = (np + 255) / 256;
+  k_download<<<(unsigned)B, 256, 0, c->stream>>>(c->stage, np, c->g.dx, c->g.dy, xv, zc);
+  ISKRA_CUDA(c, cudaGetLastError());
+  for (int k = 0; k < 2 && x; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(x + k * ld, c->stage + k * np, np * sizeof(double), cudaMemcpyDeviceToHost,
+                                  c->stream));
+  for (int k = 0; k < 3 && v; k++)
+    ISKRA_CUDA(c, cudaMemcpyAsync(v + k * ld, c->stage + (2 + k) * np, np * sizeof(double), cudaMemcpyDeviceToHost,
+                                  c->stream));
+  if (id) ISKRA_CUDA(c, cudaMemcpyAsync(id, idd, np * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ISKRA_OK;
+}
+
 }  // namespace iskra
 
 using namespace iskra;

@@ -25,6 +25,9 @@ namespace iskra {
 constexpr float kOffScale = 16777216.0f;  // 2^24
 constexpr float kOffInv = 5.9604644775390625e-08f;  // 2^-24
 constexpr int kMaxSpecies = 8;
+// A node sums the deposit weights of the particles in its four cells; with at
+// most kMaxCell particles per cell the sum stays below 4 * 16383 * 2^48 < 2^64.
+constexpr unsigned kMaxCell = 16383;
 constexpr int kMaxMcc = 8;
 
 // device error flags (bitmask in Ctx::d_err)
@@ -203,6 +206,40 @@ void invalidate_graphs(Ctx *c);      // the captured step no longer matches the 
     cudaError_t e_ = (call);                                  \
     if (e_ != cudaSuccess) return cuda_check((c), e_, #call); \
   } while (0)
+
+// ---- ensemble (batched runs) launchers ----
+struct FieldRunsHost {
+  int ns;
+  unsigned long long *acc[kMaxSpecies];  // run 0 of each species' accumulator; run stride nn
+  unsigned *cnt[kMaxSpecies];
+  double scale[kMaxSpecies];             // w0 2^-48
+  double q[kMaxSpecies];
+  double *rho, *x;                       // R x nn
+  float2 *E32;                           // R x nn
+  float4 *E4;                            // R x 2 nn
+  const double *amp;                     // R x ngroups
+  const unsigned long long *d_step;
+  double dt;
+  int *err;
+};
+int launch_field_runs(Ctx *c, int R, FieldRunsHost &H, cudaStream_t st);
+int upload_particles(Ctx *c, const double *x, const double *v, const uint32_t *id, int64_t np, int64_t ld,
+                     float4 *xv, float2 *zc, uint32_t *idd);
+int download_particles(Ctx *c, const float4 *xv, const float2 *zc, const uint32_t *idd, long long np, double *x,
+                       double *v, uint32_t *id, int64_t ld);
+int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float4 *E4, float dt, int blocks_per_run,
+                     int *err, cudaStream_t st);
+int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, const SpeciesDev *prod,
+                    const uint2 *keys, unsigned long long *counts, const float2 *E32, int nn, int blocks_per_run,
+                    const unsigned long long *d_step, int *err, cudaStream_t st);
+void mcc_key(uint64_t seed, int set_index, uint32_t &k0, uint32_t &k1);
+int mcc_nproc(Ctx *c, int mid);
+int mcc_src(Ctx *c, int mid);
+int mcc_prod(Ctx *c, int mid);
+int mcc_set_index(Ctx *c, int mid);
+int poisson_ndrive(Ctx *c);
+int poisson_upload_fp64(Ctx *c);
+double poisson_drive_amp(Ctx *c, int g);
 
 // ---- kernels / launchers shared across files ----
 int launch_advance(Ctx *c, int sid, float dt);

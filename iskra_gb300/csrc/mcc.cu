@@ -208,27 +208,20 @@ __device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsi
   return base + rank;
 }
 
-__global__ void __launch_bounds__(256) k_mcc(SpeciesDev s, SpeciesDev prod, int has_prod, MccDev M,
-                                             const float2 *__restrict__ E, int nx,
-                                             const unsigned long long *__restrict__ d_step, int *err) {
-  pdl_wait();
-  extern __shared__ float tab[];
+// Null-collision step of the warps [warp0, np/32) (stride nwarps) of one
+// species store against the tables staged in `tab`; appends go to the
+// stores' np_new cursors.  Shared by the single-run and ensemble kernels.
+__device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_prod, const MccDev &M,
+                          const float *tab, const float2 *__restrict__ E, int nx, unsigned long long step,
+                          long long warp, long long nwarps, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int ntab = M.off[M.N];
-  for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
-    tab[t] = M.eps[t];
-    tab[ntab + t] = M.sig[t];
-  }
-  __syncthreads();
   const int lane = threadIdx.x & 31;
   const long long np = s.st->np;
   const int cur = s.st->cur;
   float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
   float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
   uint32_t *__restrict__ ids = pick(s.id[0], s.id[1], cur);
-  const unsigned long long step = *d_step;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   unsigned cnt[kMaxProc];
 #pragma unroll
   for (int k = 0; k < kMaxProc; k++) cnt[k] = 0;
@@ -393,6 +386,48 @@ __global__ void __launch_bounds__(256) k_mcc(SpeciesDev s, SpeciesDev prod, int 
   if (lane == 0 && f) atomicOr(err, f);
 }
 
+// stage the cross-section tables of a set in shared memory
+__device__ __forceinline__ void stage_tables(const MccDev &M, float *tab) {
+  const int ntab = M.off[M.N];
+  for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
+    tab[t] = M.eps[t];
+    tab[ntab + t] = M.sig[t];
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_mcc(SpeciesDev s, SpeciesDev prod, int has_prod, MccDev M,
+                                             const float2 *__restrict__ E, int nx,
+                                             const unsigned long long *__restrict__ d_step, int *err) {
+  pdl_wait();
+  extern __shared__ float tab[];
+  stage_tables(M, tab);
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  mcc_warps(s, prod, has_prod, M, tab, E, nx, *d_step, warp, nwarps, err);
+}
+
+// Ensemble: run r = blockIdx.y with its own stores, field, key and counters.
+__global__ void __launch_bounds__(256) k_mcc_runs(const SpeciesDev *__restrict__ src, const SpeciesDev *__restrict__ prod,
+                                                  int has_prod, MccDev M, const uint2 *__restrict__ keys,
+                                                  unsigned long long *__restrict__ counts, const float2 *__restrict__ E,
+                                                  int nn, int nx, const unsigned long long *__restrict__ d_step,
+                                                  int *err) {
+  pdl_wait();
+  extern __shared__ float tab[];
+  stage_tables(M, tab);
+  const int r = blockIdx.y;
+  MccDev Mr = M;
+  Mr.key0 = keys[r].x;
+  Mr.key1 = keys[r].y;
+  Mr.counts = counts + (size_t)r * M.N;
+  Mr.nu = nullptr;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  mcc_warps(src[r], has_prod ? prod[r] : src[r], has_prod, Mr, tab, E + (size_t)r * nn, nx, *d_step, warp, nwarps,
+            err);
+}
+
 // Appends reserve slots from np_new so that np (the loop bound of the running
 // kernel) stays fixed during the launch; np takes the new extent afterwards,
 // clamped to the capacity (failed appends already raised DERR_CAPACITY).
@@ -406,14 +441,20 @@ __global__ void k_append_end(SpeciesState *st, long long cap) {
   st->np = st->np_new > cap ? cap : st->np_new;
 }
 
-int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host) {
-  (void)step_host;
+// Philox key of (seed, set)
+void mcc_key(uint64_t seed, int set_index, uint32_t &k0, uint32_t &k1) {
+  k0 = (uint32_t)seed;
+  k1 = (uint32_t)(seed >> 32) ^ (0x632BE5ABu * (uint32_t)(set_index + 1));
+}
+
+// Kernel parameters of MCC set mid for time step dt (keys from seed).
+static int mcc_params(Ctx *c, int mid, double dt, uint64_t seed, MccDev &M) {
   Mcc *m = c->mccs[mid];
   Species &s = c->species[m->src];
   const double maxPt = 1.0 - std::exp(-m->max_n * m->max_sigma_g * dt);
   if (maxPt > 1.0 / m->N)
     return set_err(c, ISKRA_EPROB, "maximum collision probability above 1/N (mcc.jl:244-246)");
-  MccDev M{};
+  M = MccDev{};
   M.N = m->N;
   for (int k = 0; k < m->N; k++) {
     M.types[k] = m->types[k];
@@ -436,8 +477,17 @@ int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long lo
   if (m->prod >= 0) M.mp = (int)std::llround(s.w0 / c->species[m->prod].w0);
   M.counts = m->counts;
   M.nu = m->nu;
-  M.key0 = (uint32_t)seed;
-  M.key1 = (uint32_t)(seed >> 32) ^ (0x632BE5ABu * (uint32_t)(m->set_index + 1));
+  mcc_key(seed, m->set_index, M.key0, M.key1);
+  return ISKRA_OK;
+}
+
+int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host) {
+  (void)step_host;
+  Mcc *m = c->mccs[mid];
+  Species &s = c->species[m->src];
+  MccDev M;
+  int rc = mcc_params(c, mid, dt, seed, M);
+  if (rc) return rc;
   const int ntab = m->off[m->N];
   const size_t smem = (size_t)2 * ntab * sizeof(float);
   long long want = (s.cap + 255) / 256;
@@ -462,6 +512,28 @@ int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long lo
   }
   return ISKRA_OK;
 }
+
+// Ensemble launch of MCC set mid of the template context over R runs:
+// per-run stores (src/prod views), keys (2 words per run), counters (R x N)
+// and node fields (R x nn).
+int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, const SpeciesDev *prod,
+                    const uint2 *keys, unsigned long long *counts, const float2 *E32, int nn, int blocks_per_run,
+                    const unsigned long long *d_step, int *err, cudaStream_t st) {
+  Mcc *m = c->mccs[mid];
+  MccDev M;
+  int rc = mcc_params(c, mid, dt, 0, M);
+  if (rc) return rc;
+  const int ntab = m->off[m->N];
+  const size_t smem = (size_t)2 * ntab * sizeof(float);
+  ISKRA_CUDA(c, launch_pdl(k_mcc_runs, dim3(blocks_per_run, R), 256, smem, st, src, prod, (int)(m->prod >= 0), M, keys,
+                           counts, E32, nn, c->nx, d_step, err));
+  return ISKRA_OK;
+}
+
+int mcc_nproc(Ctx *c, int mid) { return c->mccs[mid]->N; }
+int mcc_src(Ctx *c, int mid) { return c->mccs[mid]->src; }
+int mcc_prod(Ctx *c, int mid) { return c->mccs[mid]->prod; }
+int mcc_set_index(Ctx *c, int mid) { return c->mccs[mid]->set_index; }
 
 }  // namespace iskra
 

@@ -149,8 +149,8 @@ struct PushShared {
 template <bool PUSH, int MX, int MY, bool WIN>
 __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
                                           long long p, bool valid, float4 a, float2 b,
-                                          const float4 *__restrict__ E4, PushShared &sh, int ox, int oy,
-                                          const PushParams &P, unsigned ab[4], int &flags) {
+                                          const float4 *__restrict__ E4, PushShared &sh, int ox, int oy, int ww,
+                                          int wh, const PushParams &P, unsigned ab[4], int &flags) {
   const int nx = P.nx;
   int key = -1;
   Moments m = {0u, 0u, 0u, 0u};
@@ -162,8 +162,8 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
       if (PUSH) {
         float4 r0, r1;  // the cell's corner fields
         const int la = i0 - ox, lb = j0 - oy;
-        if (WIN && (unsigned)la < (unsigned)kWin && (unsigned)lb < (unsigned)kWin) {
-          const int w = la + kWin * lb;
+        if (WIN && (unsigned)la < (unsigned)ww && (unsigned)lb < (unsigned)wh) {
+          const int w = la + ww * lb;
           r0 = sh.e[2 * w];
           r1 = sh.e[2 * w + 1];
         } else {
@@ -207,8 +207,8 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
       }
       if (cell >= 0) {
         const int la = i0 - ox, lb = j0 - oy;
-        key = (WIN && (unsigned)la < (unsigned)kWin && (unsigned)lb < (unsigned)kWin) ? la + kWin * lb
-                                                                                        : kWinCells + i0 + nx * j0;
+        key = (WIN && (unsigned)la < (unsigned)ww && (unsigned)lb < (unsigned)wh) ? la + ww * lb
+                                                                                  : kWinCells + i0 + nx * j0;
         const unsigned ux = __float2uint_rn(hx * kOffScale);
         const unsigned uy = __float2uint_rn(hy * kOffScale);
         const unsigned long long uv = (unsigned long long)ux * uy;
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev 
           a2 = __ldcs(xv + nb + lane);
           b2 = __ldcs(zc + nb + lane);
         }
-        push_warp<PUSH, MX, MY, true>(s, xv, zc, base + lane, v, a, b, E4, sh, ox, oy, P, ab, flags);
+        push_warp<PUSH, MX, MY, true>(s, xv, zc, base + lane, v, a, b, E4, sh, ox, oy, kWin, kWin, P, ab, flags);
         a = a2;
         b = b2;
         v = nv;
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev 
         a = __ldcs(xv + p);
         b = __ldcs(zc + p);
       }
-      push_warp<PUSH, MX, MY, false>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, P, ab, flags);
+      push_warp<PUSH, MX, MY, false>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, 0, 0, P, ab, flags);
     }
   }
   if (PUSH) {
@@ -445,9 +445,7 @@ struct FinalizeArgs {
   int consume[kMaxSpecies];
 };
 
-// A node sums the weights of the particles in its four cells; with at most
-// kMaxCell particles per cell the sum stays below 4 * 16383 * 2^48 < 2^64.
-constexpr unsigned kMaxCell = 16383;
+
 
 __global__ void k_finalize(FinalizeArgs A, const double *__restrict__ vol_inv, const double *__restrict__ bg,
                            double *__restrict__ rho, int nn, int *err) {
@@ -754,6 +752,117 @@ int launch_sort(Ctx *c, int sid) {
   k_sort_finish<<<1, 1, 0, c->stream>>>(s.dev.st, c->cell_count + nk);
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// ensemble push: run r = blockIdx.y; every block of a run stages the run's
+// whole E grid (cx*cy <= kWinCells cells), pushes a grid-stride share of the
+// run's particles (any order), deposits into shared memory and adds the
+// node sums to the run's accumulator.
+// ---------------------------------------------------------------------------
+template <int MX, int MY>
+__global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push_runs(const SpeciesDev *__restrict__ runs,
+                                                                          const float4 *__restrict__ E4, int ncell4,
+                                                                          PushParams P, int *err) {
+  pdl_wait();
+  __shared__ PushShared sh;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  const int r = blockIdx.y;
+  const SpeciesDev s = runs[r];
+  const int nx = P.nx, cx = P.nx - 1, cy = P.ny - 1;
+  E4 += (size_t)r * ncell4;
+  for (int t = threadIdx.x; t < cx * cy; t += blockDim.x) {
+    const int i = t % cx, j = t / cx;
+    const int n0 = i + nx * j;
+    sh.e[2 * t] = __ldg(E4 + 2 * n0);
+    sh.e[2 * t + 1] = __ldg(E4 + 2 * n0 + 1);
+#pragma unroll
+    for (int q = 0; q < kMoms; q++) sh.mom[q][t] = 0u;
+  }
+  __syncthreads();
+  const long long np = s.st->np;
+  const int cur = s.st->cur;
+  float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
+  float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
+  unsigned ab[4] = {0, 0, 0, 0};
+  int flags = 0;
+  const long long warp = (long long)blockIdx.x * nwb + wib, nwarps = (long long)gridDim.x * nwb;
+  for (long long base = warp * 32; base < np; base += nwarps * 32) {
+    const long long p = base + lane;
+    const bool v = p < np;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 b = make_float2(0.f, 0.f);
+    if (v) {
+      a = __ldcs(xv + p);
+      b = __ldcs(zc + p);
+    }
+    push_warp<true, MX, MY, true>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, cx, cy, P, ab, flags);
+  }
+  __syncthreads();
+  const int wn = cx + 1;
+  for (int t = threadIdx.x; t < (cx + 1) * (cy + 1); t += blockDim.x) {
+    const int a = t % wn, b = t / wn;
+    unsigned long long v = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int ca = a - (c & 1), cb = b - (c >> 1);
+      if (ca < 0 || cb < 0 || ca >= cx || cb >= cy) continue;
+      const int w = ca + cx * cb;
+      const unsigned long long n = sh.mom[kMomN][w];
+      if (!n) continue;
+      const unsigned long long U = (((unsigned long long)sh.mom[kMomUh][w] << 12) + sh.mom[kMomUl][w]) << 24;
+      const unsigned long long V = (((unsigned long long)sh.mom[kMomVh][w] << 12) + sh.mom[kMomVl][w]) << 24;
+      const unsigned long long UV = ((((unsigned long long)sh.mom[kMomHh][w] << 12) + sh.mom[kMomHl][w]) << 24) +
+                                    (((unsigned long long)sh.mom[kMomLh][w] << 12) + sh.mom[kMomLl][w]);
+      if (c == 0) v += (n << 48) - U - V + UV;
+      else if (c == 1) v += U - UV;
+      else if (c == 2) v += V - UV;
+      else v += UV;
+    }
+    if (v) atomicAdd(s.acc + a + nx * b, v);
+  }
+  for (int t = threadIdx.x; t < cx * cy; t += blockDim.x) {
+    const unsigned v = sh.mom[kMomN][t];
+    if (v) atomicAdd(s.cnt + (t % cx) + nx * (t / cx), v);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    unsigned t = __reduce_add_sync(FULL, ab[k]);
+    if (lane == 0 && t) atomicAdd(&s.st->absorbed[k], (unsigned long long)t);
+  }
+  int f = __reduce_or_sync(FULL, flags);
+  if (lane == 0 && f) atomicOr(err, f);
+}
+
+// Ensemble push of one species (runs: device array of R run views).
+int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float4 *E4, float dt, int blocks_per_run,
+                     int *err, cudaStream_t st) {
+  Species &s = c->species[sid];
+  if ((c->nx - 1) * (c->ny - 1) > kWinCells) return set_err(c, ISKRA_EINVAL, "ensemble grid larger than one window");
+  PushParams P;
+  P.h = (float)(0.5 * (double)dt * (s.q / s.m));
+  P.dtdx = (float)((double)dt / c->g.dx);
+  P.dtdy = (float)((double)dt / c->g.dy);
+  P.nx = c->nx;
+  P.ny = c->ny;
+  P.mode_x = s.bnd[0];
+  P.mode_y = s.bnd[1];
+  P.tiles_x = 0;
+  const int ncell4 = 2 * c->nn;
+  const dim3 grid(blocks_per_run, R);
+#define ISKRA_PUSH_RUNS_CASE(MX, MY)                                                                           \
+  if (P.mode_x == MX && P.mode_y == MY) {                                                                       \
+    cudaFuncSetAttribute(k_push_runs<MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,                   \
+                         (int)cudaSharedmemCarveoutMaxShared);                                                  \
+    ISKRA_CUDA(c, launch_pdl(k_push_runs<MX, MY>, grid, 256, 0, st, runs, E4, ncell4, P, err));                 \
+    return ISKRA_OK;                                                                                            \
+  }
+  ISKRA_PUSH_RUNS_CASE(0, 0) ISKRA_PUSH_RUNS_CASE(0, 1) ISKRA_PUSH_RUNS_CASE(0, 2)
+  ISKRA_PUSH_RUNS_CASE(1, 0) ISKRA_PUSH_RUNS_CASE(1, 1) ISKRA_PUSH_RUNS_CASE(1, 2)
+  ISKRA_PUSH_RUNS_CASE(2, 0) ISKRA_PUSH_RUNS_CASE(2, 1) ISKRA_PUSH_RUNS_CASE(2, 2)
+#undef ISKRA_PUSH_RUNS_CASE
+  return set_err(c, ISKRA_EINVAL, "bad boundary mode");
 }
 
 // Σ (vx² + vy²) and the number of live particles (for the sort cadence)

@@ -112,6 +112,10 @@ struct Poisson {
   bool rho_fixed = false;       // some identity row takes its value from ρ (rewritten every solve)
   int last_iters = 0;
   double last_relres = 0;
+  // FP64 Thomas factors of the separable operator (host copy; uploaded on
+  // demand for the ensemble field solve)
+  std::vector<double> lo64, inv64, cp64;
+  double *lo64_d = nullptr, *inv64_d = nullptr, *cp64_d = nullptr;
 };
 
 constexpr int kPartials = 1024;
@@ -130,6 +134,9 @@ void poisson_destroy(Poisson *p) {
   cudaFree(p->part);
   cudaFree(p->scal);
   if (p->scal_h) cudaFreeHost(p->scal_h);
+  cudaFree(p->lo64_d);
+  cudaFree(p->inv64_d);
+  cudaFree(p->cp64_d);
   cudaFree(p->r32);
   cudaFree(p->spec);
   cudaFree(p->tw);
@@ -1358,6 +1365,13 @@ static int build_device(Ctx *c, Poisson *P) {
       const double ang = -2.0 * M_PI * m / N;
       tw[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
+    P->lo64 = lo;
+    P->inv64 = inv;
+    P->cp64 = cpv;
+    cudaFree(P->lo64_d);
+    cudaFree(P->inv64_d);
+    cudaFree(P->cp64_d);
+    P->lo64_d = P->inv64_d = P->cp64_d = nullptr;
     const std::vector<float> lo32 = f32(lo), up32 = f32(upv), inv32 = f32(inv), cp32 = f32(cpv), gk32 = f32(gkv),
                              q32 = f32(qv), backb32 = f32(cr_backb), top32 = f32(cr_top);
     const std::vector<float2> fwd32 = f32x2(cr_fwd), back32 = f32x2(cr_back);
@@ -1662,6 +1676,244 @@ double *poisson_sigma_ptr(Ctx *c) { return c->ps ? c->ps->sigma_d : nullptr; }
 const double *poisson_x_ptr(Ctx *c) { return c->ps ? c->ps->x : nullptr; }
 bool poisson_separable(Ctx *c) { return c->ps && c->ps->separable; }
 int poisson_solve_blocking(Ctx *c, double rtol, int maxit) { return solve_sync(c, rtol, maxit, nullptr, nullptr); }
+
+// ---------------------------------------------------------------------------
+// Ensemble field solve: one block per run forms ρ from the run's deposit,
+// sets the fixed rows (drive amplitudes per run), and solves the separable
+// operator directly in FP64 -- residual of the previous potential, DFT along
+// y (N <= 16, direct), one Thomas sweep per Fourier mode along x with the
+// host's FP64 factors staged in shared memory, inverse DFT -- then writes E.
+// The same operator and algorithm as one FP64 sweep of the single-run solver,
+// which is exact to rounding.
+// ---------------------------------------------------------------------------
+struct FieldRuns {
+  int ns;
+  unsigned long long *acc[kMaxSpecies];  // run 0; run stride nn
+  unsigned *cnt[kMaxSpecies];
+  double scale[kMaxSpecies];             // w0 2^-48
+  double q[kMaxSpecies];
+  const double *vol_inv, *bg;
+  double *rho, *x;                       // R x nn
+  float2 *E32;                           // R x nn
+  float4 *E4;                            // R x 2 nn
+  const double *amp;                     // R x ngroups drive amplitudes
+  int ngroups;
+  const int *drive_node, *drive_group;
+  const double *drive_par;               // 4 per group; par[0] replaced by amp[r][g]
+  int ndrive_nodes;
+  const unsigned long long *d_step;
+  double dt, neg_inv_eps0;
+  const double *lo, *inv, *cp;           // FP64 Thomas factors
+  int N, K;
+  float idx2, idx1, idy2, idy1;
+  int *err;
+};
+
+__global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
+  pdl_wait();
+  extern __shared__ double fsm[];
+  __shared__ RowClass cls_sh[kSmemClasses];
+  const int nx = op.nx, ny = op.ny, nn = nx * ny, N = F.N, K = F.K;
+  double *xs = fsm, *rs = xs + nn, *spec = rs + nn, *sinv = spec + 2 * nx * K, *scp = sinv + nx * K;
+  const int r = blockIdx.x;
+  const size_t o = (size_t)r * nn;
+  const RowClass *__restrict__ CT = stage_classes(op, cls_sh);
+  for (int t = threadIdx.x; t < nx * K; t += blockDim.x) {
+    sinv[t] = F.inv[t];
+    scp[t] = F.cp[t];
+  }
+  int flags = 0;
+  // ρ from the run's deposit (consumed); ϕ of the previous step
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+    const double vi = F.vol_inv[k];
+    double rho = 0.0;
+    for (int s = 0; s < F.ns; s++) {
+      const unsigned long long a = F.acc[s][o + k];
+      if (F.cnt[s][o + k] > kMaxCell) flags |= DERR_OVERFLOW;
+      F.acc[s][o + k] = 0ull;
+      F.cnt[s][o + k] = 0u;
+      rho += ((double)a * F.scale[s] * vi) * F.q[s];
+    }
+    if (F.bg) rho += F.bg[k];
+    F.rho[o + k] = rho;
+    xs[k] = F.x[o + k];
+  }
+  __syncthreads();
+  // driven rows: V((n-2)Δt) with this run's amplitude, as k_set_fixed
+  const unsigned long long n_step = *F.d_step;
+  for (int t = threadIdx.x; t < F.ndrive_nodes; t += blockDim.x) {
+    const int k = F.drive_node[t], g = F.drive_group[t];
+    const double *par = F.drive_par + 4 * g;
+    if (n_step >= 2) {
+      const double tt = (double)(n_step - 2) * F.dt;
+      xs[k] = F.amp[(size_t)r * F.ngroups + g] * sin(2.0 * M_PI * par[1] * tt + par[2]) + par[3];
+    } else {
+      xs[k] = op.bfix[k];
+    }
+  }
+  __syncthreads();
+  // scaled residual of the free rows
+  double a2 = 0, b2 = 0;
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+    const int j = k / nx, i = k - j * nx;
+    const double rhoc = F.rho[o + k];
+    const unsigned ck = op.cls[k];
+    if (ck & kFixedBit) {
+      rs[k] = 0.0;
+      continue;
+    }
+    const RowClass &C = CT[ck];
+    const int w = i > 0 ? k - 1 : k + nx - 1;
+    const int e = i < nx - 1 ? k + 1 : k - nx + 1;
+    const int s = j > 0 ? k - nx : k + nx * (ny - 1);
+    const int n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
+    const double b = C.rho ? rhoc * F.neg_inv_eps0 : op.bfix[k];
+    double ax = C.c0 * xs[k];
+    ax = fma(C.cW, xs[w], ax);
+    ax = fma(C.cE, xs[e], ax);
+    ax = fma(C.cS, xs[s], ax);
+    ax = fma(C.cN, xs[n], ax);
+    rs[k] = -C.d * (b - ax);
+  }
+  __syncthreads();
+  // DFT along y: spec[i][k] = Σ_j r[i, j] e^{-2πi jk/N}
+  for (int t = threadIdx.x; t < nx * K; t += blockDim.x) {
+    const int i = t / K, k = t - i * K;
+    double re = 0, im = 0;
+    for (int j = 0; j < N; j++) {
+      double sn, cs;
+      sincospi(-2.0 * (double)((j * k) % N) / N, &sn, &cs);
+      const double v = rs[i + nx * j];
+      re += v * cs;
+      im += v * sn;
+    }
+    spec[2 * t] = re;
+    spec[2 * t + 1] = im;
+  }
+  __syncthreads();
+  // Thomas per mode and part (sequential along x)
+  if (threadIdx.x < 2 * K) {
+    const int k = threadIdx.x >> 1, part = threadIdx.x & 1;
+    const bool real_mode = k == 0 || 2 * k == N;
+    if (!(part && real_mode)) {
+      double y = 0.0;
+      for (int i = 0; i < nx; i++) {
+        const double a = i > 0 ? F.lo[i] : 0.0;
+        y = (spec[2 * (i * K + k) + part] - a * y) * sinv[i * K + k];
+        spec[2 * (i * K + k) + part] = y;
+      }
+      double xn = y;
+      for (int i = nx - 2; i >= 0; i--) {
+        xn = spec[2 * (i * K + k) + part] - scp[i * K + k] * xn;
+        spec[2 * (i * K + k) + part] = xn;
+      }
+    }
+  }
+  __syncthreads();
+  // inverse DFT (Hermitian spectrum) and update of the free rows
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+    if (op.cls[k] & kFixedBit) continue;
+    const int j = k / nx, i = k - j * nx;
+    double v = 0;
+    for (int m = 0; m < N; m++) {
+      const int mm = m < K ? m : N - m;
+      const double re = spec[2 * (i * K + mm)];
+      const double im = m < K ? spec[2 * (i * K + mm) + 1] : -spec[2 * (i * K + mm) + 1];
+      double sn, cs;
+      sincospi(2.0 * (double)((j * m) % N) / N, &sn, &cs);
+      v += re * cs - im * sn;
+    }
+    xs[k] += v / N;
+  }
+  __syncthreads();
+  // ϕ and E = -∇ϕ
+  EOut eo;
+  eo.E32 = F.E32 + o;
+  eo.E4 = F.E4 + 2 * o;
+  eo.idx2 = F.idx2;
+  eo.idx1 = F.idx1;
+  eo.idy2 = F.idy2;
+  eo.idy1 = F.idy1;
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+    const int j = k / nx, i = k - j * nx;
+    F.x[o + k] = xs[k];
+    efield_at(xs, k, i, j, nx, ny, eo);
+  }
+  (void)a2;
+  (void)b2;
+  if (flags) atomicOr(F.err, flags);
+}
+
+// Ensemble field solve over R runs (separable, non-cyclic, non-singular
+// operators with N = ny <= 16 and no σ dof).
+int launch_field_runs(Ctx *c, int R, FieldRunsHost &H, cudaStream_t st) {
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  Poisson *P = c->ps;
+  if (!P->separable || P->cyclic || P->singular || P->N > 16 || P->nsig > 0 || P->rho_fixed)
+    return set_err(c, ISKRA_EINVAL, "ensemble field solve needs a separable, non-periodic-x operator with ny <= 16");
+  const int nx = P->nx, K = P->K, nn = P->nn;
+  if (!P->lo64_d) return set_err(c, ISKRA_EINVAL, "FP64 factors not uploaded (poisson_upload_fp64)");
+  FieldRuns F{};
+  F.ns = H.ns;
+  for (int s = 0; s < H.ns; s++) {
+    F.acc[s] = H.acc[s];
+    F.cnt[s] = H.cnt[s];
+    F.scale[s] = H.scale[s];
+    F.q[s] = H.q[s];
+  }
+  F.vol_inv = c->vol_inv;
+  F.bg = c->rho_bg;
+  F.rho = H.rho;
+  F.x = H.x;
+  F.E32 = H.E32;
+  F.E4 = H.E4;
+  F.amp = H.amp;
+  F.ngroups = P->ndrive;
+  F.drive_node = P->drive_node;
+  F.drive_group = P->drive_group;
+  F.drive_par = P->drive_par;
+  F.ndrive_nodes = P->ndrive_nodes;
+  F.d_step = H.d_step;
+  F.dt = H.dt;
+  F.neg_inv_eps0 = -1.0 / P->eps0;
+  F.lo = P->lo64_d;
+  F.inv = P->inv64_d;
+  F.cp = P->cp64_d;
+  F.N = P->N;
+  F.K = K;
+  const EOut e = eout(c, true);
+  F.idx2 = e.idx2;
+  F.idx1 = e.idx1;
+  F.idy2 = e.idy2;
+  F.idy1 = e.idy1;
+  F.err = H.err;
+  const size_t smem = (2 * (size_t)nn + 4 * (size_t)nx * K) * sizeof(double);
+  if (smem > 200 * 1024) return set_err(c, ISKRA_EINVAL, "ensemble grid too large for the per-run field solve");
+  ISKRA_CUDA(c, cudaFuncSetAttribute(k_field_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ISKRA_CUDA(c, launch_pdl(k_field_runs, R, 256, smem, st, opview(P), F));
+  return ISKRA_OK;
+}
+
+// FP64 Thomas factors on the device (outside any stream capture)
+int poisson_upload_fp64(Ctx *c) {
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  Poisson *P = c->ps;
+  if (!P->separable) return set_err(c, ISKRA_EINVAL, "ensemble field solve needs a separable operator");
+  if (P->lo64_d) return ISKRA_OK;
+  const int nx = P->nx, K = P->K;
+  ISKRA_CUDA(c, cudaMalloc(&P->lo64_d, nx * sizeof(double)));
+  ISKRA_CUDA(c, cudaMalloc(&P->inv64_d, (size_t)nx * K * sizeof(double)));
+  ISKRA_CUDA(c, cudaMalloc(&P->cp64_d, (size_t)nx * K * sizeof(double)));
+  ISKRA_CUDA(c, cudaMemcpy(P->lo64_d, P->lo64.data(), nx * sizeof(double), cudaMemcpyHostToDevice));
+  ISKRA_CUDA(c, cudaMemcpy(P->inv64_d, P->inv64.data(), (size_t)nx * K * sizeof(double), cudaMemcpyHostToDevice));
+  ISKRA_CUDA(c, cudaMemcpy(P->cp64_d, P->cp64.data(), (size_t)nx * K * sizeof(double), cudaMemcpyHostToDevice));
+  return ISKRA_OK;
+}
+
+int poisson_ndrive(Ctx *c) { return c->ps ? c->ps->ndrive : 0; }
+double poisson_drive_amp(Ctx *c, int g) { return c->ps ? c->ps->drives[g].amp : 0.0; }
 
 }  // namespace iskra
 

@@ -253,3 +253,90 @@ class Context:
 
     def set_sort_every(self, every):
         self._c(self.lib.iskra_set_sort_every(self.h, every))
+
+
+class Ensemble:
+    """Batched independent runs of a configured template Context (the
+    GPUEnsemble of the batched configuration): per-run particles, fields,
+    MCC seeds and drive amplitudes; one step advances every run.  The
+    template must stay open while the ensemble lives."""
+
+    def __init__(self, template: Context, nruns: int, capacity_per_run: int):
+        self.lib = template.lib
+        self.template = template
+        h = c_void_p()
+        rc = self.lib.iskra_ens_create(template.h, nruns, capacity_per_run, byref(h))
+        if rc != 0:
+            raise _lib.IskraError(rc, self.lib.iskra_last_error(template.h).decode())
+        self.h = h
+        self.R = nruns
+        self.nx, self.ny = template.nx, template.ny
+
+    def _c(self, rc):
+        if rc != _lib.ISKRA_OK:
+            msg = self.lib.iskra_ens_last_error(self.h)
+            raise _lib.IskraError(rc, msg.decode() if msg else "")
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.iskra_ens_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_seeds(self, seeds):
+        a = (c_uint64 * self.R)(*[int(s) for s in seeds])
+        self._c(self.lib.iskra_ens_set_seeds(self.h, a))
+
+    def set_drive_amplitude(self, group, amps):
+        a = np.ascontiguousarray(amps, dtype=np.float64)
+        self._c(self.lib.iskra_ens_set_drive_amplitude(self.h, group, _ptr(a)))
+
+    def upload(self, run, sid, x, v, ids=None):
+        x = _f64(x)
+        v = _f64(v)
+        n = x.shape[0]
+        ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+        self._c(self.lib.iskra_ens_upload(self.h, run, sid, _ptr(x), _ptr(v), _ptr(ids, _lib.u32p), n, n))
+
+    def count(self, run, sid):
+        n = c_int64()
+        self._c(self.lib.iskra_ens_count(self.h, run, sid, byref(n)))
+        return n.value
+
+    def download(self, run, sid):
+        n = self.count(run, sid)
+        cap = max(n, 1)
+        x = np.zeros((cap, 2), order="F")
+        v = np.zeros((cap, 3), order="F")
+        ids = np.zeros(cap, dtype=np.uint32)
+        got = c_int64()
+        self._c(self.lib.iskra_ens_download(self.h, run, sid, _ptr(x), _ptr(v), _ptr(ids, _lib.u32p), cap,
+                                            byref(got)))
+        n = got.value
+        return np.asfortranarray(x[:n]), np.asfortranarray(v[:n]), ids[:n].copy()
+
+    def step(self, dt, nsteps=1):
+        self._c(self.lib.iskra_ens_step(self.h, dt, nsteps))
+
+    def sync(self):
+        self._c(self.lib.iskra_ens_sync(self.h))
+
+    def mcc_counts(self, run, mid, nproc):
+        a = (c_uint64 * nproc)()
+        self._c(self.lib.iskra_ens_mcc_counts(self.h, run, mid, a))
+        return list(a)
+
+    def field(self, run, which):
+        shape = (self.nx, self.ny, 3) if which == _lib.FIELD_E else (self.nx, self.ny)
+        out = np.zeros(shape, order="F")
+        self._c(self.lib.iskra_ens_field(self.h, run, which, _ptr(out)))
+        return out
+
+    def set_compact_every(self, every):
+        self._c(self.lib.iskra_ens_set_compact_every(self.h, every))

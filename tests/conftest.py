@@ -4,8 +4,10 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-if ROOT not in sys.path:
-    sys.path.insert(0, ROOT)
+TESTS = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, TESTS):  # the package, and test modules sharing setups
+    if p not in sys.path:
+        sys.path.insert(0, p)
 
 
 def pytest_configure(config):

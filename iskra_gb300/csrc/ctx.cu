@@ -266,6 +266,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   if (!h) return ISKRA_OK;
   Ctx *c = &h->c;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  ensembles_detach(c);  // ensembles built on this template lose their device state
   invalidate_graphs(c);
   for (auto &s : c->species) {
     for (int b = 0; b < 2; b++) {
@@ -277,6 +278,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
     cudaFree(s.dev.acc);
     cudaFree(s.dev.cnt);
     cudaFree(s.dev.tile_begin);
+    cudaFree(s.dview);
     cudaFree(s.n);
   }
   for (auto *m : c->mccs) mcc_destroy(m);
@@ -297,6 +299,8 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   cudaFree(c->stage);
   cudaFree(c->d_step);
   cudaFree(c->d_scratch);
+  cudaFree(c->mcc_work);
+  cudaFree(c->mcc_nwork);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete h;
   return ISKRA_OK;
@@ -337,19 +341,22 @@ int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t ca
   ISKRA_CUDA(c, cudaMalloc(&s.dev.acc, nn * sizeof(unsigned long long)));
   ISKRA_CUDA(c, cudaMalloc(&s.dev.cnt, nn * sizeof(unsigned)));
   ISKRA_CUDA(c, cudaMalloc(&s.dev.tile_begin, ((size_t)c->ntiles + 1) * sizeof(int)));
+  ISKRA_CUDA(c, cudaMalloc(&s.dview, sizeof(SpeciesDev)));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.tile_begin, 0, ((size_t)c->ntiles + 1) * sizeof(int), c->stream));
   ISKRA_CUDA(c, cudaMalloc(&s.n, nn * sizeof(double)));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.st, 0, sizeof(SpeciesState), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, nn * sizeof(unsigned long long), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, nn * sizeof(unsigned), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.n, 0, nn * sizeof(double), c->stream));
+  ISKRA_CUDA(c, cudaMemcpyAsync(s.dview, &s.dev, sizeof(SpeciesDev), cudaMemcpyHostToDevice, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   s.acc_valid = false;
   s.acc_zero = true;
   s.n_valid = true;  // empty species: zero density is current
   c->species.push_back(s);
   *sid = (int)c->species.size() - 1;
   invalidate_graphs(c);
-  return ISKRA_OK;
+  return ensure_mcc_work(c);
 }
 
 int iskra_species_set_boundary(iskra_ctx *h, int sid, int mx, int my) {

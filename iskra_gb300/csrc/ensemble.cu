@@ -60,6 +60,9 @@ struct Ens {
   double graph_dt = 0;
   cudaGraphExec_t compact_graph = nullptr;
   int compact_every = 32;
+  void *work = nullptr;                   // MCC work list (R x capacity entries)
+  unsigned long long work_cap = 0;
+  unsigned long long *nwork = nullptr;
   std::string err;
 };
 
@@ -160,7 +163,8 @@ static int ens_queue_step(Ens *e, double dt) {
     if (prod >= 0)
       ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[prod].st, R, e->sp[prod].cap, (int)kRunsAppendBegin));
     int rc = launch_mcc_runs(c, m, dt, R, e->sp[src].views, prod >= 0 ? e->sp[prod].views : e->sp[src].views,
-                             e->mcc[m].keys, e->mcc[m].counts, e->E32, e->nn, bpr, e->d_step, e->d_err, st);
+                             e->mcc[m].keys, e->mcc[m].counts, e->E32, e->nn, bpr, e->work, e->nwork, e->work_cap,
+                             e->d_step, e->d_err, st);
     if (rc) return ens_err(e, rc, c->err);
     ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[src].st, R, e->sp[src].cap, (int)kRunsAppendEnd));
     if (prod >= 0)
@@ -238,8 +242,10 @@ static int ens_collect(Ens *e) {
 }
 
 static void ens_free(Ens *e) {
-  if (!e) return;
-  if (e->c && e->c->stream) cudaStreamSynchronize(e->c->stream);
+  if (!e || !e->c) return;
+  if (e->c->stream) cudaStreamSynchronize(e->c->stream);
+  auto &v = e->c->ensembles;
+  v.erase(std::remove(v.begin(), v.end(), (void *)e), v.end());
   if (e->graph) cudaGraphExecDestroy(e->graph);
   if (e->compact_graph) cudaGraphExecDestroy(e->compact_graph);
   for (auto &s : e->sp) {
@@ -264,7 +270,16 @@ static void ens_free(Ens *e) {
   cudaFree(e->amp);
   cudaFree(e->d_step);
   cudaFree(e->d_err);
+  cudaFree(e->work);
+  cudaFree(e->nwork);
   if (e->h_err) cudaFreeHost(e->h_err);
+  *e = Ens{};  // detached: every later call but destroy fails
+}
+
+void ensembles_detach(Ctx *c) {
+  std::vector<void *> v = c->ensembles;
+  for (void *p : v) ens_free((Ens *)p);
+  c->ensembles.clear();
 }
 
 static int ens_update_keys(Ens *e) {
@@ -376,6 +391,11 @@ int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t cap_per_run, iskra_ens 
       for (int g = 0; g < e->ngroups; g++) a[r * ng + g] = poisson_drive_amp(c, g);
     cudaMemcpy(e->amp, a.data(), a.size() * sizeof(double), cudaMemcpyHostToDevice);
   }
+  if (!c->mccs.empty()) {
+    e->work_cap = (unsigned long long)cap_per_run;  // per run segment
+    ENS_ALLOC(e->work, R * e->work_cap * mcc_work_entry_bytes());
+    ENS_ALLOC(e->nwork, R * sizeof(unsigned long long));
+  }
   ENS_ALLOC(e->d_step, sizeof(unsigned long long));
   cudaMemset(e->d_step, 0, sizeof(unsigned long long));
   ENS_ALLOC(e->d_err, sizeof(int));
@@ -385,6 +405,7 @@ int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t cap_per_run, iskra_ens 
   e->seeds.resize(R);
   for (size_t r = 0; r < R; r++) e->seeds[r] = 1000 + r;
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(ISKRA_ECUDA);
+  c->ensembles.push_back((void *)e);
   *out = h;
   return ISKRA_OK;
 }
@@ -399,6 +420,7 @@ int iskra_ens_destroy(iskra_ens *h) {
 const char *iskra_ens_last_error(const iskra_ens *h) { return h ? h->e.err.c_str() : "null ensemble"; }
 
 int iskra_ens_set_seeds(iskra_ens *h, const uint64_t *seeds) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h || !seeds) return ISKRA_EINVAL;
   Ens *e = &h->e;
   e->seeds.assign(seeds, seeds + e->R);
@@ -407,6 +429,7 @@ int iskra_ens_set_seeds(iskra_ens *h, const uint64_t *seeds) {
 }
 
 int iskra_ens_set_drive_amplitude(iskra_ens *h, int group, const double *amp) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h || !amp) return ISKRA_EINVAL;
   Ens *e = &h->e;
   if (group < 0 || group >= e->ngroups) return ens_err(e, ISKRA_EINVAL, "bad drive group");
@@ -420,6 +443,7 @@ int iskra_ens_set_drive_amplitude(iskra_ens *h, int group, const double *amp) {
 
 int iskra_ens_upload(iskra_ens *h, int run, int sid, const double *x, const double *v, const uint32_t *id,
                      int64_t np, int64_t ld) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h) return ISKRA_EINVAL;
   Ens *e = &h->e;
   if (run < 0 || run >= e->R || sid < 0 || sid >= (int)e->sp.size()) return ens_err(e, ISKRA_EINVAL, "bad run or species");
@@ -441,6 +465,7 @@ int iskra_ens_upload(iskra_ens *h, int run, int sid, const double *x, const doub
 }
 
 int iskra_ens_count(iskra_ens *h, int run, int sid, int64_t *np) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h || !np) return ISKRA_EINVAL;
   Ens *e = &h->e;
   if (run < 0 || run >= e->R || sid < 0 || sid >= (int)e->sp.size()) return ens_err(e, ISKRA_EINVAL, "bad run or species");
@@ -461,6 +486,7 @@ int iskra_ens_count(iskra_ens *h, int run, int sid, int64_t *np) {
 
 int iskra_ens_download(iskra_ens *h, int run, int sid, double *x, double *v, uint32_t *id, int64_t ld,
                        int64_t *np_out) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h) return ISKRA_EINVAL;
   Ens *e = &h->e;
   int64_t np = 0;
@@ -478,6 +504,7 @@ int iskra_ens_download(iskra_ens *h, int run, int sid, double *x, double *v, uin
 }
 
 int iskra_ens_step(iskra_ens *h, double dt, int nsteps) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h) return ISKRA_EINVAL;
   Ens *e = &h->e;
   if (!(dt > 0) || nsteps < 0) return ens_err(e, ISKRA_EINVAL, "bad dt / nsteps");
@@ -507,11 +534,13 @@ int iskra_ens_step(iskra_ens *h, double dt, int nsteps) {
 }
 
 int iskra_ens_sync(iskra_ens *h) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h) return ISKRA_EINVAL;
   return ens_collect(&h->e);
 }
 
 int iskra_ens_mcc_counts(iskra_ens *h, int run, int mid, uint64_t *counts) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h || !counts) return ISKRA_EINVAL;
   Ens *e = &h->e;
   if (run < 0 || run >= e->R || mid < 0 || mid >= (int)e->mcc.size()) return ens_err(e, ISKRA_EINVAL, "bad run or set");
@@ -523,6 +552,7 @@ int iskra_ens_mcc_counts(iskra_ens *h, int run, int mid, uint64_t *counts) {
 }
 
 int iskra_ens_field(iskra_ens *h, int run, int which, double *out) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h || !out) return ISKRA_EINVAL;
   Ens *e = &h->e;
   if (run < 0 || run >= e->R) return ens_err(e, ISKRA_EINVAL, "bad run");
@@ -548,6 +578,7 @@ int iskra_ens_field(iskra_ens *h, int run, int which, double *out) {
 }
 
 int iskra_ens_set_compact_every(iskra_ens *h, int every) {
+  if (h && !h->e.c) return ens_err(&h->e, ISKRA_EINVAL, "the ensemble's template context was destroyed");
   if (!h || every < 0) return ISKRA_EINVAL;
   h->e.compact_every = every;
   return ISKRA_OK;

@@ -101,6 +101,7 @@ struct Species {
   long long cap = 0;
   int bnd[2] = {ISKRA_BND_NONE, ISKRA_BND_NONE};
   SpeciesDev dev{};
+  SpeciesDev *dview = nullptr; // device copy of dev (kernels over run views take arrays)
   double *n = nullptr;         // FP64 density (nx*ny)
   // accumulator / density bookkeeping (host side):
   bool acc_valid = false;      // acc holds the unconsumed deposit of the current positions
@@ -161,6 +162,10 @@ struct Ctx {
   cudaGraphExec_t sort_graph[kMaxSpecies] = {};  // tile sort of one species
   unsigned long long graph_kernels = 0, sort_graph_kernels[kMaxSpecies] = {};
   double *d_scratch = nullptr;           // 16 doubles of reduction scratch
+  std::vector<void *> ensembles;         // ensembles built on this context (as template)
+  void *mcc_work = nullptr;              // MCC work list (entries of the largest species)
+  unsigned long long mcc_work_cap = 0;
+  unsigned long long *mcc_nwork = nullptr;
   unsigned long long launches = 0;       // kernels launched by iskra_step
   double graph_dt = 0;
   double graph_rtol = 0;
@@ -231,7 +236,11 @@ int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float
                      int *err, cudaStream_t st);
 int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, const SpeciesDev *prod,
                     const uint2 *keys, unsigned long long *counts, const float2 *E32, int nn, int blocks_per_run,
+                    void *work, unsigned long long *nwork, unsigned long long cap_work,
                     const unsigned long long *d_step, int *err, cudaStream_t st);
+size_t mcc_work_entry_bytes();
+int ensure_mcc_work(Ctx *c);
+void ensembles_detach(Ctx *c);
 void mcc_key(uint64_t seed, int set_index, uint32_t &k0, uint32_t &k1);
 int mcc_nproc(Ctx *c, int mid);
 int mcc_src(Ctx *c, int mid);

@@ -48,6 +48,8 @@ struct MccDev {
   unsigned long long *counts;  // N
   unsigned int *nu;      // (nx*ny*N) accepted collisions per node and process
   uint32_t key0, key1;
+  int logu[kMaxProc];    // table energies log-uniform: O(1) bracket guess
+  float log_e0[kMaxProc], inv_dlog[kMaxProc];
 };
 
 struct Mcc {
@@ -64,6 +66,8 @@ struct Mcc {
   unsigned long long *counts = nullptr;
   unsigned int *nu = nullptr;
   int set_index = 0;
+  std::vector<int> logu;            // per process: energies on a log-uniform grid
+  std::vector<float> log_e0, inv_dlog;
 };
 
 void mcc_destroy(Mcc *m) {
@@ -176,15 +180,29 @@ __device__ __forceinline__ void diffuse_reflection(const float v[3], float u1, f
 }
 
 // CrossSection: linear interpolation, flat extrapolation (cross_section.jl:8-14)
-__device__ __forceinline__ float sigma_at(const float *e, const float *s, int n, float x) {
+// The bracket e[lo] <= x < e[lo+1] is found by bisection, or for tables on a
+// log-uniform grid from log(x) and then corrected against the table itself
+// (the same bracket either way).
+__device__ __forceinline__ float sigma_at(const float *e, const float *s, int n, float x, int logu, float le0,
+                                          float idl) {
   if (x <= e[0]) return s[0];
   if (x >= e[n - 1]) return s[n - 1];
-  int lo = 0, hi = n - 1;
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (e[mid] <= x) lo = mid;
-    else hi = mid;
+  int lo;
+  if (logu) {
+    lo = (int)((__logf(x) - le0) * idl);
+    lo = max(0, min(n - 2, lo));
+    while (lo > 0 && e[lo] > x) lo--;
+    while (lo < n - 2 && e[lo + 1] <= x) lo++;
+  } else {
+    lo = 0;
+    int hi = n - 1;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (e[mid] <= x) lo = mid;
+      else hi = mid;
+    }
   }
+  const int hi = lo + 1;
   const float t = (x - e[lo]) / (e[hi] - e[lo]);
   return (1.0f - t) * s[lo] + t * s[hi];
 }
@@ -208,70 +226,172 @@ __device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsi
   return base + rank;
 }
 
-// Null-collision step of the warps [warp0, np/32) (stride nwarps) of one
-// species store against the tables staged in `tab`; appends go to the
-// stores' np_new cursors.  Shared by the single-run and ensemble kernels.
-__device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_prod, const MccDev &M,
-                          const float *tab, const float2 *__restrict__ E, int nx, unsigned long long step,
-                          long long warp, long long nwarps, int *err) {
+// ---- two-phase null-collision step --------------------------------------
+// Phase 1 (k_mcc_select, every live particle): the particle's first draw
+// gives its number of selections c ~ Poisson(N maxPt); particles with c > 0
+// go to a work list (run, slot, c).  Phase 2 (k_mcc_collide, the work list
+// only): each entry replays its particle's stream past that draw and runs
+// the c selections -- the k choice, acceptance test and kinematics -- in
+// order.  With N maxPt ~ 0.1 a warp of phase 2 holds 32 colliding particles
+// instead of the ~3 a single pass over all particles would.
+struct MccWork {
+  uint32_t slot;
+  uint32_t nsel;
+};
+
+constexpr int kSelChunk = 2048;  // particles per block pass of k_mcc_select
+
+__device__ __forceinline__ Stream particle_stream(uint32_t pid, unsigned long long step, uint2 key) {
+  Stream R;
+  R.ctr = U4{pid, (uint32_t)step, (uint32_t)(step >> 32), 0u};
+  R.k0 = key.x;
+  R.k1 = key.y;
+  R.left = 0;
+  return R;
+}
+
+// selections ~ Poisson(lam) by inversion (bounded)
+__device__ __forceinline__ int draw_selections(Stream &R, float lam, float expl) {
+  const float u = R.next();
+  float pk = expl, cdf = expl;
+  int nsel = 0;
+  while (u > cdf && nsel < 16) {
+    nsel++;
+    pk *= lam / nsel;
+    cdf += pk;
+  }
+  return nsel;
+}
+
+// Phase 1 over the particles of run blockIdx.y (R = 1 for a single context):
+// a block collects the selected particles of a chunk in shared memory and
+// appends them to its run's segment [r cap_run, ...) of the work list with
+// one atomic on the run's counter nwork[r].
+__global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict__ src, float lam, uint2 key1,
+                                                    const uint2 *__restrict__ keys,
+                                                    const unsigned long long *__restrict__ d_step,
+                                                    MccWork *__restrict__ work, unsigned long long *__restrict__ nwork,
+                                                    unsigned long long cap_run, int *err) {
+  pdl_wait();
+  __shared__ MccWork buf[kSelChunk];
+  __shared__ unsigned cnt;
+  __shared__ unsigned long long base;
   const unsigned FULL = 0xffffffffu;
-  const int ntab = M.off[M.N];
+  const int r = blockIdx.y;
+  const SpeciesDev s = src[r];
+  const uint2 key = keys ? keys[r] : key1;
   const int lane = threadIdx.x & 31;
   const long long np = s.st->np;
   const int cur = s.st->cur;
+  const float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
+  const uint32_t *__restrict__ ids = pick(s.id[0], s.id[1], cur);
+  const unsigned long long step = *d_step;
+  const float expl = __expf(-lam);
+  MccWork *__restrict__ seg = work + (size_t)r * cap_run;
+  int flags = 0;
+  for (long long c0 = (long long)blockIdx.x * kSelChunk; c0 < np; c0 += (long long)gridDim.x * kSelChunk) {
+    if (threadIdx.x == 0) cnt = 0u;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kSelChunk; i += blockDim.x) {
+      const long long p = c0 + i;
+      int nsel = 0;
+      if (p < np && __float_as_int(zc[p].y) >= 0) {
+        Stream R = particle_stream(ids[p], step, key);
+        nsel = draw_selections(R, lam, expl);
+      }
+      const unsigned m = __ballot_sync(FULL, nsel > 0);
+      if (!m) continue;
+      const int leader = __ffs(m) - 1;
+      unsigned at = 0;
+      if (lane == leader) at = atomicAdd(&cnt, (unsigned)__popc(m));
+      at = __shfl_sync(FULL, at, leader) + __popc(m & ((1u << lane) - 1u));
+      if (nsel > 0) buf[at] = MccWork{(uint32_t)p, (uint32_t)nsel};
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) base = atomicAdd(nwork + r, (unsigned long long)cnt);
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) {
+      const unsigned long long at = base + i;
+      if (at < cap_run) seg[at] = buf[i];
+      else flags |= DERR_CAPACITY;
+    }
+    __syncthreads();
+  }
+  const int f = __reduce_or_sync(FULL, flags);
+  if (lane == 0 && f) atomicOr(err, f);
+}
+
+// Phase 2 over the work list segment of run r = blockIdx.y: the run's stores
+// src[r] / prod[r], node field E + r nn, key keys[r] (or M's key for a single
+// context), counters counts_runs + r N (or M.counts).
+__global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restrict__ src,
+                                                     const SpeciesDev *__restrict__ prod, int has_prod, MccDev M,
+                                                     const uint2 *__restrict__ keys, unsigned long long *counts_runs,
+                                                     const float2 *__restrict__ E, int nn, int nx,
+                                                     const unsigned long long *__restrict__ d_step,
+                                                     const MccWork *__restrict__ work,
+                                                     const unsigned long long *__restrict__ nwork,
+                                                     unsigned long long cap_run, int *err) {
+  pdl_wait();
+  extern __shared__ float tab[];
+  const unsigned FULL = 0xffffffffu;
+  const int ntab = M.off[M.N];
+  for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
+    tab[t] = M.eps[t];
+    tab[ntab + t] = M.sig[t];
+  }
+  __syncthreads();
+  const unsigned long long step = *d_step;
+  const int r = blockIdx.y;
+  const long long nw = (long long)min(nwork[r], cap_run);
+  const MccWork *__restrict__ seg = work + (size_t)r * cap_run;
+  const float expl = __expf(-M.lam);
+  int flags = 0;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const SpeciesDev s = src[r];
+  const int cur = s.st->cur;
   float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
   float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
-  uint32_t *__restrict__ ids = pick(s.id[0], s.id[1], cur);
-  unsigned cnt[kMaxProc];
+  unsigned long long *cnts = keys ? counts_runs + (size_t)r * M.N : M.counts;
+  const float2 *Er = E + (size_t)r * nn;
+  unsigned acc_k[kMaxProc];
 #pragma unroll
-  for (int k = 0; k < kMaxProc; k++) cnt[k] = 0;
-  int flags = 0;
-  const float expl = __expf(-M.lam);
-  for (long long base = warp * 32; base < np; base += nwarps * 32) {
-    const long long p = base + lane;
-    int cell = -1;
-    float4 a = make_float4(0, 0, 0, 0);
-    float2 b = make_float2(0, 0);
-    uint32_t pid = 0;
-    if (p < np) {
-      b = zc[p];
-      cell = __float_as_int(b.y);
-    }
-    Stream R;
+  for (int k = 0; k < kMaxProc; k++) acc_k[k] = 0u;
+  for (long long base = warp * 32; base < nw; base += nwarps * 32) {
+    const long long w = base + lane;
+    const bool act = w < nw;
     int nsel = 0;
-    if (cell >= 0) {
-      pid = ids[p];
-      R.ctr = U4{pid, (uint32_t)step, (uint32_t)(step >> 32), 0u};
-      R.k0 = M.key0;
-      R.k1 = M.key1;
-      R.left = 0;
-      // selections ~ Poisson(lam) by inversion (bounded)
-      float u = R.next();
-      float pk = expl, cdf = expl;
-      while (u > cdf && nsel < 16) {
-        nsel++;
-        pk *= M.lam / nsel;
-        cdf += pk;
-      }
+    long long p = 0;
+    if (act) {
+      const MccWork e = seg[w];
+      p = e.slot;
+      nsel = (int)e.nsel;
     }
-    bool any_sel = __any_sync(FULL, nsel > 0);
-    if (!any_sel) continue;
     bool ion_child = false;
     float cv[3] = {0, 0, 0};
     float tv_ion[3] = {0, 0, 0};
-    bool changed = false;
     float v[3] = {0, 0, 0};
-    int node = 0;
-    if (nsel > 0) {
+    float4 a = make_float4(0, 0, 0, 0);
+    float2 b = make_float2(0, 0);
+    int cell = -1;
+    if (act) {
+      b = zc[p];
+      cell = __float_as_int(b.y);
       a = xv[p];
+      const uint32_t pid = pick(s.id[0], s.id[1], cur)[p];
+      Stream R = particle_stream(pid, step, keys ? keys[r] : make_uint2(M.key0, M.key1));
+      (void)draw_selections(R, M.lam, expl);  // the phase-1 draw
       v[0] = a.z;
       v[1] = a.w;
       v[2] = b.x;
       const int i0 = cell & 0xffff, j0 = cell >> 16;
-      node = i0 + nx * j0;
+      const int node = i0 + nx * j0;
       const float n = __ldg(M.gas_n + node);
-      const float2 e = __ldg(E + node);
+      const float2 e = __ldg(Er + node);
       const float tvx = M.qmt_dt * e.x, tvy = M.qmt_dt * e.y;
+      bool changed = false;
       for (int sidx = 0; sidx < nsel && n >= 0.0f; sidx++) {
         const float U = R.next();
         int k = (int)floorf(M.N * U);
@@ -279,7 +399,9 @@ __device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_p
         const float gx = tvx - v[0], gy = tvy - v[1], gz = -v[2];
         const float g = sqrtf(gx * gx + gy * gy + gz * gz);
         const float eps = 0.5f * M.m_ev * g * g;
-        const float sg = sigma_at(tab + M.off[k], tab + ntab + M.off[k], M.off[k + 1] - M.off[k], eps) * g;
+        const float sg = sigma_at(tab + M.off[k], tab + ntab + M.off[k], M.off[k + 1] - M.off[k], eps, M.logu[k],
+                                  M.log_e0[k], M.inv_dlog[k]) *
+                         g;
         float Pk = -expm1f(-n * sg * M.dt);
         Pk *= M.inv_nmaxpt;
         if (Pk > 1.0f) {
@@ -287,15 +409,15 @@ __device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_p
           break;
         }
         if (!(U > (float)(k + 1) / M.N - Pk)) continue;
-        cnt[k]++;
-        if (M.nu) atomicAdd(M.nu + (size_t)node * M.N + k, 1u);
+        acc_k[k]++;
+        if (M.nu && !keys) atomicAdd(M.nu + (size_t)node * M.N + k, 1u);
         const int type = M.types[k];
         if (type <= ISKRA_MCC_INELASTIC_BACKWARD) {
           float tv[3] = {R.normal() * M.vth_t, R.normal() * M.vth_t, R.normal() * M.vth_t};
-          float vr[3], w[3], dir[3];
+          float vr[3], wv[3], dir[3];
           for (int c = 0; c < 3; c++) {
             vr[c] = v[c] - tv[c];
-            w[c] = M.mr1 * v[c] + M.mr2 * tv[c];
+            wv[c] = M.mr1 * v[c] + M.mr2 * tv[c];
           }
           const float nvr = sqrtf(vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2]);
           float scale = nvr;
@@ -303,7 +425,7 @@ __device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_p
           const float u1 = R.next(), u2 = R.next();
           if (type == ISKRA_MCC_ELASTIC_ISOTROPIC) isotropic_scattering(vr, u1, u2, dir);
           else diffuse_reflection(vr, u1, u2, dir);
-          for (int c = 0; c < 3; c++) v[c] = w[c] + M.mr2 * (scale * dir[c]);
+          for (int c = 0; c < 3; c++) v[c] = wv[c] + M.mr2 * (scale * dir[c]);
           changed = true;
           continue;
         }
@@ -337,9 +459,7 @@ __device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_p
         }
       }
       if (changed) {
-        if (!isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2])) {
-          flags |= DERR_NAN;
-        }
+        if (!isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2])) flags |= DERR_NAN;
         xv[p] = make_float4(a.x, a.y, v[0], v[1]);
         zc[p] = make_float2(v[2], b.y);
       }
@@ -347,27 +467,27 @@ __device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_p
     // appends: child electron into the source species, ions into the product
     if (__any_sync(FULL, ion_child)) {
       uint32_t nid;
-      long long slot = warp_reserve(ion_child, &s.st->np_new, &s.st->next_id, nid);
+      const long long slot = warp_reserve(ion_child, &s.st->np_new, &s.st->next_id, nid);
       if (ion_child) {
         if (slot < s.cap) {
-          const int cb = s.st->cur;  // unchanged during the kernel
-          pick(s.xv[0], s.xv[1], cb)[slot] = make_float4(a.x, a.y, cv[0], cv[1]);
-          pick(s.zc[0], s.zc[1], cb)[slot] = make_float2(cv[2], __int_as_float(cell));
-          pick(s.id[0], s.id[1], cb)[slot] = nid;
+          xv[slot] = make_float4(a.x, a.y, cv[0], cv[1]);
+          zc[slot] = make_float2(cv[2], __int_as_float(cell));
+          pick(s.id[0], s.id[1], cur)[slot] = nid;
         } else {
           flags |= DERR_CAPACITY;
         }
       }
       if (has_prod) {
+        const SpeciesDev pd = prod[r];
+        const int pb = pd.st->cur;
         for (int m = 0; m < M.mp; m++) {
           uint32_t pid2;
-          long long ps = warp_reserve(ion_child, &prod.st->np_new, &prod.st->next_id, pid2);
+          const long long ps = warp_reserve(ion_child, &pd.st->np_new, &pd.st->next_id, pid2);
           if (ion_child) {
-            if (ps < prod.cap) {
-              const int pb = prod.st->cur;
-              pick(prod.xv[0], prod.xv[1], pb)[ps] = make_float4(a.x, a.y, tv_ion[0], tv_ion[1]);
-              pick(prod.zc[0], prod.zc[1], pb)[ps] = make_float2(tv_ion[2], __int_as_float(cell));
-              pick(prod.id[0], prod.id[1], pb)[ps] = pid2;
+            if (ps < pd.cap) {
+              pick(pd.xv[0], pd.xv[1], pb)[ps] = make_float4(a.x, a.y, tv_ion[0], tv_ion[1]);
+              pick(pd.zc[0], pd.zc[1], pb)[ps] = make_float2(tv_ion[2], __int_as_float(cell));
+              pick(pd.id[0], pd.id[1], pb)[ps] = pid2;
             } else {
               flags |= DERR_CAPACITY;
             }
@@ -379,53 +499,16 @@ __device__ void mcc_warps(const SpeciesDev &s, const SpeciesDev &prod, int has_p
 #pragma unroll
   for (int k = 0; k < kMaxProc; k++) {
     if (k >= M.N) break;
-    unsigned t = __reduce_add_sync(FULL, cnt[k]);
-    if (lane == 0 && t) atomicAdd(M.counts + k, (unsigned long long)t);
+    const unsigned t = __reduce_add_sync(FULL, acc_k[k]);
+    if (lane == 0 && t) atomicAdd(cnts + k, (unsigned long long)t);
   }
-  int f = __reduce_or_sync(FULL, flags);
+  const int f = __reduce_or_sync(FULL, flags);
   if (lane == 0 && f) atomicOr(err, f);
 }
 
-// stage the cross-section tables of a set in shared memory
-__device__ __forceinline__ void stage_tables(const MccDev &M, float *tab) {
-  const int ntab = M.off[M.N];
-  for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
-    tab[t] = M.eps[t];
-    tab[ntab + t] = M.sig[t];
-  }
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(256) k_mcc(SpeciesDev s, SpeciesDev prod, int has_prod, MccDev M,
-                                             const float2 *__restrict__ E, int nx,
-                                             const unsigned long long *__restrict__ d_step, int *err) {
+__global__ void k_zero_u64(unsigned long long *p, int n) {
   pdl_wait();
-  extern __shared__ float tab[];
-  stage_tables(M, tab);
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  mcc_warps(s, prod, has_prod, M, tab, E, nx, *d_step, warp, nwarps, err);
-}
-
-// Ensemble: run r = blockIdx.y with its own stores, field, key and counters.
-__global__ void __launch_bounds__(256) k_mcc_runs(const SpeciesDev *__restrict__ src, const SpeciesDev *__restrict__ prod,
-                                                  int has_prod, MccDev M, const uint2 *__restrict__ keys,
-                                                  unsigned long long *__restrict__ counts, const float2 *__restrict__ E,
-                                                  int nn, int nx, const unsigned long long *__restrict__ d_step,
-                                                  int *err) {
-  pdl_wait();
-  extern __shared__ float tab[];
-  stage_tables(M, tab);
-  const int r = blockIdx.y;
-  MccDev Mr = M;
-  Mr.key0 = keys[r].x;
-  Mr.key1 = keys[r].y;
-  Mr.counts = counts + (size_t)r * M.N;
-  Mr.nu = nullptr;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  mcc_warps(src[r], has_prod ? prod[r] : src[r], has_prod, Mr, tab, E + (size_t)r * nn, nx, *d_step, warp, nwarps,
-            err);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0ull;
 }
 
 // Appends reserve slots from np_new so that np (the loop bound of the running
@@ -478,6 +561,32 @@ static int mcc_params(Ctx *c, int mid, double dt, uint64_t seed, MccDev &M) {
   M.counts = m->counts;
   M.nu = m->nu;
   mcc_key(seed, m->set_index, M.key0, M.key1);
+  for (int k = 0; k < m->N; k++) {
+    M.logu[k] = m->logu[k];
+    M.log_e0[k] = m->log_e0[k];
+    M.inv_dlog[k] = m->inv_dlog[k];
+  }
+  return ISKRA_OK;
+}
+
+// Both phases for R runs: src/prod device views (R each), keys (R, or
+// nullptr with key1 for a single context), per-run counters, node fields E
+// (R x nn), work list of cap_work entries with its counter.
+static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const SpeciesDev *src, const SpeciesDev *prod,
+                            const uint2 *keys, unsigned long long *counts, const float2 *E, int nn, int select_blocks,
+                            MccWork *work, unsigned long long *nwork, unsigned long long cap_work,
+                            const unsigned long long *d_step, int *err, cudaStream_t st) {
+  Mcc *m = c->mccs[mid];
+  const int ntab = m->off[m->N];
+  const size_t smem = (size_t)2 * ntab * sizeof(float);
+  const uint2 key1 = make_uint2(M.key0, M.key1);
+  ISKRA_CUDA(c, launch_pdl(k_zero_u64, (R + 255) / 256, 256, 0, st, nwork, R));
+  ISKRA_CUDA(c, launch_pdl(k_mcc_select, dim3(select_blocks, R), 256, 0, st, src, M.lam, key1, keys, d_step, work, nwork,
+                           cap_work, err));
+  const int collide_blocks = R == 1 ? c->num_sms * 8 : select_blocks;
+  ISKRA_CUDA(c, launch_pdl(k_mcc_collide, dim3(collide_blocks, R), 256, smem, st, src, prod, (int)(m->prod >= 0), M,
+                           keys, counts, E, nn, c->nx, d_step, (const MccWork *)work, (const unsigned long long *)nwork,
+                           cap_work, err));
   return ISKRA_OK;
 }
 
@@ -488,16 +597,16 @@ int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long lo
   MccDev M;
   int rc = mcc_params(c, mid, dt, seed, M);
   if (rc) return rc;
-  const int ntab = m->off[m->N];
-  const size_t smem = (size_t)2 * ntab * sizeof(float);
-  long long want = (s.cap + 255) / 256;
-  long long maxb = (long long)c->num_sms * 8;
+  if (!c->mcc_work) return set_err(c, ISKRA_EINVAL, "MCC work list missing");
+  long long want = (s.cap + kSelChunk - 1) / kSelChunk;
+  long long maxb = (long long)c->num_sms * 4;
   int blocks = (int)(want < maxb ? (want < 1 ? 1 : want) : maxb);
-  SpeciesDev pd = m->prod >= 0 ? c->species[m->prod].dev : s.dev;
+  const SpeciesDev *pd = m->prod >= 0 ? c->species[m->prod].dview : s.dview;
   SpeciesState *pst = m->prod >= 0 ? c->species[m->prod].dev.st : nullptr;
   ISKRA_CUDA(c, launch_pdl(k_append_begin, 1, 1, 0, c->stream, s.dev.st, pst));
-  ISKRA_CUDA(c, launch_pdl(k_mcc, blocks, 256, smem, c->stream, s.dev, pd, (int)(m->prod >= 0), M, c->E32, c->nx,
-                           d_step, c->d_err));
+  rc = queue_mcc_phases(c, mid, M, 1, s.dview, pd, nullptr, nullptr, c->E32, c->nn, blocks, (MccWork *)c->mcc_work,
+                        c->mcc_nwork, c->mcc_work_cap, d_step, c->d_err, c->stream);
+  if (rc) return rc;
   ISKRA_CUDA(c, launch_pdl(k_append_end, 1, 1, 0, c->stream, s.dev.st, s.cap));
   if (m->prod >= 0)
     ISKRA_CUDA(c, launch_pdl(k_append_end, 1, 1, 0, c->stream, c->species[m->prod].dev.st, c->species[m->prod].cap));
@@ -515,18 +624,34 @@ int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long lo
 
 // Ensemble launch of MCC set mid of the template context over R runs:
 // per-run stores (src/prod views), keys (2 words per run), counters (R x N)
-// and node fields (R x nn).
+// and node fields (R x nn); work list of cap_work entries.
 int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, const SpeciesDev *prod,
                     const uint2 *keys, unsigned long long *counts, const float2 *E32, int nn, int blocks_per_run,
+                    void *work, unsigned long long *nwork, unsigned long long cap_work,
                     const unsigned long long *d_step, int *err, cudaStream_t st) {
-  Mcc *m = c->mccs[mid];
   MccDev M;
   int rc = mcc_params(c, mid, dt, 0, M);
   if (rc) return rc;
-  const int ntab = m->off[m->N];
-  const size_t smem = (size_t)2 * ntab * sizeof(float);
-  ISKRA_CUDA(c, launch_pdl(k_mcc_runs, dim3(blocks_per_run, R), 256, smem, st, src, prod, (int)(m->prod >= 0), M, keys,
-                           counts, E32, nn, c->nx, d_step, err));
+  return queue_mcc_phases(c, mid, M, R, src, prod, keys, counts, E32, nn, blocks_per_run, (MccWork *)work, nwork,
+                          cap_work, d_step, err, st);
+}
+
+size_t mcc_work_entry_bytes() { return sizeof(MccWork); }
+
+// Work list sized for the largest species; called where no stream capture can
+// be active (MCC set and species creation).
+int ensure_mcc_work(Ctx *c) {
+  if (c->mccs.empty()) return ISKRA_OK;
+  long long cap = 1;
+  for (auto &sp : c->species) cap = std::max(cap, sp.cap);
+  if (c->mcc_work && c->mcc_work_cap >= (unsigned long long)cap) return ISKRA_OK;
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  cudaFree(c->mcc_work);
+  c->mcc_work = nullptr;
+  c->mcc_work_cap = 0;
+  ISKRA_CUDA(c, cudaMalloc(&c->mcc_work, (size_t)cap * sizeof(MccWork)));
+  if (!c->mcc_nwork) ISKRA_CUDA(c, cudaMalloc(&c->mcc_nwork, sizeof(unsigned long long)));
+  c->mcc_work_cap = (unsigned long long)cap;
   return ISKRA_OK;
 }
 
@@ -571,6 +696,22 @@ int iskra_mcc_create(iskra_ctx *h, int src, int nproc, const int *types, const d
   m->gas_T = gas_T;
   m->gas_q = gas_q;
   m->set_index = (int)c->mccs.size();
+  // tables on a log-uniform energy grid get an O(1) bracket guess
+  m->logu.assign(nproc, 0);
+  m->log_e0.assign(nproc, 0.f);
+  m->inv_dlog.assign(nproc, 0.f);
+  for (int k = 0; k < nproc; k++) {
+    const double *E = eps + off[k];
+    const int n = off[k + 1] - off[k];
+    if (n < 3 || !(E[0] > 0)) continue;
+    const double d = std::log(E[n - 1] / E[0]) / (n - 1);
+    bool uni = d > 0;
+    for (int t = 1; t < n && uni; t++) uni = std::fabs(std::log(E[t] / E[t - 1]) - d) <= 1e-6 * d;
+    if (!uni) continue;
+    m->logu[k] = 1;
+    m->log_e0[k] = (float)std::log((double)(float)E[0]);
+    m->inv_dlog[k] = (float)(1.0 / d);
+  }
   // MonteCarloCollisions constructor (mcc.jl:27-51): max over the union of
   // table energies (plus 0) of Σ_k σ_k(ε) v(ε), v = sqrt(2ε/m_eV)
   std::vector<double> e = {0.0};
@@ -625,7 +766,7 @@ int iskra_mcc_create(iskra_ctx *h, int src, int nproc, const int *types, const d
   *mid = (int)c->mccs.size() - 1;
   if (max_sigma_g) *max_sigma_g = best;
   invalidate_graphs(c);
-  return ISKRA_OK;
+  return ensure_mcc_work(c);
 }
 
 int iskra_mcc_perform(iskra_ctx *h, int mid, double dt, uint64_t seed, uint64_t step) {

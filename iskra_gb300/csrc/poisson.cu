@@ -1713,7 +1713,9 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
   pdl_wait();
   extern __shared__ double fsm[];
   __shared__ RowClass cls_sh[kSmemClasses];
+  __shared__ double twc[16], tws[16];  // cos, sin of 2π m/N
   const int nx = op.nx, ny = op.ny, nn = nx * ny, N = F.N, K = F.K;
+  if (threadIdx.x < N) sincospi(2.0 * threadIdx.x / N, &tws[threadIdx.x], &twc[threadIdx.x]);
   double *xs = fsm, *rs = xs + nn, *spec = rs + nn, *sinv = spec + 2 * nx * K, *scp = sinv + nx * K;
   const int r = blockIdx.x;
   const size_t o = (size_t)r * nn;
@@ -1781,11 +1783,10 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
     const int i = t / K, k = t - i * K;
     double re = 0, im = 0;
     for (int j = 0; j < N; j++) {
-      double sn, cs;
-      sincospi(-2.0 * (double)((j * k) % N) / N, &sn, &cs);
+      const int m = (j * k) % N;  // e^{-2πi jk/N}
       const double v = rs[i + nx * j];
-      re += v * cs;
-      im += v * sn;
+      re += v * twc[m];
+      im -= v * tws[m];
     }
     spec[2 * t] = re;
     spec[2 * t + 1] = im;
@@ -1819,9 +1820,8 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
       const int mm = m < K ? m : N - m;
       const double re = spec[2 * (i * K + mm)];
       const double im = m < K ? spec[2 * (i * K + mm) + 1] : -spec[2 * (i * K + mm) + 1];
-      double sn, cs;
-      sincospi(2.0 * (double)((j * m) % N) / N, &sn, &cs);
-      v += re * cs - im * sn;
+      const int q = (j * m) % N;
+      v += re * twc[q] - im * tws[q];
     }
     xs[k] += v / N;
   }

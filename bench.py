@@ -164,6 +164,86 @@ def committed_traffic():
 
 
 # ----------------------------------------------------------------------------
+# Batched ensemble (the C4 configuration): 256 independent runs of the
+# capacitively coupled argon discharge (257 x 2 nodes, gap 0.025 m, 3 Pa,
+# 300 K, driven electrode 13.56 MHz with amplitudes U[100, 500] V drawn with
+# seed 4, MCC seeds 1000 + r), uneven per-run particle counts from 20 k to
+# 400 k (electrons + ions; ~58 M in total), one graph per step for all runs.
+# Synthetic cross sections as specified for the discharge configuration.
+# ----------------------------------------------------------------------------
+C4_RUNS, C4_NX, C4_GAP, C4_DT, C4_F = 256, 257, 0.025, 7.4e-11, 13.56e6
+
+
+def c3_tables(ne=1024):
+    eps = np.logspace(-2, 3, ne)
+    el = np.full(ne, 1e-19)
+    ex = np.where(eps > 11.5, np.minimum((eps - 11.5) / (100.0 - 11.5), 1.0) * 3e-21, 0.0)
+    iz = np.where(eps > 15.76, 3e-20 * np.log(eps / 15.76) / np.log(100 / 15.76) * np.sqrt(100 / eps), 0.0)
+    cx = np.full(ne, 5e-19)
+    return eps, el, ex, iz, cx
+
+
+def c4_measure(steps):
+    import torch
+    from iskra_gb300 import _lib
+    from iskra_gb300.device import Context, Ensemble
+    R, NXc = C4_RUNS, C4_NX
+    dxc = C4_GAP / (NXc - 1)
+    rng = np.random.default_rng(4)
+    amps = rng.uniform(100, 500, R)
+    nps = (10000 + (amps - 100) / 400 * 190000).astype(int)  # per species and run
+    w = 1e15 * C4_GAP * dxc / 100000
+    ctx = Context(NXc, 2, dxc, dxc)
+    se = ctx.species_create(-QE, ME, w, 16)
+    si = ctx.species_create(QE, M_AR, w, 16)
+    for s in (se, si):
+        ctx.set_boundary(s, _lib.BND_DISCARD, _lib.BND_WRAP)
+    ctx.poisson_create(EPS0)
+    ctx.apply_periodic(1)
+    left = np.zeros((NXc, 2), bool)
+    left[0, :] = True
+    right = np.zeros((NXc, 2), bool)
+    right[-1, :] = True
+    ctx.apply_dirichlet(left, 0.0)
+    ctx.apply_dirichlet(right, 0.0)
+    ctx.drive_dirichlet(left, 300.0, C4_F)
+    eps, el, ex, iz, cx = c3_tables()
+    gas = np.full((NXc, 2), 3.0 / (KB * 300.0))
+    ctx.mcc_create(se, [(_lib.MCC_ELASTIC_ISOTROPIC, 0.0, eps, el), (_lib.MCC_EXCITATION, 11.5, eps, ex),
+                        (_lib.MCC_IONIZATION, 15.76, eps, iz)], M_AR, 300.0, gas, product=si)
+    ctx.mcc_create(si, [(_lib.MCC_ELASTIC_BACKWARD, 0.0, eps, cx)], M_AR, 300.0, gas)
+    ens = Ensemble(ctx, R, int(nps.max() * 1.5))
+    ens.set_seeds([1000 + r for r in range(R)])
+    ens.set_drive_amplitude(0, amps)
+    for r in range(R):
+        n = int(nps[r])
+        for s, T, m in ((se, 4.0, ME), (si, 0.03, M_AR)):
+            x = np.asfortranarray(np.column_stack([rng.uniform(0, C4_GAP, n), rng.uniform(0, dxc, n)]))
+            v = np.asfortranarray(rng.standard_normal((n, 3)) * np.sqrt(2 * T * QE / m))
+            ens.upload(r, s, x, v)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ens.step(C4_DT, 5)
+    ens.sync()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ens.step(C4_DT, steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ens.sync()
+    ms = a.elapsed_time(b)
+    n_end = sum(ens.count(r, s) for r in range(R) for s in (se, si))
+    n0 = int(2 * nps.sum())
+    ens.close()
+    ctx.close()
+    return {"metric": "particle-steps/s", "value": 0.5 * (n0 + n_end) * steps / (ms * 1e-3),
+            "unit": "particle-steps/s", "ms_per_step": ms / steps, "steps": steps, "runs": R,
+            "particles": [n0, n_end], "workload": "256 x (1D CCP argon discharge, 257x2 nodes, e- and Ar+ MCC, "
+            "drive U[100,500] V), one ensemble step graph", "data": "synthetic"}
+
+
+# ----------------------------------------------------------------------------
 # CPU arm: the FP64 oracle (the reference's step restated), all host threads
 # ----------------------------------------------------------------------------
 def cpu_run(w, e, i, max_seconds=20.0, max_steps=None):
@@ -218,6 +298,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
+    ap.add_argument("--no-c4", action="store_true", help="skip the batched-ensemble (C4) leg")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -344,10 +425,11 @@ def main():
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 push / i64 deposit / f64 Poisson", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 push / i64 deposit / f64 Poisson residual", "data": "synthetic",
         "config": {"workload": WORKLOAD, "grid": [NX, NY], "particles": 2 * NP * world,
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (224 MB particle store)",
-                   "poisson": f"FP64 FFT(y)/tridiagonal(x) to relres {RTOL:g}; last relres {relres:.2e} in {it} sweep(s)",
+                   "poisson": f"FP32 FFT(y)/cyclic-reduction(x) corrections of the FP64 residual to relres {RTOL:g}; "
+                              f"last relres {relres:.2e} in {it} sweep(s)",
                    "sort_every": "per species (automatic)" if SORT_EVERY < 0 else SORT_EVERY},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_push (gather+push+discard/wrap+deposit)",
@@ -357,6 +439,8 @@ def main():
         "clocks": clocks,
         "e2e": e2e,
     }
+    if rank == 0 and not args.no_c4:
+        line["batched_c4"] = c4_measure(min(max(args.steps // 5, 20), 200))
     if rank == 0 and not args.no_cpu_baseline:
         r = cpu_run(w, e, i, max_seconds=20.0)
         line["cpu_baseline"] = {

@@ -127,18 +127,48 @@ constexpr int kWin = kTile + 2 * kHalo;  // window cells per axis
 constexpr int kWinN = kWin + 1;          // window nodes per axis
 constexpr int kWinCells = kWin * kWin;
 
-// Per window cell, the deposit moments of the run sums added there, in 32-bit
-// limbs that cannot overflow while the cell holds at most kMaxCell particles
-// (shared-memory atomics on 32-bit words run at ~7x the rate of 64-bit ones
-// on GB300): n; Σu as Σ(su >> 12), Σ(su & 0xfff); Σv likewise; Σuv as
-// Σ(hi >> 12), Σ(hi & 0xfff), Σ(lo >> 12), Σ(lo & 0xfff) with
-// uv = hi 2^24 + lo.  Every limb sum stays below 2^26.
-enum { kMomN, kMomUh, kMomUl, kMomVh, kMomVl, kMomHh, kMomHl, kMomLh, kMomLl, kMoms };
+// Per window cell, the deposit moments n, Σu, Σv and Σuv of the particles
+// deposited there (u, v < 2^24; a cell holds at most kMaxCell particles, so
+// Σu, Σv < 2^38 and Σuv < 2^62).  Shared-memory atomics on 64-bit words run at
+// ~1/7 the rate of 32-bit ones on GB300, so each 64-bit sum is kept as two
+// 32-bit words: the low word's atomic returns the old value, from which the
+// carry into the high word is known (for Σu and Σv the high word then moves
+// only on a carry).
+enum { kMomN, kMomUlo, kMomUhi, kMomVlo, kMomVhi, kMomQlo, kMomQhi, kMoms };
 
 struct PushShared {
   float4 e[2 * kWinCells];        // E records of the window cells
   unsigned mom[kMoms][kWinCells];  // deposit moments of the window cells
 };
+
+// adds v (< 2^64) to the two-word sum (lo, hi)
+__device__ __forceinline__ void add64(unsigned *lo, unsigned *hi, unsigned long long v) {
+  const unsigned vl = (unsigned)v, vh = (unsigned)(v >> 32);
+  const unsigned old = atomicAdd(lo, vl);
+  const unsigned h = vh + (old + vl < old ? 1u : 0u);
+  if (h) atomicAdd(hi, h);
+}
+
+// a run of n particles of window cell `key` with moment sums m
+__device__ __forceinline__ void window_add(PushShared &sh, int key, unsigned n, const Moments &m) {
+  atomicAdd(&sh.mom[kMomN][key], n);
+  add64(&sh.mom[kMomUlo][key], &sh.mom[kMomUhi][key], m.su);
+  add64(&sh.mom[kMomVlo][key], &sh.mom[kMomVhi][key], m.sv);
+  add64(&sh.mom[kMomQlo][key], &sh.mom[kMomQhi][key], ((unsigned long long)m.hi << 24) + m.lo);
+}
+
+// CIC node weights of window cell w: W00 at its lower-left node, W10, W01, W11
+__device__ __forceinline__ void window_cell(const PushShared &sh, int w, unsigned long long W[4]) {
+  const unsigned long long n = sh.mom[kMomN][w];
+  const unsigned long long su = ((unsigned long long)sh.mom[kMomUhi][w] << 32) | sh.mom[kMomUlo][w];
+  const unsigned long long sv = ((unsigned long long)sh.mom[kMomVhi][w] << 32) | sh.mom[kMomVlo][w];
+  const unsigned long long UV = ((unsigned long long)sh.mom[kMomQhi][w] << 32) | sh.mom[kMomQlo][w];
+  const unsigned long long U = su << 24, V = sv << 24;
+  W[0] = (n << 48) - U - V + UV;
+  W[1] = U - UV;
+  W[2] = V - UV;
+  W[3] = UV;
+}
 
 // One warp step over the slots base + lane: gather, Boris push, boundary
 // rules and the deposit of the new positions.  Cells inside the block's
@@ -222,15 +252,7 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
   unsigned n;
   if (reduce_runs(key, m, n) && key >= 0) {
     if (WIN && key < kWinCells) {
-      atomicAdd(&sh.mom[kMomN][key], n);
-      atomicAdd(&sh.mom[kMomUh][key], m.su >> 12);
-      atomicAdd(&sh.mom[kMomUl][key], m.su & 0xfffu);
-      atomicAdd(&sh.mom[kMomVh][key], m.sv >> 12);
-      atomicAdd(&sh.mom[kMomVl][key], m.sv & 0xfffu);
-      atomicAdd(&sh.mom[kMomHh][key], m.hi >> 12);
-      atomicAdd(&sh.mom[kMomHl][key], m.hi & 0xfffu);
-      atomicAdd(&sh.mom[kMomLh][key], m.lo >> 12);
-      atomicAdd(&sh.mom[kMomLl][key], m.lo & 0xfffu);
+      window_add(sh, key, n, m);
     } else {
       const unsigned long long U = (unsigned long long)m.su << 24, V = (unsigned long long)m.sv << 24;
       const unsigned long long UV = ((unsigned long long)m.hi << 24) + m.lo;
@@ -317,17 +339,10 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev 
           const int ca = a - (c & 1), cb = b - (c >> 1);  // cell whose corner (c & 1, c >> 1) is this node
           if (ca < 0 || cb < 0 || ca >= kWin || cb >= kWin) continue;
           const int w = ca + kWin * cb;
-          const unsigned long long n = sh.mom[kMomN][w];
-          if (!n) continue;
-          const unsigned long long U = (((unsigned long long)sh.mom[kMomUh][w] << 12) + sh.mom[kMomUl][w]) << 24;
-          const unsigned long long V = (((unsigned long long)sh.mom[kMomVh][w] << 12) + sh.mom[kMomVl][w]) << 24;
-          const unsigned long long UV =
-              ((((unsigned long long)sh.mom[kMomHh][w] << 12) + sh.mom[kMomHl][w]) << 24) +
-              (((unsigned long long)sh.mom[kMomLh][w] << 12) + sh.mom[kMomLl][w]);
-          if (c == 0) v += (n << 48) - U - V + UV;
-          else if (c == 1) v += U - UV;
-          else if (c == 2) v += V - UV;
-          else v += UV;
+          if (!sh.mom[kMomN][w]) continue;
+          unsigned long long W[4];
+          window_cell(sh, w, W);
+          v += W[c];
         }
         if (v) atomicAdd(s.acc + (ox + a) + nx * (oy + b), v);
       }
@@ -809,16 +824,10 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push_runs(const 
       const int ca = a - (c & 1), cb = b - (c >> 1);
       if (ca < 0 || cb < 0 || ca >= cx || cb >= cy) continue;
       const int w = ca + cx * cb;
-      const unsigned long long n = sh.mom[kMomN][w];
-      if (!n) continue;
-      const unsigned long long U = (((unsigned long long)sh.mom[kMomUh][w] << 12) + sh.mom[kMomUl][w]) << 24;
-      const unsigned long long V = (((unsigned long long)sh.mom[kMomVh][w] << 12) + sh.mom[kMomVl][w]) << 24;
-      const unsigned long long UV = ((((unsigned long long)sh.mom[kMomHh][w] << 12) + sh.mom[kMomHl][w]) << 24) +
-                                    (((unsigned long long)sh.mom[kMomLh][w] << 12) + sh.mom[kMomLl][w]);
-      if (c == 0) v += (n << 48) - U - V + UV;
-      else if (c == 1) v += U - UV;
-      else if (c == 2) v += V - UV;
-      else v += UV;
+      if (!sh.mom[kMomN][w]) continue;
+      unsigned long long W[4];
+      window_cell(sh, w, W);
+      v += W[c];
     }
     if (v) atomicAdd(s.acc + a + nx * b, v);
   }

@@ -248,6 +248,8 @@ int mcc_prod(Ctx *c, int mid);
 int mcc_set_index(Ctx *c, int mid);
 int poisson_ndrive(Ctx *c);
 int poisson_upload_fp64(Ctx *c);
+int poisson_sync_x(Ctx *c);
+int poisson_set_precision(Ctx *c, double rtol);
 double poisson_drive_amp(Ctx *c, int g);
 
 // ---- kernels / launchers shared across files ----

@@ -81,6 +81,15 @@ __device__ __forceinline__ bool reduce_runs(int key, Moments &m, unsigned &n) {
 // Move by d cells along one axis in FP32: offset h in [0,1) on the 2^-24 grid,
 // cell index i (int).  Returns the new offset; i is updated in place.
 __device__ __forceinline__ float move_axis(float h, float d, int &i) {
+  const float t0 = h + d;
+  if (t0 >= 0.0f && t0 < 1.0f) {  // stays in its cell: one rounding, then onto the grid
+    int u = __float2int_rn(t0 * kOffScale);
+    if (u >= (1 << 24)) {
+      u -= (1 << 24);
+      i += 1;
+    }
+    return (float)u * kOffInv;
+  }
   d = fminf(fmaxf(d, -1.0e9f), 1.0e9f);
   float fd = floorf(d);
   float fr = d - fd;           // [0,1)

@@ -41,6 +41,7 @@ struct RowClass {
   int fixed;                  // identity row
   int rho;                    // b = -ρ/ε0 (ρ dof) else b = bfix
   float nd32;                 // -d in FP32 (scaling of the FP32 residual)
+  float2 c0f, cWf, cEf, cSf, cNf;  // the coefficients as double-float pairs
 };
 
 struct DriveGroup {
@@ -80,7 +81,11 @@ struct Poisson {
   double *bfix_d = nullptr;     // nn
   double *sigma_d = nullptr;    // nsig
   int nsig = 0;
-  double *x = nullptr;          // ϕ (nn)
+  double *x = nullptr;          // ϕ (nn); for separable operators a view refreshed from xd on demand
+  float2 *xd = nullptr;         // ϕ as double-float pairs (separable operators: the solver's state)
+  float2 *bd = nullptr;         // b of the free rows as double-float pairs (first residual pass)
+  bool df_mode = false;         // the solver's state is xd (double-float), x a view
+  bool x_stale = false;         // (df_mode) x lags xd
   double *r = nullptr, *z = nullptr, *p = nullptr, *ap = nullptr;  // nn
   double *part = nullptr;       // reduction partials (kPartials * 4)
   PoissonScal *scal = nullptr;
@@ -127,6 +132,8 @@ void poisson_destroy(Poisson *p) {
   cudaFree(p->bfix_d);
   cudaFree(p->sigma_d);
   cudaFree(p->x);
+  cudaFree(p->xd);
+  cudaFree(p->bd);
   cudaFree(p->r);
   cudaFree(p->z);
   cudaFree(p->p);
@@ -163,6 +170,42 @@ void poisson_destroy(Poisson *p) {
 constexpr unsigned kFixedBit = 0x8000u;
 constexpr unsigned kClassMask = 0x7fffu;
 
+// ---- double-float arithmetic (a value is hi + lo, two FP32 words, |lo| <=
+// ulp(hi)/2: ~48 significant bits) with the error-free transformations
+// two-sum (Knuth) and two-product by FMA.  GB300 runs FP32 at ~64x its FP64
+// rate; the separable solver keeps ϕ and b in this form.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 df_fast(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  float2 s = df_two_sum(a.x, b.x);
+  s.y += a.y + b.y;
+  return df_fast(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ float2 df_add_f(float2 a, float b) {
+  float2 s = df_two_sum(a.x, b);
+  s.y += a.y;
+  return df_fast(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_from(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_value(float2 a) { return (double)a.x + (double)a.y; }
+
 struct OpView {
   const uint16_t *cls;
   const RowClass *classes;
@@ -187,7 +230,7 @@ __device__ __forceinline__ double drive_value(const double *par, double t) {
 // fixed-row values: Dirichlet / driven
 __global__ void k_set_fixed(OpView op, const int *__restrict__ dnode, const int *__restrict__ dgroup,
                             const double *__restrict__ dpar, int ndn, const unsigned long long *__restrict__ step,
-                            double dt, double *__restrict__ bfix_mut, double *__restrict__ x,
+                            double dt, double *__restrict__ bfix_mut, double *__restrict__ x, float2 *__restrict__ xd,
                             const double *__restrict__ rho, double eps0, int nn) {
   pdl_wait();
   // driven groups update bfix (solve of step n uses V((n-2)Δt), n >= 2)
@@ -199,16 +242,31 @@ __global__ void k_set_fixed(OpView op, const int *__restrict__ dnode, const int 
       bfix_mut[k] = drive_value(dpar + 4 * dgroup[t], tt);
     }
     x[k] = bfix_mut[k];
+    if (xd) xd[k] = df_from(bfix_mut[k]);
   }
 }
 
-__global__ void k_fixed_to_x(OpView op, double *__restrict__ x, const double *__restrict__ rho, double neg_inv_eps0,
-                             int nn) {
+__global__ void k_fixed_to_x(OpView op, double *__restrict__ x, float2 *__restrict__ xd,
+                             const double *__restrict__ rho, double neg_inv_eps0, int nn) {
   pdl_wait();
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const unsigned ck = op.cls[k];
-    if (ck & kFixedBit) x[k] = op.classes[ck & kClassMask].rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+    if (ck & kFixedBit) {
+      const double v = op.classes[ck & kClassMask].rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+      x[k] = v;
+      if (xd) xd[k] = df_from(v);
+    }
   }
+}
+
+// ϕ conversions between the FP64 view and the double-float state
+__global__ void k_df_to_x(const float2 *__restrict__ xd, double *__restrict__ x, int nn) {
+  pdl_wait();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) x[k] = df_value(xd[k]);
+}
+__global__ void k_x_to_df(const double *__restrict__ x, float2 *__restrict__ xd, int nn) {
+  pdl_wait();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) xd[k] = df_from(x[k]);
 }
 
 __device__ __forceinline__ double block_sum(double v, double *sh) {
@@ -430,6 +488,117 @@ __global__ void __launch_bounds__(256) k_residual(OpView op, const double *__res
   finish_norms<FIRST>(sc, part, a2, b2, rtol2, loop, sh, &last);
 }
 
+// E = -∇ϕ from the double-float ϕ: node differences of the pairs in FP32
+// (hi parts of neighbours subtract exactly when within a factor 2)
+__device__ __forceinline__ void efield_at_df(const float2 *__restrict__ x, int k, int i, int j, int nx, int ny,
+                                             const EOut &eo) {
+  auto dif = [&](int a, int b) {
+    const float2 p = x[a], q = x[b];
+    return (p.x - q.x) + (p.y - q.y);
+  };
+  float ex, ey;
+  if (i == 0) ex = dif(k, k + 1) * eo.idx1;
+  else if (i == nx - 1) ex = dif(k - 1, k) * eo.idx1;
+  else ex = dif(k - 1, k + 1) * eo.idx2;
+  if (j == 0) ey = dif(k, k + nx) * eo.idy1;
+  else if (j == ny - 1) ey = dif(k - nx, k) * eo.idy1;
+  else ey = dif(k - nx, k + nx) * eo.idy2;
+  const float2 e = make_float2(ex, ey);
+  eo.E32[k] = e;
+  store_corners(eo.E4, nx, ny, i, j, e);
+}
+
+// Residual pass of the separable solver on the double-float ϕ: the stencil
+// A x is summed in double-float arithmetic (FP32 pipes); the FIRST pass forms
+// b (FP64, then split) for the free rows into bd and the rhs norm, later
+// passes reuse bd.  Scaled FP32 residual to r32, E, convergence test as
+// k_residual (norms in FP64).
+template <bool FIRST>
+__global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__restrict__ x,
+                                                     const double *__restrict__ rho, double neg_inv_eps0,
+                                                     float2 *__restrict__ bd, PoissonScal *sc, float *__restrict__ r32,
+                                                     double *__restrict__ part, int nn, int singular, double rtol2,
+                                                     EOut eo, SweepLoop loop) {
+  pdl_wait();
+  __shared__ double sh[40];
+  __shared__ RowClass cls_sh[kSmemClasses];
+  __shared__ int last;
+  if (!FIRST && sc->done) return;
+  const RowClass *__restrict__ CT = stage_classes(op, cls_sh);
+  const double lam = singular ? sc->lambda : 0.0;
+  const int nx = op.nx, ny = op.ny;
+  double a2 = 0, b2 = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const int j = k / nx, i = k - j * nx;
+    efield_at_df(x, k, i, j, nx, ny, eo);
+    const unsigned ck = op.cls[k];
+    if (ck & kFixedBit) {
+      r32[k] = 0.f;
+      continue;
+    }
+    const RowClass &C = CT[ck];
+    const int w = i > 0 ? k - 1 : k + nx - 1;
+    const int e = i < nx - 1 ? k + 1 : k - nx + 1;
+    const int s = j > 0 ? k - nx : k + nx * (ny - 1);
+    const int n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
+    float2 b;
+    if (FIRST) {
+      double bv = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+      if (singular) bv -= lam;
+      if (C.sig_dof >= 0) bv -= C.sig_coef * op.sigma[C.sig_dof];
+      b = df_from(bv);
+      bd[k] = b;
+    } else {
+      b = bd[k];
+    }
+    float2 res;
+    if (FIRST) {
+      float2 afix = make_float2(0.f, 0.f), afree = df_mul(C.c0f, x[k]);
+      const int nb[4] = {w, e, s, n};
+      const float2 cf[4] = {C.cWf, C.cEf, C.cSf, C.cNf};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float2 t = df_mul(cf[q], x[nb[q]]);
+        if (op.cls[nb[q]] & kFixedBit) afix = df_add(afix, t);
+        else afree = df_add(afree, t);
+      }
+      const float2 rhs = df_add(b, df_neg(afix));
+      res = df_add(rhs, df_neg(afree));
+      const double rh = df_value(rhs);
+      b2 = fma(rh, rh, b2);
+    } else {
+      float2 ax = df_mul(C.c0f, x[k]);
+      ax = df_add(ax, df_mul(C.cWf, x[w]));
+      ax = df_add(ax, df_mul(C.cEf, x[e]));
+      ax = df_add(ax, df_mul(C.cSf, x[s]));
+      ax = df_add(ax, df_mul(C.cNf, x[n]));
+      res = df_add(b, df_neg(ax));
+    }
+    const float resf = res.x + res.y;
+    r32[k] = resf * C.nd32;
+    const double rv = (double)resf;
+    a2 = fma(rv, rv, a2);
+  }
+  finish_norms<FIRST>(sc, part, a2, b2, rtol2, loop, sh, &last);
+}
+
+// mean-zero projection of the double-float ϕ (singular operators)
+__global__ void k_sum_xd(const float2 *__restrict__ x, int nn, double *__restrict__ part) {
+  pdl_wait();
+  __shared__ double sh[40];
+  double v = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) v += df_value(x[k]);
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+__global__ void k_shift_xd(float2 *__restrict__ x, int nn, const double *__restrict__ part, int nparts) {
+  pdl_wait();
+  __shared__ double sh[40];
+  double s = sum_partials(part, nparts, sh);
+  const float2 m = df_neg(df_from(s / nn));
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) x[k] = df_add(x[k], m);
+}
+
 // ---------------- separable correction: FFT(y) x tridiagonal(x), FP32 ----------------
 // One sweep computes δ ≈ S^-1 r in FP32 and adds it to the FP64 ϕ; the FP64
 // residual pass that follows decides convergence (iterative refinement), so
@@ -647,10 +816,11 @@ __global__ void __launch_bounds__(256) k_tridiag_cr(float *__restrict__ spec, in
 }
 
 // spec -> δ (nx, ny) by the inverse of k_fft_fwd; x += δ on free rows
+template <bool DF>
 __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict__ spec, int nx, int N, int logN,
                                                         int TP, const float2 *__restrict__ tw,
-                                                        const uint16_t *__restrict__ cls, double *__restrict__ x,
-                                                        const PoissonScal *__restrict__ sc) {
+                                                        const uint16_t *__restrict__ cls, float2 *__restrict__ xd,
+                                                        double *__restrict__ x64, const PoissonScal *__restrict__ sc) {
   pdl_wait();
   extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
   if (sc->done) return;
@@ -660,7 +830,8 @@ __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict
   for (int t = threadIdx.x; t < (N >> 1); t += blockDim.x) tws[t] = __ldg(tw + t);
   // the update's ϕ values and row classes, fetched before the transform
   constexpr int kPre = 8;
-  double xp[kPre];
+  float2 xp[kPre];
+  double xq[kPre];
   bool freep[kPre];
 #pragma unroll
   for (int u = 0; u < kPre; u++) {
@@ -668,11 +839,15 @@ __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict
     const int j = t / W, c = t - j * W;
     const int i = i0 + c;
     freep[u] = false;
-    xp[u] = 0.0;
+    xp[u] = make_float2(0.f, 0.f);
+    xq[u] = 0.0;
     if (t < W * N && i < nx) {
       const size_t kk = i + (size_t)nx * j;
       freep[u] = !(cls[kk] & kFixedBit);
-      if (freep[u]) xp[u] = x[kk];
+      if (freep[u]) {
+        if (DF) xp[u] = xd[kk];
+        else xq[u] = x64[kk];
+      }
     }
   }
   for (int t = threadIdx.x; t < TP * N; t += blockDim.x) {
@@ -699,7 +874,9 @@ __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict
     const int i = i0 + c;
     if (freep[u]) {
       const float2 z = fbuf[(c >> 1) * S + j];
-      x[i + (size_t)nx * j] = xp[u] + (double)((c & 1 ? z.y : z.x) * invN);
+      const float dz = (c & 1 ? z.y : z.x) * invN;
+      if (DF) xd[i + (size_t)nx * j] = df_add_f(xp[u], dz);
+      else x64[i + (size_t)nx * j] = xq[u] + (double)dz;
     }
   }
   for (int t = threadIdx.x + kPre * blockDim.x; t < W * N; t += blockDim.x) {
@@ -709,7 +886,9 @@ __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict
       const size_t kk = i + (size_t)nx * j;
       if (!(cls[kk] & kFixedBit)) {
         const float2 z = fbuf[(c >> 1) * S + j];
-        x[kk] += (double)((c & 1 ? z.y : z.x) * invN);
+        const float dz = (c & 1 ? z.y : z.x) * invN;
+        if (DF) xd[kk] = df_add_f(xd[kk], dz);
+        else x64[kk] += (double)dz;
       }
     }
   }
@@ -1098,6 +1277,15 @@ static int build_device(Ctx *c, Poisson *P) {
       rc.cN = e.cN;
       rc.d = e.fixed ? 1.0 : d[r];
       rc.nd32 = (float)(-rc.d);
+      auto split = [](double v) {
+        const float h = (float)v;
+        return make_float2(h, (float)(v - (double)h));
+      };
+      rc.c0f = split(e.c0);
+      rc.cWf = split(e.cW);
+      rc.cEf = split(e.cE);
+      rc.cSf = split(e.cS);
+      rc.cNf = split(e.cN);
       rc.sig_coef = e.sig_coef;
       rc.sig_dof = e.sig_dof;
       rc.fixed = e.fixed;
@@ -1161,6 +1349,12 @@ static int build_device(Ctx *c, Poisson *P) {
   }
   if (!P->sigma_d) ISKRA_CUDA(c, cudaMalloc(&P->sigma_d, (nsig > 0 ? nsig : 1) * sizeof(double)));
   if (nsig) ISKRA_CUDA(c, cudaMemcpy(P->sigma_d, P->sig_b.data(), nsig * sizeof(double), cudaMemcpyHostToDevice));
+  if (P->df_mode && P->x_stale) {  // the FP64 view takes over the double-float state before a rebuild
+    k_df_to_x<<<std::max(1, std::min(c->num_sms * 2, (nn + 255) / 256)), 256, 0, c->stream>>>(P->xd, P->x, nn);
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  P->df_mode = false;
+  P->x_stale = false;
   if (!P->x) {
     ISKRA_CUDA(c, cudaMalloc(&P->x, nn * sizeof(double)));
     ISKRA_CUDA(c, cudaMemset(P->x, 0, nn * sizeof(double)));
@@ -1411,6 +1605,8 @@ static int build_device(Ctx *c, Poisson *P) {
   if (sep) {
     int rc = fft_smem_attr(c, P->N);
     if (rc) return rc;
+    if (!P->xd) ISKRA_CUDA(c, cudaMalloc(&P->xd, nn * sizeof(float2)));
+    if (!P->bd) ISKRA_CUDA(c, cudaMalloc(&P->bd, nn * sizeof(float2)));
   }
   P->dirty = false;
   return ISKRA_OK;
@@ -1457,7 +1653,8 @@ static EOut eout(Ctx *c, bool on) {
 // written here, after an operator build or a host update of Dirichlet values.
 static int fixed_to_x_now(Ctx *c) {
   Poisson *P = c->ps;
-  k_fixed_to_x<<<P->blocks, 256, 0, c->stream>>>(opview(P), P->x, c->rho, -1.0 / P->eps0, P->nn);
+  k_fixed_to_x<<<P->blocks, 256, 0, c->stream>>>(opview(P), P->x, P->xd, c->rho,
+                                                  -1.0 / P->eps0, P->nn);
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }
@@ -1498,7 +1695,8 @@ static size_t cr_smem(const Poisson *P, int G) {
 static int fft_smem_attr(Ctx *c, int N) {
   const int smem = (int)fft_smem(N, fft_tp(N, c->ps->nx, c->num_sms));
   ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ISKRA_CUDA(c, cudaFuncSetAttribute(k_fft_inv_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   const int G = cr_modes_per_block(c->ps->nx, c->ps->K, c->num_sms);
   const int crsm = (int)cr_smem(c->ps, G);
   if (G && crsm > 48 * 1024)
@@ -1535,14 +1733,20 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
     ISKRA_CUDA(c, launch_pdl(k_set_fixed, (P->ndrive_nodes + 255) / 256, 256, 0, st, op,
                              (const int *)P->drive_node, (const int *)P->drive_group, (const double *)P->drive_par,
                              P->ndrive_nodes, (const unsigned long long *)c->d_step, dt_for_drive, P->bfix_d, P->x,
-                             (const double *)c->rho, P->eps0, nn));
+                             P->xd, (const double *)c->rho, P->eps0, nn));
   // k_set_fixed wrote the driven rows; ρ-valued identity rows follow ρ
-  if (P->rho_fixed) ISKRA_CUDA(c, launch_pdl(k_fixed_to_x, B, T, 0, st, op, P->x, (const double *)c->rho, nie, nn));
+  if (P->rho_fixed)
+    ISKRA_CUDA(c, launch_pdl(k_fixed_to_x, B, T, 0, st, op, P->x, P->xd,
+                             (const double *)c->rho, nie, nn));
   if (P->singular) {
     ISKRA_CUDA(c, launch_pdl(k_sum_db, B, T, 0, st, op, (const double *)c->rho, nie, nn, P->part));
     ISKRA_CUDA(c, launch_pdl(k_lambda, 1, T, 0, st, (const double *)P->part, B, P->dsum, P->scal));
   }
-  if (P->separable) {
+  if (P->separable && P->df_mode) {
+    ISKRA_CUDA(c, launch_pdl(k_residual_df<true>, B, T, 0, st, op, (const float2 *)P->xd, (const double *)c->rho,
+                             nie, P->bd, P->scal, P->r32, P->part, nn, (int)P->singular, rtol * rtol, eout(c, true),
+                             loop));
+  } else if (P->separable) {
     ISKRA_CUDA(c, launch_pdl(k_residual<true, true>, B, T, 0, st, op, (const double *)P->x, (const double *)c->rho,
                              nie, P->scal, (double *)nullptr, P->r32, P->part, nn, (int)P->singular, rtol * rtol,
                              eout(c, true), loop));
@@ -1585,11 +1789,21 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
                                  (const float *)P->low, (const float *)P->inv, (const float *)P->cp,
                                  (const float *)P->q, (const float *)P->gk, (int)P->cyclic, P->pin_k0, sc));
       }
-      ISKRA_CUDA(c, launch_pdl(k_fft_inv_update, sh.fb, 256, sh.smem, st, (const float2 *)P->spec, P->nx, N,
-                               P->logN, sh.TP, (const float2 *)P->tw, (const uint16_t *)P->cls, P->x, sc));
-      ISKRA_CUDA(c, launch_pdl(k_residual<false, true>, B, T, 0, st, op, (const double *)P->x,
-                               (const double *)c->rho, nie, P->scal, (double *)nullptr, P->r32, P->part, nn,
-                               (int)P->singular, rtol2, eout(c, true), last ? loop : none));
+      if (P->df_mode) {
+        ISKRA_CUDA(c, launch_pdl(k_fft_inv_update<true>, sh.fb, 256, sh.smem, st, (const float2 *)P->spec, P->nx, N,
+                                 P->logN, sh.TP, (const float2 *)P->tw, (const uint16_t *)P->cls, P->xd,
+                                 (double *)nullptr, sc));
+        ISKRA_CUDA(c, launch_pdl(k_residual_df<false>, B, T, 0, st, op, (const float2 *)P->xd,
+                                 (const double *)c->rho, nie, P->bd, P->scal, P->r32, P->part, nn,
+                                 (int)P->singular, rtol2, eout(c, true), last ? loop : none));
+      } else {
+        ISKRA_CUDA(c, launch_pdl(k_fft_inv_update<false>, sh.fb, 256, sh.smem, st, (const float2 *)P->spec, P->nx,
+                                 N, P->logN, sh.TP, (const float2 *)P->tw, (const uint16_t *)P->cls,
+                                 (float2 *)nullptr, P->x, sc));
+        ISKRA_CUDA(c, launch_pdl(k_residual<false, true>, B, T, 0, st, op, (const double *)P->x,
+                                 (const double *)c->rho, nie, P->scal, (double *)nullptr, P->r32, P->part, nn,
+                                 (int)P->singular, rtol2, eout(c, true), last ? loop : none));
+      }
     }
   } else {
     if (reset_cg) k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);  // rhs2 is already in scal
@@ -1613,7 +1827,11 @@ static int graph_sweeps(double rtol) {
 
 static int finish_solve(Ctx *c) {
   Poisson *P = c->ps;
-  if (P->singular) {
+  if (P->singular && P->df_mode) {
+    ISKRA_CUDA(c, launch_pdl(k_sum_xd, P->blocks, 256, 0, c->stream, (const float2 *)P->xd, P->nn, P->part));
+    ISKRA_CUDA(c, launch_pdl(k_shift_xd, P->blocks, 256, 0, c->stream, P->xd, P->nn, (const double *)P->part,
+                             P->blocks));
+  } else if (P->singular) {
     ISKRA_CUDA(c, launch_pdl(k_sum_x, P->blocks, 256, 0, c->stream, (const double *)P->x, P->nn, P->part));
     ISKRA_CUDA(c, launch_pdl(k_shift_x, P->blocks, 256, 0, c->stream, P->x, P->nn, (const double *)P->part,
                              P->blocks));
@@ -1621,6 +1839,7 @@ static int finish_solve(Ctx *c) {
   // the separable path wrote E in its residual passes (the mean shift of the
   // singular case leaves E unchanged); CG computes it here
   c->e_from_phi = true;
+  if (P->df_mode) P->x_stale = true;
   if (P->separable) return ISKRA_OK;
   return launch_efield_from(c, P->x);
 }
@@ -1642,6 +1861,8 @@ int poisson_solve_graph(Ctx *c, double rtol) {
 
 static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres) {
   int rc = poisson_prepare(c);
+  if (rc) return rc;
+  rc = poisson_set_precision(c, rtol);
   if (rc) return rc;
   Poisson *P = c->ps;
   bool first = true;
@@ -1674,6 +1895,46 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
 
 double *poisson_sigma_ptr(Ctx *c) { return c->ps ? c->ps->sigma_d : nullptr; }
 const double *poisson_x_ptr(Ctx *c) { return c->ps ? c->ps->x : nullptr; }
+const float2 *poisson_xd_ptr(Ctx *c) { return c->ps && c->ps->df_mode ? c->ps->xd : nullptr; }
+void poisson_mark_x_stale(Ctx *c) {
+  if (c->ps && c->ps->df_mode) c->ps->x_stale = true;
+}
+
+// FP64 view of ϕ brought up to date with the double-float state (stream-ordered)
+int poisson_sync_x(Ctx *c) {
+  Poisson *P = c->ps;
+  if (!P || !P->df_mode || !P->x_stale) return ISKRA_OK;
+  k_df_to_x<<<P->blocks, 256, 0, c->stream>>>(P->xd, P->x, P->nn);
+  ISKRA_CUDA(c, cudaGetLastError());
+  P->x_stale = false;
+  return ISKRA_OK;
+}
+
+// Precision of the separable solver's state for a tolerance.  Double-float
+// keeps ϕ to ~48 bits; its residual floor (~2^-47 |A||x| / ||rhs||, 5e-13
+// measured at 512^2) is far below 1e-9, so tolerances from 1e-9 up run on
+// the FP32 pipes.  Tighter tolerances and operators with σ dofs (whose rows
+// mix 1/Δx and 1/Δx^2 scales) keep the FP64 state.
+static bool want_df(const Poisson *P, double rtol) { return P->separable && P->nsig == 0 && rtol >= 1e-9; }
+
+// Switches the authoritative state (outside stream capture; stream-ordered).
+int poisson_set_precision(Ctx *c, double rtol) {
+  Poisson *P = c->ps;
+  if (!P) return ISKRA_OK;
+  const bool df = want_df(P, rtol);
+  if (df == P->df_mode) return ISKRA_OK;
+  if (df) {
+    k_x_to_df<<<P->blocks, 256, 0, c->stream>>>(P->x, P->xd, P->nn);
+    P->x_stale = false;
+  } else {
+    if (P->x_stale) k_df_to_x<<<P->blocks, 256, 0, c->stream>>>(P->xd, P->x, P->nn);
+    P->x_stale = false;
+  }
+  ISKRA_CUDA(c, cudaGetLastError());
+  P->df_mode = df;
+  invalidate_graphs(c);
+  return ISKRA_OK;
+}
 bool poisson_separable(Ctx *c) { return c->ps && c->ps->separable; }
 int poisson_solve_blocking(Ctx *c, double rtol, int maxit) { return solve_sync(c, rtol, maxit, nullptr, nullptr); }
 
@@ -2071,6 +2332,8 @@ int iskra_poisson_solve_host(iskra_ctx *h, const double *f, double rtol, int max
   int rc = solve_sync(c, rtol, maxit, iters, relres);
   if (rc && rc != ISKRA_ENOTCONV) return rc;
   if (phi_out) {
+    int rs = poisson_sync_x(c);
+    if (rs) return rs;
     ISKRA_CUDA(c, cudaMemcpyAsync(phi_out, c->ps->x, c->nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   }
@@ -2097,9 +2360,13 @@ int iskra_field_download(iskra_ctx *h, int which, double *out) {
     src = c->rho;
   } else if (which == ISKRA_FIELD_PHI) {
     if (!c->ps || !c->ps->x) return set_err(c, ISKRA_EINVAL, "no potential yet");
+    int rs = poisson_sync_x(c);
+    if (rs) return rs;
     src = c->ps->x;
   } else if (which == ISKRA_FIELD_E) {
     if (c->e_from_phi && c->ps && c->ps->x) {
+      int rs = poisson_sync_x(c);
+      if (rs) return rs;
       int rc = launch_efield64(c, c->ps->x);
       if (rc) return rc;
     }

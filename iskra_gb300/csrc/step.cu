@@ -11,6 +11,8 @@ namespace iskra {
 
 double *poisson_sigma_ptr(Ctx *c);
 const double *poisson_x_ptr(Ctx *c);
+const float2 *poisson_xd_ptr(Ctx *c);
+void poisson_mark_x_stale(Ctx *c);
 bool poisson_separable(Ctx *c);
 int poisson_solve_blocking(Ctx *c, double rtol, int maxit);
 int poisson_solve_graph(Ctx *c, double rtol);
@@ -18,6 +20,7 @@ int poisson_solve_graph(Ctx *c, double rtol);
 struct CircuitArgs {
   CircuitDev *cd;
   const double *phi;
+  const float2 *phid;          // ϕ as double-float pairs (separable solver), else nullptr
   double *sigma;
   int pos_ref, neg_ref;
   int wall;                    // discard wall feeding the floating electrode, -1 none
@@ -34,7 +37,8 @@ __global__ void k_circuit(CircuitArgs A, double dt, unsigned long long *seen) {
   pdl_wait();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   CircuitDev &c = *A.cd;
-  const double vext = A.phi[A.pos_ref] - A.phi[A.neg_ref];
+  auto phi_at = [&](int k) { return A.phid ? (double)A.phid[k].x + (double)A.phid[k].y : A.phi[k]; };
+  const double vext = phi_at(A.pos_ref) - phi_at(A.neg_ref);
   const double i = c.i, q = c.q, t = c.t;
   const double vsrc = c.amp * sin(2.0 * M_PI * c.freq * t) + c.dc;
   double in = (c.L / dt - c.R / 2) * i + vext - vsrc;
@@ -67,6 +71,7 @@ int launch_circuit(Ctx *c, double dt) {
   CircuitArgs A{};
   A.cd = c->cir_d;
   A.phi = poisson_x_ptr(c);
+  A.phid = poisson_xd_ptr(c);
   A.sigma = poisson_sigma_ptr(c);
   A.pos_ref = c->cir_pos_ref;
   A.neg_ref = c->cir_neg_ref;
@@ -274,6 +279,8 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
                                   c->stream));
   }
   c->graph_dt = dt;
+  rc = poisson_set_precision(c, rtol);  // (may invalidate the captured step)
+  if (rc) return rc;
   if (!c->periods_valid || c->periods_dt != dt) {
     rc = update_sort_periods(c, dt);
     if (rc) return rc;
@@ -316,6 +323,7 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
     ISKRA_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
     c->launches += c->graph_kernels;
     c->e_from_phi = true;
+    poisson_mark_x_stale(c);
     c->step++;
     c->d_step_known = c->step;
     for (int s = 0; s < (int)c->species.size(); s++) {

@@ -80,7 +80,7 @@ __device__ __forceinline__ bool reduce_runs(int key, Moments &m, unsigned &n) {
 
 // Move by d cells along one axis in FP32: offset h in [0,1) on the 2^-24 grid,
 // cell index i (int).  Returns the new offset; i is updated in place.
-__device__ __forceinline__ float move_axis(float h, float d, int &i) {
+__device__ __forceinline__ float move_axis(float h, float d, int &i, unsigned &uq) {
   const float t0 = h + d;
   if (t0 >= 0.0f && t0 < 1.0f) {  // stays in its cell: one rounding, then onto the grid
     int u = __float2int_rn(t0 * kOffScale);
@@ -88,6 +88,7 @@ __device__ __forceinline__ float move_axis(float h, float d, int &i) {
       u -= (1 << 24);
       i += 1;
     }
+    uq = (unsigned)u;
     return (float)u * kOffInv;
   }
   d = fminf(fmaxf(d, -1.0e9f), 1.0e9f);
@@ -105,6 +106,7 @@ __device__ __forceinline__ float move_axis(float h, float d, int &i) {
     carry += 1;
   }
   i += (int)fd + carry;
+  uq = (unsigned)u;
   return (float)u * kOffInv;
 }
 
@@ -124,11 +126,24 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
   return 3;
 }
 
-// Minimum resident blocks per SM requested from the register allocator
-// (256-thread blocks); tuned on GB300.
-#ifndef ISKRA_PUSH_MIN_BLOCKS
-#define ISKRA_PUSH_MIN_BLOCKS 5
+// Tile-block size of the push and the minimum resident blocks per SM asked
+// of the register allocator, tuned on GB300: 128-thread blocks, 7 per SM
+// (72 registers) ran the 512x512 slab step 2 % faster than 256 x 5 and
+// 256 x 4, and 192 x 5 8 % slower.  The ensemble push keeps 256 x 5.
+#ifndef ISKRA_PUSH_THREADS
+#define ISKRA_PUSH_THREADS 128
 #endif
+#ifndef ISKRA_PUSH_MIN_BLOCKS
+#define ISKRA_PUSH_MIN_BLOCKS 7
+#endif
+#ifndef ISKRA_PUSH_RUNS_MIN_BLOCKS
+#define ISKRA_PUSH_RUNS_MIN_BLOCKS 5
+#endif
+#ifndef ISKRA_PUSH_DEPTH
+#define ISKRA_PUSH_DEPTH 1
+#endif
+// warp iterations loaded ahead (2, 3 and 4 measured 0.7-5 % slower steps)
+constexpr int kPushDepth = ISKRA_PUSH_DEPTH;
 
 // Shared-memory window of a tile block: the tile's cells and a kHalo-cell
 // margin (particles drift off their tile between sorts).
@@ -186,18 +201,19 @@ __device__ __forceinline__ void window_cell(const PushShared &sh, int w, unsigne
 // global records and 64-bit atomics.  The deposit key is the window cell, or
 // kWinCells + the global cell index, so runs never mix the two.
 template <bool PUSH, int MX, int MY, bool WIN>
-__device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
-                                          long long p, bool valid, float4 a, float2 b,
-                                          const float4 *__restrict__ E4, PushShared &sh, int ox, int oy, int ww,
-                                          int wh, const PushParams &P, unsigned ab[4], int &flags) {
+__device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restrict__ zc, long long p, bool valid,
+                                        float4 a, float2 b, const float4 *__restrict__ E4, const PushShared &sh,
+                                        int ox, int oy, int ww, int wh, const PushParams &P, unsigned ab[4],
+                                        int &flags, Moments &m) {
   const int nx = P.nx;
   int key = -1;
-  Moments m = {0u, 0u, 0u, 0u};
+  m = Moments{0u, 0u, 0u, 0u};
   if (valid) {
     int cell = __float_as_int(b.y);
     if (cell >= 0) {
       int i0 = cell & 0xffff, j0 = cell >> 16;
       float hx = a.x, hy = a.y;
+      unsigned ux, uy;  // offsets on the 2^-24 grid as integers
       if (PUSH) {
         float4 r0, r1;  // the cell's corner fields
         const int la = i0 - ox, lb = j0 - oy;
@@ -224,8 +240,8 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
           flags |= DERR_NAN;
           cell = -1;
         } else {
-          hx = move_axis(hx, vx * P.dtdx, i0);
-          hy = move_axis(hy, vy * P.dtdy, j0);
+          hx = move_axis(hx, vx * P.dtdx, i0, ux);
+          hy = move_axis(hy, vy * P.dtdy, j0, uy);
           int rx = apply_boundary<MX>(i0, nx - 1);
           int ry = rx ? 0 : apply_boundary<MY>(j0, P.ny - 1);
           if (rx == 3 || ry == 3) {
@@ -248,8 +264,10 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
         const int la = i0 - ox, lb = j0 - oy;
         key = (WIN && (unsigned)la < (unsigned)ww && (unsigned)lb < (unsigned)wh) ? la + ww * lb
                                                                                   : kWinCells + i0 + nx * j0;
-        const unsigned ux = __float2uint_rn(hx * kOffScale);
-        const unsigned uy = __float2uint_rn(hy * kOffScale);
+        if (!PUSH) {
+          ux = __float2uint_rn(hx * kOffScale);
+          uy = __float2uint_rn(hy * kOffScale);
+        }
         const unsigned long long uv = (unsigned long long)ux * uy;
         m.su = ux;
         m.sv = uy;
@@ -258,6 +276,12 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
       }
     }
   }
+  return key;
+}
+
+// Warp-collective deposit of one particle per lane (key from push_one).
+template <bool WIN>
+__device__ __forceinline__ void deposit_warp(const SpeciesDev &s, PushShared &sh, int key, Moments m, int nx) {
   unsigned n;
   if (reduce_runs(key, m, n) && key >= 0) {
     if (WIN && key < kWinCells) {
@@ -275,13 +299,23 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
   }
 }
 
+template <bool PUSH, int MX, int MY, bool WIN>
+__device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
+                                          long long p, bool valid, float4 a, float2 b,
+                                          const float4 *__restrict__ E4, PushShared &sh, int ox, int oy, int ww,
+                                          int wh, const PushParams &P, unsigned ab[4], int &flags) {
+  Moments m;
+  const int key = push_one<PUSH, MX, MY, WIN>(xv, zc, p, valid, a, b, E4, sh, ox, oy, ww, wh, P, ab, flags, m);
+  deposit_warp<WIN>(s, sh, key, m, P.nx);
+}
+
 // Blocks [0, ntiles) each take the particles the last sort grouped in their
 // tile: stage the window's E records, push, deposit into the window, then add
 // the window's nonzero node sums and cell counts to the global accumulators.
 // Blocks from ntiles on walk the slots appended since that sort.  Integer
 // sums: the density is the same bit for bit whichever block adds what.
 template <bool PUSH, int MX, int MY>
-__global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev s, const float4 *__restrict__ E4,
+__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev s, const float4 *__restrict__ E4,
                                                                      PushParams P, int ntiles, int *err) {
   pdl_wait();
   __shared__ PushShared sh;
@@ -316,27 +350,35 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev 
       const long long len = end - begin;
       const long long slice = ((len + nwb * 32 - 1) / (nwb * 32)) * 32;
       const long long w0 = begin + wib * slice, w1 = min(end, w0 + slice);
-      // the next slot's record is loaded while this one is processed
-      bool v = w0 + lane < w1;
-      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-      float2 b = make_float2(0.f, 0.f);
-      if (v) {
-        a = __ldcs(xv + w0 + lane);
-        b = __ldcs(zc + w0 + lane);
+      // the records of the next kPushDepth slots are in flight while one is
+      // processed (the deposit lengthens an iteration; the loads must not wait)
+      float4 qa[kPushDepth];
+      float2 qb[kPushDepth];
+#pragma unroll
+      for (int k = 0; k < kPushDepth; k++) {
+        const long long q = w0 + 32 * k + lane;
+        qa[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        qb[k] = make_float2(0.f, 0.f);
+        if (q < w1) {
+          qa[k] = __ldcs(xv + q);
+          qb[k] = __ldcs(zc + q);
+        }
       }
       for (long long base = w0; base < w1; base += 32) {
-        const long long nb = base + 32;
-        const bool nv = nb + lane < w1;
-        float4 a2 = a;
-        float2 b2 = b;
-        if (nv) {
-          a2 = __ldcs(xv + nb + lane);
-          b2 = __ldcs(zc + nb + lane);
+        const float4 a = qa[0];
+        const float2 b = qb[0];
+#pragma unroll
+        for (int k = 0; k + 1 < kPushDepth; k++) {
+          qa[k] = qa[k + 1];
+          qb[k] = qb[k + 1];
         }
-        push_warp<PUSH, MX, MY, true>(s, xv, zc, base + lane, v, a, b, E4, sh, ox, oy, kWin, kWin, P, ab, flags);
-        a = a2;
-        b = b2;
-        v = nv;
+        const long long q = base + 32 * kPushDepth + lane;
+        if (q < w1) {
+          qa[kPushDepth - 1] = __ldcs(xv + q);
+          qb[kPushDepth - 1] = __ldcs(zc + q);
+        }
+        push_warp<PUSH, MX, MY, true>(s, xv, zc, base + lane, base + lane < w1, a, b, E4, sh, ox, oy, kWin, kWin,
+                                      P, ab, flags);
       }
       __syncthreads();
       // node sums from the moments of the up to four window cells around each node
@@ -388,7 +430,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev 
 }
 
 static cudaError_t launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
-  const int T = 256;
+  const int T = ISKRA_PUSH_THREADS;
 #define ISKRA_PUSH_CASE(MX, MY)                                                                 \
   if (P.mode_x == MX && P.mode_y == MY) {                                                       \
     cudaFuncSetAttribute(k_push<true, MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,  \
@@ -449,7 +491,7 @@ int launch_deposit(Ctx *c, int sid) {
   P.tiles_x = c->tiles_x;
   cudaFuncSetAttribute(k_push<false, 0, 0>, cudaFuncAttributePreferredSharedMemoryCarveout,
                        (int)cudaSharedmemCarveoutMaxShared);
-  k_push<false, 0, 0><<<push_blocks(c), 256, 0, c->stream>>>(s.dev, c->E4, P, c->ntiles, c->d_err);
+  k_push<false, 0, 0><<<push_blocks(c), ISKRA_PUSH_THREADS, 0, c->stream>>>(s.dev, c->E4, P, c->ntiles, c->d_err);
   ISKRA_CUDA(c, cudaGetLastError());
   s.acc_valid = true;
   s.acc_zero = false;
@@ -785,7 +827,7 @@ int launch_sort(Ctx *c, int sid) {
 // node sums to the run's accumulator.
 // ---------------------------------------------------------------------------
 template <int MX, int MY>
-__global__ void __launch_bounds__(256, ISKRA_PUSH_MIN_BLOCKS) k_push_runs(const SpeciesDev *__restrict__ runs,
+__global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(const SpeciesDev *__restrict__ runs,
                                                                           const float4 *__restrict__ E4, int ncell4,
                                                                           PushParams P, int *err) {
   pdl_wait();

@@ -58,15 +58,16 @@ __device__ __forceinline__ bool reduce_runs(int key, Moments &m, unsigned &n) {
   const int start = 31 - __clz(heads & ((2u << lane) - 1u));  // first lane of my run
   if (heads != FULL) {  // warp-uniform: some run is longer than one lane
     // rounds up to the longest run only (d < its length)
-    const int pos = lane - start;
+    const unsigned pos = (unsigned)(lane - start);
+    const unsigned last = __reduce_max_sync(FULL, pos);
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      if (!__any_sync(FULL, pos >= d)) break;
+    for (unsigned d = 1; d < 32; d <<= 1) {
+      if (d > last) break;
       const unsigned su = __shfl_up_sync(FULL, m.su, d);
       const unsigned sv = __shfl_up_sync(FULL, m.sv, d);
       const unsigned hi = __shfl_up_sync(FULL, m.hi, d);
       const unsigned lo = __shfl_up_sync(FULL, m.lo, d);
-      if (lane - d >= start) {
+      if (pos >= d) {
         m.su += su;
         m.sv += sv;
         m.hi += hi;
@@ -152,17 +153,24 @@ constexpr int kWinN = kWin + 1;          // window nodes per axis
 constexpr int kWinCells = kWin * kWin;
 
 // Per window cell, the deposit moments n, Σu, Σv and Σuv of the particles
-// deposited there (u, v < 2^24; a cell holds at most kMaxCell particles, so
-// Σu, Σv < 2^38 and Σuv < 2^62).  Shared-memory atomics on 64-bit words run at
-// ~1/7 the rate of 32-bit ones on GB300, so each 64-bit sum is kept as two
-// 32-bit words: the low word's atomic returns the old value, from which the
-// carry into the high word is known (for Σu and Σv the high word then moves
-// only on a carry).
-enum { kMomN, kMomUlo, kMomUhi, kMomVlo, kMomVhi, kMomQlo, kMomQhi, kMoms };
+// deposited there (u, v < 2^24; uv = hi 2^24 + lo).  While a cell has taken
+// at most kWinFast particles every sum fits one 32-bit word (256 (2^24 - 1) <
+// 2^32), so a run costs one returning atomic (the count, which decides) and
+// four fire-and-forget ones.  Runs past that bound add to two-word sums: the
+// low word's atomic returns the old value, from which the carry into the high
+// word is known (64-bit shared-memory atomics run at ~1/7 the rate of 32-bit
+// ones on GB300).  A cell holds at most kMaxCell particles, so Σu, Σv < 2^38
+// and Σuv < 2^62.
+enum {
+  kMomN, kMomU, kMomV, kMomQh, kMomQl,                       // one-word sums
+  kMomUlo, kMomUhi, kMomVlo, kMomVhi, kMomQlo, kMomQhi, kMoms  // two-word sums
+};
+constexpr unsigned kWinFast = 256;
 
 struct PushShared {
   float4 e[2 * kWinCells];        // E records of the window cells
   unsigned mom[kMoms][kWinCells];  // deposit moments of the window cells
+  unsigned over;                   // some run went to the two-word sums
 };
 
 // adds v (< 2^64) to the two-word sum (lo, hi)
@@ -175,19 +183,40 @@ __device__ __forceinline__ void add64(unsigned *lo, unsigned *hi, unsigned long 
 
 // a run of n particles of window cell `key` with moment sums m
 __device__ __forceinline__ void window_add(PushShared &sh, int key, unsigned n, const Moments &m) {
-  atomicAdd(&sh.mom[kMomN][key], n);
-  add64(&sh.mom[kMomUlo][key], &sh.mom[kMomUhi][key], m.su);
-  add64(&sh.mom[kMomVlo][key], &sh.mom[kMomVhi][key], m.sv);
-  add64(&sh.mom[kMomQlo][key], &sh.mom[kMomQhi][key], ((unsigned long long)m.hi << 24) + m.lo);
+  const unsigned old = atomicAdd(&sh.mom[kMomN][key], n);
+  if (old + n <= kWinFast) {
+    atomicAdd(&sh.mom[kMomU][key], m.su);
+    atomicAdd(&sh.mom[kMomV][key], m.sv);
+    atomicAdd(&sh.mom[kMomQh][key], m.hi);
+    atomicAdd(&sh.mom[kMomQl][key], m.lo);
+  } else {
+    sh.over = 1u;
+    add64(&sh.mom[kMomUlo][key], &sh.mom[kMomUhi][key], m.su);
+    add64(&sh.mom[kMomVlo][key], &sh.mom[kMomVhi][key], m.sv);
+    add64(&sh.mom[kMomQlo][key], &sh.mom[kMomQhi][key], ((unsigned long long)m.hi << 24) + m.lo);
+  }
 }
 
-// CIC node weights of window cell w: W00 at its lower-left node, W10, W01, W11
-__device__ __forceinline__ void window_cell(const PushShared &sh, int w, unsigned long long W[4]) {
-  const unsigned long long n = sh.mom[kMomN][w];
-  const unsigned long long su = ((unsigned long long)sh.mom[kMomUhi][w] << 32) | sh.mom[kMomUlo][w];
-  const unsigned long long sv = ((unsigned long long)sh.mom[kMomVhi][w] << 32) | sh.mom[kMomVlo][w];
-  const unsigned long long UV = ((unsigned long long)sh.mom[kMomQhi][w] << 32) | sh.mom[kMomQlo][w];
-  const unsigned long long U = su << 24, V = sv << 24;
+// zeroes the window's moments (threads of the block, before its barrier)
+__device__ __forceinline__ void window_clear(PushShared &sh, int t) {
+#pragma unroll
+  for (int q = 0; q < kMoms; q++) sh.mom[q][t] = 0u;
+  if (t == 0) sh.over = 0u;
+}
+
+// CIC node weights of window cell w: W00 at its lower-left node, W10, W01,
+// W11 (over: some run of the block used the two-word sums; block-uniform)
+__device__ __forceinline__ void window_cell(const PushShared &sh, int w, bool over, unsigned long long W[4]) {
+  typedef unsigned long long u64;
+  const u64 n = sh.mom[kMomN][w];
+  u64 su = sh.mom[kMomU][w], sv = sh.mom[kMomV][w];
+  u64 UV = ((u64)sh.mom[kMomQh][w] << 24) + sh.mom[kMomQl][w];
+  if (over) {
+    su += ((u64)sh.mom[kMomUhi][w] << 32) | sh.mom[kMomUlo][w];
+    sv += ((u64)sh.mom[kMomVhi][w] << 32) | sh.mom[kMomVlo][w];
+    UV += ((u64)sh.mom[kMomQhi][w] << 32) | sh.mom[kMomQlo][w];
+  }
+  const u64 U = su << 24, V = sv << 24;
   W[0] = (n << 48) - U - V + UV;
   W[1] = U - UV;
   W[2] = V - UV;
@@ -341,8 +370,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
             sh.e[2 * t + 1] = __ldg(E4 + 2 * n0 + 1);
           }
         }
-#pragma unroll
-        for (int q = 0; q < kMoms; q++) sh.mom[q][t] = 0u;
+        window_clear(sh, t);
       }
       __syncthreads();
       // each warp takes a contiguous slice of the tile's slots (cell-sorted
@@ -382,6 +410,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
       }
       __syncthreads();
       // node sums from the moments of the up to four window cells around each node
+      const bool over = sh.over != 0u;
       for (int t = threadIdx.x; t < kWinN * kWinN; t += blockDim.x) {
         const int a = t % kWinN, b = t / kWinN;
         unsigned long long v = 0;
@@ -392,7 +421,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
           const int w = ca + kWin * cb;
           if (!sh.mom[kMomN][w]) continue;
           unsigned long long W[4];
-          window_cell(sh, w, W);
+          window_cell(sh, w, over, W);
           v += W[c];
         }
         if (v) atomicAdd(s.acc + (ox + a) + nx * (oy + b), v);
@@ -843,8 +872,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
     const int n0 = i + nx * j;
     sh.e[2 * t] = __ldg(E4 + 2 * n0);
     sh.e[2 * t + 1] = __ldg(E4 + 2 * n0 + 1);
-#pragma unroll
-    for (int q = 0; q < kMoms; q++) sh.mom[q][t] = 0u;
+    window_clear(sh, t);
   }
   __syncthreads();
   const long long np = s.st->np;
@@ -867,6 +895,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   }
   __syncthreads();
   const int wn = cx + 1;
+  const bool over = sh.over != 0u;
   for (int t = threadIdx.x; t < (cx + 1) * (cy + 1); t += blockDim.x) {
     const int a = t % wn, b = t / wn;
     unsigned long long v = 0;
@@ -877,7 +906,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
       const int w = ca + cx * cb;
       if (!sh.mom[kMomN][w]) continue;
       unsigned long long W[4];
-      window_cell(sh, w, W);
+      window_cell(sh, w, over, W);
       v += W[c];
     }
     if (v) atomicAdd(s.acc + a + nx * b, v);

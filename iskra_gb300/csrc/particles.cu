@@ -34,6 +34,22 @@ struct PushParams {
   int tiles_x;      // tiles per row
 };
 
+// Particle-record loads of the push: read once, so they bypass L1
+// (L1::no_allocate measured 1.5 % faster steps than evict-first loads; the
+// shared-memory window leaves ~28 KB of L1 per SM).
+__device__ __forceinline__ float4 ld_stream(const float4 *p) {
+  float4 r;
+  asm volatile("ld.global.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+               : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float2 ld_stream(const float2 *p) {
+  float2 r;
+  asm volatile("ld.global.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(r.x), "=f"(r.y) : "l"(p));
+  return r;
+}
+
 // Moments of one particle: u, v < 2^24 and uv = hi 2^24 + lo with hi, lo < 2^24,
 // so every sum over at most 32 lanes fits in 32 bits.
 struct Moments {
@@ -388,8 +404,8 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
         qa[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         qb[k] = make_float2(0.f, 0.f);
         if (q < w1) {
-          qa[k] = __ldcs(xv + q);
-          qb[k] = __ldcs(zc + q);
+          qa[k] = ld_stream(xv + q);
+          qb[k] = ld_stream(zc + q);
         }
       }
       for (long long base = w0; base < w1; base += 32) {
@@ -402,8 +418,8 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
         }
         const long long q = base + 32 * kPushDepth + lane;
         if (q < w1) {
-          qa[kPushDepth - 1] = __ldcs(xv + q);
-          qb[kPushDepth - 1] = __ldcs(zc + q);
+          qa[kPushDepth - 1] = ld_stream(xv + q);
+          qb[kPushDepth - 1] = ld_stream(zc + q);
         }
         push_warp<PUSH, MX, MY, true>(s, xv, zc, base + lane, base + lane < w1, a, b, E4, sh, ox, oy, kWin, kWin,
                                       P, ab, flags);
@@ -441,8 +457,8 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
       float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
       float2 b = make_float2(0.f, 0.f);
       if (v) {
-        a = __ldcs(xv + p);
-        b = __ldcs(zc + p);
+        a = ld_stream(xv + p);
+        b = ld_stream(zc + p);
       }
       push_warp<PUSH, MX, MY, false>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, 0, 0, P, ab, flags);
     }
@@ -888,8 +904,8 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
     float2 b = make_float2(0.f, 0.f);
     if (v) {
-      a = __ldcs(xv + p);
-      b = __ldcs(zc + p);
+      a = ld_stream(xv + p);
+      b = ld_stream(zc + p);
     }
     push_warp<true, MX, MY, true>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, cx, cy, P, ab, flags);
   }

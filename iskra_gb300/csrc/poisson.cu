@@ -59,6 +59,7 @@ struct PoissonScal {           // device-resident solver scalars
   unsigned ticket;             // blocks of the running k_residual that have finished
   double rz, rz_new, pap;
   int hist;                    // xh holds the previous step solve's ϕ (warm start)
+  int e_pending;               // the first residual pass met rtol but wrote no E
   unsigned hticket;            // blocks of the running k_extrapolate that have finished
 };
 
@@ -491,6 +492,7 @@ __device__ __forceinline__ void finish_norms(PoissonScal *sc, double *__restrict
     sc->relres = rhs2 > 0 ? sqrt(a / rhs2) : sqrt(a);
     const int done = (rhs2 > 0 && a <= rtol2 * rhs2) || a == 0.0;
     sc->done = done;
+    if (FIRST) sc->e_pending = done;
     if (loop.notconv && !done) atomicOr(loop.notconv, DERR_NOTCONV);
   }
 }
@@ -530,21 +532,19 @@ __global__ void __launch_bounds__(256) k_residual(OpView op, const double *__res
   finish_norms<FIRST>(sc, part, a2, b2, rtol2, loop, sh, &last);
 }
 
-// E = -∇ϕ from the double-float ϕ: node differences of the pairs in FP32
-// (hi parts of neighbours subtract exactly when within a factor 2)
-__device__ __forceinline__ void efield_at_df(const float2 *__restrict__ x, int k, int i, int j, int nx, int ny,
-                                             const EOut &eo) {
-  auto dif = [&](int a, int b) {
-    const float2 p = x[a], q = x[b];
-    return (p.x - q.x) + (p.y - q.y);
-  };
+// E = -∇ϕ at node k from ϕ at the node and its four stencil neighbours
+// (double-float pairs, differenced in FP32: the hi parts of neighbours
+// subtract exactly when within a factor 2; one-sided at the walls as efield_at)
+__device__ __forceinline__ void efield_df5(float2 xk, float2 xw, float2 xe, float2 xs, float2 xn, int k, int i, int j,
+                                           int nx, int ny, const EOut &eo) {
+  auto dif = [](float2 p, float2 q) { return (p.x - q.x) + (p.y - q.y); };
   float ex, ey;
-  if (i == 0) ex = dif(k, k + 1) * eo.idx1;
-  else if (i == nx - 1) ex = dif(k - 1, k) * eo.idx1;
-  else ex = dif(k - 1, k + 1) * eo.idx2;
-  if (j == 0) ey = dif(k, k + nx) * eo.idy1;
-  else if (j == ny - 1) ey = dif(k - nx, k) * eo.idy1;
-  else ey = dif(k - nx, k + nx) * eo.idy2;
+  if (i == 0) ex = dif(xk, xe) * eo.idx1;
+  else if (i == nx - 1) ex = dif(xw, xk) * eo.idx1;
+  else ex = dif(xw, xe) * eo.idx2;
+  if (j == 0) ey = dif(xk, xn) * eo.idy1;
+  else if (j == ny - 1) ey = dif(xs, xk) * eo.idy1;
+  else ey = dif(xs, xn) * eo.idy2;
   const float2 e = make_float2(ex, ey);
   eo.E32[k] = e;
   store_corners(eo.E4, nx, ny, i, j, e);
@@ -553,9 +553,13 @@ __device__ __forceinline__ void efield_at_df(const float2 *__restrict__ x, int k
 // Residual pass of the separable solver on the double-float ϕ: the stencil
 // A x is summed in double-float arithmetic (FP32 pipes); the FIRST pass forms
 // b (FP64, then split) for the free rows into bd and the rhs norm, later
-// passes reuse bd.  Scaled FP32 residual to r32, E, convergence test as
-// k_residual (norms in FP64).
-template <bool FIRST>
+// passes reuse bd.  Scaled FP32 residual to r32, E (EOUT), convergence test
+// as k_residual (norms in FP64).  A node's loads (its row class, ϕ at the
+// five stencil nodes, b) are all issued before its branch on the row class:
+// the pass is bound by memory latency, not bandwidth.  In a step graph the
+// FIRST pass writes no E (a correction nearly always follows); when it meets
+// rtol already, the next pass, otherwise skipped, writes E instead.
+template <bool FIRST, bool EOUT>
 __global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__restrict__ x,
                                                      const double *__restrict__ rho, double neg_inv_eps0,
                                                      float2 *__restrict__ bd, PoissonScal *sc, float *__restrict__ r32,
@@ -565,55 +569,72 @@ __global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__
   __shared__ double sh[40];
   __shared__ RowClass cls_sh[kSmemClasses];
   __shared__ int last;
-  if (!FIRST && sc->done) return;
+  const int nx = op.nx, ny = op.ny;
+  if (!FIRST && sc->done) {
+    if (!EOUT || !sc->e_pending) return;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+      const int j = k / nx, i = k - j * nx;
+      const int w = i > 0 ? k - 1 : k + nx - 1, e = i < nx - 1 ? k + 1 : k - nx + 1;
+      const int s = j > 0 ? k - nx : k + nx * (ny - 1), n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
+      efield_df5(x[k], x[w], x[e], x[s], x[n], k, i, j, nx, ny, eo);
+    }
+    return;
+  }
   const RowClass *__restrict__ CT = stage_classes(op, cls_sh);
   const double lam = singular ? sc->lambda : 0.0;
-  const int nx = op.nx, ny = op.ny;
   double a2 = 0, b2 = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const int j = k / nx, i = k - j * nx;
-    efield_at_df(x, k, i, j, nx, ny, eo);
+    const int w = i > 0 ? k - 1 : k + nx - 1;
+    const int e = i < nx - 1 ? k + 1 : k - nx + 1;
+    const int s = j > 0 ? k - nx : k + nx * (ny - 1);
+    const int n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
     const unsigned ck = op.cls[k];
+    const float2 xk = x[k], xw = x[w], xe = x[e], xs = x[s], xn = x[n];
+    double rk = 0.0, fk = 0.0;
+    unsigned cw = 0, ce = 0, cs = 0, cn = 0;
+    float2 b = make_float2(0.f, 0.f);
+    if (FIRST) {
+      rk = rho[k];
+      fk = op.bfix[k];
+      cw = op.cls[w];
+      ce = op.cls[e];
+      cs = op.cls[s];
+      cn = op.cls[n];
+    } else {
+      b = bd[k];
+    }
+    if (EOUT) efield_df5(xk, xw, xe, xs, xn, k, i, j, nx, ny, eo);
     if (ck & kFixedBit) {
       r32[k] = 0.f;
       continue;
     }
     const RowClass &C = CT[ck];
-    const int w = i > 0 ? k - 1 : k + nx - 1;
-    const int e = i < nx - 1 ? k + 1 : k - nx + 1;
-    const int s = j > 0 ? k - nx : k + nx * (ny - 1);
-    const int n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
-    float2 b;
+    float2 res;
     if (FIRST) {
-      double bv = C.rho ? rho[k] * neg_inv_eps0 : op.bfix[k];
+      double bv = C.rho ? rk * neg_inv_eps0 : fk;
       if (singular) bv -= lam;
       if (C.sig_dof >= 0) bv -= C.sig_coef * op.sigma[C.sig_dof];
       b = df_from(bv);
       bd[k] = b;
-    } else {
-      b = bd[k];
-    }
-    float2 res;
-    if (FIRST) {
-      float2 afix = make_float2(0.f, 0.f), afree = df_mul(C.c0f, x[k]);
-      const int nb[4] = {w, e, s, n};
-      const float2 cf[4] = {C.cWf, C.cEf, C.cSf, C.cNf};
+      float2 afix = make_float2(0.f, 0.f), afree = df_mul(C.c0f, xk);
+      const float2 t[4] = {df_mul(C.cWf, xw), df_mul(C.cEf, xe), df_mul(C.cSf, xs), df_mul(C.cNf, xn)};
+      const unsigned cq[4] = {cw, ce, cs, cn};
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        const float2 t = df_mul(cf[q], x[nb[q]]);
-        if (op.cls[nb[q]] & kFixedBit) afix = df_add(afix, t);
-        else afree = df_add(afree, t);
+        if (cq[q] & kFixedBit) afix = df_add(afix, t[q]);
+        else afree = df_add(afree, t[q]);
       }
       const float2 rhs = df_add(b, df_neg(afix));
       res = df_add(rhs, df_neg(afree));
       const double rh = df_value(rhs);
       b2 = fma(rh, rh, b2);
     } else {
-      float2 ax = df_mul(C.c0f, x[k]);
-      ax = df_add(ax, df_mul(C.cWf, x[w]));
-      ax = df_add(ax, df_mul(C.cEf, x[e]));
-      ax = df_add(ax, df_mul(C.cSf, x[s]));
-      ax = df_add(ax, df_mul(C.cNf, x[n]));
+      float2 ax = df_mul(C.c0f, xk);
+      ax = df_add(ax, df_mul(C.cWf, xw));
+      ax = df_add(ax, df_mul(C.cEf, xe));
+      ax = df_add(ax, df_mul(C.cSf, xs));
+      ax = df_add(ax, df_mul(C.cNf, xn));
       res = df_add(b, df_neg(ax));
     }
     const float resf = res.x + res.y;
@@ -1796,9 +1817,15 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
     ISKRA_CUDA(c, launch_pdl(k_lambda, 1, T, 0, st, (const double *)P->part, B, P->dsum, P->scal));
   }
   if (P->separable && P->df_mode) {
-    ISKRA_CUDA(c, launch_pdl(k_residual_df<true>, B, T, 0, st, op, (const float2 *)P->xd, (const double *)c->rho,
-                             nie, P->bd, P->scal, P->r32, P->part, nn, (int)P->singular, rtol * rtol, eout(c, true),
-                             loop));
+    // (step graphs: E comes from the following pass)
+    if (warm)
+      ISKRA_CUDA(c, launch_pdl(k_residual_df<true, false>, B, T, 0, st, op, (const float2 *)P->xd,
+                               (const double *)c->rho, nie, P->bd, P->scal, P->r32, P->part, nn, (int)P->singular,
+                               rtol * rtol, eout(c, false), loop));
+    else
+      ISKRA_CUDA(c, launch_pdl(k_residual_df<true, true>, B, T, 0, st, op, (const float2 *)P->xd,
+                               (const double *)c->rho, nie, P->bd, P->scal, P->r32, P->part, nn, (int)P->singular,
+                               rtol * rtol, eout(c, true), loop));
   } else if (P->separable) {
     ISKRA_CUDA(c, launch_pdl(k_residual<true, true>, B, T, 0, st, op, (const double *)P->x, (const double *)c->rho,
                              nie, P->scal, (double *)nullptr, P->r32, P->part, nn, (int)P->singular, rtol * rtol,
@@ -1846,7 +1873,7 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
         ISKRA_CUDA(c, launch_pdl(k_fft_inv_update<true>, sh.fb, 256, sh.smem, st, (const float2 *)P->spec, P->nx, N,
                                  P->logN, sh.TP, (const float2 *)P->tw, (const uint16_t *)P->cls, P->xd,
                                  (double *)nullptr, sc));
-        ISKRA_CUDA(c, launch_pdl(k_residual_df<false>, B, T, 0, st, op, (const float2 *)P->xd,
+        ISKRA_CUDA(c, launch_pdl(k_residual_df<false, true>, B, T, 0, st, op, (const float2 *)P->xd,
                                  (const double *)c->rho, nie, P->bd, P->scal, P->r32, P->part, nn,
                                  (int)P->singular, rtol2, eout(c, true), last ? loop : none));
       } else {

@@ -172,6 +172,10 @@ int iskra_poisson_solve(iskra_ctx *ctx, double rtol, int maxit, int *iters,
 int iskra_poisson_solve_host(iskra_ctx *ctx, const double *f, double rtol,
                              int maxit, double *phi_out, int *iters,
                              double *relres);
+/* Initial guess of the solves inside iskra_step: 0 = the previous step's ϕ,
+ * 1 = ϕ extrapolated linearly from the last two steps, 2 ϕ_n - ϕ_(n-1)
+ * (default; either way the solve iterates to the same tolerance). */
+int iskra_poisson_set_warm_start(iskra_ctx *ctx, int mode);
 /* Solver method: 0 = automatic (the exact FFT(y)/tridiagonal(x) solve when
  * the assembled operator is separable, else CG), 1 = CG with Jacobi scaling
  * only.  Returns the method in effect through *active when non-NULL. */
@@ -290,6 +294,50 @@ int iskra_ens_field(iskra_ens *ens, int run, int which, double *out);
 /* steps between compactions of discarded particles (0 = only on count /
  * download) */
 int iskra_ens_set_compact_every(iskra_ens *ens, int every);
+
+/* ---- learned warm start of CG solves (config C5) ------------------------
+ * A 4-level convolutional encoder-decoder (32 channels, BF16 weights and
+ * activations, FP32 accumulation) predicts, from the first residual of a CG
+ * Poisson solve, the correction the solve will make; "use" mode adds it to ϕ
+ * before CG starts, scaled by an exact line search in CG's energy norm (so
+ * the CG error never grows; CG still iterates to the requested tolerance,
+ * so only the iteration count changes).  No reference counterpart: this replaces
+ * nothing in generalized_poisson.jl, it accelerates the CG fallback of
+ * iskra_poisson_solve / iskra_step for non-separable operators (and for
+ * iskra_poisson_set_method(ctx, 1, ...)).  nx and ny must be multiples of 8.
+ * The network is trained on the GPU on (residual, correction) pairs the
+ * simulation's own CG solves record in "harvest" mode. */
+/* network with He-initialised weights (seeded) and a ring of `capacity`
+ * harvested pairs (0: inference only) */
+int iskra_lws_create(iskra_ctx *ctx, int capacity, uint64_t seed);
+int iskra_lws_destroy(iskra_ctx *ctx);
+/* harvest: record the pair of every CG solve; use: warm-start CG solves;
+ * smooth: binomial [1 2 1]^2/16 passes over the prediction before it is
+ * applied (its value to CG is in the smooth, slowly converging modes) */
+int iskra_lws_set_mode(iskra_ctx *ctx, int harvest, int use, int smooth);
+/* harvested pairs, parameter count, CG solves seen, solves warm-started,
+ * the mean line-search step of those warm starts (1 = the network's
+ * correction taken as predicted) and their mean residual ratio (norm after
+ * the warm start / before it) */
+int iskra_lws_info(iskra_ctx *ctx, int *pairs, int *nparams, int64_t *solves,
+                   int64_t *warm_solves, double *mean_alpha,
+                   double *mean_ratio);
+/* mean training loss of the network over the harvested pairs (the energy
+ * norm e.Se / P of the error e of the predicted correction under the
+ * 5-point stencil S, the norm CG minimises), and the same loss of the zero
+ * predictor */
+int iskra_lws_eval(iskra_ctx *ctx, double *loss, double *zero_loss);
+/* FP32 master weights (nparams): read into w_out and/or replace by w_in */
+int iskra_lws_weights(iskra_ctx *ctx, float *w_out, const float *w_in);
+/* one network pass on a host image in[ny][nx] (x fastest) -> out[ny][nx] */
+int iskra_lws_forward(iskra_ctx *ctx, const float *in, float *out);
+/* mean squared error against target[ny][nx] and its gradient (nparams) */
+int iskra_lws_loss_grad(iskra_ctx *ctx, const float *in, const float *target,
+                        double *loss, float *grad);
+/* iters Adam steps (learning rate lr) on the harvested pairs, one pair per
+ * step drawn with `seed`; *loss = mean loss of the last min(iters, 64) */
+int iskra_lws_train(iskra_ctx *ctx, int iters, double lr, uint64_t seed,
+                    double *loss);
 
 #ifdef __cplusplus
 }

@@ -39,6 +39,7 @@ u32p = POINTER(c_uint32)
 i64p = POINTER(c_int64)
 ip = POINTER(c_int)
 i32p = POINTER(c_int32)
+f32p = POINTER(ctypes.c_float)
 CTX = c_void_p
 
 # (name, restype, argtypes) of every exported entry point, in header order
@@ -71,6 +72,7 @@ SIGNATURES = [
     ("iskra_poisson_drive_dirichlet", c_int, [CTX, u8p, c_double, c_double, c_double, c_double]),
     ("iskra_poisson_solve", c_int, [CTX, c_double, c_int, ip, dp]),
     ("iskra_poisson_solve_host", c_int, [CTX, dp, c_double, c_int, dp, ip, dp]),
+    ("iskra_poisson_set_warm_start", c_int, [CTX, c_int]),
     ("iskra_poisson_set_method", c_int, [CTX, c_int, ip]),
     ("iskra_mcc_create", c_int, [CTX, c_int, c_int, ip, dp, i32p, dp, dp, c_double, c_double, c_double, dp, c_int,
                                  dp, ip]),
@@ -99,6 +101,15 @@ SIGNATURES = [
     ("iskra_ens_mcc_counts", c_int, [c_void_p, c_int, c_int, POINTER(c_uint64)]),
     ("iskra_ens_field", c_int, [c_void_p, c_int, c_int, dp]),
     ("iskra_ens_set_compact_every", c_int, [c_void_p, c_int]),
+    ("iskra_lws_create", c_int, [CTX, c_int, c_uint64]),
+    ("iskra_lws_destroy", c_int, [CTX]),
+    ("iskra_lws_set_mode", c_int, [CTX, c_int, c_int, c_int]),
+    ("iskra_lws_info", c_int, [CTX, ip, ip, i64p, i64p, dp, dp]),
+    ("iskra_lws_eval", c_int, [CTX, dp, dp]),
+    ("iskra_lws_weights", c_int, [CTX, f32p, f32p]),
+    ("iskra_lws_forward", c_int, [CTX, f32p, f32p]),
+    ("iskra_lws_loss_grad", c_int, [CTX, f32p, f32p, dp, f32p]),
+    ("iskra_lws_train", c_int, [CTX, c_int, c_double, c_uint64, dp]),
 ]
 
 _LIB = None

@@ -111,6 +111,7 @@ struct Species {
 
 struct Poisson;                // poisson.cu
 struct Mcc;                    // mcc.cu
+struct Lws;                    // lws.cu (learned warm start of CG solves)
 struct CircuitDev {            // device-resident circuit state (FP64)
   double R, L, C, amp, freq, dc, area, scale;
   double t, i, q, vext;
@@ -144,6 +145,7 @@ struct Ctx {
   double *stage = nullptr;     // upload/download staging (device)
   size_t stage_bytes = 0;
   Poisson *ps = nullptr;
+  Lws *lws = nullptr;
   std::vector<Mcc *> mccs;
   CircuitDev *cir_d = nullptr;
   CircuitDev cir_h{};
@@ -265,6 +267,14 @@ int launch_circuit(Ctx *c, double dt);
 int poisson_prepare(Ctx *c);
 void poisson_destroy(Poisson *p);
 void mcc_destroy(Mcc *m);
+
+// learned warm start (lws.cu), called by CG solves after their first residual
+bool lws_active(Ctx *c);
+int lws_begin(Ctx *c, const double *r, const float **y, double *scale);
+int lws_mark_start(Ctx *c, const double *phi);
+void lws_note_applied(Ctx *c, double alpha, double ratio);
+int lws_end(Ctx *c, const double *phi, bool converged);
+void lws_destroy_ctx(Ctx *c);
 
 }  // namespace iskra
 

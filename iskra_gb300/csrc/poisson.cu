@@ -88,6 +88,7 @@ struct Poisson {
   float2 *xd = nullptr;         // ϕ as double-float pairs (separable operators: the solver's state)
   float2 *bd = nullptr;         // b of the free rows as double-float pairs (first residual pass)
   void *xh = nullptr;           // previous step solve's ϕ in the state's representation (8 B per node)
+  int warm_mode = 1;            // step solves start from 0: ϕ_n, 1: 2 ϕ_n - ϕ_(n-1)
   bool df_mode = false;         // the solver's state is xd (double-float), x a view
   bool x_stale = false;         // (df_mode) x lags xd
   double *r = nullptr, *z = nullptr, *p = nullptr, *ap = nullptr;  // nn
@@ -1670,8 +1671,8 @@ static int build_device(Ctx *c, Poisson *P) {
     if (rc) return rc;
     if (!P->xd) ISKRA_CUDA(c, cudaMalloc(&P->xd, nn * sizeof(float2)));
     if (!P->bd) ISKRA_CUDA(c, cudaMalloc(&P->bd, nn * sizeof(float2)));
-    if (!P->xh) ISKRA_CUDA(c, cudaMalloc(&P->xh, nn * sizeof(double)));
   }
+  if (!P->xh) ISKRA_CUDA(c, cudaMalloc(&P->xh, nn * sizeof(double)));
   // a new operator: the next step solve starts from ϕ itself
   ISKRA_CUDA(c, cudaMemset(&P->scal->hist, 0, sizeof(int)));
   P->dirty = false;
@@ -1795,7 +1796,7 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
   OpView op = opview(P);
   const double nie = -1.0 / P->eps0;
   cudaStream_t st = c->stream;
-  if (warm && P->separable) {
+  if (warm && P->separable && P->warm_mode == 1) {
     if (P->df_mode)
       ISKRA_CUDA(c, launch_pdl(k_extrapolate<true>, B, T, 0, st, (const uint16_t *)P->cls, (void *)P->xd, P->xh,
                                nn, P->scal));
@@ -1939,13 +1940,68 @@ int poisson_solve_graph(Ctx *c, double rtol) {
   return finish_solve(c);
 }
 
-static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres) {
+// Learned warm start of a CG solve: δ = scale y on the free rows (the
+// network's predicted correction), applied as ϕ += α δ with the exact line
+// search α = δ·r / δ·Sδ in the energy norm of the scaled system S ϕ = c
+// (r = c - S ϕ the scaled residual), so the CG error never grows.
+__global__ void k_lws_dir(OpView op, const float *__restrict__ y, double scale, const double *__restrict__ r,
+                          double *__restrict__ p, double *__restrict__ part, int nn) {
+  __shared__ double sh[40];
+  double v = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k] & kClassMask];
+    const double d = C.fixed ? 0.0 : scale * (double)y[k];
+    p[k] = d;
+    v += d * r[k];
+  }
+  const double t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_lws_axpy(double *__restrict__ x, const double *__restrict__ p, double alpha, int nn) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) x[k] += alpha * p[k];
+}
+
+static int lws_line_search(Ctx *c, const float *y, double scale, double *applied_alpha) {
+  *applied_alpha = 0.0;
+  Poisson *P = c->ps;
+  const int B = P->blocks, T = 256, nn = P->nn;
+  OpView op = opview(P);
+  k_lws_dir<<<B, T, 0, c->stream>>>(op, y, scale, P->r, P->p, P->part, nn);
+  k_cg_ap<<<B, T, 0, c->stream>>>(op, P->p, P->ap, P->part, nn, P->scal);
+  ISKRA_CUDA(c, cudaGetLastError());
+  std::vector<double> h(2 * (size_t)B);
+  ISKRA_CUDA(c, cudaMemcpyAsync(h.data(), P->part, B * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaMemcpyAsync(h.data() + B, P->part + kPartials, B * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  double dr = 0, dsd = 0;
+  for (int b = 0; b < B; b++) {
+    dr += h[b];
+    dsd += h[B + b];
+  }
+  const double alpha = dsd > 0 ? dr / dsd : 0.0;
+  if (!(alpha > 0) || !std::isfinite(alpha)) return ISKRA_OK;
+  k_lws_axpy<<<B, T, 0, c->stream>>>(P->x, P->p, alpha, nn);
+  ISKRA_CUDA(c, cudaGetLastError());
+  *applied_alpha = alpha;
+  return ISKRA_OK;
+}
+
+// A solve with host convergence checks (CG; the separable solver outside
+// step graphs).  step: the solve of an iskra_step (CG operators), which
+// starts from ϕ extrapolated in time like the graph path; other solves
+// start from ϕ and end the extrapolation history.
+static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres, bool step = false) {
   int rc = poisson_prepare(c);
   if (rc) return rc;
   rc = poisson_set_precision(c, rtol);
   if (rc) return rc;
   Poisson *P = c->ps;
-  bool first = true;
+  if (step && !P->separable && P->warm_mode == 1)
+    ISKRA_CUDA(c, launch_pdl(k_extrapolate<false>, P->blocks, 256, 0, c->stream, (const uint16_t *)P->cls,
+                             (void *)P->x, P->xh, P->nn, P->scal));
+  bool first = true, lws_pending = false;
   int done_it = 0;
   const SweepLoop none{};
   for (;;) {
@@ -1953,6 +2009,35 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
     if (first) {
       rc = queue_prologue(c, rtol, c->graph_dt, none, false);
       if (rc) return rc;
+      if (!P->separable && lws_active(c)) {
+        // learned warm start: the network's correction from the first residual,
+        // then the residual again (CG restarts from the corrected ϕ)
+        ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost, c->stream));
+        ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (!P->scal_h->done) {
+          const float *y = nullptr;
+          double scale = 0.0;
+          lws_pending = true;
+          rc = lws_begin(c, P->r, &y, &scale);
+          if (rc) return rc;
+          rc = lws_mark_start(c, P->x);
+          if (rc) return rc;
+          if (y) {
+            const double res2 = P->scal_h->res2;
+            double alpha = 0.0;
+            rc = lws_line_search(c, y, scale, &alpha);
+            if (rc) return rc;
+            if (alpha > 0) {
+              rc = queue_prologue(c, rtol, c->graph_dt, none, false);
+              if (rc) return rc;
+              ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost,
+                                            c->stream));
+              ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+              lws_note_applied(c, alpha, res2 > 0 ? std::sqrt(P->scal_h->res2 / res2) : 0.0);
+            }
+          }
+        }
+      }
     }
     rc = queue_sweeps(c, rtol, chunk, first, none);
     if (rc) return rc;
@@ -1964,8 +2049,12 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
   }
   rc = finish_solve(c);
   if (rc) return rc;
+  if (lws_pending) {
+    rc = lws_end(c, P->x, P->scal_h->done != 0);
+    if (rc) return rc;
+  }
   // ϕ moved outside the step sequence: the next step solve starts from it
-  ISKRA_CUDA(c, cudaMemsetAsync(&P->scal->hist, 0, sizeof(int), c->stream));
+  if (!step) ISKRA_CUDA(c, cudaMemsetAsync(&P->scal->hist, 0, sizeof(int), c->stream));
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   P->last_iters = P->scal_h->iters;
   P->last_relres = P->scal_h->relres;
@@ -2019,7 +2108,9 @@ int poisson_set_precision(Ctx *c, double rtol) {
   return ISKRA_OK;
 }
 bool poisson_separable(Ctx *c) { return c->ps && c->ps->separable; }
-int poisson_solve_blocking(Ctx *c, double rtol, int maxit) { return solve_sync(c, rtol, maxit, nullptr, nullptr); }
+int poisson_solve_blocking(Ctx *c, double rtol, int maxit) {
+  return solve_sync(c, rtol, maxit, nullptr, nullptr, true);
+}
 
 // ---------------------------------------------------------------------------
 // Ensemble field solve: one block per run forms ρ from the run's deposit,
@@ -2390,6 +2481,19 @@ int iskra_poisson_set_method(iskra_ctx *h, int method, int *active) {
   int rc = poisson_prepare(c);
   if (rc) return rc;
   if (active) *active = c->ps->separable ? 0 : 1;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_set_warm_start(iskra_ctx *h, int mode) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  if (mode != 0 && mode != 1) return set_err(c, ISKRA_EINVAL, "warm-start mode must be 0 or 1");
+  if (c->ps->warm_mode != mode) {
+    c->ps->warm_mode = mode;
+    invalidate_graphs(c);
+    if (c->ps->scal) ISKRA_CUDA(c, cudaMemsetAsync(&c->ps->scal->hist, 0, sizeof(int), c->stream));
+  }
   return ISKRA_OK;
 }
 

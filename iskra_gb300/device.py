@@ -179,6 +179,9 @@ class Context:
         m = _mask(nodes, self.nx, self.ny)
         self._c(self.lib.iskra_poisson_drive_dirichlet(self.h, _ptr(m, _lib.u8p), amp, freq, phase, dc))
 
+    def set_warm_start(self, mode):
+        self._c(self.lib.iskra_poisson_set_warm_start(self.h, mode))
+
     def set_method(self, method):
         a = c_int()
         self._c(self.lib.iskra_poisson_set_method(self.h, method, byref(a)))
@@ -253,6 +256,60 @@ class Context:
 
     def set_sort_every(self, every):
         self._c(self.lib.iskra_set_sort_every(self.h, every))
+
+    # -- learned warm start of CG solves --
+    def lws_create(self, capacity=0, seed=0):
+        self._c(self.lib.iskra_lws_create(self.h, capacity, seed))
+
+    def lws_destroy(self):
+        self._c(self.lib.iskra_lws_destroy(self.h))
+
+    def lws_set_mode(self, harvest=False, use=False, smooth=4):
+        self._c(self.lib.iskra_lws_set_mode(self.h, int(harvest), int(use), int(smooth)))
+
+    def lws_info(self):
+        pairs, npar, solves, warm, alpha, ratio = c_int(), c_int(), c_int64(), c_int64(), c_double(), c_double()
+        self._c(self.lib.iskra_lws_info(self.h, byref(pairs), byref(npar), byref(solves), byref(warm),
+                                        byref(alpha), byref(ratio)))
+        return dict(pairs=pairs.value, nparams=npar.value, solves=solves.value, warm_solves=warm.value,
+                    mean_alpha=alpha.value, mean_ratio=ratio.value)
+
+    def lws_eval(self):
+        loss, zero = c_double(), c_double()
+        self._c(self.lib.iskra_lws_eval(self.h, byref(loss), byref(zero)))
+        return loss.value, zero.value
+
+    def lws_weights(self, new=None):
+        n = self.lws_info()["nparams"]
+        out = np.empty(n, np.float32)
+        w_in = None
+        if new is not None:
+            w_in = np.ascontiguousarray(new, np.float32)
+            assert w_in.size == n
+        self._c(self.lib.iskra_lws_weights(self.h, _ptr(out, _lib.f32p),
+                                           _ptr(w_in, _lib.f32p) if w_in is not None else None))
+        return out
+
+    def lws_forward(self, img):
+        """img: (ny, nx) float32 (x fastest); returns the (ny, nx) output."""
+        x = np.ascontiguousarray(img, np.float32).reshape(self.ny, self.nx)
+        y = np.empty_like(x)
+        self._c(self.lib.iskra_lws_forward(self.h, _ptr(x, _lib.f32p), _ptr(y, _lib.f32p)))
+        return y
+
+    def lws_loss_grad(self, img, target):
+        x = np.ascontiguousarray(img, np.float32).reshape(self.ny, self.nx)
+        t = np.ascontiguousarray(target, np.float32).reshape(self.ny, self.nx)
+        g = np.empty(self.lws_info()["nparams"], np.float32)
+        loss = c_double()
+        self._c(self.lib.iskra_lws_loss_grad(self.h, _ptr(x, _lib.f32p), _ptr(t, _lib.f32p), byref(loss),
+                                             _ptr(g, _lib.f32p)))
+        return loss.value, g
+
+    def lws_train(self, iters, lr=1e-3, seed=0):
+        loss = c_double()
+        self._c(self.lib.iskra_lws_train(self.h, iters, lr, seed, byref(loss)))
+        return loss.value
 
 
 class Ensemble:

@@ -1,0 +1,123 @@
+"""Learned warm start of CG solves (config C5's network, iskra_gb300/csrc/lws.cu):
+
+* the GPU forward pass, loss and parameter gradients against the CPU oracle
+  (oracle/lws_oracle.py, same BF16 rounding points, FP64 sums): the GPU sums
+  in FP32, so values differ by about one BF16 rounding per stored tensor;
+  tolerances 2 % on y and the loss, 3 % (relative L2) on the gradient;
+* training on pairs the simulation harvests lowers the loss, and a
+  warm-started CG solve needs fewer iterations than the plain one at the same
+  tolerance (the physics is unchanged: the same residual test ends both).
+"""
+import numpy as np
+import pytest
+
+from oracle import lws_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+
+def test_lws_forward_and_gradient_match_oracle(lib):
+    from iskra_gb300.device import Context
+    nx, ny = 48, 32
+    ctx = Context(nx, ny, 1e-4, 1e-4, (0, 0, 0, 0))
+    ctx.lws_create(0, seed=3)
+    w = ctx.lws_weights().astype(np.float64)
+    assert w.size == lo.NPARAMS
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((ny, nx)).astype(np.float32)
+    t = (0.1 * rng.standard_normal((ny, nx))).astype(np.float32)
+    y = ctx.lws_forward(x)
+    loss, g = ctx.lws_loss_grad(x, t)
+    lo_loss, lo_g, lo_y = lo.loss_grad(w, x, t, bf16=True)
+    assert np.max(np.abs(y - lo_y)) <= 2e-2 * np.max(np.abs(lo_y)), np.max(np.abs(y - lo_y))
+    assert abs(loss - lo_loss) <= 2e-2 * lo_loss, (loss, lo_loss)
+    rel = np.linalg.norm(g - lo_g) / np.linalg.norm(lo_g)
+    assert rel <= 3e-2, rel
+    for k, s in enumerate(lo.layer_slices()):
+        rk = np.linalg.norm(g[s] - lo_g[s]) / np.linalg.norm(lo_g[s])
+        assert rk <= 6e-2, (k, rk)
+    ctx.close()
+
+
+QE, ME, MAR, EPS0 = 1.602176634e-19, 9.1093837015e-31, 6.6335209e-26, 8.8541878128e-12
+
+
+def _slab_cg(lib, n=64, npart=200000):
+    """The 2D slab (x Dirichlet 0 / 100 V absorbing, y periodic) at n x n
+    nodes with CG forced, so that step solves iterate."""
+    from iskra_gb300.device import Context
+    rng = np.random.default_rng(2)
+    dx = 1e-4
+    L = (n - 1) * dx
+    w = 1e15 * L * L / npart
+    ctx = Context(n, n, dx, dx, (0, 0, 0, 0))
+    for q, m, T in ((-QE, ME, 2.0), (QE, MAR, 0.03)):
+        s = ctx.species_create(q, m, w, npart)
+        ctx.set_boundary(s, lib.BND_DISCARD, lib.BND_WRAP)
+        x = np.asfortranarray(np.column_stack([rng.uniform(0, L, npart), rng.uniform(0, L, npart)]))
+        v = np.asfortranarray(rng.standard_normal((npart, 3)) * np.sqrt(T * QE / m))
+        ctx.upload(s, x, v)
+    ctx.poisson_create(EPS0)
+    ctx.apply_periodic(1)
+    left = np.zeros((n, n), bool)
+    left[0, :] = True
+    right = np.zeros((n, n), bool)
+    right[-1, :] = True
+    ctx.apply_dirichlet(left, 0.0)
+    ctx.apply_dirichlet(right, 100.0)
+    assert ctx.set_method(1) == 1
+    return ctx
+
+
+def _steps(ctx, k):
+    its = []
+    for _ in range(k):
+        ctx.step(1e-11, 1, seed=1, rtol=1e-8)
+        it, rr = ctx.solve_info()
+        assert rr <= 1e-8
+        its.append(it)
+    return np.array(its, float)
+
+
+def test_lws_training_and_warm_start_gain(lib):
+    ctx = _slab_cg(lib)
+    ctx.lws_create(512, seed=5)
+    _steps(ctx, 300)                       # past the sheath-forming transient
+    # the time-extrapolated start of step solves against the previous ϕ
+    ctx.set_warm_start(0)
+    prev = _steps(ctx, 30).mean()
+    ctx.set_warm_start(1)
+    extrap = _steps(ctx, 30)[1:].mean()
+    assert extrap < prev, (extrap, prev)
+    # harvest, train on the GPU, check the loss on pairs it did not see
+    ctx.lws_set_mode(harvest=True)
+    _steps(ctx, 200)
+    ctx.lws_set_mode()
+    loss0, zero = ctx.lws_eval()
+    for lr in (1e-3, 3e-4, 1e-4):
+        ctx.lws_train(1500, lr=lr, seed=int(lr * 1e6))
+    train_loss, _ = ctx.lws_eval()
+    assert train_loss < 0.1 * zero and train_loss < loss0
+    ctx.lws_set_mode(harvest=True)
+    _steps(ctx, 30)
+    ctx.lws_set_mode()
+    all_loss, _ = ctx.lws_eval()
+    held_out = (230 * all_loss - 200 * train_loss) / 30
+    assert held_out < 0.6 * zero, (held_out, zero)
+    # warm-started solves: the network's correction (line search in the energy
+    # norm) removes most of the starting residual, and CG, iterated to the
+    # same tolerance, needs no more iterations than from the extrapolated ϕ
+    use, plain = [], []
+    for _ in range(2):
+        ctx.lws_set_mode(use=True, smooth=0)
+        i0 = ctx.lws_info()
+        use.append(_steps(ctx, 30))
+        i1 = ctx.lws_info()
+        ctx.lws_set_mode()
+        plain.append(_steps(ctx, 30))
+        n = i1["warm_solves"] - i0["warm_solves"]
+        ratio = (i1["mean_ratio"] * i1["warm_solves"] - i0["mean_ratio"] * i0["warm_solves"]) / n
+        assert n == 30 and ratio < 0.5, (n, ratio)
+    use, plain = np.concatenate(use), np.concatenate(plain)
+    assert use.mean() <= 1.05 * plain.mean(), (use.mean(), plain.mean())
+    ctx.close()

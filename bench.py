@@ -76,7 +76,7 @@ def electrode_masks():
     return left, right
 
 
-def setup_context(w, e, i, stream=0):
+def setup_context(w, e, i, stream=0, upload=True):
     from iskra_gb300 import _lib
     from iskra_gb300.device import Context
     ctx = Context(NX, NY, DX, DX, (0, 0, 0, 0), stream)
@@ -84,8 +84,9 @@ def setup_context(w, e, i, stream=0):
     si = ctx.species_create(QE, M_AR, w, NP)
     for s in (se, si):
         ctx.set_boundary(s, _lib.BND_DISCARD, _lib.BND_WRAP)
-    ctx.upload(se, *e)
-    ctx.upload(si, *i)
+    if upload:
+        ctx.upload(se, *e)
+        ctx.upload(si, *i)
     ctx.poisson_create(EPS0)
     ctx.apply_periodic(1)
     left, right = electrode_masks()
@@ -243,6 +244,83 @@ def c4_measure(steps):
             "drive U[100,500] V), one ensemble step graph", "data": "synthetic"}
 
 
+def c5_measure():
+    """Learned warm start of CG step solves (config C5's method at a reduced
+    size): the slab (x Dirichlet 0 / 100 V absorbing, y periodic) at 128^2
+    nodes, 1M e- + 1M Ar+, CG forced to relres 1e-8.  CG iterations and
+    particle-steps/s per step solve started from the previous ϕ, from ϕ
+    extrapolated in time, and from the extrapolation plus the network's
+    correction (trained on the GPU on 300 pairs harvested from the same run)."""
+    from iskra_gb300 import _lib
+    from iskra_gb300.device import Context
+    n, npart, dx = 128, 1 << 20, 1e-4
+    rng = np.random.default_rng(2)
+    L = (n - 1) * dx
+    w = 1e15 * L * L / npart
+    ctx = Context(n, n, dx, dx, (0, 0, 0, 0))
+    for q, m, T in ((-QE, ME, TE_EV), (QE, M_AR, TI_EV)):
+        sid = ctx.species_create(q, m, w, npart)
+        ctx.set_boundary(sid, _lib.BND_DISCARD, _lib.BND_WRAP)
+        x = np.asfortranarray(np.column_stack([rng.uniform(0, L, npart), rng.uniform(0, L, npart)]))
+        v = np.asfortranarray(rng.standard_normal((npart, 3)) * thermal_speed(T, m))
+        ctx.upload(sid, x, v)
+    ctx.poisson_create(EPS0)
+    ctx.apply_periodic(1)
+    left = np.zeros((n, n), bool)
+    left[0, :] = True
+    right = np.zeros((n, n), bool)
+    right[-1, :] = True
+    ctx.apply_dirichlet(left, 0.0)
+    ctx.apply_dirichlet(right, V_RIGHT)
+    ctx.set_method(1)
+    ctx.lws_create(512, seed=5)
+
+    def run(k):
+        its = []
+        t0 = time.perf_counter()
+        for _ in range(k):
+            ctx.step(DT, 1, seed=1, rtol=1e-8)
+            its.append(ctx.solve_info()[0])
+        dt = time.perf_counter() - t0
+        return float(np.mean(its)), 2 * npart * k / dt
+
+    run(300)  # past the sheath-forming transient
+    ctx.set_warm_start(0)
+    prev = run(50)
+    ctx.set_warm_start(1)
+    run(1)
+    extrap = run(50)
+    ctx.lws_set_mode(harvest=True)
+    run(300)
+    ctx.lws_set_mode()
+    t0 = time.perf_counter()
+    for lr in (1e-3, 3e-4, 1e-4):
+        ctx.lws_train(1500, lr=lr, seed=int(lr * 1e6))
+    t_train = time.perf_counter() - t0
+    train_loss, zero = ctx.lws_eval()
+    learned, plain = [], []
+    for _ in range(2):
+        ctx.lws_set_mode(use=True, smooth=0)
+        learned.append(run(50))
+        ctx.lws_set_mode()
+        plain.append(run(50))
+    info = ctx.lws_info()
+    ctx.close()
+    mean = lambda r, k: float(np.mean([x[k] for x in r]))
+    return {"workload": "2D slab 128x128, 1M e- + 1M Ar+, CG (Jacobi) forced to relres 1e-8, dt=1e-11 s",
+            "cg_iters_per_step": {"previous_phi": prev[0], "extrapolated": extrap[0],
+                                  "extrapolated_plus_network": mean(learned, 0),
+                                  "extrapolated_same_window": mean(plain, 0)},
+            "particle_steps_per_s": {"previous_phi": prev[1], "extrapolated": extrap[1],
+                                     "extrapolated_plus_network": mean(learned, 1),
+                                     "extrapolated_same_window": mean(plain, 1)},
+            "network": {"params": info["nparams"], "pairs": info["pairs"], "train_iters": 4500,
+                        "train_seconds": t_train, "energy_loss_vs_zero_predictor": train_loss / zero,
+                        "mean_line_search_step": info["mean_alpha"],
+                        "mean_residual_ratio_after_warm_start": info["mean_ratio"]},
+            "data": "synthetic"}
+
+
 # ----------------------------------------------------------------------------
 # CPU arm: the FP64 oracle (the reference's step restated), all host threads
 # ----------------------------------------------------------------------------
@@ -299,6 +377,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     ap.add_argument("--no-c4", action="store_true", help="skip the batched-ensemble (C4) leg")
+    ap.add_argument("--no-c5", action="store_true", help="skip the learned-warm-start (C5 method) leg")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -404,14 +483,18 @@ def main():
     ctx.close()
     e2e = None
     if not args.no_e2e:
-        phi_host = np.zeros((NX, NY), order="F")
-        k_e2e = min(args.steps, 200)
+        # ϕ is read each step into pinned host memory (direct DMA)
+        phi_pinned = torch.empty(NX * NY, dtype=torch.float64, pin_memory=True)
+        phi_host = phi_pinned.numpy().reshape((NX, NY), order="F")
+        k_e2e = args.steps
+        ctx2, se2, si2 = setup_context(w, e, i, upload=False)  # grid, species, solver: configuration
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ctx2, se2, si2 = setup_context(w, e, i)
+        ctx2.upload(se2, *e)
+        ctx2.upload(si2, *i)
         for k in range(k_e2e):
             ctx2.step(DT, 1, seed=1, rtol=RTOL)
-            phi_host[...] = ctx2.field(1)
+            ctx2.field(1, out=phi_host)
         xe_o, ve_o, _ = ctx2.download(se2)
         xi_o, vi_o, _ = ctx2.download(si2)
         t_e2e = time.perf_counter() - t0
@@ -419,7 +502,7 @@ def main():
         e2e = {"value": np_e2e * k_e2e / t_e2e, "unit": "particle-steps/s",
                "h2d_bytes_per_step": 2 * NP * 5 * 8 / k_e2e,
                "d2h_bytes_per_step": NX * NY * 8 + (xe_o.shape[0] + xi_o.shape[0]) * 5 * 8 / k_e2e, "steps": k_e2e,
-               "note": "C-ABI from host FP64 arrays: upload, per-step step+phi readback, final download"}
+               "note": "C-ABI from host FP64 arrays: upload, per-step step + phi read into pinned memory, final download"}
         ctx2.close()
 
     line = {
@@ -441,6 +524,8 @@ def main():
     }
     if rank == 0 and not args.no_c4:
         line["batched_c4"] = c4_measure(min(max(args.steps // 5, 20), 200))
+    if rank == 0 and not args.no_c5:
+        line["learned_warm_start_c5"] = c5_measure()
     if rank == 0 and not args.no_cpu_baseline:
         r = cpu_run(w, e, i, max_seconds=20.0)
         line["cpu_baseline"] = {

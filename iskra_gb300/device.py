@@ -118,9 +118,14 @@ class Context:
         E = _f64(E, (self.nx, self.ny, 3))
         self._c(self.lib.iskra_field_upload_E(self.h, _ptr(E)))
 
-    def field(self, which):
+    def field(self, which, out=None):
+        """ρ, ϕ or E as a Julia-layout FP64 array; `out` (Fortran-ordered, e.g.
+        a view of pinned host memory) receives it in place when given."""
         shape = (self.nx, self.ny, 3) if which == _lib.FIELD_E else (self.nx, self.ny)
-        out = np.zeros(shape, order="F")
+        if out is None:
+            out = np.zeros(shape, order="F")
+        elif out.shape != shape or out.dtype != np.float64 or not out.flags.f_contiguous:
+            raise ValueError(f"out must be a Fortran-ordered float64 array of shape {shape}")
         self._c(self.lib.iskra_field_download(self.h, which, _ptr(out)))
         return out
 

@@ -652,7 +652,10 @@ int lws_backward(Ctx *c, Lws *L, const float *t, float tscale, bool energy = fal
   const int T = 256;
   const int *h = L->h, *w = L->w;
   const int P0 = h[0] * w[0];
-  const int dwb = std::max(1, std::min(2 * c->num_sms, ((w[0] + kTx - 1) / kTx) * ((h[0] + kTy - 1) / kTy)));
+  // weight-gradient blocks: at most two per SM, at most one per tile of the level
+  auto dwb = [&](int l) {
+    return std::max(1, std::min(2 * c->num_sms, ((w[l] + kTx - 1) / kTx) * ((h[l] + kTy - 1) / kTy)));
+  };
   ISKRA_CUDA(c, cudaMemsetAsync(L->g32, 0, kParams * sizeof(float), st));
   if (energy) {
     k_err<<<blocks_for(c, P0, T), T, 0, st>>>(L->y, t, tscale, L->te, P0);
@@ -666,7 +669,7 @@ int lws_backward(Ctx *c, Lws *L, const float *t, float tscale, bool energy = fal
   for (int l = 0; l <= 2; l++) {
     const int li = 6 - l;
     k_conv32<false><<<conv_grid(h[l], w[l]), 128, 0, st>>>(L->dz[li], L->wt + layer_off(li), L->du[l], h[l], w[l]);
-    k_conv32_dw<<<dwb, 288, 0, st>>>(L->u[l], L->dz[li], L->g32 + layer_off(li), h[l], w[l]);
+    k_conv32_dw<<<dwb(l), 288, 0, st>>>(L->u[l], L->dz[li], L->g32 + layer_off(li), h[l], w[l]);
     // the upsampled input came from layer li - 1 one level down
     k_up_bwd_mask<<<blocks_for(c, (long long)h[l + 1] * w[l + 1] * 4, T), T, 0, st>>>(
         L->du[l], L->a[li - 1], L->dz[li - 1], h[l + 1], w[l + 1]);
@@ -675,7 +678,7 @@ int lws_backward(Ctx *c, Lws *L, const float *t, float tscale, bool energy = fal
   // pooling gradient plus the skip gradient du[l - 1]
   for (int l = 3; l >= 1; l--) {
     k_conv32<false><<<conv_grid(h[l], w[l]), 128, 0, st>>>(L->dz[l], L->wt + layer_off(l), L->dp[l], h[l], w[l]);
-    k_conv32_dw<<<dwb, 288, 0, st>>>(L->p[l], L->dz[l], L->g32 + layer_off(l), h[l], w[l]);
+    k_conv32_dw<<<dwb(l), 288, 0, st>>>(L->p[l], L->dz[l], L->g32 + layer_off(l), h[l], w[l]);
     k_pool_bwd_mask<<<blocks_for(c, (long long)h[l - 1] * w[l - 1] * 4, T), T, 0, st>>>(
         L->dp[l], L->du[l - 1], L->a[l - 1], L->dz[l - 1], h[l - 1], w[l - 1]);
   }

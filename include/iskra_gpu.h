@@ -228,6 +228,15 @@ int iskra_step(iskra_ctx *ctx, double dt, int nsteps, uint64_t seed,
  * `every` steps, 0 never, < 0 (default) per species from its rms speed.
  * Sorting only reorders particles in memory; the deposit is order-independent. */
 int iskra_set_sort_every(iskra_ctx *ctx, int every);
+/* Autotunes the sort cadence on the caller's own run: `trial` steps (as
+ * iskra_step with dt, seed, rtol) under each factor 0.5, 1, 2, 4 on the
+ * speed-based per-species sort periods, each after a sort of every species,
+ * timed on the device; keeps the fastest and returns it with its time per
+ * step.  Advances the simulation by 4 (trial + 1) steps; results do not
+ * depend on the cadence (the sort is a permutation).  Needs the automatic
+ * cadence (iskra_set_sort_every(ctx, -1)). */
+int iskra_autotune_sort(iskra_ctx *ctx, double dt, int trial, uint64_t seed,
+                        double rtol, double *scale, double *ms_per_step);
 /* Last Poisson solve: iterations and relative residual (synchronises). */
 int iskra_solve_info(iskra_ctx *ctx, int *iters, double *relres);
 /* Diagnostic with no reference counterpart: number of kernels iskra_step has

@@ -157,6 +157,7 @@ struct Ctx {
   // step state
   unsigned long long step = 0;  // steps completed by iskra_step
   int sort_every = -1;                   // > 0 fixed period, 0 never, < 0 per species from its speed
+  double sort_scale = 1.0;               // factor on the speed-based periods (iskra_autotune_sort)
   int sort_period[kMaxSpecies] = {};     // steps between sorts of each species (0 = never)
   bool periods_valid = false;
   double periods_dt = 0;

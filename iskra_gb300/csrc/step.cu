@@ -127,7 +127,8 @@ static int update_sort_periods(Ctx *c, double dt) {
     if (rc) return rc;
     const double cells = std::sqrt(v2) * dt / h;  // rms cells moved per step
     double p = cells > 0 ? 1.5 * kHalo / cells : 64.0;
-    c->sort_period[s] = (int)std::max(4.0, std::min(64.0, std::floor(p)));
+    p = std::max(4.0, std::min(64.0, std::floor(p)));
+    c->sort_period[s] = (int)std::max(2.0, std::min(256.0, std::round(p * c->sort_scale)));
   }
   c->periods_valid = true;
   return ISKRA_OK;
@@ -334,6 +335,56 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
     }
   }
   return ISKRA_OK;
+}
+
+// Sort-cadence autotuner: runs `trial` steps of the caller's own simulation
+// under each factor on the speed-based sort periods (0.5, 1, 2, 4), each trial
+// after a sort of every species so that all start from the same order, timed
+// with CUDA events on the library stream, and keeps the fastest factor.  The
+// sort is a permutation and every per-step result is order-independent, so
+// the trials change the run's speed, not its physics.
+int iskra_autotune_sort(iskra_ctx *h, double dt, int trial, uint64_t seed, double rtol, double *scale_out,
+                        double *ms_out) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (trial < 1) return set_err(c, ISKRA_EINVAL, "trial steps must be >= 1");
+  if (c->sort_every >= 0) return set_err(c, ISKRA_EINVAL, "autotuning needs the automatic sort cadence");
+  const double factors[] = {0.5, 1.0, 2.0, 4.0};
+  double best = 0, best_ms = 0;
+  cudaEvent_t e0, e1;
+  ISKRA_CUDA(c, cudaEventCreate(&e0));
+  ISKRA_CUDA(c, cudaEventCreate(&e1));
+  int rc = ISKRA_OK;
+  for (double f : factors) {
+    c->sort_scale = f;
+    c->periods_valid = false;
+    for (int s = 0; s < (int)c->species.size() && !rc; s++) rc = launch_sort(c, s);
+    if (!rc) rc = iskra_step(h, dt, 1, seed, rtol);  // periods, graphs
+    if (rc) break;
+    cudaEventRecord(e0, c->stream);
+    rc = iskra_step(h, dt, trial, seed, rtol);
+    if (rc) break;
+    cudaEventRecord(e1, c->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = set_err(c, ISKRA_ECUDA, "autotune timing");
+      break;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per = ms / trial;
+    if (best == 0 || per < best_ms) {
+      best = f;
+      best_ms = per;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  c->sort_scale = best;
+  c->periods_valid = false;
+  if (scale_out) *scale_out = best;
+  if (ms_out) *ms_out = best_ms;
+  return collect_device_errors(c);
 }
 
 int iskra_kernel_launches(iskra_ctx *h, uint64_t *count) {

@@ -262,6 +262,12 @@ class Context:
     def set_sort_every(self, every):
         self._c(self.lib.iskra_set_sort_every(self.h, every))
 
+    def autotune_sort(self, dt, trial=64, seed=0, rtol=1e-8):
+        """Returns (chosen factor on the speed-based sort periods, ms per step)."""
+        f, ms = c_double(), c_double()
+        self._c(self.lib.iskra_autotune_sort(self.h, dt, trial, seed, rtol, byref(f), byref(ms)))
+        return f.value, ms.value
+
     # -- learned warm start of CG solves --
     def lws_create(self, capacity=0, seed=0):
         self._c(self.lib.iskra_lws_create(self.h, capacity, seed))

@@ -1,0 +1,70 @@
+"""Sort cadence: results do not depend on it, and the autotuner picks one.
+
+The sort only permutes the particle store; push and boundary rules act per
+particle, the deposit sums integers (order-independent), so two runs from the
+same particles with very different sort periods must agree bit for bit (ρ,
+every particle by id, wall-absorbed counts).  iskra_autotune_sort then times
+the speed-based periods scaled by 0.5, 1, 2 and 4 on the run itself and keeps
+one of them."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+QE, ME, MAR, EPS0 = 1.602176634e-19, 9.1093837015e-31, 6.6335209e-26, 8.8541878128e-12
+N, NP, DX, DT = 128, 300000, 1e-4, 1e-11
+
+
+def _slab(lib, sort_every):
+    from iskra_gb300.device import Context
+    rng = np.random.default_rng(9)
+    L = (N - 1) * DX
+    ctx = Context(N, N, DX, DX, (0, 0, 0, 0))
+    sids = []
+    for q, m, T in ((-QE, ME, 2.0), (QE, MAR, 0.03)):
+        s = ctx.species_create(q, m, 1e15 * L * L / NP, NP)
+        ctx.set_boundary(s, lib.BND_DISCARD, lib.BND_WRAP)
+        x = np.asfortranarray(np.column_stack([rng.uniform(0, L, NP), rng.uniform(0, L, NP)]))
+        v = np.asfortranarray(rng.standard_normal((NP, 3)) * np.sqrt(T * QE / m))
+        ctx.upload(s, x, v)
+        sids.append(s)
+    ctx.poisson_create(EPS0)
+    ctx.apply_periodic(1)
+    left = np.zeros((N, N), bool)
+    left[0, :] = True
+    right = np.zeros((N, N), bool)
+    right[-1, :] = True
+    ctx.apply_dirichlet(left, 0.0)
+    ctx.apply_dirichlet(right, 100.0)
+    ctx.set_sort_every(sort_every)
+    return ctx, sids
+
+
+def test_results_do_not_depend_on_sort_cadence(lib):
+    a, sa = _slab(lib, 3)
+    b, sb = _slab(lib, 40)
+    a.step(DT, 40, seed=1, rtol=1e-8)
+    b.step(DT, 40, seed=1, rtol=1e-8)
+    assert np.array_equal(a.field(lib.FIELD_RHO), b.field(lib.FIELD_RHO))
+    for s in (0, 1):
+        xa, va, ia = a.download(sa[s])
+        xb, vb, ib = b.download(sb[s])
+        oa, ob = np.argsort(ia), np.argsort(ib)
+        assert np.array_equal(ia[oa], ib[ob])
+        assert np.array_equal(xa[oa], xb[ob]) and np.array_equal(va[oa], vb[ob])
+        assert a.absorbed(sa[s]) == b.absorbed(sb[s])
+    a.close()
+    b.close()
+
+
+def test_autotune_sort_picks_a_factor(lib):
+    ctx, _ = _slab(lib, -1)
+    f, ms = ctx.autotune_sort(DT, trial=16, seed=1)
+    assert f in (0.5, 1.0, 2.0, 4.0) and ms > 0
+    ctx.step(DT, 10, seed=1, rtol=1e-8)
+    ctx.sync()
+    assert ctx.solve_info()[1] <= 1e-8
+    ctx.set_sort_every(5)
+    with pytest.raises(Exception):
+        ctx.autotune_sort(DT, trial=4)
+    ctx.close()

@@ -244,6 +244,61 @@ def c4_measure(steps):
             "drive U[100,500] V), one ensemble step graph", "data": "synthetic"}
 
 
+def c3_measure(steps, amp=300.0, n=105000):
+    """One run of the discharge the ensemble batches (257 x 2 nodes, 300 V
+    drive, e- and Ar+ MCC, n particles per species: the ensemble's median run),
+    stepped through the single-run step graph: the plain single-run GPU PIC the
+    batched ensemble is compared with."""
+    import torch
+    from iskra_gb300 import _lib
+    from iskra_gb300.device import Context
+    NXc = C4_NX
+    dxc = C4_GAP / (NXc - 1)
+    rng = np.random.default_rng(5)
+    w = 1e15 * C4_GAP * dxc / 100000
+    ctx = Context(NXc, 2, dxc, dxc)
+    se = ctx.species_create(-QE, ME, w, 4 * n)
+    si = ctx.species_create(QE, M_AR, w, 4 * n)
+    for s, T, m in ((se, 4.0, ME), (si, 0.03, M_AR)):
+        ctx.set_boundary(s, _lib.BND_DISCARD, _lib.BND_WRAP)
+        x = np.asfortranarray(np.column_stack([rng.uniform(0, C4_GAP, n), rng.uniform(0, dxc, n)]))
+        v = np.asfortranarray(rng.standard_normal((n, 3)) * np.sqrt(2 * T * QE / m))
+        ctx.upload(s, x, v)
+    ctx.poisson_create(EPS0)
+    ctx.apply_periodic(1)
+    left = np.zeros((NXc, 2), bool)
+    left[0, :] = True
+    right = np.zeros((NXc, 2), bool)
+    right[-1, :] = True
+    ctx.apply_dirichlet(left, 0.0)
+    ctx.apply_dirichlet(right, 0.0)
+    ctx.drive_dirichlet(left, amp, C4_F)
+    eps, el, ex, iz, cx = c3_tables()
+    gas = np.full((NXc, 2), 3.0 / (KB * 300.0))
+    ctx.mcc_create(se, [(_lib.MCC_ELASTIC_ISOTROPIC, 0.0, eps, el), (_lib.MCC_EXCITATION, 11.5, eps, ex),
+                        (_lib.MCC_IONIZATION, 15.76, eps, iz)], M_AR, 300.0, gas, product=si)
+    ctx.mcc_create(si, [(_lib.MCC_ELASTIC_BACKWARD, 0.0, eps, cx)], M_AR, 300.0, gas)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ctx.step(C4_DT, 5, seed=1000, rtol=RTOL)
+    ctx.sync()
+    n0 = ctx.count(se) + ctx.count(si)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ctx.step(C4_DT, steps, seed=1000, rtol=RTOL)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ctx.sync()
+    ms = a.elapsed_time(b)
+    n1 = ctx.count(se) + ctx.count(si)
+    ctx.close()
+    return {"metric": "particle-steps/s", "value": 0.5 * (n0 + n1) * steps / (ms * 1e-3), "unit": "particle-steps/s",
+            "ms_per_step": ms / steps, "steps": steps, "particles": [n0, n1],
+            "workload": "1 x (1D CCP argon discharge, 257x2 nodes, e- and Ar+ MCC, 300 V drive), single-run step graph",
+            "data": "synthetic"}
+
+
 def c5_measure():
     """Learned warm start of CG step solves (config C5's method at a reduced
     size): the slab (x Dirichlet 0 / 100 V absorbing, y periodic) at 128^2
@@ -524,6 +579,8 @@ def main():
     }
     if rank == 0 and not args.no_c4:
         line["batched_c4"] = c4_measure(min(max(args.steps // 5, 20), 200))
+        line["plain_c3"] = c3_measure(min(max(args.steps // 5, 20), 200))
+        line["batched_over_plain"] = line["batched_c4"]["value"] / line["plain_c3"]["value"]
     if rank == 0 and not args.no_c5:
         line["learned_warm_start_c5"] = c5_measure()
     if rank == 0 and not args.no_cpu_baseline:

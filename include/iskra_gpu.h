@@ -120,6 +120,13 @@ int iskra_species_sort(iskra_ctx *ctx, int sid);
 int iskra_field_upload_E(iskra_ctx *ctx, const double *E);
 /* Copies ρ, ϕ or E (FP64) to the host (synchronises). */
 int iskra_field_download(iskra_ctx *ctx, int which, double *out);
+/* Same without waiting: the field as the calls queued so far leave it is
+ * snapshotted on the device and copied to `out` while later calls (steps)
+ * run; `out` holds it after the next synchronising call (iskra_sync, a
+ * blocking download or count) and must stay valid until then.  Pinned host
+ * memory makes the copy overlap; a later non-blocking download first waits
+ * for this one's copy. */
+int iskra_field_download_async(iskra_ctx *ctx, int which, double *out);
 
 /* ---- ParticleInCell.advance!(::KineticSpecies, E, B, Δt, config) --------
  * ParticleInCell.jl:51-72: grid_to_particle (cloud_in_cell.jl:20-36), Boris

@@ -58,6 +58,7 @@ SIGNATURES = [
     ("iskra_species_sort", c_int, [CTX, c_int]),
     ("iskra_field_upload_E", c_int, [CTX, dp]),
     ("iskra_field_download", c_int, [CTX, c_int, dp]),
+    ("iskra_field_download_async", c_int, [CTX, c_int, dp]),
     ("iskra_advance", c_int, [CTX, c_int, c_double]),
     ("iskra_density", c_int, [CTX, c_int, dp]),
     ("iskra_charge_density", c_int, [CTX]),

@@ -37,6 +37,10 @@ void invalidate_graphs(Ctx *c) {
 }
 
 int collect_device_errors(Ctx *c) {
+  if (c->dl_pending) {  // a synchronising call also completes the non-blocking downloads
+    ISKRA_CUDA(c, cudaEventSynchronize(c->dl_done));
+    c->dl_pending = false;
+  }
   ISKRA_CUDA(c, cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   int f = *c->h_err;
@@ -298,6 +302,11 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   cudaFree(c->cell_cursor);
   cudaFree(c->scan_tmp);
   cudaFree(c->stage);
+  if (c->dl_stream) cudaStreamSynchronize(c->dl_stream);
+  if (c->dl_ready) cudaEventDestroy(c->dl_ready);
+  if (c->dl_done) cudaEventDestroy(c->dl_done);
+  if (c->dl_stream) cudaStreamDestroy(c->dl_stream);
+  cudaFree(c->dl_stage);
   cudaFree(c->d_step);
   cudaFree(c->d_scratch);
   cudaFree(c->mcc_work);

@@ -144,6 +144,12 @@ struct Ctx {
   int *scan_tmp = nullptr;
   double *stage = nullptr;     // upload/download staging (device)
   size_t stage_bytes = 0;
+  // non-blocking field downloads: snapshot on the context stream, copy to the
+  // host on dl_stream
+  double *dl_stage = nullptr;            // (nx*ny*3)
+  cudaStream_t dl_stream = nullptr;
+  cudaEvent_t dl_ready = nullptr, dl_done = nullptr;
+  bool dl_pending = false;
   Poisson *ps = nullptr;
   Lws *lws = nullptr;
   std::vector<Mcc *> mccs;

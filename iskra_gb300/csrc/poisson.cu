@@ -2538,18 +2538,18 @@ int iskra_solve_info(iskra_ctx *h, int *iters, double *relres) {
   return ISKRA_OK;
 }
 
-int iskra_field_download(iskra_ctx *h, int which, double *out) {
-  if (!h || !out) return ISKRA_EINVAL;
-  Ctx *c = &h->c;
-  const double *src = nullptr;
-  size_t n = (size_t)c->nn;
+}  // extern "C"
+
+// device source of a field download (bringing ϕ and E up to date)
+static int field_source(Ctx *c, int which, const double **src, size_t *n) {
+  *n = (size_t)c->nn;
   if (which == ISKRA_FIELD_RHO) {
-    src = c->rho;
+    *src = c->rho;
   } else if (which == ISKRA_FIELD_PHI) {
     if (!c->ps || !c->ps->x) return set_err(c, ISKRA_EINVAL, "no potential yet");
     int rs = poisson_sync_x(c);
     if (rs) return rs;
-    src = c->ps->x;
+    *src = c->ps->x;
   } else if (which == ISKRA_FIELD_E) {
     if (c->e_from_phi && c->ps && c->ps->x) {
       int rs = poisson_sync_x(c);
@@ -2557,14 +2557,55 @@ int iskra_field_download(iskra_ctx *h, int which, double *out) {
       int rc = launch_efield64(c, c->ps->x);
       if (rc) return rc;
     }
-    src = c->E64;
-    n *= 3;
+    *src = c->E64;
+    *n *= 3;
   } else {
     return set_err(c, ISKRA_EINVAL, "bad field selector");
   }
+  return ISKRA_OK;
+}
+
+extern "C" {
+
+int iskra_field_download(iskra_ctx *h, int which, double *out) {
+  if (!h || !out) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  const double *src = nullptr;
+  size_t n = 0;
+  int rc = field_source(c, which, &src, &n);
+  if (rc) return rc;
   ISKRA_CUDA(c, cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   return collect_device_errors(c);
+}
+
+// Non-blocking download: the field as the work queued so far leaves it is
+// copied to a device staging buffer on the context stream, then to `out` on
+// a second stream, so the copy overlaps the next queued steps.  `out` (pinned
+// host memory for a true overlap) holds the values after the next
+// synchronising call.  A later download first waits for this one's copy to
+// leave the staging buffer.
+int iskra_field_download_async(iskra_ctx *h, int which, double *out) {
+  if (!h || !out) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  const double *src = nullptr;
+  size_t n = 0;
+  int rc = field_source(c, which, &src, &n);
+  if (rc) return rc;
+  if (!c->dl_stage) {
+    ISKRA_CUDA(c, cudaMalloc(&c->dl_stage, (size_t)c->nn * 3 * sizeof(double)));
+    ISKRA_CUDA(c, cudaStreamCreateWithFlags(&c->dl_stream, cudaStreamNonBlocking));
+    ISKRA_CUDA(c, cudaEventCreateWithFlags(&c->dl_ready, cudaEventDisableTiming));
+    ISKRA_CUDA(c, cudaEventCreateWithFlags(&c->dl_done, cudaEventDisableTiming));
+  }
+  if (c->dl_pending) ISKRA_CUDA(c, cudaStreamWaitEvent(c->stream, c->dl_done, 0));
+  ISKRA_CUDA(c, cudaMemcpyAsync(c->dl_stage, src, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  ISKRA_CUDA(c, cudaEventRecord(c->dl_ready, c->stream));
+  ISKRA_CUDA(c, cudaStreamWaitEvent(c->dl_stream, c->dl_ready, 0));
+  ISKRA_CUDA(c, cudaMemcpyAsync(out, c->dl_stage, n * sizeof(double), cudaMemcpyDeviceToHost, c->dl_stream));
+  ISKRA_CUDA(c, cudaEventRecord(c->dl_done, c->dl_stream));
+  c->dl_pending = true;
+  return ISKRA_OK;
 }
 
 }  // extern "C"

@@ -90,7 +90,22 @@ class Context:
         self._c(self.lib.iskra_species_count(self.h, sid, byref(n)))
         return n.value
 
-    def download(self, sid):
+    def download(self, sid, out=None):
+        """Live particles (x, v, id).  out = (x (ld, 2), v (ld, 3), id (ld,)),
+        Fortran-ordered float64 / uint32 (e.g. views of pinned host memory),
+        receives them in place; views of its first np rows are returned."""
+        if out is not None:
+            x, v, ids = out
+            cap = x.shape[0]
+            if (x.shape != (cap, 2) or v.shape != (cap, 3) or ids.shape != (cap,) or not x.flags.f_contiguous
+                    or not v.flags.f_contiguous or x.dtype != np.float64 or v.dtype != np.float64
+                    or ids.dtype != np.uint32):
+                raise ValueError("out must be (x (ld,2) F float64, v (ld,3) F float64, id (ld,) uint32)")
+            got = c_int64()
+            self._c(self.lib.iskra_species_download(self.h, sid, _ptr(x), _ptr(v), None, _ptr(ids, _lib.u32p), cap,
+                                                    byref(got)))
+            n = got.value
+            return x[:n], v[:n], ids[:n]
         n = self.count(sid)
         cap = max(n, 1)
         x = np.zeros((cap, 2), order="F")
@@ -127,6 +142,15 @@ class Context:
         elif out.shape != shape or out.dtype != np.float64 or not out.flags.f_contiguous:
             raise ValueError(f"out must be a Fortran-ordered float64 array of shape {shape}")
         self._c(self.lib.iskra_field_download(self.h, which, _ptr(out)))
+        return out
+
+    def field_async(self, which, out):
+        """Non-blocking field download into `out` (Fortran-ordered float64, best
+        a view of pinned host memory); valid after the next sync()."""
+        shape = (self.nx, self.ny, 3) if which == _lib.FIELD_E else (self.nx, self.ny)
+        if out.shape != shape or out.dtype != np.float64 or not out.flags.f_contiguous:
+            raise ValueError(f"out must be a Fortran-ordered float64 array of shape {shape}")
+        self._c(self.lib.iskra_field_download_async(self.h, which, _ptr(out)))
         return out
 
     def advance(self, sid, dt):

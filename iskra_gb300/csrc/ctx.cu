@@ -232,6 +232,8 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
             cudaMalloc(&c->E64, nn * 3 * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&c->rho, nn * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&c->vol_inv, nn * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&c->rho_df, nn * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&c->vol_inv_df, nn * sizeof(float2)) == cudaSuccess &&
             cudaMalloc(&c->d_err, sizeof(int)) == cudaSuccess &&
             cudaMallocHost(&c->h_err, sizeof(int)) == cudaSuccess &&
             cudaMalloc(&c->cell_count, ((size_t)c->nkeys + 1) * sizeof(int)) == cudaSuccess &&
@@ -261,6 +263,11 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
   if (cudaMemcpyAsync(c->vol_inv, vinv.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->stream) !=
       cudaSuccess)
     return fail(ISKRA_ECUDA);
+  std::vector<float2> vinv_df(nn);
+  for (size_t k = 0; k < nn; k++) vinv_df[k] = df_host(vinv[k]);
+  if (cudaMemcpyAsync(c->vol_inv_df, vinv_df.data(), nn * sizeof(float2), cudaMemcpyHostToDevice, c->stream) !=
+      cudaSuccess)
+    return fail(ISKRA_ECUDA);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(ISKRA_ECUDA);
   *out = h;
   return ISKRA_OK;
@@ -285,6 +292,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
     cudaFree(s.dev.tile_begin);
     cudaFree(s.dview);
     cudaFree(s.n);
+    cudaFree(s.n_df);
   }
   for (auto *m : c->mccs) mcc_destroy(m);
   if (c->ps) poisson_destroy(c->ps);
@@ -296,6 +304,9 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   cudaFree(c->rho);
   cudaFree(c->rho_bg);
   cudaFree(c->vol_inv);
+  cudaFree(c->rho_df);
+  cudaFree(c->vol_inv_df);
+  cudaFree(c->bg_df);
   cudaFree(c->d_err);
   if (c->h_err) cudaFreeHost(c->h_err);
   cudaFree(c->cell_count);
@@ -354,6 +365,7 @@ int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t ca
   ISKRA_CUDA(c, cudaMalloc(&s.dview, sizeof(SpeciesDev)));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.tile_begin, 0, ((size_t)c->ntiles + 1) * sizeof(int), c->stream));
   ISKRA_CUDA(c, cudaMalloc(&s.n, nn * sizeof(double)));
+  ISKRA_CUDA(c, cudaMalloc(&s.n_df, nn * sizeof(float2)));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.st, 0, sizeof(SpeciesState), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, nn * sizeof(unsigned long long), c->stream));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, nn * sizeof(unsigned), c->stream));
@@ -519,11 +531,19 @@ int iskra_set_background(iskra_ctx *h, const double *rho_bg) {
   if (!h) return ISKRA_EINVAL;
   Ctx *c = &h->c;
   if (!rho_bg) {
+    cudaStreamSynchronize(c->stream);
     cudaFree(c->rho_bg);
+    cudaFree(c->bg_df);
     c->rho_bg = nullptr;
+    c->bg_df = nullptr;
   } else {
     if (!c->rho_bg) ISKRA_CUDA(c, cudaMalloc(&c->rho_bg, (size_t)c->nn * sizeof(double)));
+    if (!c->bg_df) ISKRA_CUDA(c, cudaMalloc(&c->bg_df, (size_t)c->nn * sizeof(float2)));
+    std::vector<float2> bdf(c->nn);
+    for (int k = 0; k < c->nn; k++) bdf[k] = df_host(rho_bg[k]);
     ISKRA_CUDA(c, cudaMemcpyAsync(c->rho_bg, rho_bg, (size_t)c->nn * sizeof(double), cudaMemcpyHostToDevice,
+                                  c->stream));
+    ISKRA_CUDA(c, cudaMemcpyAsync(c->bg_df, bdf.data(), (size_t)c->nn * sizeof(float2), cudaMemcpyHostToDevice,
                                   c->stream));
     ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   }

@@ -103,6 +103,9 @@ struct Species {
   SpeciesDev dev{};
   SpeciesDev *dview = nullptr; // device copy of dev (kernels over run views take arrays)
   double *n = nullptr;         // FP64 density (nx*ny)
+  float2 *n_df = nullptr;      // double-float density (written when ρ is formed in double-float)
+  bool n64_valid = true;       // n holds the density
+  bool n_df_valid = false;     // n_df holds the density
   // accumulator / density bookkeeping (host side):
   bool acc_valid = false;      // acc holds the unconsumed deposit of the current positions
   bool acc_zero = true;        // acc is all zero
@@ -136,6 +139,11 @@ struct Ctx {
   double *rho = nullptr;       // (nx*ny)
   double *rho_bg = nullptr;    // optional background charge density
   double *vol_inv = nullptr;   // 1 / cell_volume
+  // ρ in double-float, formed on the FP32 pipes when the separable solver's
+  // state is double-float (the FP64 copy is produced on demand)
+  float2 *rho_df = nullptr, *vol_inv_df = nullptr, *bg_df = nullptr;
+  bool rho64_valid = true;     // rho holds ρ
+  bool rho_df_valid = false;   // rho_df holds ρ
   int *d_err = nullptr;        // device error flags
   int *h_err = nullptr;        // pinned mirror
   // scratch for scans / sort
@@ -183,6 +191,55 @@ struct Ctx {
   unsigned long long d_step_known = ~0ull;  // value d_step holds, when known on the host
   unsigned long long d_step_host = 0;       // source of the d_step upload
 };
+
+// ---- double-float arithmetic (a value is hi + lo, two FP32 words, |lo| <=
+// ulp(hi)/2: ~48 significant bits) with the error-free transformations
+// two-sum (Knuth) and two-product by FMA.  GB300 runs FP32 at ~64x its FP64
+// rate; the separable solver keeps ϕ, b and ρ in this form.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 df_fast(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  float2 s = df_two_sum(a.x, b.x);
+  s.y += a.y + b.y;
+  return df_fast(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ float2 df_add_f(float2 a, float b) {
+  float2 s = df_two_sum(a.x, b);
+  s.y += a.y;
+  return df_fast(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_from(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_value(float2 a) { return (double)a.x + (double)a.y; }
+// an unsigned 64-bit integer as a double-float: three exact FP32 pieces
+// of at most 24 bits, summed (error below 2^-48 relative)
+__device__ __forceinline__ float2 df_from_u64(unsigned long long a) {
+  const float p2 = (float)(unsigned)(a >> 48) * 281474976710656.0f;          // x 2^48, exact
+  const float p1 = (float)(unsigned)((a >> 24) & 0xffffffu) * 16777216.0f;  // x 2^24, exact
+  const float p0 = (float)(unsigned)(a & 0xffffffu);
+  return df_add_f(df_add_f(make_float2(p2, 0.f), p1), p0);
+}
+// host split of a double into a double-float constant
+inline float2 df_host(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
 
 // ---- programmatic dependent launch ----
 // Step kernels are launched with programmatic stream serialisation: the next
@@ -272,6 +329,8 @@ int species_speed2(Ctx *c, int sid, double *mean_v2);  // <vx² + vy²> of the l
 int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host);
 int launch_circuit(Ctx *c, double dt);
 int poisson_prepare(Ctx *c);
+bool poisson_df_rho(Ctx *c);   // ρ of the next solve may be formed in double-float
+int sync_rho64(Ctx *c);        // FP64 ρ up to date (particles.cu)
 void poisson_destroy(Poisson *p);
 void mcc_destroy(Mcc *m);
 

@@ -20,6 +20,7 @@
 // is bit-identical for any particle order or launch shape.  A node's sum
 // stays below 2^64 while each of its four cells holds at most 16383
 // particles; the per-cell counts are kept alongside and checked by k_finalize.
+#include <algorithm>
 #include <cmath>
 
 #include "internal.cuh"
@@ -601,12 +602,98 @@ __global__ void k_finalize(FinalizeArgs A, const double *__restrict__ vol_inv, c
   if (flags) atomicOr(err, flags);
 }
 
+// The same in double-float arithmetic on the FP32 pipes (GB300 runs FP64 at
+// ~1/64 of its FP32 rate): the int64 sums split exactly into three FP32
+// pieces, products by two-product FMA; ρ and the densities to ~2^-48
+// relative, written as double-float pairs (FP64 copies on download).
+struct FinalizeDfArgs {
+  int ns;
+  unsigned long long *acc[kMaxSpecies];
+  unsigned *cnt[kMaxSpecies];
+  float2 *n[kMaxSpecies];
+  float2 scale[kMaxSpecies];  // w0 * 2^-48
+  float2 q[kMaxSpecies];
+  int consume[kMaxSpecies];
+};
+
+__global__ void k_finalize_df(FinalizeDfArgs A, const float2 *__restrict__ vol_inv, const float2 *__restrict__ bg,
+                              float2 *__restrict__ rho, int nn, int *err) {
+  pdl_wait();
+  int flags = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const float2 vi = vol_inv[k];
+    float2 r = bg ? bg[k] : make_float2(0.f, 0.f);
+    unsigned long long a[kMaxSpecies];
+    unsigned cn[kMaxSpecies];
+    float2 nold[kMaxSpecies];
+#pragma unroll
+    for (int s = 0; s < kMaxSpecies; s++) {
+      if (s >= A.ns) break;
+      if (A.consume[s]) {
+        a[s] = A.acc[s][k];
+        cn[s] = A.cnt[s][k];
+      } else {
+        nold[s] = A.n[s][k];
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < kMaxSpecies; s++) {
+      if (s >= A.ns) break;
+      float2 n;
+      if (A.consume[s]) {
+        if (cn[s] > kMaxCell) flags |= DERR_OVERFLOW;
+        n = df_mul(df_mul(df_from_u64(a[s]), A.scale[s]), vi);
+        A.n[s][k] = n;
+        A.acc[s][k] = 0ull;
+        A.cnt[s][k] = 0u;
+      } else {
+        n = nold[s];
+      }
+      r = df_add(r, df_mul(n, A.q[s]));
+    }
+    rho[k] = r;
+  }
+  if (flags) atomicOr(err, flags);
+}
+
+__global__ void k_df_to_f64(const float2 *__restrict__ a, double *__restrict__ b, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    b[k] = (double)a[k].x + (double)a[k].y;
+}
+__global__ void k_f64_to_df(const double *__restrict__ a, float2 *__restrict__ b, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float h = (float)a[k];
+    b[k] = make_float2(h, (float)(a[k] - (double)h));
+  }
+}
+
+static int node_blocks(Ctx *c) { return std::max(1, std::min(c->num_sms * 4, (c->nn + 255) / 256)); }
+
+// FP64 copies on demand
+int sync_rho64(Ctx *c) {
+  if (c->rho64_valid) return ISKRA_OK;
+  k_df_to_f64<<<node_blocks(c), 256, 0, c->stream>>>(c->rho_df, c->rho, c->nn);
+  ISKRA_CUDA(c, cudaGetLastError());
+  c->rho64_valid = true;
+  return ISKRA_OK;
+}
+static int sync_n64(Ctx *c, Species &sp) {
+  if (sp.n64_valid) return ISKRA_OK;
+  k_df_to_f64<<<node_blocks(c), 256, 0, c->stream>>>(sp.n_df, sp.n, c->nn);
+  ISKRA_CUDA(c, cudaGetLastError());
+  sp.n64_valid = true;
+  return ISKRA_OK;
+}
+
 // Brings every species' density up to date (depositing species whose
 // positions changed without a deposit, consuming unconsumed accumulators) and,
-// when with_rho, forms ρ.
+// when with_rho, forms ρ -- in double-float when the next solve takes it so
+// (separable operator with a double-float state), else in FP64.
 static int finalize(Ctx *c, bool with_rho) {
+  const bool df = with_rho && poisson_df_rho(c);
   FinalizeArgs A{};
-  A.ns = (int)c->species.size();
+  FinalizeDfArgs D{};
+  A.ns = D.ns = (int)c->species.size();
   bool any = false;
   for (int s = 0; s < A.ns; s++) {
     Species &sp = c->species[s];
@@ -614,26 +701,48 @@ static int finalize(Ctx *c, bool with_rho) {
       int rc = launch_deposit(c, s);
       if (rc) return rc;
     }
-    A.acc[s] = sp.dev.acc;
-    A.cnt[s] = sp.dev.cnt;
+    if (!sp.acc_valid) {  // the stored density enters: in the form this pass reads
+      if (df && !sp.n_df_valid) {
+        k_f64_to_df<<<node_blocks(c), 256, 0, c->stream>>>(sp.n, sp.n_df, c->nn);
+        sp.n_df_valid = true;
+      } else if (!df) {
+        int rc = sync_n64(c, sp);
+        if (rc) return rc;
+      }
+    }
+    A.acc[s] = D.acc[s] = sp.dev.acc;
+    A.cnt[s] = D.cnt[s] = sp.dev.cnt;
     A.n[s] = sp.n;
+    D.n[s] = sp.n_df;
     A.scale[s] = sp.w0 * ldexp(1.0, -48);
+    D.scale[s] = df_host(A.scale[s]);
     A.q[s] = sp.q;
-    A.consume[s] = sp.acc_valid ? 1 : 0;
+    D.q[s] = df_host(sp.q);
+    A.consume[s] = D.consume[s] = sp.acc_valid ? 1 : 0;
     any |= sp.acc_valid;
   }
   if (!any && !with_rho) return ISKRA_OK;
-  int blocks = c->num_sms * 4;
-  int need = (c->nn + 255) / 256;
-  if (need < blocks) blocks = need;
-  ISKRA_CUDA(c, launch_pdl(k_finalize, blocks, 256, 0, c->stream, A, (const double *)c->vol_inv,
-                           (const double *)c->rho_bg, with_rho ? c->rho : nullptr, c->nn, c->d_err));
+  if (df) {
+    ISKRA_CUDA(c, launch_pdl(k_finalize_df, node_blocks(c), 256, 0, c->stream, D, (const float2 *)c->vol_inv_df,
+                             (const float2 *)c->bg_df, c->rho_df, c->nn, c->d_err));
+    c->rho_df_valid = true;
+    c->rho64_valid = false;
+  } else {
+    ISKRA_CUDA(c, launch_pdl(k_finalize, node_blocks(c), 256, 0, c->stream, A, (const double *)c->vol_inv,
+                             (const double *)c->rho_bg, with_rho ? c->rho : nullptr, c->nn, c->d_err));
+    if (with_rho) {
+      c->rho64_valid = true;
+      c->rho_df_valid = false;
+    }
+  }
   ISKRA_CUDA(c, cudaGetLastError());
   for (int s = 0; s < A.ns; s++) {
     Species &sp = c->species[s];
     if (sp.acc_valid) {
       sp.acc_valid = false;
       sp.acc_zero = true;
+      sp.n64_valid = !df;
+      sp.n_df_valid = df;
     }
     sp.n_valid = true;
   }
@@ -1040,6 +1149,8 @@ int iskra_density(iskra_ctx *h, int sid, double *n_out) {
     if (rc) return rc;
   }
   if (n_out) {
+    int rc = sync_n64(c, s);
+    if (rc) return rc;
     ISKRA_CUDA(c, cudaMemcpyAsync(n_out, s.n, (size_t)c->nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
     return collect_device_errors(c);

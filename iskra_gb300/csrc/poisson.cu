@@ -176,41 +176,7 @@ void poisson_destroy(Poisson *p) {
 constexpr unsigned kFixedBit = 0x8000u;
 constexpr unsigned kClassMask = 0x7fffu;
 
-// ---- double-float arithmetic (a value is hi + lo, two FP32 words, |lo| <=
-// ulp(hi)/2: ~48 significant bits) with the error-free transformations
-// two-sum (Knuth) and two-product by FMA.  GB300 runs FP32 at ~64x its FP64
-// rate; the separable solver keeps ϕ and b in this form.
-__device__ __forceinline__ float2 df_two_sum(float a, float b) {
-  const float s = a + b, bb = s - a;
-  return make_float2(s, (a - (s - bb)) + (b - bb));
-}
-__device__ __forceinline__ float2 df_fast(float a, float b) {  // |a| >= |b|
-  const float s = a + b;
-  return make_float2(s, b - (s - a));
-}
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-  float2 s = df_two_sum(a.x, b.x);
-  s.y += a.y + b.y;
-  return df_fast(s.x, s.y);
-}
-__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
-  const float p = a.x * b.x;
-  float e = fmaf(a.x, b.x, -p);
-  e = fmaf(a.x, b.y, e);
-  e = fmaf(a.y, b.x, e);
-  return df_fast(p, e);
-}
-__device__ __forceinline__ float2 df_add_f(float2 a, float b) {
-  float2 s = df_two_sum(a.x, b);
-  s.y += a.y;
-  return df_fast(s.x, s.y);
-}
-__device__ __forceinline__ float2 df_from(double v) {
-  const float h = (float)v;
-  return make_float2(h, (float)(v - (double)h));
-}
-__device__ __forceinline__ double df_value(float2 a) { return (double)a.x + (double)a.y; }
+// (double-float arithmetic: df_* in internal.cuh)
 
 struct OpView {
   const uint16_t *cls;
@@ -562,7 +528,8 @@ __device__ __forceinline__ void efield_df5(float2 xk, float2 xw, float2 xe, floa
 // rtol already, the next pass, otherwise skipped, writes E instead.
 template <bool FIRST, bool EOUT>
 __global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__restrict__ x,
-                                                     const double *__restrict__ rho, double neg_inv_eps0,
+                                                     const double *__restrict__ rho, const float2 *__restrict__ rho_df,
+                                                     float2 nie_df, double neg_inv_eps0,
                                                      float2 *__restrict__ bd, PoissonScal *sc, float *__restrict__ r32,
                                                      double *__restrict__ part, int nn, int singular, double rtol2,
                                                      EOut eo, SweepLoop loop) {
@@ -593,10 +560,12 @@ __global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__
     const unsigned ck = op.cls[k];
     const float2 xk = x[k], xw = x[w], xe = x[e], xs = x[s], xn = x[n];
     double rk = 0.0, fk = 0.0;
+    float2 rdk = make_float2(0.f, 0.f);
     unsigned cw = 0, ce = 0, cs = 0, cn = 0;
     float2 b = make_float2(0.f, 0.f);
     if (FIRST) {
-      rk = rho[k];
+      if (rho_df) rdk = rho_df[k];
+      else rk = rho[k];
       fk = op.bfix[k];
       cw = op.cls[w];
       ce = op.cls[e];
@@ -613,10 +582,14 @@ __global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__
     const RowClass &C = CT[ck];
     float2 res;
     if (FIRST) {
-      double bv = C.rho ? rk * neg_inv_eps0 : fk;
-      if (singular) bv -= lam;
-      if (C.sig_dof >= 0) bv -= C.sig_coef * op.sigma[C.sig_dof];
-      b = df_from(bv);
+      if (rho_df && C.rho) {  // ρ formed in double-float (no λ, no σ dofs then)
+        b = df_mul(rdk, nie_df);
+      } else {
+        double bv = C.rho ? rk * neg_inv_eps0 : fk;
+        if (singular) bv -= lam;
+        if (C.sig_dof >= 0) bv -= C.sig_coef * op.sigma[C.sig_dof];
+        b = df_from(bv);
+      }
       bd[k] = b;
       float2 afix = make_float2(0.f, 0.f), afree = df_mul(C.c0f, xk);
       const float2 t[4] = {df_mul(C.cWf, xw), df_mul(C.cEf, xe), df_mul(C.cSf, xs), df_mul(C.cNf, xn)};
@@ -1720,6 +1693,8 @@ static EOut eout(Ctx *c, bool on) {
 // written here, after an operator build or a host update of Dirichlet values.
 static int fixed_to_x_now(Ctx *c) {
   Poisson *P = c->ps;
+  int rc = sync_rho64(c);  // ρ-valued fixed rows read the FP64 ρ
+  if (rc) return rc;
   k_fixed_to_x<<<P->blocks, 256, 0, c->stream>>>(opview(P), P->x, P->xd, c->rho,
                                                   -1.0 / P->eps0, P->nn);
   ISKRA_CUDA(c, cudaGetLastError());
@@ -1795,7 +1770,16 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
   const int nn = P->nn, B = P->blocks, T = 256;
   OpView op = opview(P);
   const double nie = -1.0 / P->eps0;
+  const float2 nie_df = df_host(nie);
   cudaStream_t st = c->stream;
+  // the first residual takes ρ in double-float when it was formed so; every
+  // other reader takes the FP64 copy
+  const float2 *rdf = (P->separable && P->df_mode && !P->singular && !P->rho_fixed && c->rho_df_valid)
+                          ? c->rho_df : nullptr;
+  if (!rdf) {
+    int rc = sync_rho64(c);
+    if (rc) return rc;
+  }
   if (warm && P->separable && P->warm_mode == 1) {
     if (P->df_mode)
       ISKRA_CUDA(c, launch_pdl(k_extrapolate<true>, B, T, 0, st, (const uint16_t *)P->cls, (void *)P->xd, P->xh,
@@ -1821,12 +1805,12 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
     // (step graphs: E comes from the following pass)
     if (warm)
       ISKRA_CUDA(c, launch_pdl(k_residual_df<true, false>, B, T, 0, st, op, (const float2 *)P->xd,
-                               (const double *)c->rho, nie, P->bd, P->scal, P->r32, P->part, nn, (int)P->singular,
-                               rtol * rtol, eout(c, false), loop));
+                               (const double *)c->rho, rdf, nie_df, nie, P->bd, P->scal, P->r32, P->part, nn,
+                               (int)P->singular, rtol * rtol, eout(c, false), loop));
     else
       ISKRA_CUDA(c, launch_pdl(k_residual_df<true, true>, B, T, 0, st, op, (const float2 *)P->xd,
-                               (const double *)c->rho, nie, P->bd, P->scal, P->r32, P->part, nn, (int)P->singular,
-                               rtol * rtol, eout(c, true), loop));
+                               (const double *)c->rho, rdf, nie_df, nie, P->bd, P->scal, P->r32, P->part, nn,
+                               (int)P->singular, rtol * rtol, eout(c, true), loop));
   } else if (P->separable) {
     ISKRA_CUDA(c, launch_pdl(k_residual<true, true>, B, T, 0, st, op, (const double *)P->x, (const double *)c->rho,
                              nie, P->scal, (double *)nullptr, P->r32, P->part, nn, (int)P->singular, rtol * rtol,
@@ -1875,7 +1859,8 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
                                  P->logN, sh.TP, (const float2 *)P->tw, (const uint16_t *)P->cls, P->xd,
                                  (double *)nullptr, sc));
         ISKRA_CUDA(c, launch_pdl(k_residual_df<false, true>, B, T, 0, st, op, (const float2 *)P->xd,
-                                 (const double *)c->rho, nie, P->bd, P->scal, P->r32, P->part, nn,
+                                 (const double *)nullptr, (const float2 *)nullptr, make_float2(0.f, 0.f), nie,
+                                 P->bd, P->scal, P->r32, P->part, nn,
                                  (int)P->singular, rtol2, eout(c, true), last ? loop : none));
       } else {
         ISKRA_CUDA(c, launch_pdl(k_fft_inv_update<false>, sh.fb, 256, sh.smem, st, (const float2 *)P->spec, P->nx,
@@ -2067,6 +2052,10 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
 double *poisson_sigma_ptr(Ctx *c) { return c->ps ? c->ps->sigma_d : nullptr; }
 const double *poisson_x_ptr(Ctx *c) { return c->ps ? c->ps->x : nullptr; }
 const float2 *poisson_xd_ptr(Ctx *c) { return c->ps && c->ps->df_mode ? c->ps->xd : nullptr; }
+bool poisson_df_rho(Ctx *c) {
+  const Poisson *P = c->ps;
+  return P && !P->dirty && P->separable && P->df_mode && !P->singular && !P->rho_fixed;
+}
 void poisson_mark_x_stale(Ctx *c) {
   if (c->ps && c->ps->df_mode) c->ps->x_stale = true;
 }
@@ -2516,6 +2505,8 @@ int iskra_poisson_solve_host(iskra_ctx *h, const double *f, double rtol, int max
   for (int k = 0; k < c->nn; k++) negf[k] = -f[k];
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   ISKRA_CUDA(c, cudaMemcpy(c->rho, negf.data(), c->nn * sizeof(double), cudaMemcpyHostToDevice));
+  c->rho64_valid = true;
+  c->rho_df_valid = false;
   int rc = solve_sync(c, rtol, maxit, iters, relres);
   if (rc && rc != ISKRA_ENOTCONV) return rc;
   if (phi_out) {
@@ -2544,6 +2535,8 @@ int iskra_solve_info(iskra_ctx *h, int *iters, double *relres) {
 static int field_source(Ctx *c, int which, const double **src, size_t *n) {
   *n = (size_t)c->nn;
   if (which == ISKRA_FIELD_RHO) {
+    int rs = sync_rho64(c);
+    if (rs) return rs;
     *src = c->rho;
   } else if (which == ISKRA_FIELD_PHI) {
     if (!c->ps || !c->ps->x) return set_err(c, ISKRA_EINVAL, "no potential yet");

@@ -143,6 +143,7 @@ struct Ctx {
   // state is double-float (the FP64 copy is produced on demand)
   float2 *rho_df = nullptr, *vol_inv_df = nullptr, *bg_df = nullptr;
   bool rho64_valid = true;     // rho holds ρ
+  bool warm_fused = false;     // the ρ pass of the step being queued ran the warm start
   bool rho_df_valid = false;   // rho_df holds ρ
   int *d_err = nullptr;        // device error flags
   int *h_err = nullptr;        // pinned mirror
@@ -331,6 +332,17 @@ int launch_circuit(Ctx *c, double dt);
 int poisson_prepare(Ctx *c);
 bool poisson_df_rho(Ctx *c);   // ρ of the next solve may be formed in double-float
 int sync_rho64(Ctx *c);        // FP64 ρ up to date (particles.cu)
+// the step solve's warm start (ϕ <- 2ϕ_n - ϕ_(n-1) on free rows), run inside
+// the double-float ρ pass of a step
+struct WarmArgs {
+  const uint16_t *cls;         // row classes, fixed_bit on fixed rows
+  float2 *xd, *xh;             // ϕ and the previous step's ϕ (double-float)
+  int *hist;                   // xh is valid
+  unsigned *ticket;            // blocks finished (last-block marking of hist)
+  unsigned fixed_bit;
+};
+bool poisson_warm_args(Ctx *c, WarmArgs *w);
+int launch_step_density(Ctx *c);  // ρ of a graph step (with the fused warm start)
 void poisson_destroy(Poisson *p);
 void mcc_destroy(Mcc *m);
 

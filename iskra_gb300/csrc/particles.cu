@@ -616,9 +616,14 @@ struct FinalizeDfArgs {
   int consume[kMaxSpecies];
 };
 
+// WARM: the step solve's warm start on the same nodes (ϕ <- 2ϕ_n - ϕ_(n-1)
+// on free rows once the history is valid; the last block marks it valid)
+template <bool WARM>
 __global__ void k_finalize_df(FinalizeDfArgs A, const float2 *__restrict__ vol_inv, const float2 *__restrict__ bg,
-                              float2 *__restrict__ rho, int nn, int *err) {
+                              float2 *__restrict__ rho, int nn, int *err, WarmArgs W) {
   pdl_wait();
+  __shared__ int last;
+  const bool hist = WARM && *W.hist != 0;
   int flags = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const float2 vi = vol_inv[k];
@@ -652,8 +657,25 @@ __global__ void k_finalize_df(FinalizeDfArgs A, const float2 *__restrict__ vol_i
       r = df_add(r, df_mul(n, A.q[s]));
     }
     rho[k] = r;
+    if (WARM) {
+      const float2 xa = W.xd[k];
+      if (hist && !(W.cls[k] & W.fixed_bit)) W.xd[k] = df_add(make_float2(2.f * xa.x, 2.f * xa.y), df_neg(W.xh[k]));
+      W.xh[k] = xa;
+    }
   }
   if (flags) atomicOr(err, flags);
+  if (WARM) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last = atomicAdd(W.ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+      *W.ticket = 0u;
+      *W.hist = 1;
+    }
+  }
 }
 
 __global__ void k_df_to_f64(const float2 *__restrict__ a, double *__restrict__ b, int n) {
@@ -689,8 +711,9 @@ static int sync_n64(Ctx *c, Species &sp) {
 // positions changed without a deposit, consuming unconsumed accumulators) and,
 // when with_rho, forms ρ -- in double-float when the next solve takes it so
 // (separable operator with a double-float state), else in FP64.
-static int finalize(Ctx *c, bool with_rho) {
+static int finalize(Ctx *c, bool with_rho, bool step = false) {
   const bool df = with_rho && poisson_df_rho(c);
+  c->warm_fused = false;
   FinalizeArgs A{};
   FinalizeDfArgs D{};
   A.ns = D.ns = (int)c->species.size();
@@ -723,8 +746,15 @@ static int finalize(Ctx *c, bool with_rho) {
   }
   if (!any && !with_rho) return ISKRA_OK;
   if (df) {
-    ISKRA_CUDA(c, launch_pdl(k_finalize_df, node_blocks(c), 256, 0, c->stream, D, (const float2 *)c->vol_inv_df,
-                             (const float2 *)c->bg_df, c->rho_df, c->nn, c->d_err));
+    WarmArgs W{};
+    if (step && poisson_warm_args(c, &W)) {
+      ISKRA_CUDA(c, launch_pdl(k_finalize_df<true>, node_blocks(c), 256, 0, c->stream, D,
+                               (const float2 *)c->vol_inv_df, (const float2 *)c->bg_df, c->rho_df, c->nn, c->d_err, W));
+      c->warm_fused = true;
+    } else {
+      ISKRA_CUDA(c, launch_pdl(k_finalize_df<false>, node_blocks(c), 256, 0, c->stream, D,
+                               (const float2 *)c->vol_inv_df, (const float2 *)c->bg_df, c->rho_df, c->nn, c->d_err, W));
+    }
     c->rho_df_valid = true;
     c->rho64_valid = false;
   } else {
@@ -750,6 +780,7 @@ static int finalize(Ctx *c, bool with_rho) {
 }
 
 int launch_charge_density(Ctx *c) { return finalize(c, true); }
+int launch_step_density(Ctx *c) { return finalize(c, true, true); }
 
 // ---------------------------------------------------------------------------
 // E = -∇ϕ  (generalized_poisson.jl:398-410)

@@ -1780,7 +1780,9 @@ static int queue_prologue(Ctx *c, double rtol, double dt_for_drive, SweepLoop lo
     int rc = sync_rho64(c);
     if (rc) return rc;
   }
-  if (warm && P->separable && P->warm_mode == 1) {
+  if (warm && P->separable && P->warm_mode == 1 && c->warm_fused) {
+    c->warm_fused = false;  // the step's ρ pass ran it
+  } else if (warm && P->separable && P->warm_mode == 1) {
     if (P->df_mode)
       ISKRA_CUDA(c, launch_pdl(k_extrapolate<true>, B, T, 0, st, (const uint16_t *)P->cls, (void *)P->xd, P->xh,
                                nn, P->scal));
@@ -2052,6 +2054,18 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
 double *poisson_sigma_ptr(Ctx *c) { return c->ps ? c->ps->sigma_d : nullptr; }
 const double *poisson_x_ptr(Ctx *c) { return c->ps ? c->ps->x : nullptr; }
 const float2 *poisson_xd_ptr(Ctx *c) { return c->ps && c->ps->df_mode ? c->ps->xd : nullptr; }
+bool poisson_warm_args(Ctx *c, WarmArgs *w) {
+  Poisson *P = c->ps;
+  if (!P || !P->separable || !P->df_mode || P->warm_mode != 1 || !P->xh || !P->xd) return false;
+  w->cls = P->cls;
+  w->xd = P->xd;
+  w->xh = (float2 *)P->xh;
+  w->hist = &P->scal->hist;
+  w->ticket = &P->scal->hticket;
+  w->fixed_bit = kFixedBit;
+  return true;
+}
+
 bool poisson_df_rho(Ctx *c) {
   const Poisson *P = c->ps;
   return P && !P->dirty && P->separable && P->df_mode && !P->singular && !P->rho_fixed;

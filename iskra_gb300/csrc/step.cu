@@ -103,7 +103,7 @@ static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocki
     rc = launch_circuit(c, dt);
     if (rc) return rc;
   }
-  rc = launch_charge_density(c);
+  rc = blocking_solve ? launch_charge_density(c) : launch_step_density(c);
   if (rc) return rc;
   if (blocking_solve) return poisson_solve_blocking(c, rtol, 10000);
   return poisson_solve_graph(c, rtol);

@@ -144,6 +144,10 @@ struct Ctx {
   float2 *rho_df = nullptr, *vol_inv_df = nullptr, *bg_df = nullptr;
   bool rho64_valid = true;     // rho holds ρ
   bool warm_fused = false;     // the ρ pass of the step being queued ran the warm start
+  // which copies of ρ / the densities a replay of the step graph leaves
+  // current (recorded at capture, re-applied after replays)
+  bool g_rho64 = true, g_rho_df = false;
+  bool g_n64[kMaxSpecies] = {}, g_n_df[kMaxSpecies] = {};
   bool rho_df_valid = false;   // rho_df holds ρ
   int *d_err = nullptr;        // device error flags
   int *h_err = nullptr;        // pinned mirror
@@ -321,6 +325,7 @@ double poisson_drive_amp(Ctx *c, int g);
 
 // ---- kernels / launchers shared across files ----
 int launch_advance(Ctx *c, int sid, float dt);
+int launch_advance_all(Ctx *c, float dt);  // every species of a step (two in one launch when they can)
 int launch_deposit(Ctx *c, int sid);
 int launch_charge_density(Ctx *c);
 int launch_efield_from(Ctx *c, const double *phi);

@@ -99,7 +99,7 @@ __device__ __forceinline__ bool reduce_runs(int key, Moments &m, unsigned &n) {
 // Move by d cells along one axis in FP32: offset h in [0,1) on the 2^-24 grid,
 // cell index i (int).  Returns the new offset; i is updated in place.
 __device__ __forceinline__ float move_axis(float h, float d, int &i, unsigned &uq) {
-  const float t0 = h + d;
+  const float t0 = __fadd_rn(h, d);  // (rounded ops: no context-dependent contraction)
   if (t0 >= 0.0f && t0 < 1.0f) {  // stays in its cell: one rounding, then onto the grid
     int u = __float2int_rn(t0 * kOffScale);
     if (u >= (1 << 24)) {
@@ -111,8 +111,8 @@ __device__ __forceinline__ float move_axis(float h, float d, int &i, unsigned &u
   }
   d = fminf(fmaxf(d, -1.0e9f), 1.0e9f);
   float fd = floorf(d);
-  float fr = d - fd;           // [0,1)
-  float t = h + fr;            // [0,2)
+  float fr = __fsub_rn(d, fd);  // [0,1)
+  float t = __fadd_rn(h, fr);   // [0,2)
   int carry = 0;
   if (t >= 1.0f) {
     t -= 1.0f;
@@ -272,11 +272,16 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
           r0 = __ldg(E4 + 2 * n0);
           r1 = __ldg(E4 + 2 * n0 + 1);
         }
-        const float gx = 1.0f - hx, gy = 1.0f - hy;
+        // CIC weights and interpolation with explicitly rounded products and
+        // fused sums, so that every kernel inlining this code (single species,
+        // species pairs, ensemble runs) computes the same bits
+        const float gx = __fsub_rn(1.0f, hx), gy = __fsub_rn(1.0f, hy);
+        const float w00 = __fmul_rn(gx, gy), w10 = __fmul_rn(hx, gy);
+        const float w01 = __fmul_rn(gx, hy), w11 = __fmul_rn(hx, hy);
         const float2 e00 = make_float2(r0.x, r0.y), e10 = make_float2(r0.z, r0.w);
         const float2 e01 = make_float2(r1.x, r1.y), e11 = make_float2(r1.z, r1.w);
-        const float ex = gx * gy * e00.x + hx * gy * e10.x + gx * hy * e01.x + hx * hy * e11.x;
-        const float ey = gx * gy * e00.y + hx * gy * e10.y + gx * hy * e01.y + hx * hy * e11.y;
+        const float ex = fmaf(w00, e00.x, fmaf(w10, e10.x, fmaf(w01, e01.x, __fmul_rn(w11, e11.x))));
+        const float ey = fmaf(w00, e00.y, fmaf(w10, e10.y, fmaf(w01, e01.y, __fmul_rn(w11, e11.y))));
         // Boris with B = 0: v- = v + hE ; v = hE + v+ (v+ = v-)
         float vx = fmaf(P.h, ex, a.z);
         float vy = fmaf(P.h, ey, a.w);
@@ -286,8 +291,8 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
           flags |= DERR_NAN;
           cell = -1;
         } else {
-          hx = move_axis(hx, vx * P.dtdx, i0, ux);
-          hy = move_axis(hy, vy * P.dtdy, j0, uy);
+          hx = move_axis(hx, __fmul_rn(vx, P.dtdx), i0, ux);
+          hy = move_axis(hy, __fmul_rn(vy, P.dtdy), j0, uy);
           int rx = apply_boundary<MX>(i0, nx - 1);
           int ry = rx ? 0 : apply_boundary<MY>(j0, P.ny - 1);
           if (rx == 3 || ry == 3) {
@@ -355,16 +360,15 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
   deposit_warp<WIN>(s, sh, key, m, P.nx);
 }
 
-// Blocks [0, ntiles) each take the particles the last sort grouped in their
-// tile: stage the window's E records, push, deposit into the window, then add
-// the window's nonzero node sums and cell counts to the global accumulators.
-// Blocks from ntiles on walk the slots appended since that sort.  Integer
-// sums: the density is the same bit for bit whichever block adds what.
+// One block of the push: a tile block (tile >= 0) takes the particles the
+// last sort grouped in its tile: stage the window's E records, push, deposit
+// into the window, then add the window's nonzero node sums and cell counts to
+// the global accumulators.  A tail block (tile < 0, tail_block of
+// tail_blocks) walks the slots appended since that sort.  Integer sums: the
+// density is the same bit for bit whichever block adds what.
 template <bool PUSH, int MX, int MY>
-__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_push(SpeciesDev s, const float4 *__restrict__ E4,
-                                                                     PushParams P, int ntiles, int *err) {
-  pdl_wait();
-  __shared__ PushShared sh;
+__device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams &P, const float4 *__restrict__ E4,
+                                           PushShared &sh, int tile, int tail_block, int tail_blocks, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
   const int cur = s.st->cur;
@@ -373,8 +377,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
   unsigned ab[4] = {0, 0, 0, 0};
   int flags = 0;
   const int nx = P.nx;
-  if ((int)blockIdx.x < ntiles) {
-    const int tile = blockIdx.x;
+  if (tile >= 0) {
     const long long begin = s.tile_begin[tile], end = s.tile_begin[tile + 1];
     if (begin < end) {  // block-uniform
       const int ox = (tile % P.tiles_x) * kTile - kHalo, oy = (tile / P.tiles_x) * kTile - kHalo;
@@ -450,8 +453,8 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
     }
   } else {
     const long long np = s.st->np, t0 = s.st->sorted_n;
-    const long long warp = (long long)(blockIdx.x - ntiles) * nwb + wib;
-    const long long nwarps = (long long)(gridDim.x - ntiles) * nwb;
+    const long long warp = (long long)tail_block * nwb + wib;
+    const long long nwarps = (long long)tail_blocks * nwb;
     for (long long base = t0 + warp * 32; base < np; base += nwarps * 32) {
       const long long p = base + lane;
       const bool v = p < np;
@@ -472,6 +475,39 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS) k_p
     }
     int f = __reduce_or_sync(FULL, flags);
     if (lane == 0 && f) atomicOr(err, f);
+  }
+}
+
+template <bool PUSH, int MX, int MY>
+__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
+    k_push(SpeciesDev s, const float4 *__restrict__ E4, PushParams P, int ntiles, int *err) {
+  pdl_wait();
+  __shared__ PushShared sh;
+  const int b = blockIdx.x;
+  if (b < ntiles) push_block<PUSH, MX, MY>(s, P, E4, sh, b, 0, 0, err);
+  else push_block<PUSH, MX, MY>(s, P, E4, sh, -1, b - ntiles, gridDim.x - ntiles, err);
+}
+
+// Two species in one launch (the step's electrons and ions): their pushes
+// are independent until ρ is formed, so the second species' tiles fill the
+// SMs as the first species' tiles drain instead of waiting for a second
+// launch.  Blocks [0, ntiles) first species' tiles, [ntiles, 2 ntiles) the
+// second's, the rest both tails.
+template <int MX, int MY>
+__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
+    k_push2(SpeciesDev s0, SpeciesDev s1, const float4 *__restrict__ E4, PushParams P0, PushParams P1, int ntiles,
+            int *err) {
+  pdl_wait();
+  __shared__ PushShared sh;
+  const int b = blockIdx.x;
+  if (b < ntiles) {
+    push_block<true, MX, MY>(s0, P0, E4, sh, b, 0, 0, err);
+  } else if (b < 2 * ntiles) {
+    push_block<true, MX, MY>(s1, P1, E4, sh, b - ntiles, 0, 0, err);
+  } else {
+    const int tb = b - 2 * ntiles, nt = gridDim.x - 2 * ntiles;
+    push_block<true, MX, MY>(s0, P0, E4, sh, -1, tb, nt, err);
+    push_block<true, MX, MY>(s1, P1, E4, sh, -1, tb, nt, err);
   }
 }
 
@@ -501,13 +537,7 @@ static int sort_blocks(Ctx *c, Species &s) {
   return (int)(want < maxb ? want : maxb);
 }
 
-int launch_advance(Ctx *c, int sid, float dt) {
-  Species &s = c->species[sid];
-  if (!s.acc_zero) {
-    // accumulator holds an old deposit: clear it first
-    ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, (size_t)c->nn * sizeof(unsigned long long), c->stream));
-    ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, (size_t)c->nn * sizeof(unsigned), c->stream));
-  }
+static PushParams push_params(Ctx *c, const Species &s, float dt) {
   PushParams P;
   P.h = (float)(0.5 * (double)dt * (s.q / s.m));
   P.dtdx = (float)((double)dt / c->g.dx);
@@ -517,11 +547,66 @@ int launch_advance(Ctx *c, int sid, float dt) {
   P.mode_x = s.bnd[0];
   P.mode_y = s.bnd[1];
   P.tiles_x = c->tiles_x;
-  ISKRA_CUDA(c, launch_push_modes(c, s, P, push_blocks(c)));
-  ISKRA_CUDA(c, cudaGetLastError());
+  return P;
+}
+
+// a species' accumulator before its push: cleared unless known zero
+static int clear_acc(Ctx *c, Species &s) {
+  if (s.acc_zero) return ISKRA_OK;
+  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.acc, 0, (size_t)c->nn * sizeof(unsigned long long), c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.cnt, 0, (size_t)c->nn * sizeof(unsigned), c->stream));
+  return ISKRA_OK;
+}
+
+static void mark_pushed(Species &s) {
   s.acc_valid = true;  // accumulator = deposit of the pushed positions (unconsumed)
   s.acc_zero = false;
   s.n_valid = false;
+}
+
+int launch_advance(Ctx *c, int sid, float dt) {
+  Species &s = c->species[sid];
+  int rc = clear_acc(c, s);
+  if (rc) return rc;
+  ISKRA_CUDA(c, launch_push_modes(c, s, push_params(c, s, dt), push_blocks(c)));
+  ISKRA_CUDA(c, cudaGetLastError());
+  mark_pushed(s);
+  return ISKRA_OK;
+}
+
+// Every species of a step: two species with the same boundary rules in one
+// launch (k_push2), otherwise one launch each.
+int launch_advance_all(Ctx *c, float dt) {
+  const int ns = (int)c->species.size();
+  if (ns == 2 && c->species[0].bnd[0] == c->species[1].bnd[0] && c->species[0].bnd[1] == c->species[1].bnd[1]) {
+    Species &a = c->species[0], &b = c->species[1];
+    int rc = clear_acc(c, a);
+    if (!rc) rc = clear_acc(c, b);
+    if (rc) return rc;
+    const PushParams Pa = push_params(c, a, dt), Pb = push_params(c, b, dt);
+    const int blocks = 2 * c->ntiles + c->num_sms;
+    cudaError_t e = cudaErrorInvalidValue;
+#define ISKRA_PUSH2_CASE(MX, MY)                                                                           \
+  if (Pa.mode_x == MX && Pa.mode_y == MY) {                                                                \
+    cudaFuncSetAttribute(k_push2<MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,                  \
+                         (int)cudaSharedmemCarveoutMaxShared);                                             \
+    e = launch_pdl(k_push2<MX, MY>, blocks, ISKRA_PUSH_THREADS, 0, c->stream, a.dev, b.dev,                \
+                   (const float4 *)c->E4, Pa, Pb, c->ntiles, c->d_err);                                    \
+  }
+    ISKRA_PUSH2_CASE(0, 0) ISKRA_PUSH2_CASE(0, 1) ISKRA_PUSH2_CASE(0, 2)
+    ISKRA_PUSH2_CASE(1, 0) ISKRA_PUSH2_CASE(1, 1) ISKRA_PUSH2_CASE(1, 2)
+    ISKRA_PUSH2_CASE(2, 0) ISKRA_PUSH2_CASE(2, 1) ISKRA_PUSH2_CASE(2, 2)
+#undef ISKRA_PUSH2_CASE
+    ISKRA_CUDA(c, e);
+    ISKRA_CUDA(c, cudaGetLastError());
+    mark_pushed(a);
+    mark_pushed(b);
+    return ISKRA_OK;
+  }
+  for (int s = 0; s < ns; s++) {
+    int rc = launch_advance(c, s, dt);
+    if (rc) return rc;
+  }
   return ISKRA_OK;
 }
 

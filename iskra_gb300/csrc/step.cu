@@ -95,10 +95,8 @@ static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocki
     rc = launch_mcc(c, m, dt, seed, c->d_step, 0);
     if (rc) return rc;
   }
-  for (int s = 0; s < (int)c->species.size(); s++) {
-    rc = launch_advance(c, s, (float)dt);
-    if (rc) return rc;
-  }
+  rc = launch_advance_all(c, (float)dt);
+  if (rc) return rc;
   if (c->cir_d) {
     rc = launch_circuit(c, dt);
     if (rc) return rc;
@@ -313,12 +311,25 @@ int iskra_step(iskra_ctx *h, double dt, int nsteps, uint64_t seed, double rtol) 
     c->graph_rtol = rtol;
     c->graph_seed = seed;
     c->graph_dt = dt;
+    // the host flags now describe the state one replay leaves
+    c->g_rho64 = c->rho64_valid;
+    c->g_rho_df = c->rho_df_valid;
+    for (int s = 0; s < (int)c->species.size(); s++) {
+      c->g_n64[s] = c->species[s].n64_valid;
+      c->g_n_df[s] = c->species[s].n_df_valid;
+    }
   }
   for (int s = 0; s < (int)c->species.size(); s++) {
     if (!c->sort_graph[s] && c->sort_period[s] > 0) {
       rc = capture(c, &c->sort_graph[s], &c->sort_graph_kernels[s], [&]() { return launch_sort(c, s); });
       if (rc) return rc;
     }
+  }
+  c->rho64_valid = c->g_rho64;
+  c->rho_df_valid = c->g_rho_df;
+  for (int s = 0; s < (int)c->species.size(); s++) {
+    c->species[s].n64_valid = c->g_n64[s];
+    c->species[s].n_df_valid = c->g_n_df[s];
   }
   for (int n = 0; n < nsteps; n++) {
     ISKRA_CUDA(c, cudaGraphLaunch(c->graph, c->stream));

@@ -68,3 +68,60 @@ def test_autotune_sort_picks_a_factor(lib):
     with pytest.raises(Exception):
         ctx.autotune_sort(DT, trial=4)
     ctx.close()
+
+
+def test_double_float_rho_matches_fp64_rho(lib):
+    """ρ and the densities formed in double-float (tolerance 1e-8: the
+    separable solver's double-float state) equal the FP64 ones (tolerance
+    1e-12) of the same deposit to ~2^-48 relative."""
+    a, sa = _slab(lib, -1)
+    b, sb = _slab(lib, -1)
+    a.step(DT, 1, seed=1, rtol=1e-8)
+    b.step(DT, 1, seed=1, rtol=1e-12)
+    ra, rb = a.field(lib.FIELD_RHO), b.field(lib.FIELD_RHO)
+    scale = np.max(np.abs(rb))
+    assert scale > 0 and np.max(np.abs(ra - rb)) <= 1e-13 * scale
+    for s in (0, 1):
+        na, nb = a.density(sa[s]), b.density(sb[s])
+        assert np.max(np.abs(na - nb)) <= 1e-13 * np.max(np.abs(nb))
+    a.close()
+    b.close()
+
+
+def test_rho_download_between_steps_is_current(lib):
+    """ρ read between iskra_step calls (each read makes the FP64 copy) is the
+    ρ of the latest step: equal to a run that reads only at the end."""
+    a, _ = _slab(lib, -1)
+    b, _ = _slab(lib, -1)
+    seen = []
+    for _ in range(3):
+        a.step(DT, 1, seed=1, rtol=1e-8)
+        seen.append(a.field(lib.FIELD_RHO))
+    b.step(DT, 3, seed=1, rtol=1e-8)
+    assert not np.array_equal(seen[0], seen[2])
+    assert np.array_equal(seen[2], b.field(lib.FIELD_RHO))
+    a.close()
+    b.close()
+
+
+def test_species_pair_push_matches_single_species_pushes(lib):
+    """The step's two-species push launch and one push launch per species
+    (iskra_advance) move every particle to the same bits in the same field."""
+    rng = np.random.default_rng(12)
+    E = np.asfortranarray(rng.standard_normal((N, N, 3)) * 2e4)
+    E[:, :, 2] = 0.0
+    a, sa = _slab(lib, -1)
+    b, sb = _slab(lib, -1)
+    a.upload_E(E)
+    b.upload_E(E)
+    a.step(DT, 1, seed=1, rtol=1e-8)          # the push reads the uploaded E
+    for s in sb:
+        b.advance(s, DT)
+    for s in (0, 1):
+        xa, va, ia = a.download(sa[s])
+        xb, vb, ib = b.download(sb[s])
+        oa, ob = np.argsort(ia), np.argsort(ib)
+        assert np.array_equal(ia[oa], ib[ob])
+        assert np.array_equal(xa[oa], xb[ob]) and np.array_equal(va[oa], vb[ob])
+    a.close()
+    b.close()

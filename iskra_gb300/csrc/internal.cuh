@@ -325,7 +325,9 @@ double poisson_drive_amp(Ctx *c, int g);
 
 // ---- kernels / launchers shared across files ----
 int launch_advance(Ctx *c, int sid, float dt);
-int launch_advance_all(Ctx *c, float dt);  // every species of a step (two in one launch when they can)
+// every species of a step (two in one launch when they can; that launch also
+// advances step_ctr when given, reported through *folded)
+int launch_advance_all(Ctx *c, float dt, unsigned long long *step_ctr, bool *folded);
 int launch_deposit(Ctx *c, int sid);
 int launch_charge_density(Ctx *c);
 int launch_efield_from(Ctx *c, const double *phi);

@@ -493,13 +493,16 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
 // SMs as the first species' tiles drain instead of waiting for a second
 // launch.  Blocks [0, ntiles) first species' tiles, [ntiles, 2 ntiles) the
 // second's, the rest both tails.
+// step_ctr (optional): the step counter, advanced here when no MCC set reads
+// it earlier in the step (saves the step's opening launch).
 template <int MX, int MY>
 __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
     k_push2(SpeciesDev s0, SpeciesDev s1, const float4 *__restrict__ E4, PushParams P0, PushParams P1, int ntiles,
-            int *err) {
+            int *err, unsigned long long *step_ctr) {
   pdl_wait();
   __shared__ PushShared sh;
   const int b = blockIdx.x;
+  if (step_ctr && b == 0 && threadIdx.x == 0) *step_ctr += 1ull;
   if (b < ntiles) {
     push_block<true, MX, MY>(s0, P0, E4, sh, b, 0, 0, err);
   } else if (b < 2 * ntiles) {
@@ -575,8 +578,10 @@ int launch_advance(Ctx *c, int sid, float dt) {
 }
 
 // Every species of a step: two species with the same boundary rules in one
-// launch (k_push2), otherwise one launch each.
-int launch_advance_all(Ctx *c, float dt) {
+// launch (k_push2, which also advances step_ctr when given: *folded), otherwise
+// one launch each.
+int launch_advance_all(Ctx *c, float dt, unsigned long long *step_ctr, bool *folded) {
+  if (folded) *folded = false;
   const int ns = (int)c->species.size();
   if (ns == 2 && c->species[0].bnd[0] == c->species[1].bnd[0] && c->species[0].bnd[1] == c->species[1].bnd[1]) {
     Species &a = c->species[0], &b = c->species[1];
@@ -591,7 +596,7 @@ int launch_advance_all(Ctx *c, float dt) {
     cudaFuncSetAttribute(k_push2<MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,                  \
                          (int)cudaSharedmemCarveoutMaxShared);                                             \
     e = launch_pdl(k_push2<MX, MY>, blocks, ISKRA_PUSH_THREADS, 0, c->stream, a.dev, b.dev,                \
-                   (const float4 *)c->E4, Pa, Pb, c->ntiles, c->d_err);                                    \
+                   (const float4 *)c->E4, Pa, Pb, c->ntiles, c->d_err, step_ctr);                          \
   }
     ISKRA_PUSH2_CASE(0, 0) ISKRA_PUSH2_CASE(0, 1) ISKRA_PUSH2_CASE(0, 2)
     ISKRA_PUSH2_CASE(1, 0) ISKRA_PUSH2_CASE(1, 1) ISKRA_PUSH2_CASE(1, 2)
@@ -601,6 +606,7 @@ int launch_advance_all(Ctx *c, float dt) {
     ISKRA_CUDA(c, cudaGetLastError());
     mark_pushed(a);
     mark_pushed(b);
+    if (folded) *folded = step_ctr != nullptr;
     return ISKRA_OK;
   }
   for (int s = 0; s < ns; s++) {

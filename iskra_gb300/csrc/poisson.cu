@@ -129,6 +129,10 @@ struct Poisson {
 };
 
 constexpr int kPartials = 1024;
+// blocks per SM of the node passes (residuals, conversions); tuned on GB300
+#ifndef ISKRA_RES_BLOCKS_PER_SM
+#define ISKRA_RES_BLOCKS_PER_SM 2
+#endif
 
 void poisson_destroy(Poisson *p) {
   if (!p) return;
@@ -1432,7 +1436,7 @@ static int build_device(Ctx *c, Poisson *P) {
       ISKRA_CUDA(c, cudaMemcpy(P->drive_par, dp.data(), dp.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
   }
-  P->blocks = std::min(kPartials, std::max(1, std::min(c->num_sms * 2, (nn + 255) / 256)));
+  P->blocks = std::min(kPartials, std::max(1, std::min(c->num_sms * ISKRA_RES_BLOCKS_PER_SM, (nn + 255) / 256)));
   // ---- separable factorisation ----
   cudaFree(P->r32);
   cudaFree(P->spec);

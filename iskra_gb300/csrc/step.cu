@@ -88,15 +88,25 @@ int launch_circuit(Ctx *c, double dt) {
 
 // queue one PIC step (async; separable Poisson)
 static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocking_solve) {
-  ISKRA_CUDA(c, launch_pdl(k_step_begin, 1, 1, 0, c->stream, c->d_step));
-  ISKRA_CUDA(c, cudaGetLastError());
   int rc;
-  for (int m = 0; m < (int)c->mccs.size(); m++) {
-    rc = launch_mcc(c, m, dt, seed, c->d_step, 0);
+  if (!c->mccs.empty()) {  // MCC keys read the step counter first
+    ISKRA_CUDA(c, launch_pdl(k_step_begin, 1, 1, 0, c->stream, c->d_step));
+    ISKRA_CUDA(c, cudaGetLastError());
+    for (int m = 0; m < (int)c->mccs.size(); m++) {
+      rc = launch_mcc(c, m, dt, seed, c->d_step, 0);
+      if (rc) return rc;
+    }
+    rc = launch_advance_all(c, (float)dt, nullptr, nullptr);
     if (rc) return rc;
+  } else {  // the push can advance it (nothing reads it before ρ)
+    bool folded = false;
+    rc = launch_advance_all(c, (float)dt, c->d_step, &folded);
+    if (rc) return rc;
+    if (!folded) {
+      ISKRA_CUDA(c, launch_pdl(k_step_begin, 1, 1, 0, c->stream, c->d_step));
+      ISKRA_CUDA(c, cudaGetLastError());
+    }
   }
-  rc = launch_advance_all(c, (float)dt);
-  if (rc) return rc;
   if (c->cir_d) {
     rc = launch_circuit(c, dt);
     if (rc) return rc;

@@ -511,23 +511,25 @@ def main():
         psteps = float(pt.item())
     value = psteps / (ms * 1e-3)
 
-    # roofline of the dominant kernel (fused gather+push+boundary+deposit), timed
-    # live with CUDA events on the library stream, one launch per event pair
+    # roofline of the dominant kernel (fused gather+push+boundary+deposit of both
+    # species in one launch, as in the step), timed live with CUDA events on the
+    # library stream, one launch per event pair
     durs = []
     for rep in range(20):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
-        n_e = ctx.count(se)
+        n_p = ctx.count(se) + ctx.count(si)
         a.record(stream)
-        ctx.advance(se, DT)
+        ctx.advance_all(DT)
         b.record(stream)
         ctx.finalize(se)
+        ctx.finalize(si)
         torch.cuda.synchronize()
-        durs.append((a.elapsed_time(b) * 1e-3, n_e))
+        durs.append((a.elapsed_time(b) * 1e-3, n_p))
     durs = durs[3:]
     t_push = statistics.median(d for d, _ in durs)
     n_push = statistics.median(n for _, n in durs)
-    bytes_launch = 48.0 * n_push + 16.0 * NX * NY
+    bytes_launch = 48.0 * n_push + 2 * 16.0 * NX * NY
     peak, peak_kind = peaks()
     achieved = bytes_launch / t_push / 1e9
     traffic = committed_traffic()
@@ -584,7 +586,7 @@ def main():
                               f"last relres {relres:.2e} in {it} sweep(s)",
                    "sort_every": "per species (automatic)" if SORT_EVERY < 0 else SORT_EVERY},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "k_push (gather+push+discard/wrap+deposit)",
+        "roofline": {"bound": "hbm", "kernel": "k_push2 (both species: gather+push+discard/wrap+deposit)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": t_push * 1e3},

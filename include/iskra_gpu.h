@@ -135,6 +135,10 @@ int iskra_field_download_async(iskra_ctx *ctx, int which, double *out);
  * deposits the pushed particles (cloud_in_cell.jl:1-18) into the species'
  * int64 fixed-point density accumulator, consumed by iskra_density. (async) */
 int iskra_advance(iskra_ctx *ctx, int sid, double dt);
+/* The same for every species (the loop over species of
+ * ParticleInCell.solve, ParticleInCell.jl:113-115); two species with the
+ * same boundary rules are pushed by one launch, as inside iskra_step. (async) */
+int iskra_advance_all(iskra_ctx *ctx, double dt);
 
 /* ---- density(species, grid) = particle_to_grid(wg) ./ cell_volume -------
  * kinetic.jl:53, cloud_in_cell.jl:1-18, RegularGrids.jl:26-38.  Writes the

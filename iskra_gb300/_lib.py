@@ -60,6 +60,7 @@ SIGNATURES = [
     ("iskra_field_download", c_int, [CTX, c_int, dp]),
     ("iskra_field_download_async", c_int, [CTX, c_int, dp]),
     ("iskra_advance", c_int, [CTX, c_int, c_double]),
+    ("iskra_advance_all", c_int, [CTX, c_double]),
     ("iskra_density", c_int, [CTX, c_int, dp]),
     ("iskra_charge_density", c_int, [CTX]),
     ("iskra_set_background", c_int, [CTX, dp]),

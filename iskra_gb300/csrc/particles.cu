@@ -1261,6 +1261,13 @@ int iskra_advance(iskra_ctx *h, int sid, double dt) {
   return launch_advance(c, sid, (float)dt);
 }
 
+int iskra_advance_all(iskra_ctx *h, double dt) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!(dt > 0)) return set_err(c, ISKRA_EINVAL, "dt must be positive");
+  return launch_advance_all(c, (float)dt, nullptr, nullptr);
+}
+
 int iskra_density(iskra_ctx *h, int sid, double *n_out) {
   if (!h) return ISKRA_EINVAL;
   Ctx *c = &h->c;

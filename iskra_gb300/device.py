@@ -156,6 +156,9 @@ class Context:
     def advance(self, sid, dt):
         self._c(self.lib.iskra_advance(self.h, sid, dt))
 
+    def advance_all(self, dt):
+        self._c(self.lib.iskra_advance_all(self.h, dt))
+
     def density(self, sid):
         out = np.zeros((self.nx, self.ny), order="F")
         self._c(self.lib.iskra_density(self.h, sid, _ptr(out)))

@@ -397,22 +397,27 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
       // slices touch few cells in common)
       const long long len = end - begin;
       const long long slice = ((len + nwb * 32 - 1) / (nwb * 32)) * 32;
-      const long long w0 = begin + wib * slice, w1 = min(end, w0 + slice);
+      const long long w0 = begin + wib * slice;
+      // the warp's slice as pointers and a 32-bit count (a tile holds far
+      // fewer than 2^31 slots): 32-bit loop arithmetic
+      const int cnt = (int)max(0LL, min(end, w0 + slice) - w0);
+      float4 *__restrict__ xw = xv + w0;
+      float2 *__restrict__ zw = zc + w0;
       // the records of the next kPushDepth slots are in flight while one is
       // processed (the deposit lengthens an iteration; the loads must not wait)
       float4 qa[kPushDepth];
       float2 qb[kPushDepth];
 #pragma unroll
       for (int k = 0; k < kPushDepth; k++) {
-        const long long q = w0 + 32 * k + lane;
+        const int q = 32 * k + lane;
         qa[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         qb[k] = make_float2(0.f, 0.f);
-        if (q < w1) {
-          qa[k] = ld_stream(xv + q);
-          qb[k] = ld_stream(zc + q);
+        if (q < cnt) {
+          qa[k] = ld_stream(xw + q);
+          qb[k] = ld_stream(zw + q);
         }
       }
-      for (long long base = w0; base < w1; base += 32) {
+      for (int o = 0; o < cnt; o += 32) {
         const float4 a = qa[0];
         const float2 b = qb[0];
 #pragma unroll
@@ -420,13 +425,13 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
           qa[k] = qa[k + 1];
           qb[k] = qb[k + 1];
         }
-        const long long q = base + 32 * kPushDepth + lane;
-        if (q < w1) {
-          qa[kPushDepth - 1] = ld_stream(xv + q);
-          qb[kPushDepth - 1] = ld_stream(zc + q);
+        const int q = o + 32 * kPushDepth + lane;
+        if (q < cnt) {
+          qa[kPushDepth - 1] = ld_stream(xw + q);
+          qb[kPushDepth - 1] = ld_stream(zw + q);
         }
-        push_warp<PUSH, MX, MY, true>(s, xv, zc, base + lane, base + lane < w1, a, b, E4, sh, ox, oy, kWin, kWin,
-                                      P, ab, flags);
+        push_warp<PUSH, MX, MY, true>(s, xw, zw, o + lane, o + lane < cnt, a, b, E4, sh, ox, oy, kWin, kWin, P, ab,
+                                      flags);
       }
       __syncthreads();
       // node sums from the moments of the up to four window cells around each node

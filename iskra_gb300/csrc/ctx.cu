@@ -116,13 +116,12 @@ __global__ void k_download(double *__restrict__ st, long long np, double dx, dou
   st[p + 4 * np] = b.x;
 }
 
-__global__ void k_upload_E(const double *__restrict__ E, int nx, int ny, float2 *E32, float4 *E4, double *E64) {
+__global__ void k_upload_E(const double *__restrict__ E, int nx, int ny, float2 *E32, double *E64) {
   const int nn = nx * ny;
   int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nn) return;
   double ex = E[n], ey = E[n + nn], ez = E[n + 2 * nn];
   E32[n] = make_float2((float)ex, (float)ey);
-  store_corners(E4, nx, ny, n % nx, n / nx, make_float2((float)ex, (float)ey));
   E64[n] = ex;
   E64[n + nn] = ey;
   E64[n + 2 * nn] = ez;
@@ -228,7 +227,6 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
   }
   size_t nn = (size_t)c->nn;
   bool ok = cudaMalloc(&c->E32, nn * sizeof(float2)) == cudaSuccess &&
-            cudaMalloc(&c->E4, nn * 2 * sizeof(float4)) == cudaSuccess &&
             cudaMalloc(&c->E64, nn * 3 * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&c->rho, nn * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&c->vol_inv, nn * sizeof(double)) == cudaSuccess &&
@@ -243,7 +241,6 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
             cudaMalloc(&c->d_scratch, 16 * sizeof(double)) == cudaSuccess;
   if (!ok) return fail(ISKRA_ENOMEM);
   cudaMemsetAsync(c->E32, 0, nn * sizeof(float2), c->stream);
-  cudaMemsetAsync(c->E4, 0, nn * 2 * sizeof(float4), c->stream);
   cudaMemsetAsync(c->E64, 0, nn * 3 * sizeof(double), c->stream);
   cudaMemsetAsync(c->rho, 0, nn * sizeof(double), c->stream);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
@@ -299,7 +296,6 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   cudaFree(c->cir_d);
   cudaFree(c->cir_seen);
   cudaFree(c->E32);
-  cudaFree(c->E4);
   cudaFree(c->E64);
   cudaFree(c->rho);
   cudaFree(c->rho_bg);
@@ -520,7 +516,7 @@ int iskra_field_upload_E(iskra_ctx *h, const double *E) {
   if (rc) return rc;
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   ISKRA_CUDA(c, cudaMemcpyAsync(c->stage, E, (size_t)c->nn * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  k_upload_E<<<(c->nn + 255) / 256, 256, 0, c->stream>>>(c->stage, c->nx, c->ny, c->E32, c->E4, c->E64);
+  k_upload_E<<<(c->nn + 255) / 256, 256, 0, c->stream>>>(c->stage, c->nx, c->ny, c->E32, c->E64);
   c->e_from_phi = false;
   ISKRA_CUDA(c, cudaGetLastError());
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -48,7 +48,6 @@ struct Ens {
   std::vector<EnsMcc> mcc;
   double *rho = nullptr, *x = nullptr;
   float2 *E32 = nullptr;
-  float4 *E4 = nullptr;
   double *amp = nullptr;  // R x ngroups
   int ngroups = 0;
   unsigned long long *d_step = nullptr;
@@ -171,7 +170,7 @@ static int ens_queue_step(Ens *e, double dt) {
       ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[prod].st, R, e->sp[prod].cap, (int)kRunsAppendEnd));
   }
   for (int s = 0; s < (int)e->sp.size(); s++) {
-    int rc = launch_push_runs(c, s, e->sp[s].views, R, e->E4, (float)dt, bpr, e->d_err, st);
+    int rc = launch_push_runs(c, s, e->sp[s].views, R, e->E32, (float)dt, bpr, e->d_err, st);
     if (rc) return ens_err(e, rc, c->err);
   }
   FieldRunsHost H{};
@@ -185,7 +184,6 @@ static int ens_queue_step(Ens *e, double dt) {
   H.rho = e->rho;
   H.x = e->x;
   H.E32 = e->E32;
-  H.E4 = e->E4;
   H.amp = e->amp;
   H.d_step = e->d_step;
   H.dt = dt;
@@ -266,7 +264,6 @@ static void ens_free(Ens *e) {
   cudaFree(e->rho);
   cudaFree(e->x);
   cudaFree(e->E32);
-  cudaFree(e->E4);
   cudaFree(e->amp);
   cudaFree(e->d_step);
   cudaFree(e->d_err);
@@ -375,11 +372,9 @@ int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t cap_per_run, iskra_ens 
   ENS_ALLOC(e->rho, R * nn * sizeof(double));
   ENS_ALLOC(e->x, R * nn * sizeof(double));
   ENS_ALLOC(e->E32, R * nn * sizeof(float2));
-  ENS_ALLOC(e->E4, R * nn * 2 * sizeof(float4));
   cudaMemset(e->rho, 0, R * nn * sizeof(double));
   cudaMemset(e->x, 0, R * nn * sizeof(double));
   cudaMemset(e->E32, 0, R * nn * sizeof(float2));
-  cudaMemset(e->E4, 0, R * nn * 2 * sizeof(float4));
   int rc = poisson_upload_fp64(c);
   if (rc) return fail(rc);
   e->ngroups = poisson_ndrive(c);

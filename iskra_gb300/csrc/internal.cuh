@@ -83,17 +83,15 @@ __device__ __forceinline__ T *pick(T *a, T *b, int cur) {
   return cur ? b : a;
 }
 
-// Per-cell E record of cell (ci, cj) (index ci + nx cj): float4 {E(ci,cj),
-// E(ci+1,cj)} then float4 {E(ci,cj+1), E(ci+1,cj+1)}, so the CIC gather of a
-// particle reads one 32-byte record.  Node (i, j) is a corner of up to four
-// cells; this writes its value into each of them.
-__device__ __forceinline__ void store_corners(float4 *E4, int nx, int ny, int i, int j, float2 e) {
-  float2 *r = reinterpret_cast<float2 *>(E4);
-  const int k = i + nx * j;
-  if (i <= nx - 2 && j <= ny - 2) r[4 * k + 0] = e;
-  if (i >= 1 && j <= ny - 2) r[4 * (k - 1) + 1] = e;
-  if (i <= nx - 2 && j >= 1) r[4 * (k - nx) + 2] = e;
-  if (i >= 1 && j >= 1) r[4 * (k - nx - 1) + 3] = e;
+// The gather's record of cell (ci, cj) (index k = ci + nx cj) from the node
+// field E2 (FP32 {Ex, Ey} per node): float4 {E(ci,cj), E(ci+1,cj)} and float4
+// {E(ci,cj+1), E(ci+1,cj+1)}.  The push stages the records of its window in
+// shared memory from the node values, so the field passes write E once per
+// node (coalesced) instead of into the four cell records around each node.
+__device__ __forceinline__ void cell_record(const float2 *__restrict__ E2, int k, int nx, float4 &r0, float4 &r1) {
+  const float2 a = __ldg(E2 + k), b = __ldg(E2 + k + 1), c = __ldg(E2 + k + nx), d = __ldg(E2 + k + nx + 1);
+  r0 = make_float4(a.x, a.y, b.x, b.y);
+  r1 = make_float4(c.x, c.y, d.x, d.y);
 }
 
 struct Species {
@@ -133,7 +131,6 @@ struct Ctx {
   std::vector<Species> species;
   // fields
   float2 *E32 = nullptr;       // (nx*ny) {Ex, Ey} at the nodes (MCC target term)
-  float4 *E4 = nullptr;        // (nx*ny*2) per cell: the 4 corner fields, gather input
   double *E64 = nullptr;       // (nx*ny*3) download scratch
   bool e_from_phi = false;     // E comes from the last solve (E64 is rebuilt from ϕ on download)
   double *rho = nullptr;       // (nx*ny)
@@ -292,7 +289,6 @@ struct FieldRunsHost {
   double q[kMaxSpecies];
   double *rho, *x;                       // R x nn
   float2 *E32;                           // R x nn
-  float4 *E4;                            // R x 2 nn
   const double *amp;                     // R x ngroups
   const unsigned long long *d_step;
   double dt;
@@ -303,7 +299,7 @@ int upload_particles(Ctx *c, const double *x, const double *v, const uint32_t *i
                      float4 *xv, float2 *zc, uint32_t *idd);
 int download_particles(Ctx *c, const float4 *xv, const float2 *zc, const uint32_t *idd, long long np, double *x,
                        double *v, uint32_t *id, int64_t ld);
-int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float4 *E4, float dt, int blocks_per_run,
+int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float2 *E2, float dt, int blocks_per_run,
                      int *err, cudaStream_t st);
 int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, const SpeciesDev *prod,
                     const uint2 *keys, unsigned long long *counts, const float2 *E32, int nn, int blocks_per_run,

@@ -248,7 +248,7 @@ __device__ __forceinline__ void window_cell(const PushShared &sh, int w, bool ov
 // kWinCells + the global cell index, so runs never mix the two.
 template <bool PUSH, int MX, int MY, bool WIN>
 __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restrict__ zc, long long p, bool valid,
-                                        float4 a, float2 b, const float4 *__restrict__ E4, const PushShared &sh,
+                                        float4 a, float2 b, const float2 *__restrict__ E2, const PushShared &sh,
                                         int ox, int oy, int ww, int wh, const PushParams &P, unsigned ab[4],
                                         int &flags, Moments &m) {
   const int nx = P.nx;
@@ -269,8 +269,7 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
           r1 = sh.e[2 * w + 1];
         } else {
           const int n0 = i0 + nx * j0;
-          r0 = __ldg(E4 + 2 * n0);
-          r1 = __ldg(E4 + 2 * n0 + 1);
+          cell_record(E2, n0, nx, r0, r1);
         }
         // CIC weights and interpolation with explicitly rounded products and
         // fused sums, so that every kernel inlining this code (single species,
@@ -353,10 +352,10 @@ __device__ __forceinline__ void deposit_warp(const SpeciesDev &s, PushShared &sh
 template <bool PUSH, int MX, int MY, bool WIN>
 __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
                                           long long p, bool valid, float4 a, float2 b,
-                                          const float4 *__restrict__ E4, PushShared &sh, int ox, int oy, int ww,
+                                          const float2 *__restrict__ E2, PushShared &sh, int ox, int oy, int ww,
                                           int wh, const PushParams &P, unsigned ab[4], int &flags) {
   Moments m;
-  const int key = push_one<PUSH, MX, MY, WIN>(xv, zc, p, valid, a, b, E4, sh, ox, oy, ww, wh, P, ab, flags, m);
+  const int key = push_one<PUSH, MX, MY, WIN>(xv, zc, p, valid, a, b, E2, sh, ox, oy, ww, wh, P, ab, flags, m);
   deposit_warp<WIN>(s, sh, key, m, P.nx);
 }
 
@@ -367,7 +366,7 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
 // tail_blocks) walks the slots appended since that sort.  Integer sums: the
 // density is the same bit for bit whichever block adds what.
 template <bool PUSH, int MX, int MY>
-__device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams &P, const float4 *__restrict__ E4,
+__device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams &P, const float2 *__restrict__ E2,
                                            PushShared &sh, int tile, int tail_block, int tail_blocks, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
@@ -386,8 +385,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
           const int i = ox + t % kWin, j = oy + t / kWin;
           if (i >= 0 && i < nx - 1 && j >= 0 && j < P.ny - 1) {
             const int n0 = i + nx * j;
-            sh.e[2 * t] = __ldg(E4 + 2 * n0);
-            sh.e[2 * t + 1] = __ldg(E4 + 2 * n0 + 1);
+            cell_record(E2, n0, nx, sh.e[2 * t], sh.e[2 * t + 1]);
           }
         }
         window_clear(sh, t);
@@ -430,7 +428,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
           qa[kPushDepth - 1] = ld_stream(xw + q);
           qb[kPushDepth - 1] = ld_stream(zw + q);
         }
-        push_warp<PUSH, MX, MY, true>(s, xw, zw, o + lane, o + lane < cnt, a, b, E4, sh, ox, oy, kWin, kWin, P, ab,
+        push_warp<PUSH, MX, MY, true>(s, xw, zw, o + lane, o + lane < cnt, a, b, E2, sh, ox, oy, kWin, kWin, P, ab,
                                       flags);
       }
       __syncthreads();
@@ -469,7 +467,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
         a = ld_stream(xv + p);
         b = ld_stream(zc + p);
       }
-      push_warp<PUSH, MX, MY, false>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, 0, 0, P, ab, flags);
+      push_warp<PUSH, MX, MY, false>(s, xv, zc, p, v, a, b, E2, sh, 0, 0, 0, 0, P, ab, flags);
     }
   }
   if (PUSH) {
@@ -485,12 +483,12 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
 
 template <bool PUSH, int MX, int MY>
 __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
-    k_push(SpeciesDev s, const float4 *__restrict__ E4, PushParams P, int ntiles, int *err) {
+    k_push(SpeciesDev s, const float2 *__restrict__ E2, PushParams P, int ntiles, int *err) {
   pdl_wait();
   __shared__ PushShared sh;
   const int b = blockIdx.x;
-  if (b < ntiles) push_block<PUSH, MX, MY>(s, P, E4, sh, b, 0, 0, err);
-  else push_block<PUSH, MX, MY>(s, P, E4, sh, -1, b - ntiles, gridDim.x - ntiles, err);
+  if (b < ntiles) push_block<PUSH, MX, MY>(s, P, E2, sh, b, 0, 0, err);
+  else push_block<PUSH, MX, MY>(s, P, E2, sh, -1, b - ntiles, gridDim.x - ntiles, err);
 }
 
 // Two species in one launch (the step's electrons and ions): their pushes
@@ -502,20 +500,20 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
 // it earlier in the step (saves the step's opening launch).
 template <int MX, int MY>
 __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
-    k_push2(SpeciesDev s0, SpeciesDev s1, const float4 *__restrict__ E4, PushParams P0, PushParams P1, int ntiles,
+    k_push2(SpeciesDev s0, SpeciesDev s1, const float2 *__restrict__ E2, PushParams P0, PushParams P1, int ntiles,
             int *err, unsigned long long *step_ctr) {
   pdl_wait();
   __shared__ PushShared sh;
   const int b = blockIdx.x;
   if (step_ctr && b == 0 && threadIdx.x == 0) *step_ctr += 1ull;
   if (b < ntiles) {
-    push_block<true, MX, MY>(s0, P0, E4, sh, b, 0, 0, err);
+    push_block<true, MX, MY>(s0, P0, E2, sh, b, 0, 0, err);
   } else if (b < 2 * ntiles) {
-    push_block<true, MX, MY>(s1, P1, E4, sh, b - ntiles, 0, 0, err);
+    push_block<true, MX, MY>(s1, P1, E2, sh, b - ntiles, 0, 0, err);
   } else {
     const int tb = b - 2 * ntiles, nt = gridDim.x - 2 * ntiles;
-    push_block<true, MX, MY>(s0, P0, E4, sh, -1, tb, nt, err);
-    push_block<true, MX, MY>(s1, P1, E4, sh, -1, tb, nt, err);
+    push_block<true, MX, MY>(s0, P0, E2, sh, -1, tb, nt, err);
+    push_block<true, MX, MY>(s1, P1, E2, sh, -1, tb, nt, err);
   }
 }
 
@@ -525,7 +523,7 @@ static cudaError_t launch_push_modes(Ctx *c, Species &s, PushParams P, int block
   if (P.mode_x == MX && P.mode_y == MY) {                                                       \
     cudaFuncSetAttribute(k_push<true, MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,  \
                          (int)cudaSharedmemCarveoutMaxShared);                                  \
-    return launch_pdl(k_push<true, MX, MY>, blocks, T, 0, c->stream, s.dev, (const float4 *)c->E4, P,  \
+    return launch_pdl(k_push<true, MX, MY>, blocks, T, 0, c->stream, s.dev, (const float2 *)c->E32, P,  \
                       c->ntiles, c->d_err);                                                     \
   }
   ISKRA_PUSH_CASE(0, 0) ISKRA_PUSH_CASE(0, 1) ISKRA_PUSH_CASE(0, 2)
@@ -601,7 +599,7 @@ int launch_advance_all(Ctx *c, float dt, unsigned long long *step_ctr, bool *fol
     cudaFuncSetAttribute(k_push2<MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,                  \
                          (int)cudaSharedmemCarveoutMaxShared);                                             \
     e = launch_pdl(k_push2<MX, MY>, blocks, ISKRA_PUSH_THREADS, 0, c->stream, a.dev, b.dev,                \
-                   (const float4 *)c->E4, Pa, Pb, c->ntiles, c->d_err, step_ctr);                          \
+                   (const float2 *)c->E32, Pa, Pb, c->ntiles, c->d_err, step_ctr);                          \
   }
     ISKRA_PUSH2_CASE(0, 0) ISKRA_PUSH2_CASE(0, 1) ISKRA_PUSH2_CASE(0, 2)
     ISKRA_PUSH2_CASE(1, 0) ISKRA_PUSH2_CASE(1, 1) ISKRA_PUSH2_CASE(1, 2)
@@ -633,7 +631,7 @@ int launch_deposit(Ctx *c, int sid) {
   P.tiles_x = c->tiles_x;
   cudaFuncSetAttribute(k_push<false, 0, 0>, cudaFuncAttributePreferredSharedMemoryCarveout,
                        (int)cudaSharedmemCarveoutMaxShared);
-  k_push<false, 0, 0><<<push_blocks(c), ISKRA_PUSH_THREADS, 0, c->stream>>>(s.dev, c->E4, P, c->ntiles, c->d_err);
+  k_push<false, 0, 0><<<push_blocks(c), ISKRA_PUSH_THREADS, 0, c->stream>>>(s.dev, c->E32, P, c->ntiles, c->d_err);
   ISKRA_CUDA(c, cudaGetLastError());
   s.acc_valid = true;
   s.acc_zero = false;
@@ -882,7 +880,7 @@ int launch_step_density(Ctx *c) { return finalize(c, true, true); }
 // E = -∇ϕ  (generalized_poisson.jl:398-410)
 // ---------------------------------------------------------------------------
 __global__ void k_efield(const double *__restrict__ phi, int nx, int ny, double idx2, double idx1, double idy2,
-                         double idy1, float2 *__restrict__ E32, float4 *__restrict__ E4, double *__restrict__ E64) {
+                         double idy1, float2 *__restrict__ E32, double *__restrict__ E64) {
   const int nn = nx * ny;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const int i = k % nx, j = k / nx;
@@ -893,10 +891,7 @@ __global__ void k_efield(const double *__restrict__ phi, int nx, int ny, double 
     if (j == 0) ey = (phi[k] - phi[k + nx]) * idy1;
     else if (j == ny - 1) ey = (phi[k - nx] - phi[k]) * idy1;
     else ey = (phi[k - nx] - phi[k + nx]) * idy2;
-    if (E32) {
-      E32[k] = make_float2((float)ex, (float)ey);
-      store_corners(E4, nx, ny, i, j, make_float2((float)ex, (float)ey));
-    }
+    if (E32) E32[k] = make_float2((float)ex, (float)ey);
     E64[k] = ex;
     E64[k + nn] = ey;
     E64[k + 2 * nn] = 0.0;
@@ -908,7 +903,7 @@ int launch_efield_from(Ctx *c, const double *phi) {
   int need = (c->nn + 255) / 256;
   if (need < blocks) blocks = need;
   k_efield<<<blocks, 256, 0, c->stream>>>(phi, c->nx, c->ny, 1.0 / (2 * c->g.dx), 1.0 / c->g.dx,
-                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, c->E32, c->E4, c->E64);
+                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, c->E32, c->E64);
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }
@@ -919,7 +914,7 @@ int launch_efield64(Ctx *c, const double *phi) {
   int need = (c->nn + 255) / 256;
   if (need < blocks) blocks = need;
   k_efield<<<blocks, 256, 0, c->stream>>>(phi, c->nx, c->ny, 1.0 / (2 * c->g.dx), 1.0 / c->g.dx,
-                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, nullptr, nullptr, c->E64);
+                                          1.0 / (2 * c->g.dy), 1.0 / c->g.dy, nullptr, c->E64);
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }
@@ -1109,7 +1104,7 @@ int launch_sort(Ctx *c, int sid) {
 // ---------------------------------------------------------------------------
 template <int MX, int MY>
 __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(const SpeciesDev *__restrict__ runs,
-                                                                          const float4 *__restrict__ E4, int ncell4,
+                                                                          const float2 *__restrict__ E2, int nnode,
                                                                           PushParams P, int *err) {
   pdl_wait();
   __shared__ PushShared sh;
@@ -1118,12 +1113,11 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   const int r = blockIdx.y;
   const SpeciesDev s = runs[r];
   const int nx = P.nx, cx = P.nx - 1, cy = P.ny - 1;
-  E4 += (size_t)r * ncell4;
+  E2 += (size_t)r * nnode;
   for (int t = threadIdx.x; t < cx * cy; t += blockDim.x) {
     const int i = t % cx, j = t / cx;
     const int n0 = i + nx * j;
-    sh.e[2 * t] = __ldg(E4 + 2 * n0);
-    sh.e[2 * t + 1] = __ldg(E4 + 2 * n0 + 1);
+    cell_record(E2, n0, nx, sh.e[2 * t], sh.e[2 * t + 1]);
     window_clear(sh, t);
   }
   __syncthreads();
@@ -1143,7 +1137,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
       a = ld_stream(xv + p);
       b = ld_stream(zc + p);
     }
-    push_warp<true, MX, MY, true>(s, xv, zc, p, v, a, b, E4, sh, 0, 0, cx, cy, P, ab, flags);
+    push_warp<true, MX, MY, true>(s, xv, zc, p, v, a, b, E2, sh, 0, 0, cx, cy, P, ab, flags);
   }
   __syncthreads();
   const int wn = cx + 1;
@@ -1177,7 +1171,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
 }
 
 // Ensemble push of one species (runs: device array of R run views).
-int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float4 *E4, float dt, int blocks_per_run,
+int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float2 *E2, float dt, int blocks_per_run,
                      int *err, cudaStream_t st) {
   Species &s = c->species[sid];
   if ((c->nx - 1) * (c->ny - 1) > kWinCells) return set_err(c, ISKRA_EINVAL, "ensemble grid larger than one window");
@@ -1190,13 +1184,13 @@ int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float
   P.mode_x = s.bnd[0];
   P.mode_y = s.bnd[1];
   P.tiles_x = 0;
-  const int ncell4 = 2 * c->nn;
+  const int nnode = c->nn;
   const dim3 grid(blocks_per_run, R);
 #define ISKRA_PUSH_RUNS_CASE(MX, MY)                                                                           \
   if (P.mode_x == MX && P.mode_y == MY) {                                                                       \
     cudaFuncSetAttribute(k_push_runs<MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,                   \
                          (int)cudaSharedmemCarveoutMaxShared);                                                  \
-    ISKRA_CUDA(c, launch_pdl(k_push_runs<MX, MY>, grid, 256, 0, st, runs, E4, ncell4, P, err));                 \
+    ISKRA_CUDA(c, launch_pdl(k_push_runs<MX, MY>, grid, 256, 0, st, runs, E2, nnode, P, err));                 \
     return ISKRA_OK;                                                                                            \
   }
   ISKRA_PUSH_RUNS_CASE(0, 0) ISKRA_PUSH_RUNS_CASE(0, 1) ISKRA_PUSH_RUNS_CASE(0, 2)

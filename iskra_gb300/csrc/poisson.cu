@@ -337,12 +337,11 @@ __global__ void k_lambda(const double *__restrict__ part, int nparts, double dsu
 }
 
 // Optional E = -∇ϕ output of k_residual (generalized_poisson.jl:398-410):
-// FP32 node values for the MCC target term and per-cell records for the gather.
+// FP32 node values: the MCC target term and, staged per tile, the gather.
 // The node differences are taken in FP64 (ϕ is ~10^2-10^3 V while neighbour
 // differences are ~10^-1 V) and scaled in FP32.
 struct EOut {
   float2 *E32;
-  float4 *E4;
   float idx2, idx1, idy2, idy1;  // 1/(2Δx), 1/Δx, 1/(2Δy), 1/Δy
 };
 
@@ -355,9 +354,7 @@ __device__ __forceinline__ void efield_at(const double *__restrict__ x, int k, i
   if (j == 0) ey = (float)(x[k] - x[k + nx]) * eo.idy1;
   else if (j == ny - 1) ey = (float)(x[k - nx] - x[k]) * eo.idy1;
   else ey = (float)(x[k - nx] - x[k + nx]) * eo.idy2;
-  const float2 e = make_float2(ex, ey);
-  eo.E32[k] = e;
-  store_corners(eo.E4, nx, ny, i, j, e);
+  eo.E32[k] = make_float2(ex, ey);
 }
 
 constexpr int kSmemClasses = 128;  // row-class table held in shared memory up to this size
@@ -516,9 +513,7 @@ __device__ __forceinline__ void efield_df5(float2 xk, float2 xw, float2 xe, floa
   if (j == 0) ey = dif(xk, xn) * eo.idy1;
   else if (j == ny - 1) ey = dif(xs, xk) * eo.idy1;
   else ey = dif(xs, xn) * eo.idy2;
-  const float2 e = make_float2(ex, ey);
-  eo.E32[k] = e;
-  store_corners(eo.E4, nx, ny, i, j, e);
+  eo.E32[k] = make_float2(ex, ey);
 }
 
 // Residual pass of the separable solver on the double-float ϕ: the stencil
@@ -1684,7 +1679,6 @@ static EOut eout(Ctx *c, bool on) {
   EOut e{};
   if (!on) return e;
   e.E32 = c->E32;
-  e.E4 = c->E4;
   e.idx2 = (float)(1.0 / (2 * c->g.dx));
   e.idx1 = (float)(1.0 / c->g.dx);
   e.idy2 = (float)(1.0 / (2 * c->g.dy));
@@ -2137,7 +2131,6 @@ struct FieldRuns {
   const double *vol_inv, *bg;
   double *rho, *x;                       // R x nn
   float2 *E32;                           // R x nn
-  float4 *E4;                            // R x 2 nn
   const double *amp;                     // R x ngroups drive amplitudes
   int ngroups;
   const int *drive_node, *drive_group;
@@ -2271,7 +2264,6 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
   // ϕ and E = -∇ϕ
   EOut eo;
   eo.E32 = F.E32 + o;
-  eo.E4 = F.E4 + 2 * o;
   eo.idx2 = F.idx2;
   eo.idx1 = F.idx1;
   eo.idy2 = F.idy2;
@@ -2309,7 +2301,6 @@ int launch_field_runs(Ctx *c, int R, FieldRunsHost &H, cudaStream_t st) {
   F.rho = H.rho;
   F.x = H.x;
   F.E32 = H.E32;
-  F.E4 = H.E4;
   F.amp = H.amp;
   F.ngroups = P->ndrive;
   F.drive_node = P->drive_node;

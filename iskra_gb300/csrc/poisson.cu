@@ -600,7 +600,9 @@ __global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__
       }
       const float2 rhs = df_add(b, df_neg(afix));
       res = df_add(rhs, df_neg(afree));
-      const double rh = df_value(rhs);
+      // the norms decide convergence to ~1e-7 relative at most: the FP32
+      // value of the pair, squared in FP64 (no overflow)
+      const double rh = (double)(rhs.x + rhs.y);
       b2 = fma(rh, rh, b2);
     } else {
       float2 ax = df_mul(C.c0f, xk);

@@ -35,9 +35,9 @@ struct PushParams {
   int tiles_x;      // tiles per row
 };
 
-// Particle-record loads of the push: read once, so they bypass L1
-// (L1::no_allocate measured 1.5 % faster steps than evict-first loads; the
-// shared-memory window leaves ~28 KB of L1 per SM).
+// Particle-record loads of the unsorted tail and the ensemble push: read
+// once, so they bypass L1 (L1::no_allocate measured 1.5 % faster steps than
+// evict-first loads).
 __device__ __forceinline__ float4 ld_stream(const float4 *p) {
   float4 r;
   asm volatile("ld.global.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
@@ -98,34 +98,23 @@ __device__ __forceinline__ bool reduce_runs(int key, Moments &m, unsigned &n) {
 
 // Move by d cells along one axis in FP32: offset h in [0,1) on the 2^-24 grid,
 // cell index i (int).  Returns the new offset; i is updated in place.
+// Move by d cells along one axis in FP32: offset h in [0,1) on the 2^-24
+// grid, cell index i (int).  t0 = h + d (one rounding), its integer part k
+// moves the cell, the fraction t0 - k goes onto the 2^-24 grid (a fraction
+// that rounds up to 1 carries into the next cell).  Branch-free: in a warp
+// some lane nearly always crosses a cell, and a branch for it would run for
+// all.  Rounded intrinsics: no context-dependent contraction, so every kernel
+// inlining this computes the same bits.  Returns the new offset; i is
+// updated in place and uq receives the offset as an integer (< 2^24).
 __device__ __forceinline__ float move_axis(float h, float d, int &i, unsigned &uq) {
-  const float t0 = __fadd_rn(h, d);  // (rounded ops: no context-dependent contraction)
-  if (t0 >= 0.0f && t0 < 1.0f) {  // stays in its cell: one rounding, then onto the grid
-    int u = __float2int_rn(t0 * kOffScale);
-    if (u >= (1 << 24)) {
-      u -= (1 << 24);
-      i += 1;
-    }
-    uq = (unsigned)u;
-    return (float)u * kOffInv;
-  }
   d = fminf(fmaxf(d, -1.0e9f), 1.0e9f);
-  float fd = floorf(d);
-  float fr = __fsub_rn(d, fd);  // [0,1)
-  float t = __fadd_rn(h, fr);   // [0,2)
-  int carry = 0;
-  if (t >= 1.0f) {
-    t -= 1.0f;
-    carry = 1;
-  }
-  int u = __float2int_rn(t * kOffScale);
-  if (u >= (1 << 24)) {
-    u -= (1 << 24);
-    carry += 1;
-  }
-  i += (int)fd + carry;
-  uq = (unsigned)u;
-  return (float)u * kOffInv;
+  const float t0 = __fadd_rn(h, d);
+  const float k = floorf(t0);
+  const float t = __fsub_rn(t0, k);  // [0, 1]
+  const int u = __float2int_rn(t * kOffScale);
+  i += (int)k + (u >> 24);
+  uq = (unsigned)u & 0xffffffu;
+  return (float)uq * kOffInv;
 }
 
 // after_push along one axis with P = n-1 cells (wrap period (n-1)Δh,
@@ -146,8 +135,8 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 
 // Tile-block size of the push and the minimum resident blocks per SM asked
 // of the register allocator, tuned on GB300: 128-thread blocks, 7 per SM
-// (72 registers) ran the 512x512 slab step 2 % faster than 256 x 5 and
-// 256 x 4, and 192 x 5 8 % slower.  The ensemble push keeps 256 x 5.
+// (at most 72 registers) ran the 512x512 slab step 2 % faster than 256 x 5
+// and 256 x 4, and 192 x 5 8 % slower.  The ensemble push keeps 256 x 5.
 #ifndef ISKRA_PUSH_THREADS
 #define ISKRA_PUSH_THREADS 128
 #endif
@@ -157,11 +146,17 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 #ifndef ISKRA_PUSH_RUNS_MIN_BLOCKS
 #define ISKRA_PUSH_RUNS_MIN_BLOCKS 5
 #endif
-#ifndef ISKRA_PUSH_DEPTH
-#define ISKRA_PUSH_DEPTH 1
+#ifndef ISKRA_PUSH_STAGES
+#define ISKRA_PUSH_STAGES 4
 #endif
-// warp iterations loaded ahead (2, 3 and 4 measured 0.7-5 % slower steps)
-constexpr int kPushDepth = ISKRA_PUSH_DEPTH;
+// Each warp of a tile block streams its slice of particle records through a
+// ring of kStages shared-memory stages filled by asynchronous copies
+// (cp.async): kStages - 1 warp iterations (768 B each) are in flight while
+// one is pushed, without holding registers for them.  With one iteration in
+// flight per warp (register prefetch) the push was bound by the bytes in
+// flight per SM; 4 stages at 7 blocks per SM (64 KB in flight) ran the
+// 512x512 slab step 3.4 % faster, 3 stages (7 or 8 blocks) 3 %.
+constexpr int kStages = ISKRA_PUSH_STAGES;
 
 // Shared-memory window of a tile block: the tile's cells and a kHalo-cell
 // margin (particles drift off their tile between sorts).
@@ -170,69 +165,93 @@ constexpr int kWinN = kWin + 1;          // window nodes per axis
 constexpr int kWinCells = kWin * kWin;
 
 // Per window cell, the deposit moments n, Σu, Σv and Σuv of the particles
-// deposited there (u, v < 2^24; uv = hi 2^24 + lo).  While a cell has taken
-// at most kWinFast particles every sum fits one 32-bit word (256 (2^24 - 1) <
-// 2^32), so a run costs one returning atomic (the count, which decides) and
-// four fire-and-forget ones.  Runs past that bound add to two-word sums: the
-// low word's atomic returns the old value, from which the carry into the high
-// word is known (64-bit shared-memory atomics run at ~1/7 the rate of 32-bit
-// ones on GB300).  A cell holds at most kMaxCell particles, so Σu, Σv < 2^38
-// and Σuv < 2^62.
-enum {
-  kMomN, kMomU, kMomV, kMomQh, kMomQl,                       // one-word sums
-  kMomUlo, kMomUhi, kMomVlo, kMomVhi, kMomQlo, kMomQhi, kMoms  // two-word sums
-};
-constexpr unsigned kWinFast = 256;
+// deposited there (u, v < 2^24, uv < 2^48), each sum kept as 32-bit words
+// of 16-bit pieces: a run of n particles adds Σu >> 16 and Σu & 0xffff,
+// likewise Σv, and Σuv >> 32, (Σuv >> 16) & 0xffff, Σuv & 0xffff.  Every
+// word then stays below (particles of the cell) 2^16, exact for up to 65535
+// particles per cell (k_finalize rejects cells above kMaxCell), and all
+// eight additions of a run are fire-and-forget shared-memory atomics (no
+// returned value to wait for).  A cell holds at most kMaxCell particles, so
+// Σu, Σv < 2^38 and Σuv < 2^62.
+enum { kMomN, kMomU1, kMomU0, kMomV1, kMomV0, kMomQ2, kMomQ1, kMomQ0, kMoms };
 
+// Shared memory of an ensemble-run block: E records of the run's cells.
 struct PushShared {
   float4 e[2 * kWinCells];        // E records of the window cells
   unsigned mom[kMoms][kWinCells];  // deposit moments of the window cells
-  unsigned over;                   // some run went to the two-word sums
 };
 
-// adds v (< 2^64) to the two-word sum (lo, hi)
-__device__ __forceinline__ void add64(unsigned *lo, unsigned *hi, unsigned long long v) {
-  const unsigned vl = (unsigned)v, vh = (unsigned)(v >> 32);
-  const unsigned old = atomicAdd(lo, vl);
-  const unsigned h = vh + (old + vl < old ? 1u : 0u);
-  if (h) atomicAdd(hi, h);
+// Shared memory of a tile block: the warps' record rings, E at the window's
+// nodes (a cell's four corner fields are four 8-byte loads; 3.5 KB instead
+// of 12.8 KB of per-cell records) and the window moments.
+struct TileShared {
+  float4 ra[ISKRA_PUSH_THREADS / 32][kStages][32];  // staged records {hx, hy, vx, vy}
+  float2 rb[ISKRA_PUSH_THREADS / 32][kStages][32];  // staged records {vz, cell}
+  float2 ne[kWinN * kWinN];
+  unsigned mom[kMoms][kWinCells];
+};
+
+// asynchronous global -> shared copies of one lane's record (L2 only for
+// the 16-byte part; the 8-byte form exists only with L1 allocation)
+__device__ __forceinline__ void cp_async_record(float4 *sa, float2 *sb, const float4 *ga, const float2 *gb) {
+  const unsigned da = (unsigned)__cvta_generic_to_shared(sa), db = (unsigned)__cvta_generic_to_shared(sb);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(da), "l"(ga) : "memory");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(db), "l"(gb) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// a run of n particles of window cell `key` with moment sums m
-__device__ __forceinline__ void window_add(PushShared &sh, int key, unsigned n, const Moments &m) {
-  const unsigned old = atomicAdd(&sh.mom[kMomN][key], n);
-  if (old + n <= kWinFast) {
-    atomicAdd(&sh.mom[kMomU][key], m.su);
-    atomicAdd(&sh.mom[kMomV][key], m.sv);
-    atomicAdd(&sh.mom[kMomQh][key], m.hi);
-    atomicAdd(&sh.mom[kMomQl][key], m.lo);
-  } else {
-    sh.over = 1u;
-    add64(&sh.mom[kMomUlo][key], &sh.mom[kMomUhi][key], m.su);
-    add64(&sh.mom[kMomVlo][key], &sh.mom[kMomVhi][key], m.sv);
-    add64(&sh.mom[kMomQlo][key], &sh.mom[kMomQhi][key], ((unsigned long long)m.hi << 24) + m.lo);
-  }
+// E records (corner fields) of window cell (la, lb)
+__device__ __forceinline__ void win_record(const PushShared &sh, int la, int lb, int ww, float4 &r0, float4 &r1) {
+  const int w = la + ww * lb;
+  r0 = sh.e[2 * w];
+  r1 = sh.e[2 * w + 1];
+}
+__device__ __forceinline__ void win_record(const TileShared &sh, int la, int lb, int, float4 &r0, float4 &r1) {
+  const int n = la + kWinN * lb;
+  const float2 a = sh.ne[n], b = sh.ne[n + 1], c = sh.ne[n + kWinN], d = sh.ne[n + kWinN + 1];
+  r0 = make_float4(a.x, a.y, b.x, b.y);
+  r1 = make_float4(c.x, c.y, d.x, d.y);
+}
+
+// a run of n particles of window cell `key` with sums su = Σu, sv = Σv and
+// q = Σuv
+template <class SH>
+__device__ __forceinline__ void window_add(SH &sh, int key, unsigned n, unsigned long long su,
+                                           unsigned long long sv, unsigned long long q) {
+  atomicAdd(&sh.mom[kMomN][key], n);
+  atomicAdd(&sh.mom[kMomU1][key], (unsigned)(su >> 16));
+  atomicAdd(&sh.mom[kMomU0][key], (unsigned)su & 0xffffu);
+  atomicAdd(&sh.mom[kMomV1][key], (unsigned)(sv >> 16));
+  atomicAdd(&sh.mom[kMomV0][key], (unsigned)sv & 0xffffu);
+  atomicAdd(&sh.mom[kMomQ2][key], (unsigned)(q >> 32));
+  atomicAdd(&sh.mom[kMomQ1][key], (unsigned)(q >> 16) & 0xffffu);
+  atomicAdd(&sh.mom[kMomQ0][key], (unsigned)q & 0xffffu);
+}
+template <class SH>
+__device__ __forceinline__ void window_add(SH &sh, int key, unsigned n, const Moments &m) {
+  window_add(sh, key, n, m.su, m.sv, ((unsigned long long)m.hi << 24) + m.lo);
 }
 
 // zeroes the window's moments (threads of the block, before its barrier)
-__device__ __forceinline__ void window_clear(PushShared &sh, int t) {
+template <class SH>
+__device__ __forceinline__ void window_clear(SH &sh, int t) {
 #pragma unroll
   for (int q = 0; q < kMoms; q++) sh.mom[q][t] = 0u;
-  if (t == 0) sh.over = 0u;
 }
 
 // CIC node weights of window cell w: W00 at its lower-left node, W10, W01,
-// W11 (over: some run of the block used the two-word sums; block-uniform)
-__device__ __forceinline__ void window_cell(const PushShared &sh, int w, bool over, unsigned long long W[4]) {
+// W11
+template <class SH>
+__device__ __forceinline__ void window_cell(const SH &sh, int w, unsigned long long W[4]) {
   typedef unsigned long long u64;
   const u64 n = sh.mom[kMomN][w];
-  u64 su = sh.mom[kMomU][w], sv = sh.mom[kMomV][w];
-  u64 UV = ((u64)sh.mom[kMomQh][w] << 24) + sh.mom[kMomQl][w];
-  if (over) {
-    su += ((u64)sh.mom[kMomUhi][w] << 32) | sh.mom[kMomUlo][w];
-    sv += ((u64)sh.mom[kMomVhi][w] << 32) | sh.mom[kMomVlo][w];
-    UV += ((u64)sh.mom[kMomQhi][w] << 32) | sh.mom[kMomQlo][w];
-  }
+  const u64 su = ((u64)sh.mom[kMomU1][w] << 16) + sh.mom[kMomU0][w];
+  const u64 sv = ((u64)sh.mom[kMomV1][w] << 16) + sh.mom[kMomV0][w];
+  const u64 UV = ((u64)sh.mom[kMomQ2][w] << 32) + ((u64)sh.mom[kMomQ1][w] << 16) + sh.mom[kMomQ0][w];
   const u64 U = su << 24, V = sv << 24;
   W[0] = (n << 48) - U - V + UV;
   W[1] = U - UV;
@@ -246,9 +265,9 @@ __device__ __forceinline__ void window_cell(const PushShared &sh, int w, bool ov
 // cells (particles that drifted off the window, the unsorted tail) use the
 // global records and 64-bit atomics.  The deposit key is the window cell, or
 // kWinCells + the global cell index, so runs never mix the two.
-template <bool PUSH, int MX, int MY, bool WIN>
+template <bool PUSH, int MX, int MY, bool WIN, class SH>
 __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restrict__ zc, long long p, bool valid,
-                                        float4 a, float2 b, const float2 *__restrict__ E2, const PushShared &sh,
+                                        float4 a, float2 b, const float2 *__restrict__ E2, const SH &sh,
                                         int ox, int oy, int ww, int wh, const PushParams &P, unsigned ab[4],
                                         int &flags, Moments &m) {
   const int nx = P.nx;
@@ -264,9 +283,7 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
         float4 r0, r1;  // the cell's corner fields
         const int la = i0 - ox, lb = j0 - oy;
         if (WIN && (unsigned)la < (unsigned)ww && (unsigned)lb < (unsigned)wh) {
-          const int w = la + ww * lb;
-          r0 = sh.e[2 * w];
-          r1 = sh.e[2 * w + 1];
+          win_record(sh, la, lb, ww, r0, r1);
         } else {
           const int n0 = i0 + nx * j0;
           cell_record(E2, n0, nx, r0, r1);
@@ -330,8 +347,8 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
 }
 
 // Warp-collective deposit of one particle per lane (key from push_one).
-template <bool WIN>
-__device__ __forceinline__ void deposit_warp(const SpeciesDev &s, PushShared &sh, int key, Moments m, int nx) {
+template <bool WIN, class SH>
+__device__ __forceinline__ void deposit_warp(const SpeciesDev &s, SH &sh, int key, Moments m, int nx) {
   unsigned n;
   if (reduce_runs(key, m, n) && key >= 0) {
     if (WIN && key < kWinCells) {
@@ -349,10 +366,10 @@ __device__ __forceinline__ void deposit_warp(const SpeciesDev &s, PushShared &sh
   }
 }
 
-template <bool PUSH, int MX, int MY, bool WIN>
+template <bool PUSH, int MX, int MY, bool WIN, class SH>
 __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
                                           long long p, bool valid, float4 a, float2 b,
-                                          const float2 *__restrict__ E2, PushShared &sh, int ox, int oy, int ww,
+                                          const float2 *__restrict__ E2, SH &sh, int ox, int oy, int ww,
                                           int wh, const PushParams &P, unsigned ab[4], int &flags) {
   Moments m;
   const int key = push_one<PUSH, MX, MY, WIN>(xv, zc, p, valid, a, b, E2, sh, ox, oy, ww, wh, P, ab, flags, m);
@@ -360,14 +377,15 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
 }
 
 // One block of the push: a tile block (tile >= 0) takes the particles the
-// last sort grouped in its tile: stage the window's E records, push, deposit
-// into the window, then add the window's nonzero node sums and cell counts to
+// last sort grouped in its tile: stage E at the window's nodes, push (each
+// warp a contiguous slice, streamed through its record ring), deposit into
+// the window, then add the window's nonzero node sums and cell counts to
 // the global accumulators.  A tail block (tile < 0, tail_block of
 // tail_blocks) walks the slots appended since that sort.  Integer sums: the
 // density is the same bit for bit whichever block adds what.
 template <bool PUSH, int MX, int MY>
 __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams &P, const float2 *__restrict__ E2,
-                                           PushShared &sh, int tile, int tail_block, int tail_blocks, int *err) {
+                                           TileShared &sh, int tile, int tail_block, int tail_blocks, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
   const int cur = s.st->cur;
@@ -380,16 +398,13 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
     const long long begin = s.tile_begin[tile], end = s.tile_begin[tile + 1];
     if (begin < end) {  // block-uniform
       const int ox = (tile % P.tiles_x) * kTile - kHalo, oy = (tile / P.tiles_x) * kTile - kHalo;
-      for (int t = threadIdx.x; t < kWinCells; t += blockDim.x) {
-        if (PUSH) {
-          const int i = ox + t % kWin, j = oy + t / kWin;
-          if (i >= 0 && i < nx - 1 && j >= 0 && j < P.ny - 1) {
-            const int n0 = i + nx * j;
-            cell_record(E2, n0, nx, sh.e[2 * t], sh.e[2 * t + 1]);
-          }
+      if (PUSH) {
+        for (int t = threadIdx.x; t < kWinN * kWinN; t += blockDim.x) {
+          const int i = ox + t % kWinN, j = oy + t / kWinN;
+          sh.ne[t] = (i >= 0 && i < nx && j >= 0 && j < P.ny) ? __ldg(E2 + i + nx * j) : make_float2(0.f, 0.f);
         }
-        window_clear(sh, t);
       }
+      for (int t = threadIdx.x; t < kWinCells; t += blockDim.x) window_clear(sh, t);
       __syncthreads();
       // each warp takes a contiguous slice of the tile's slots (cell-sorted
       // slices touch few cells in common)
@@ -401,39 +416,31 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
       const int cnt = (int)max(0LL, min(end, w0 + slice) - w0);
       float4 *__restrict__ xw = xv + w0;
       float2 *__restrict__ zw = zc + w0;
-      // the records of the next kPushDepth slots are in flight while one is
-      // processed (the deposit lengthens an iteration; the loads must not wait)
-      float4 qa[kPushDepth];
-      float2 qb[kPushDepth];
+      // prologue: the first kStages - 1 iterations' records in flight
 #pragma unroll
-      for (int k = 0; k < kPushDepth; k++) {
-        const int q = 32 * k + lane;
-        qa[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        qb[k] = make_float2(0.f, 0.f);
-        if (q < cnt) {
-          qa[k] = ld_stream(xw + q);
-          qb[k] = ld_stream(zw + q);
-        }
+      for (int d = 0; d < kStages - 1; d++) {
+        const int q = 32 * d + lane;
+        if (q < cnt) cp_async_record(&sh.ra[wib][d][lane], &sh.rb[wib][d][lane], xw + q, zw + q);
+        cp_async_commit();
       }
+      int st = 0;  // stage of the current iteration
       for (int o = 0; o < cnt; o += 32) {
-        const float4 a = qa[0];
-        const float2 b = qb[0];
-#pragma unroll
-        for (int k = 0; k + 1 < kPushDepth; k++) {
-          qa[k] = qa[k + 1];
-          qb[k] = qb[k + 1];
+        {
+          const int q = o + 32 * (kStages - 1) + lane;
+          const int sn = st == 0 ? kStages - 1 : st - 1;  // the stage read one iteration ago
+          if (q < cnt) cp_async_record(&sh.ra[wib][sn][lane], &sh.rb[wib][sn][lane], xw + q, zw + q);
+          cp_async_commit();
         }
-        const int q = o + 32 * kPushDepth + lane;
-        if (q < cnt) {
-          qa[kPushDepth - 1] = ld_stream(xw + q);
-          qb[kPushDepth - 1] = ld_stream(zw + q);
-        }
+        cp_async_wait<kStages - 1>();  // this lane's copies of the current stage have landed
+        const float4 a = sh.ra[wib][st][lane];
+        const float2 b = sh.rb[wib][st][lane];
+        st = st + 1 == kStages ? 0 : st + 1;
         push_warp<PUSH, MX, MY, true>(s, xw, zw, o + lane, o + lane < cnt, a, b, E2, sh, ox, oy, kWin, kWin, P, ab,
                                       flags);
       }
+      cp_async_wait<0>();
       __syncthreads();
       // node sums from the moments of the up to four window cells around each node
-      const bool over = sh.over != 0u;
       for (int t = threadIdx.x; t < kWinN * kWinN; t += blockDim.x) {
         const int a = t % kWinN, b = t / kWinN;
         unsigned long long v = 0;
@@ -444,7 +451,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
           const int w = ca + kWin * cb;
           if (!sh.mom[kMomN][w]) continue;
           unsigned long long W[4];
-          window_cell(sh, w, over, W);
+          window_cell(sh, w, W);
           v += W[c];
         }
         if (v) atomicAdd(s.acc + (ox + a) + nx * (oy + b), v);
@@ -485,7 +492,7 @@ template <bool PUSH, int MX, int MY>
 __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
     k_push(SpeciesDev s, const float2 *__restrict__ E2, PushParams P, int ntiles, int *err) {
   pdl_wait();
-  __shared__ PushShared sh;
+  __shared__ TileShared sh;
   const int b = blockIdx.x;
   if (b < ntiles) push_block<PUSH, MX, MY>(s, P, E2, sh, b, 0, 0, err);
   else push_block<PUSH, MX, MY>(s, P, E2, sh, -1, b - ntiles, gridDim.x - ntiles, err);
@@ -503,7 +510,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
     k_push2(SpeciesDev s0, SpeciesDev s1, const float2 *__restrict__ E2, PushParams P0, PushParams P1, int ntiles,
             int *err, unsigned long long *step_ctr) {
   pdl_wait();
-  __shared__ PushShared sh;
+  __shared__ TileShared sh;
   const int b = blockIdx.x;
   if (step_ctr && b == 0 && threadIdx.x == 0) *step_ctr += 1ull;
   if (b < ntiles) {
@@ -1141,7 +1148,6 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   }
   __syncthreads();
   const int wn = cx + 1;
-  const bool over = sh.over != 0u;
   for (int t = threadIdx.x; t < (cx + 1) * (cy + 1); t += blockDim.x) {
     const int a = t % wn, b = t / wn;
     unsigned long long v = 0;
@@ -1152,7 +1158,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
       const int w = ca + cx * cb;
       if (!sh.mom[kMomN][w]) continue;
       unsigned long long W[4];
-      window_cell(sh, w, over, W);
+      window_cell(sh, w, W);
       v += W[c];
     }
     if (v) atomicAdd(s.acc + a + nx * b, v);

@@ -134,14 +134,15 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 }
 
 // Tile-block size of the push and the minimum resident blocks per SM asked
-// of the register allocator, tuned on GB300: 128-thread blocks, 7 per SM
-// (at most 72 registers) ran the 512x512 slab step 2 % faster than 256 x 5
-// and 256 x 4, and 192 x 5 8 % slower.  The ensemble push keeps 256 x 5.
+// of the register allocator, tuned on GB300 (interleaved 1000-step runs of
+// the 512x512 slab, ring-staged push): 192-thread blocks, 5 per SM, ran
+// 0.9 % faster than 128 x 7 and 0.2-0.5 % faster than 160 x 6, 256 x 4 and
+// 192 x 6.  The ensemble push keeps 256 x 5.
 #ifndef ISKRA_PUSH_THREADS
-#define ISKRA_PUSH_THREADS 128
+#define ISKRA_PUSH_THREADS 192
 #endif
 #ifndef ISKRA_PUSH_MIN_BLOCKS
-#define ISKRA_PUSH_MIN_BLOCKS 7
+#define ISKRA_PUSH_MIN_BLOCKS 5
 #endif
 #ifndef ISKRA_PUSH_RUNS_MIN_BLOCKS
 #define ISKRA_PUSH_RUNS_MIN_BLOCKS 5
@@ -154,8 +155,9 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 // (cp.async): kStages - 1 warp iterations (768 B each) are in flight while
 // one is pushed, without holding registers for them.  With one iteration in
 // flight per warp (register prefetch) the push was bound by the bytes in
-// flight per SM; 4 stages at 7 blocks per SM (64 KB in flight) ran the
-// 512x512 slab step 3.4 % faster, 3 stages (7 or 8 blocks) 3 %.
+// flight per SM; 4 stages (128-thread blocks, 7 per SM: 64 KB in flight)
+// ran the 512x512 slab step 3.4 % faster, 3 stages 3 %, 5 stages (6
+// blocks per SM) 2.6 %.
 constexpr int kStages = ISKRA_PUSH_STAGES;
 
 // Shared-memory window of a tile block: the tile's cells and a kHalo-cell

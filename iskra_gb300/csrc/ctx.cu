@@ -38,7 +38,7 @@ void invalidate_graphs(Ctx *c) {
 
 int collect_device_errors(Ctx *c) {
   if (c->dl_pending) {  // a synchronising call also completes the non-blocking downloads
-    ISKRA_CUDA(c, cudaEventSynchronize(c->dl_done));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->dl_stream));
     c->dl_pending = false;
   }
   ISKRA_CUDA(c, cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -311,7 +311,8 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   cudaFree(c->stage);
   if (c->dl_stream) cudaStreamSynchronize(c->dl_stream);
   if (c->dl_ready) cudaEventDestroy(c->dl_ready);
-  if (c->dl_done) cudaEventDestroy(c->dl_done);
+  for (int b = 0; b < 2; b++)
+    if (c->dl_done[b]) cudaEventDestroy(c->dl_done[b]);
   if (c->dl_stream) cudaStreamDestroy(c->dl_stream);
   cudaFree(c->dl_stage);
   cudaFree(c->d_step);

@@ -154,11 +154,13 @@ struct Ctx {
   int *scan_tmp = nullptr;
   double *stage = nullptr;     // upload/download staging (device)
   size_t stage_bytes = 0;
-  // non-blocking field downloads: snapshot on the context stream, copy to the
-  // host on dl_stream
-  double *dl_stage = nullptr;            // (nx*ny*3)
+  // non-blocking field downloads: snapshot on the context stream into one of
+  // two staging buffers (alternating), copy to the host on dl_stream
+  double *dl_stage = nullptr;            // 2 x (nx*ny*3)
   cudaStream_t dl_stream = nullptr;
-  cudaEvent_t dl_ready = nullptr, dl_done = nullptr;
+  cudaEvent_t dl_ready = nullptr, dl_done[2] = {nullptr, nullptr};
+  bool dl_used[2] = {false, false};      // dl_done[b] recorded for staging buffer b
+  int dl_next = 0;                       // staging buffer of the next download
   bool dl_pending = false;
   Poisson *ps = nullptr;
   Lws *lws = nullptr;

@@ -2584,30 +2584,44 @@ int iskra_field_download(iskra_ctx *h, int which, double *out) {
 }
 
 // Non-blocking download: the field as the work queued so far leaves it is
-// copied to a device staging buffer on the context stream, then to `out` on
-// a second stream, so the copy overlaps the next queued steps.  `out` (pinned
-// host memory for a true overlap) holds the values after the next
-// synchronising call.  A later download first waits for this one's copy to
-// leave the staging buffer.
+// written to a device staging buffer on the context stream (ϕ of the
+// double-float state converted straight into it), then copied to `out` on a
+// second stream, so the copy overlaps the next queued steps.  Two staging
+// buffers alternate: a download waits only for the copy of the one before
+// last.  `out` (pinned host memory for a true overlap) holds the values after
+// the next synchronising call.
 int iskra_field_download_async(iskra_ctx *h, int which, double *out) {
   if (!h || !out) return ISKRA_EINVAL;
   Ctx *c = &h->c;
-  const double *src = nullptr;
-  size_t n = 0;
-  int rc = field_source(c, which, &src, &n);
-  if (rc) return rc;
+  const size_t cap = (size_t)c->nn * 3;
   if (!c->dl_stage) {
-    ISKRA_CUDA(c, cudaMalloc(&c->dl_stage, (size_t)c->nn * 3 * sizeof(double)));
+    ISKRA_CUDA(c, cudaMalloc(&c->dl_stage, 2 * cap * sizeof(double)));
     ISKRA_CUDA(c, cudaStreamCreateWithFlags(&c->dl_stream, cudaStreamNonBlocking));
     ISKRA_CUDA(c, cudaEventCreateWithFlags(&c->dl_ready, cudaEventDisableTiming));
-    ISKRA_CUDA(c, cudaEventCreateWithFlags(&c->dl_done, cudaEventDisableTiming));
+    for (int b = 0; b < 2; b++) ISKRA_CUDA(c, cudaEventCreateWithFlags(&c->dl_done[b], cudaEventDisableTiming));
   }
-  if (c->dl_pending) ISKRA_CUDA(c, cudaStreamWaitEvent(c->stream, c->dl_done, 0));
-  ISKRA_CUDA(c, cudaMemcpyAsync(c->dl_stage, src, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  const int b = c->dl_next;
+  double *stage = c->dl_stage + (size_t)b * cap;
+  size_t n = 0;
+  Poisson *P = c->ps;
+  if (which == ISKRA_FIELD_PHI && P && P->x && P->df_mode && P->x_stale) {
+    if (c->dl_used[b]) ISKRA_CUDA(c, cudaStreamWaitEvent(c->stream, c->dl_done[b], 0));
+    k_df_to_x<<<P->blocks, 256, 0, c->stream>>>(P->xd, stage, P->nn);
+    ISKRA_CUDA(c, cudaGetLastError());
+    n = (size_t)P->nn;
+  } else {
+    const double *src = nullptr;
+    int rc = field_source(c, which, &src, &n);
+    if (rc) return rc;
+    if (c->dl_used[b]) ISKRA_CUDA(c, cudaStreamWaitEvent(c->stream, c->dl_done[b], 0));
+    ISKRA_CUDA(c, cudaMemcpyAsync(stage, src, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  }
   ISKRA_CUDA(c, cudaEventRecord(c->dl_ready, c->stream));
   ISKRA_CUDA(c, cudaStreamWaitEvent(c->dl_stream, c->dl_ready, 0));
-  ISKRA_CUDA(c, cudaMemcpyAsync(out, c->dl_stage, n * sizeof(double), cudaMemcpyDeviceToHost, c->dl_stream));
-  ISKRA_CUDA(c, cudaEventRecord(c->dl_done, c->dl_stream));
+  ISKRA_CUDA(c, cudaMemcpyAsync(out, stage, n * sizeof(double), cudaMemcpyDeviceToHost, c->dl_stream));
+  ISKRA_CUDA(c, cudaEventRecord(c->dl_done[b], c->dl_stream));
+  c->dl_used[b] = true;
+  c->dl_next = b ^ 1;
   c->dl_pending = true;
   return ISKRA_OK;
 }

@@ -48,6 +48,14 @@ extern "C" {
 #define ISKRA_BND_WRAP 1    /* wrap!    wrap.jl:20-33 */
 #define ISKRA_BND_DISCARD 2 /* discard! wrap.jl:1-18  */
 
+/* Surface kinds of the surface tracker (pic/surfaces/build.jl:8-11,
+ * circuit_coupling.jl:4-16) */
+#define ISKRA_SURF_ABSORB 1   /* AbsorbingSurface: hit! removes the particle      */
+#define ISKRA_SURF_REFLECT 2  /* ReflectiveSurface: mirrors the rest of the step  */
+#define ISKRA_SURF_PERIODIC 3 /* PeriodicSurface: hit! does nothing, tracking ends */
+#define ISKRA_SURF_FIXED 4    /* FixedPotentialElectrode: absorbs                 */
+#define ISKRA_SURF_FLOATING 5 /* FloatingPotentialElectrode: absorbs, σ += q w / area */
+
 /* MCC process types (Chemistry/src/mcc.jl:4-8) */
 #define ISKRA_MCC_ELASTIC_ISOTROPIC 0
 #define ISKRA_MCC_ELASTIC_BACKWARD 1
@@ -112,6 +120,32 @@ int iskra_species_set_boundary(iskra_ctx *ctx, int sid, int mode_x, int mode_y);
 int iskra_species_absorbed(iskra_ctx *ctx, int sid, int64_t counts[4]);
 /* Counting sort by cell + compaction of discarded particles (async). */
 int iskra_species_sort(iskra_ctx *ctx, int sid);
+
+/* ---- surface tracker (pic/surfaces/*.jl, circuit_coupling.jl:45-63) ------
+ * With a tracker, every push (iskra_advance, iskra_advance_all, iskra_step)
+ * runs track! + check! (track.jl:39-52, check.jl:39-68): a particle whose
+ * cell borders a surface edge has its straight path from the old position
+ * with the new velocity walked cell by cell; at a surface edge hit!
+ * (hit.jl:33-56, circuit_coupling.jl:45-63) absorbs it (ABSORB, FIXED,
+ * FLOATING -- the floating electrode's σ dof then gains q w / area before
+ * the step's field solve), reflects it (REFLECT: the rest of the step
+ * mirrored, the normal velocity component flipped, tracking continues) or
+ * ends its tracking (PERIODIC).  after_push (wrap!/discard!) follows.
+ * create_surface_tracker(grid, ds) (build.jl:91-97): the domain walls get
+ * surface kind default_kind (ISKRA_SURF_ABSORB in the reference). */
+int iskra_tracker_create(iskra_ctx *ctx, int default_kind);
+/* track_surface!(tracker, bcs, ss) (build.jl:104-106, build_surface_lookup!
+ * :41-57) and the tracker half of create_electrode (problem/
+ * configuration.jl:22-38): every cell edge whose two end nodes are set in
+ * nodes (nx*ny bytes, Julia layout) becomes surface `kind`, replacing what
+ * the edge had.  FLOATING: sigma_dof (1-based σ dof of the Poisson solver,
+ * add_new_dof) and area (electrode area, configuration.jl:43-51).  *surface
+ * receives the surface's index (0-based). */
+int iskra_tracker_add_surface(iskra_ctx *ctx, const uint8_t *nodes, int kind,
+                              int sigma_dof, double area, int *surface);
+/* Particles of species sid absorbed by `surface` since the tracker was
+ * created (synchronises). */
+int iskra_tracker_hits(iskra_ctx *ctx, int surface, int sid, int64_t *count);
 
 /* ---- fields -------------------------------------------------------------- */
 /* Replaces the device E field used by the gather with a host (nx,ny,3) array

@@ -19,6 +19,7 @@ ERRORS = {
 }
 BND_NONE, BND_WRAP, BND_DISCARD = 0, 1, 2
 FIELD_RHO, FIELD_PHI, FIELD_E = 0, 1, 2
+SURF_ABSORB, SURF_REFLECT, SURF_PERIODIC, SURF_FIXED, SURF_FLOATING = 1, 2, 3, 4, 5
 MCC_ELASTIC_ISOTROPIC, MCC_ELASTIC_BACKWARD, MCC_INELASTIC_BACKWARD, MCC_EXCITATION, MCC_IONIZATION = range(5)
 
 
@@ -56,6 +57,9 @@ SIGNATURES = [
     ("iskra_species_set_boundary", c_int, [CTX, c_int, c_int, c_int]),
     ("iskra_species_absorbed", c_int, [CTX, c_int, i64p]),
     ("iskra_species_sort", c_int, [CTX, c_int]),
+    ("iskra_tracker_create", c_int, [CTX, c_int]),
+    ("iskra_tracker_add_surface", c_int, [CTX, u8p, c_int, c_int, c_double, ip]),
+    ("iskra_tracker_hits", c_int, [CTX, c_int, c_int, i64p]),
     ("iskra_field_upload_E", c_int, [CTX, dp]),
     ("iskra_field_download", c_int, [CTX, c_int, dp]),
     ("iskra_field_download_async", c_int, [CTX, c_int, dp]),

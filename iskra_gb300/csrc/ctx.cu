@@ -276,6 +276,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   ensembles_detach(c);  // ensembles built on this template lose their device state
   lws_destroy_ctx(c);
+  tracker_destroy(c);
   invalidate_graphs(c);
   for (auto &s : c->species) {
     for (int b = 0; b < 2; b++) {

@@ -120,6 +120,23 @@ struct CircuitDev {            // device-resident circuit state (FP64)
   int pad;
 };
 
+// Surface tracker (pic/surfaces/*.jl): per cell (numbered like nodes,
+// i0 + nx j0) the surface behind each of its four edges, in the order of
+// kSurfDir, and whether track! records particles of the cell.
+constexpr int kMaxSurfaces = 64;
+enum { kSurfDirXm, kSurfDirXp, kSurfDirYm, kSurfDirYp };
+struct Tracker {
+  std::vector<unsigned char> edge;       // 4 per cell: surface index + 1, 0 = no surface
+  std::vector<unsigned char> cell;       // 1: the cell is one side of some surface edge
+  std::vector<int> kind;                 // ISKRA_SURF_* per surface
+  std::vector<int> sigma_dof;            // 0-based σ dof (FLOATING), else -1
+  std::vector<double> area;
+  unsigned char *d_edge = nullptr, *d_cell = nullptr, *d_kind = nullptr;
+  unsigned long long *d_hits = nullptr;  // [kMaxSpecies][kMaxSurfaces] absorbed particles
+  unsigned long long *d_seen = nullptr;  // same, already credited to σ
+  bool any_floating = false;
+};
+
 struct Ctx {
   iskra_grid_t g{};
   int nx = 0, ny = 0, nn = 0;
@@ -171,6 +188,7 @@ struct Ctx {
   int cir_pos_ref = -1, cir_neg_ref = -1;  // reference nodes of the electrodes
   int cir_wall = -1;                       // discard wall feeding the floating electrode
   unsigned long long *cir_seen = nullptr;  // absorbed counts already credited
+  Tracker *trk = nullptr;                  // surface tracker (optional)
 
   // step state
   unsigned long long step = 0;  // steps completed by iskra_step
@@ -334,6 +352,8 @@ int launch_sort(Ctx *c, int sid);
 int species_speed2(Ctx *c, int sid, double *mean_v2);  // <vx² + vy²> of the live particles (synchronises)
 int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long long *d_step, uint64_t step_host);
 int launch_circuit(Ctx *c, double dt);
+int launch_surface_charge(Ctx *c);  // σ credit of floating-electrode hits (after a push)
+void tracker_destroy(Ctx *c);
 int poisson_prepare(Ctx *c);
 bool poisson_df_rho(Ctx *c);   // ρ of the next solve may be formed in double-float
 int sync_rho64(Ctx *c);        // FP64 ρ up to date (particles.cu)

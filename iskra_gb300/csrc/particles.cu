@@ -33,6 +33,11 @@ struct PushParams {
   int nx, ny;
   int mode_x, mode_y;
   int tiles_x;      // tiles per row
+  // surface tracker (all nullptr without one)
+  const unsigned char *trk_edge;  // 4 per cell: surface index + 1
+  const unsigned char *trk_cell;  // 1: track! records the cell's particles
+  const unsigned char *trk_kind;  // ISKRA_SURF_* per surface
+  unsigned long long *trk_hits;   // this species' absorbed count per surface
 };
 
 // Particle-record loads of the unsorted tail and the ensemble push: read
@@ -115,6 +120,68 @@ __device__ __forceinline__ float move_axis(float h, float d, int &i, unsigned &u
   i += (int)k + (u >> 24);
   uq = (unsigned)u & 0xffffffu;
   return (float)uq * kOffInv;
+}
+
+// check! (pic/surfaces/check.jl:18-68) of one tracked particle with hit!
+// (hit.jl:33-56, circuit_coupling.jl:45-63): the straight path from the old
+// position (cell i, j; offsets hx, hy) over the step, with the new velocity
+// dX, dY in cells per step, is walked cell by cell.  At an edge without a
+// surface the walk goes on in the next cell; at a surface: PERIODIC ends the
+// walk; REFLECT mirrors the rest of the step on the crossed axis (the
+// reference's px -= v dt'; v_n = -v_n; px += v dt', so dX loses 2 u tau)
+// and goes on from the edge, back on the near side with the flipped
+// velocity (scattered!, hit.jl:17-25); the other kinds absorb.  Returns the
+// absorbing surface or -1.  Times are fractions of the step: the x edge is
+// reached after (1 - hx)/u or hx/|u| (the reference's Δh (1 - hx)/|v_x| over
+// Δt, with Δh = Δy on the y axis).  Ties go to the y edge, as in check.jl:55.
+__device__ __forceinline__ int track_path(const unsigned char *__restrict__ edge, const unsigned char *__restrict__ kinds,
+                                       int nx, int ny, int i, int j, float hx, float hy, float &vx, float &vy,
+                                       float &dX, float &dY) {
+  float ux = dX, uy = dY, tau = 1.0f;
+  for (int it = 0; it < 16; it++) {  // each pass crosses an edge; 16 bounds corner bounces
+    const float tx = ux > 0.f ? __fdiv_rn(1.f - hx, ux) : (ux < 0.f ? __fdiv_rn(hx, -ux) : INFINITY);
+    const float ty = uy > 0.f ? __fdiv_rn(1.f - hy, uy) : (uy < 0.f ? __fdiv_rn(hy, -uy) : INFINITY);
+    if (tau < tx && tau < ty) return -1;  // stays in the cell
+    if (i < 0 || j < 0 || i >= nx - 1 || j >= ny - 1) return -1;  // no surface outside the grid
+    int dir, ni = i, nj = j;
+    float t;
+    if (tx < ty) {
+      t = tx;
+      dir = ux > 0.f ? kSurfDirXp : kSurfDirXm;
+      ni += ux > 0.f ? 1 : -1;
+    } else {
+      t = ty;
+      dir = uy > 0.f ? kSurfDirYp : kSurfDirYm;
+      nj += uy > 0.f ? 1 : -1;
+    }
+    tau -= t;
+    const int s = edge[4 * (i + nx * j) + dir];
+    const bool xedge = dir <= kSurfDirXp;
+    if (xedge) hy = fmaf(uy, t, hy);
+    else hx = fmaf(ux, t, hx);
+    if (s == 0) {  // no surface: on into the next cell
+      if (xedge) hx = ux > 0.f ? 0.f : 1.f;
+      else hy = uy > 0.f ? 0.f : 1.f;
+      i = ni;
+      j = nj;
+      continue;
+    }
+    const int kind = kinds[s - 1];
+    if (kind == ISKRA_SURF_PERIODIC) return -1;
+    if (kind != ISKRA_SURF_REFLECT) return s - 1;
+    if (xedge) {
+      dX = fmaf(-2.f * ux, tau, dX);
+      ux = -ux;
+      vx = -vx;
+      hx = dir == kSurfDirXp ? 1.f : 0.f;
+    } else {
+      dY = fmaf(-2.f * uy, tau, dY);
+      uy = -uy;
+      vy = -vy;
+      hy = dir == kSurfDirYp ? 1.f : 0.f;
+    }
+  }
+  return -1;
 }
 
 // after_push along one axis with P = n-1 cells (wrap period (n-1)Δh,
@@ -267,7 +334,7 @@ __device__ __forceinline__ void window_cell(const SH &sh, int w, unsigned long l
 // cells (particles that drifted off the window, the unsorted tail) use the
 // global records and 64-bit atomics.  The deposit key is the window cell, or
 // kWinCells + the global cell index, so runs never mix the two.
-template <bool PUSH, int MX, int MY, bool WIN, class SH>
+template <bool PUSH, int MX, int MY, bool WIN, bool TRK = false, class SH>
 __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restrict__ zc, long long p, bool valid,
                                         float4 a, float2 b, const float2 *__restrict__ E2, const SH &sh,
                                         int ox, int oy, int ww, int wh, const PushParams &P, unsigned ab[4],
@@ -309,21 +376,30 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
           flags |= DERR_NAN;
           cell = -1;
         } else {
-          hx = move_axis(hx, __fmul_rn(vx, P.dtdx), i0, ux);
-          hy = move_axis(hy, __fmul_rn(vy, P.dtdy), j0, uy);
-          int rx = apply_boundary<MX>(i0, nx - 1);
-          int ry = rx ? 0 : apply_boundary<MY>(j0, P.ny - 1);
-          if (rx == 3 || ry == 3) {
-            flags |= DERR_DOMAIN;
-            cell = -1;
-          } else if (rx) {
-            ab[rx - 1]++;
-            cell = -1;
-          } else if (ry) {
-            ab[ry + 1]++;
+          float dX = __fmul_rn(vx, P.dtdx), dY = __fmul_rn(vy, P.dtdy);
+          int hit = -1;
+          if (TRK && P.trk_cell[i0 + nx * j0])
+            hit = track_path(P.trk_edge, P.trk_kind, nx, P.ny, i0, j0, hx, hy, vx, vy, dX, dY);
+          if (hit >= 0) {  // absorbed by a surface: removed like a discarded particle
+            atomicAdd(P.trk_hits + hit, 1ull);
             cell = -1;
           } else {
-            cell = i0 | (j0 << 16);
+            hx = move_axis(hx, dX, i0, ux);
+            hy = move_axis(hy, dY, j0, uy);
+            int rx = apply_boundary<MX>(i0, nx - 1);
+            int ry = rx ? 0 : apply_boundary<MY>(j0, P.ny - 1);
+            if (rx == 3 || ry == 3) {
+              flags |= DERR_DOMAIN;
+              cell = -1;
+            } else if (rx) {
+              ab[rx - 1]++;
+              cell = -1;
+            } else if (ry) {
+              ab[ry + 1]++;
+              cell = -1;
+            } else {
+              cell = i0 | (j0 << 16);
+            }
           }
         }
         __stcs(xv + p, make_float4(hx, hy, vx, vy));
@@ -368,13 +444,13 @@ __device__ __forceinline__ void deposit_warp(const SpeciesDev &s, SH &sh, int ke
   }
 }
 
-template <bool PUSH, int MX, int MY, bool WIN, class SH>
+template <bool PUSH, int MX, int MY, bool WIN, bool TRK = false, class SH>
 __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
                                           long long p, bool valid, float4 a, float2 b,
                                           const float2 *__restrict__ E2, SH &sh, int ox, int oy, int ww,
                                           int wh, const PushParams &P, unsigned ab[4], int &flags) {
   Moments m;
-  const int key = push_one<PUSH, MX, MY, WIN>(xv, zc, p, valid, a, b, E2, sh, ox, oy, ww, wh, P, ab, flags, m);
+  const int key = push_one<PUSH, MX, MY, WIN, TRK>(xv, zc, p, valid, a, b, E2, sh, ox, oy, ww, wh, P, ab, flags, m);
   deposit_warp<WIN>(s, sh, key, m, P.nx);
 }
 
@@ -385,7 +461,7 @@ __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restric
 // the global accumulators.  A tail block (tile < 0, tail_block of
 // tail_blocks) walks the slots appended since that sort.  Integer sums: the
 // density is the same bit for bit whichever block adds what.
-template <bool PUSH, int MX, int MY>
+template <bool PUSH, int MX, int MY, bool TRK = false>
 __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams &P, const float2 *__restrict__ E2,
                                            TileShared &sh, int tile, int tail_block, int tail_blocks, int *err) {
   const unsigned FULL = 0xffffffffu;
@@ -437,8 +513,8 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
         const float4 a = sh.ra[wib][st][lane];
         const float2 b = sh.rb[wib][st][lane];
         st = st + 1 == kStages ? 0 : st + 1;
-        push_warp<PUSH, MX, MY, true>(s, xw, zw, o + lane, o + lane < cnt, a, b, E2, sh, ox, oy, kWin, kWin, P, ab,
-                                      flags);
+        push_warp<PUSH, MX, MY, true, TRK>(s, xw, zw, o + lane, o + lane < cnt, a, b, E2, sh, ox, oy, kWin, kWin, P,
+                                           ab, flags);
       }
       cp_async_wait<0>();
       __syncthreads();
@@ -476,7 +552,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
         a = ld_stream(xv + p);
         b = ld_stream(zc + p);
       }
-      push_warp<PUSH, MX, MY, false>(s, xv, zc, p, v, a, b, E2, sh, 0, 0, 0, 0, P, ab, flags);
+      push_warp<PUSH, MX, MY, false, TRK>(s, xv, zc, p, v, a, b, E2, sh, 0, 0, 0, 0, P, ab, flags);
     }
   }
   if (PUSH) {
@@ -490,14 +566,16 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
   }
 }
 
-template <bool PUSH, int MX, int MY>
+// TRK: with the surface tracker (a separate instantiation keeps the walk's
+// registers out of the push without one)
+template <bool PUSH, int MX, int MY, bool TRK = false>
 __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
     k_push(SpeciesDev s, const float2 *__restrict__ E2, PushParams P, int ntiles, int *err) {
   pdl_wait();
   __shared__ TileShared sh;
   const int b = blockIdx.x;
-  if (b < ntiles) push_block<PUSH, MX, MY>(s, P, E2, sh, b, 0, 0, err);
-  else push_block<PUSH, MX, MY>(s, P, E2, sh, -1, b - ntiles, gridDim.x - ntiles, err);
+  if (b < ntiles) push_block<PUSH, MX, MY, TRK>(s, P, E2, sh, b, 0, 0, err);
+  else push_block<PUSH, MX, MY, TRK>(s, P, E2, sh, -1, b - ntiles, gridDim.x - ntiles, err);
 }
 
 // Two species in one launch (the step's electrons and ions): their pushes
@@ -507,7 +585,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
 // second's, the rest both tails.
 // step_ctr (optional): the step counter, advanced here when no MCC set reads
 // it earlier in the step (saves the step's opening launch).
-template <int MX, int MY>
+template <int MX, int MY, bool TRK = false>
 __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
     k_push2(SpeciesDev s0, SpeciesDev s1, const float2 *__restrict__ E2, PushParams P0, PushParams P1, int ntiles,
             int *err, unsigned long long *step_ctr) {
@@ -516,24 +594,25 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
   const int b = blockIdx.x;
   if (step_ctr && b == 0 && threadIdx.x == 0) *step_ctr += 1ull;
   if (b < ntiles) {
-    push_block<true, MX, MY>(s0, P0, E2, sh, b, 0, 0, err);
+    push_block<true, MX, MY, TRK>(s0, P0, E2, sh, b, 0, 0, err);
   } else if (b < 2 * ntiles) {
-    push_block<true, MX, MY>(s1, P1, E2, sh, b - ntiles, 0, 0, err);
+    push_block<true, MX, MY, TRK>(s1, P1, E2, sh, b - ntiles, 0, 0, err);
   } else {
     const int tb = b - 2 * ntiles, nt = gridDim.x - 2 * ntiles;
-    push_block<true, MX, MY>(s0, P0, E2, sh, -1, tb, nt, err);
-    push_block<true, MX, MY>(s1, P1, E2, sh, -1, tb, nt, err);
+    push_block<true, MX, MY, TRK>(s0, P0, E2, sh, -1, tb, nt, err);
+    push_block<true, MX, MY, TRK>(s1, P1, E2, sh, -1, tb, nt, err);
   }
 }
 
 static cudaError_t launch_push_modes(Ctx *c, Species &s, PushParams P, int blocks) {
   const int T = ISKRA_PUSH_THREADS;
-#define ISKRA_PUSH_CASE(MX, MY)                                                                 \
-  if (P.mode_x == MX && P.mode_y == MY) {                                                       \
-    cudaFuncSetAttribute(k_push<true, MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,  \
-                         (int)cudaSharedmemCarveoutMaxShared);                                  \
-    return launch_pdl(k_push<true, MX, MY>, blocks, T, 0, c->stream, s.dev, (const float2 *)c->E32, P,  \
-                      c->ntiles, c->d_err);                                                     \
+#define ISKRA_PUSH_CASE(MX, MY)                                                                       \
+  if (P.mode_x == MX && P.mode_y == MY) {                                                             \
+    auto kern = c->trk ? k_push<true, MX, MY, true> : k_push<true, MX, MY, false>;                   \
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                        \
+                         (int)cudaSharedmemCarveoutMaxShared);                                        \
+    return launch_pdl(kern, blocks, T, 0, c->stream, s.dev, (const float2 *)c->E32, P, c->ntiles,     \
+                      c->d_err);                                                                      \
   }
   ISKRA_PUSH_CASE(0, 0) ISKRA_PUSH_CASE(0, 1) ISKRA_PUSH_CASE(0, 2)
   ISKRA_PUSH_CASE(1, 0) ISKRA_PUSH_CASE(1, 1) ISKRA_PUSH_CASE(1, 2)
@@ -553,7 +632,7 @@ static int sort_blocks(Ctx *c, Species &s) {
 }
 
 static PushParams push_params(Ctx *c, const Species &s, float dt) {
-  PushParams P;
+  PushParams P{};
   P.h = (float)(0.5 * (double)dt * (s.q / s.m));
   P.dtdx = (float)((double)dt / c->g.dx);
   P.dtdy = (float)((double)dt / c->g.dy);
@@ -562,6 +641,16 @@ static PushParams push_params(Ctx *c, const Species &s, float dt) {
   P.mode_x = s.bnd[0];
   P.mode_y = s.bnd[1];
   P.tiles_x = c->tiles_x;
+  P.trk_edge = nullptr;
+  P.trk_cell = nullptr;
+  P.trk_kind = nullptr;
+  P.trk_hits = nullptr;
+  if (c->trk) {
+    P.trk_edge = c->trk->d_edge;
+    P.trk_cell = c->trk->d_cell;
+    P.trk_kind = c->trk->d_kind;
+    P.trk_hits = c->trk->d_hits + (size_t)(&s - c->species.data()) * kMaxSurfaces;
+  }
   return P;
 }
 
@@ -586,7 +675,7 @@ int launch_advance(Ctx *c, int sid, float dt) {
   ISKRA_CUDA(c, launch_push_modes(c, s, push_params(c, s, dt), push_blocks(c)));
   ISKRA_CUDA(c, cudaGetLastError());
   mark_pushed(s);
-  return ISKRA_OK;
+  return launch_surface_charge(c);  // hit! of floating electrodes, as part of advance!
 }
 
 // Every species of a step: two species with the same boundary rules in one
@@ -605,10 +694,11 @@ int launch_advance_all(Ctx *c, float dt, unsigned long long *step_ctr, bool *fol
     cudaError_t e = cudaErrorInvalidValue;
 #define ISKRA_PUSH2_CASE(MX, MY)                                                                           \
   if (Pa.mode_x == MX && Pa.mode_y == MY) {                                                                \
-    cudaFuncSetAttribute(k_push2<MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,                  \
+    auto kern = c->trk ? k_push2<MX, MY, true> : k_push2<MX, MY, false>;                                  \
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                             \
                          (int)cudaSharedmemCarveoutMaxShared);                                             \
-    e = launch_pdl(k_push2<MX, MY>, blocks, ISKRA_PUSH_THREADS, 0, c->stream, a.dev, b.dev,                \
-                   (const float2 *)c->E32, Pa, Pb, c->ntiles, c->d_err, step_ctr);                          \
+    e = launch_pdl(kern, blocks, ISKRA_PUSH_THREADS, 0, c->stream, a.dev, b.dev, (const float2 *)c->E32,   \
+                   Pa, Pb, c->ntiles, c->d_err, step_ctr);                                                 \
   }
     ISKRA_PUSH2_CASE(0, 0) ISKRA_PUSH2_CASE(0, 1) ISKRA_PUSH2_CASE(0, 2)
     ISKRA_PUSH2_CASE(1, 0) ISKRA_PUSH2_CASE(1, 1) ISKRA_PUSH2_CASE(1, 2)
@@ -619,7 +709,7 @@ int launch_advance_all(Ctx *c, float dt, unsigned long long *step_ctr, bool *fol
     mark_pushed(a);
     mark_pushed(b);
     if (folded) *folded = step_ctr != nullptr;
-    return ISKRA_OK;
+    return launch_surface_charge(c);
   }
   for (int s = 0; s < ns; s++) {
     int rc = launch_advance(c, s, dt);
@@ -1183,7 +1273,7 @@ int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float
                      int *err, cudaStream_t st) {
   Species &s = c->species[sid];
   if ((c->nx - 1) * (c->ny - 1) > kWinCells) return set_err(c, ISKRA_EINVAL, "ensemble grid larger than one window");
-  PushParams P;
+  PushParams P{};  // no surface tracker in ensembles
   P.h = (float)(0.5 * (double)dt * (s.q / s.m));
   P.dtdx = (float)((double)dt / c->g.dx);
   P.dtdy = (float)((double)dt / c->g.dy);

@@ -2052,6 +2052,13 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
 }
 
 double *poisson_sigma_ptr(Ctx *c) { return c->ps ? c->ps->sigma_d : nullptr; }
+// the device σ values with the operator built (outside stream capture a
+// pending rebuild runs first; a captured step has prepared it already)
+double *poisson_sigma_prepared(Ctx *c) {
+  if (!c->ps) return nullptr;
+  if (c->ps->dirty && poisson_prepare(c) != ISKRA_OK) return nullptr;
+  return c->ps->nsig > 0 ? c->ps->sigma_d : nullptr;
+}
 const double *poisson_x_ptr(Ctx *c) { return c->ps ? c->ps->x : nullptr; }
 const float2 *poisson_xd_ptr(Ctx *c) { return c->ps && c->ps->df_mode ? c->ps->xd : nullptr; }
 bool poisson_warm_args(Ctx *c, WarmArgs *w) {

@@ -128,6 +128,23 @@ class Context:
     def sort(self, sid):
         self._c(self.lib.iskra_species_sort(self.h, sid))
 
+    # -- surface tracker --
+    def tracker_create(self, default_kind=_lib.SURF_ABSORB):
+        self._c(self.lib.iskra_tracker_create(self.h, default_kind))
+
+    def tracker_add_surface(self, nodes, kind, sigma_dof=0, area=0.0):
+        """Edges with both end nodes in `nodes` (bool (nx, ny)) become surface
+        `kind`; returns the surface index."""
+        m = _mask(nodes, self.nx, self.ny)
+        f = c_int(-1)
+        self._c(self.lib.iskra_tracker_add_surface(self.h, _ptr(m, _lib.u8p), kind, sigma_dof, area, byref(f)))
+        return f.value
+
+    def tracker_hits(self, surface, sid):
+        n = c_int64(0)
+        self._c(self.lib.iskra_tracker_hits(self.h, surface, sid, byref(n)))
+        return n.value
+
     # -- fields --
     def upload_E(self, E):
         E = _f64(E, (self.nx, self.ny, 3))

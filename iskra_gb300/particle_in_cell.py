@@ -68,6 +68,126 @@ def _after_push(part, dims, mode):
     part.ctx.set_boundary(part.sid, modes[0], modes[1])
 
 
+# ---- surfaces (pic/surfaces/build.jl:8-25, circuit_coupling.jl:4-16) --------
+class Surface:
+    kind = _lib.SURF_PERIODIC
+
+
+class PeriodicSurface(Surface):
+    """PeriodicSurface: hit! does nothing (hit.jl:26-31); tracking ends."""
+    kind = _lib.SURF_PERIODIC
+
+
+class AbsorbingSurface(Surface):
+    """AbsorbingSurface: hit! removes the particle (hit.jl:33-39)."""
+    kind = _lib.SURF_ABSORB
+
+
+class ReflectiveSurface(Surface):
+    """ReflectiveSurface: hit! mirrors the rest of the step (hit.jl:40-56)."""
+    kind = _lib.SURF_REFLECT
+
+
+@dataclass
+class FixedPotentialElectrode(Surface):
+    """FixedPotentialElectrode (circuit_coupling.jl:4-8): absorbs (:57-63)."""
+    phi: float = 0.0
+    area: float = 0.0
+    kind = _lib.SURF_FIXED
+
+
+@dataclass
+class FloatingPotentialElectrode(Surface):
+    """FloatingPotentialElectrode (circuit_coupling.jl:10-15): absorbs and adds
+    q w / area to its σ dof (:45-55)."""
+    dof: int = 0
+    area: float = 0.0
+    kind = _lib.SURF_FLOATING
+
+
+def create_periodic_surface():
+    return PeriodicSurface()
+
+
+def create_absorbing_surface():
+    return AbsorbingSurface()
+
+
+def create_reflective_surface():
+    return ReflectiveSurface()
+
+
+class SurfaceTracker:
+    """SurfaceTracker{2} (build.jl:13-18) on the device of its grid: every push
+    (advance, solve) walks the particles of cells next to a surface through
+    check! and hit!."""
+
+    def __init__(self, grid, ds):
+        self.ctx = grid.device
+        self.grid = grid
+        self.ctx.tracker_create(ds.kind)
+        self.surfaces = [ds]  # index = device surface index
+
+    def index(self, ss):
+        for k, x in enumerate(self.surfaces):
+            if x is ss:
+                return k
+        raise KeyError("surface not tracked")
+
+    def hits(self, ss, part):
+        """Particles of `part` absorbed by surface `ss` so far."""
+        return self.ctx.tracker_hits(self.index(ss), part.sid)
+
+
+def create_surface_tracker(grid, ds=None):
+    """create_surface_tracker(grid::CartesianGrid{2}, ds=AbsorbingSurface())
+    (build.jl:91-97): the domain walls get surface ds."""
+    return SurfaceTracker(grid, ds if ds is not None else AbsorbingSurface())
+
+
+def track_surface(tracker: SurfaceTracker, bcs, ss: Surface):
+    """track_surface!(tracker, bcs, ss) (build.jl:104-106): cell edges with both
+    end nodes in bcs (bool (nx, ny)) become surface ss."""
+    dof = getattr(ss, "dof", 0) if ss.kind == _lib.SURF_FLOATING else 0
+    area = getattr(ss, "area", 0.0) if ss.kind == _lib.SURF_FLOATING else 0.0
+    f = tracker.ctx.tracker_add_surface(np.asarray(bcs, bool), ss.kind, dof, area)
+    tracker.surfaces.append(ss)
+    assert f == len(tracker.surfaces) - 1
+    return ss
+
+
+def electrode_area(nodes, grid):
+    """calculate_area (problem/configuration.jl:43-51): Δx Δz per node with a
+    node to its +x, Δy Δz per node with a node to its +y (Δz = 1)."""
+    m = np.asarray(nodes, bool)
+    dx, dy = grid.Δh
+    return float(dx * np.count_nonzero(m[:-1, :] & m[1:, :]) + dy * np.count_nonzero(m[:, :-1] & m[:, 1:]))
+
+
+def create_electrode(nodes, config, fixed=False, sigma=0.0, phi=0.0):
+    """create_electrode(nodes, config; fixed, σ, ϕ) (problem/configuration.jl:
+    22-72): a fixed electrode is a Dirichlet node set at ϕ; a floating one a
+    new σ dof with Neumann rows (σ = sigma).  Creates the tracker (absorbing
+    walls) if the config has none and tracks the electrode surface."""
+    from . import finite_difference_method as fdm
+    if config.grid is None or config.solver is None:
+        raise ValueError("create_electrode needs config.grid and config.solver")
+    if config.tracker is None:
+        config.tracker = create_surface_tracker(config.grid)
+    nodes = np.asarray(nodes, bool)
+    area = electrode_area(nodes, config.grid)
+    if fixed:
+        fdm.apply_dirichlet(config.solver, nodes, phi)
+        el = FixedPotentialElectrode(phi=float(phi), area=area)
+    else:
+        dof = fdm.add_new_dof(config.solver, "σ")
+        fdm.apply_neumann(config.solver, nodes, dof)
+        fdm.set_rhs(config.solver, "σ", dof, sigma)
+        el = FloatingPotentialElectrode(dof=dof, area=area)
+    track_surface(config.tracker, nodes, el)
+    return el
+
+
 def advance(part: KineticSpecies, E=None, B=None, dt=1e-5, config=None):
     """advance!(::KineticSpecies, E, B, Δt, config) (ParticleInCell.jl:51-72):
     gather + Boris push + after_push on the device.  E (host (nx,ny,3)) is

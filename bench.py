@@ -299,6 +299,40 @@ def c3_measure(steps, amp=300.0, n=105000):
             "data": "synthetic"}
 
 
+def tracker_measure(w, e, i, steps, ms_plain):
+    """The slab step with a surface tracker (the reference's
+    create_surface_tracker + track_surface!): transparent (periodic) walls, so
+    discard!/wrap! still act as in the plain step, and a reflective 64x64-node
+    block in the middle of the slab (particles in the ~1.6 % of cells next to
+    a surface walk their path; the field solve is unchanged)."""
+    import torch
+    from iskra_gb300 import _lib
+    ctx, se, si = setup_context(w, e, i)
+    ctx.tracker_create(_lib.SURF_PERIODIC)
+    block = np.zeros((NX, NY), bool)
+    block[NX // 2 - 32:NX // 2 + 32, NY // 2 - 32:NY // 2 + 32] = True
+    ctx.tracker_add_surface(block, _lib.SURF_REFLECT)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ctx.step(DT, 5, seed=1, rtol=RTOL)
+    ctx.sync()
+    n0 = ctx.count(se) + ctx.count(si)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ctx.step(DT, steps, seed=1, rtol=RTOL)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ctx.sync()
+    ms = a.elapsed_time(b)
+    n1 = ctx.count(se) + ctx.count(si)
+    ctx.close()
+    return {"metric": "particle-steps/s", "value": 0.5 * (n0 + n1) * steps / (ms * 1e-3), "unit": "particle-steps/s",
+            "ms_per_step": ms / steps, "steps": steps, "step_time_over_plain": (ms / steps) / ms_plain,
+            "workload": WORKLOAD + " + surface tracker (periodic walls, reflective 64x64-node block)",
+            "data": "synthetic"}
+
+
 def c5_measure():
     """Learned warm start of CG step solves (config C5's method at a reduced
     size): the slab (x Dirichlet 0 / 100 V absorbing, y periodic) at 128^2
@@ -433,6 +467,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     ap.add_argument("--no-c4", action="store_true", help="skip the batched-ensemble (C4) leg")
     ap.add_argument("--no-c5", action="store_true", help="skip the learned-warm-start (C5 method) leg")
+    ap.add_argument("--no-tracker", action="store_true", help="skip the surface-tracker leg")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -605,6 +640,8 @@ def main():
         line["batched_c4"] = c4_measure(min(max(args.steps // 5, 20), 200))
         line["plain_c3"] = c3_measure(min(max(args.steps // 5, 20), 200))
         line["batched_over_plain"] = line["batched_c4"]["value"] / line["plain_c3"]["value"]
+    if rank == 0 and not args.no_tracker:
+        line["tracker"] = tracker_measure(w, e, i, min(max(args.steps // 5, 20), 200), ms / args.steps)
     if rank == 0 and not args.no_c5:
         line["learned_warm_start_c5"] = c5_measure()
     if rank == 0 and not args.no_cpu_baseline:

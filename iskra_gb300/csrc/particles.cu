@@ -211,6 +211,9 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 #ifndef ISKRA_PUSH_MIN_BLOCKS
 #define ISKRA_PUSH_MIN_BLOCKS 5
 #endif
+#ifndef ISKRA_PUSH_TRK_MIN_BLOCKS  // the instantiation with a surface tracker
+#define ISKRA_PUSH_TRK_MIN_BLOCKS ISKRA_PUSH_MIN_BLOCKS
+#endif
 #ifndef ISKRA_PUSH_RUNS_MIN_BLOCKS
 #define ISKRA_PUSH_RUNS_MIN_BLOCKS 5
 #endif
@@ -258,6 +261,7 @@ struct TileShared {
   float2 rb[ISKRA_PUSH_THREADS / 32][kStages][32];  // staged records {vz, cell}
   float2 ne[kWinN * kWinN];
   unsigned mom[kMoms][kWinCells];
+  unsigned char trk[kWinCells];  // track! flags of the window cells (with a surface tracker)
 };
 
 // asynchronous global -> shared copies of one lane's record (L2 only for
@@ -279,6 +283,9 @@ __device__ __forceinline__ void win_record(const PushShared &sh, int la, int lb,
   r0 = sh.e[2 * w];
   r1 = sh.e[2 * w + 1];
 }
+// track! flag of window cell w (ensemble blocks run without a tracker)
+__device__ __forceinline__ bool win_tracked(const PushShared &, int) { return false; }
+__device__ __forceinline__ bool win_tracked(const TileShared &sh, int w) { return sh.trk[w] != 0; }
 __device__ __forceinline__ void win_record(const TileShared &sh, int la, int lb, int, float4 &r0, float4 &r1) {
   const int n = la + kWinN * lb;
   const float2 a = sh.ne[n], b = sh.ne[n + 1], c = sh.ne[n + kWinN], d = sh.ne[n + kWinN + 1];
@@ -351,7 +358,8 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
       if (PUSH) {
         float4 r0, r1;  // the cell's corner fields
         const int la = i0 - ox, lb = j0 - oy;
-        if (WIN && (unsigned)la < (unsigned)ww && (unsigned)lb < (unsigned)wh) {
+        const bool inwin = WIN && (unsigned)la < (unsigned)ww && (unsigned)lb < (unsigned)wh;
+        if (inwin) {
           win_record(sh, la, lb, ww, r0, r1);
         } else {
           const int n0 = i0 + nx * j0;
@@ -378,7 +386,7 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
         } else {
           float dX = __fmul_rn(vx, P.dtdx), dY = __fmul_rn(vy, P.dtdy);
           int hit = -1;
-          if (TRK && P.trk_cell[i0 + nx * j0])
+          if (TRK && (inwin ? win_tracked(sh, la + ww * lb) : P.trk_cell[i0 + nx * j0] != 0))
             hit = track_path(P.trk_edge, P.trk_kind, nx, P.ny, i0, j0, hx, hy, vx, vy, dX, dY);
           if (hit >= 0) {  // absorbed by a surface: removed like a discarded particle
             atomicAdd(P.trk_hits + hit, 1ull);
@@ -482,7 +490,13 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
           sh.ne[t] = (i >= 0 && i < nx && j >= 0 && j < P.ny) ? __ldg(E2 + i + nx * j) : make_float2(0.f, 0.f);
         }
       }
-      for (int t = threadIdx.x; t < kWinCells; t += blockDim.x) window_clear(sh, t);
+      for (int t = threadIdx.x; t < kWinCells; t += blockDim.x) {
+        window_clear(sh, t);
+        if (TRK) {
+          const int i = ox + t % kWin, j = oy + t / kWin;
+          sh.trk[t] = (i >= 0 && i < nx - 1 && j >= 0 && j < P.ny - 1) ? P.trk_cell[i + nx * j] : 0;
+        }
+      }
       __syncthreads();
       // each warp takes a contiguous slice of the tile's slots (cell-sorted
       // slices touch few cells in common)
@@ -569,7 +583,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
 // TRK: with the surface tracker (a separate instantiation keeps the walk's
 // registers out of the push without one)
 template <bool PUSH, int MX, int MY, bool TRK = false>
-__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
+__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, TRK ? ISKRA_PUSH_TRK_MIN_BLOCKS : ISKRA_PUSH_MIN_BLOCKS)
     k_push(SpeciesDev s, const float2 *__restrict__ E2, PushParams P, int ntiles, int *err) {
   pdl_wait();
   __shared__ TileShared sh;
@@ -586,7 +600,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
 // step_ctr (optional): the step counter, advanced here when no MCC set reads
 // it earlier in the step (saves the step's opening launch).
 template <int MX, int MY, bool TRK = false>
-__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, ISKRA_PUSH_MIN_BLOCKS)
+__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, TRK ? ISKRA_PUSH_TRK_MIN_BLOCKS : ISKRA_PUSH_MIN_BLOCKS)
     k_push2(SpeciesDev s0, SpeciesDev s1, const float2 *__restrict__ E2, PushParams P0, PushParams P1, int ntiles,
             int *err, unsigned long long *step_ctr) {
   pdl_wait();

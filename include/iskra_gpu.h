@@ -147,6 +147,25 @@ int iskra_tracker_add_surface(iskra_ctx *ctx, const uint8_t *nodes, int kind,
  * created (synchronises). */
 int iskra_tracker_hits(iskra_ctx *ctx, int surface, int sid, int64_t *count);
 
+/* ---- particle sources (pic/sources.jl, problem/configuration.jl:89-93) ----
+ * MaxwellianSource{2,3}(rate, wx, wv; dx, dv) (sources.jl:8-22) feeding
+ * species sid; create_thermalized_beam passes wv = sqrt(2 kB T / m) per
+ * component and dv = the beam velocity.  dx, dv may be NULL (zeros).
+ * *src receives the source index. */
+int iskra_source_create(iskra_ctx *ctx, int sid, double rate, const double wx[2],
+                        const double dx[2], const double wv[3], const double dv[3],
+                        int *src);
+/* sample!(src, species, Δt) (sources.jl:24-34): min(free slots,
+ * floor(rate Δt)) particles appended, x = U(0,1) wx + dx, v = N(0,1) wv + dv,
+ * identifiers continuing the species' counter; init(src, species, Δt)
+ * (ParticleInCell.jl:47-49) is one such call.  Philox keyed by seed and the
+ * call number.  A position outside the grid is ISKRA_EDOMAIN. (async) */
+int iskra_source_sample(iskra_ctx *ctx, int src, double dt, uint64_t seed);
+/* on != 0: iskra_step samples the source at the start of every step, before
+ * the MCC sets (the sources loop of ParticleInCell.solve, :104-106), keyed
+ * by the step's seed and the device step counter. */
+int iskra_source_set_every_step(iskra_ctx *ctx, int src, int on);
+
 /* ---- fields -------------------------------------------------------------- */
 /* Replaces the device E field used by the gather with a host (nx,ny,3) array
  * (the E argument of advance!, ParticleInCell.jl:51-57).  E_z is ignored: the

@@ -60,6 +60,9 @@ SIGNATURES = [
     ("iskra_tracker_create", c_int, [CTX, c_int]),
     ("iskra_tracker_add_surface", c_int, [CTX, u8p, c_int, c_int, c_double, ip]),
     ("iskra_tracker_hits", c_int, [CTX, c_int, c_int, i64p]),
+    ("iskra_source_create", c_int, [CTX, c_int, c_double, dp, dp, dp, dp, ip]),
+    ("iskra_source_sample", c_int, [CTX, c_int, c_double, c_uint64]),
+    ("iskra_source_set_every_step", c_int, [CTX, c_int, c_int]),
     ("iskra_field_upload_E", c_int, [CTX, dp]),
     ("iskra_field_download", c_int, [CTX, c_int, dp]),
     ("iskra_field_download_async", c_int, [CTX, c_int, dp]),

@@ -64,7 +64,7 @@ int collect_device_errors(Ctx *c) {
 // upload / download conversion kernels
 // ---------------------------------------------------------------------------
 // particle_cell (ParticleInCell.jl:28-35) on the upload side: f = 1 + x/Δh,
-// i = floor(f), h = f - i; see k_upload for the quantisation onto the 2^-24 grid.
+// i = floor(f), h = f - i, quantised by cell_of_position.
 __global__ void k_upload(const double *__restrict__ st, long long np, double dx, double dy,
                          int nx, int ny, const uint32_t *__restrict__ ids, float4 *xv,
                          float2 *zc, uint32_t *id, int *err) {
@@ -72,29 +72,16 @@ __global__ void k_upload(const double *__restrict__ st, long long np, double dx,
   if (p >= np) return;
   double X = st[p], Y = st[p + np];
   double vx = st[p + 2 * np], vy = st[p + 3 * np], vz = st[p + 4 * np];
-  // i0 = floor(x/Δh) (particle_cell's i - 1, formed without the 1 + ... that
-  // can round x just below the far wall onto node nx), offset rounded to the
-  // nearest point of the 2^-24 grid; a carry into the next cell is taken
-  // unless that cell does not exist (then the offset stays at 1 - 2^-24), so
-  // a download/upload round trip reproduces the state exactly.
-  const double fx = X / dx, fy = Y / dy;
-  const double ix = floor(fx), jy = floor(fy);
-  long long i0 = (long long)ix, j0 = (long long)jy;
-  long long ux = llrint((fx - ix) * 16777216.0), uy = llrint((fy - jy) * 16777216.0);
-  if (ux >= 16777216LL) {
-    if (i0 + 1 <= nx - 2) { i0 += 1; ux = 0; } else { ux = 16777215LL; }
-  }
-  if (uy >= 16777216LL) {
-    if (j0 + 1 <= ny - 2) { j0 += 1; uy = 0; } else { uy = 16777215LL; }
-  }
+  long long ux, uy;
+  const int c = cell_of_position(X, Y, dx, dy, nx, ny, ux, uy);
   int cell = -1;
   bool finite = isfinite(X) && isfinite(Y) && isfinite(vx) && isfinite(vy) && isfinite(vz);
   if (!finite) {
     atomicOr(err, DERR_NAN);
-  } else if (i0 < 0 || j0 < 0 || i0 > nx - 2 || j0 > ny - 2) {
+  } else if (c < 0) {
     atomicOr(err, DERR_DOMAIN);
   } else {
-    cell = (int)(i0 | (j0 << 16));
+    cell = c;
   }
   xv[p] = make_float4((float)ux * kOffInv, (float)uy * kOffInv, (float)vx, (float)vy);
   zc[p] = make_float2((float)vz, __int_as_float(cell));
@@ -277,6 +264,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   ensembles_detach(c);  // ensembles built on this template lose their device state
   lws_destroy_ctx(c);
   tracker_destroy(c);
+  sources_destroy(c);
   invalidate_graphs(c);
   for (auto &s : c->species) {
     for (int b = 0; b < 2; b++) {

@@ -94,6 +94,88 @@ __device__ __forceinline__ void cell_record(const float2 *__restrict__ E2, int k
   r1 = make_float4(c.x, c.y, d.x, d.y);
 }
 
+// ---- Philox4x32-10 (Salmon et al., SC'11), counter-based: the MCC and the
+// particle sources key it by (seed, stream, step, particle) ------------------
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// uniform in [0,1) with 24 random bits
+__device__ __forceinline__ float u01(uint32_t v) { return (float)(v >> 8) * 5.9604644775390625e-08f; }
+
+struct Stream {
+  U4 ctr;
+  uint32_t k0, k1;
+  U4 buf;
+  int left;
+  __device__ float next() {
+    if (left == 0) {
+      buf = philox4x32_10(ctr, k0, k1);
+      ctr.w += 1;
+      left = 4;
+    }
+    uint32_t v = left == 4 ? buf.x : left == 3 ? buf.y : left == 2 ? buf.z : buf.w;
+    left--;
+    return u01(v);
+  }
+  __device__ float normal() {  // Box-Muller (one of the pair)
+    float a = next();
+    float b = next();
+    a = fmaxf(a, 1.0e-12f);
+    float rad = sqrtf(-2.0f * logf(a));
+    return rad * cospif(2.0f * b);
+  }
+};
+
+
+// particle_cell (ParticleInCell.jl:28-35) on the device side of an upload or a
+// source: i0 = floor(x/Δh) (the reference's i - 1, formed without the 1 + ...
+// that can round x just below the far wall onto node nx), the offset rounded
+// to the nearest point of the 2^-24 grid; a carry into the next cell is taken
+// unless that cell does not exist (then the offset stays at 1 - 2^-24), so a
+// download/upload round trip reproduces the state.  Returns the packed cell
+// (i0 | j0 << 16) or -1 outside the grid.
+__device__ __forceinline__ int cell_of_position(double X, double Y, double dx, double dy, int nx, int ny,
+                                                 long long &ux, long long &uy) {
+  const double fx = X / dx, fy = Y / dy;
+  const double ix = floor(fx), jy = floor(fy);
+  long long i0 = (long long)ix, j0 = (long long)jy;
+  ux = llrint((fx - ix) * 16777216.0);
+  uy = llrint((fy - jy) * 16777216.0);
+  if (ux >= 16777216LL) {
+    if (i0 + 1 <= nx - 2) {
+      i0 += 1;
+      ux = 0;
+    } else {
+      ux = 16777215LL;
+    }
+  }
+  if (uy >= 16777216LL) {
+    if (j0 + 1 <= ny - 2) {
+      j0 += 1;
+      uy = 0;
+    } else {
+      uy = 16777215LL;
+    }
+  }
+  if (i0 < 0 || j0 < 0 || i0 > nx - 2 || j0 > ny - 2) return -1;
+  return (int)(i0 | (j0 << 16));
+}
+
 struct Species {
   double q = 0, m = 0, w0 = 0;
   long long cap = 0;
@@ -189,6 +271,7 @@ struct Ctx {
   int cir_wall = -1;                       // discard wall feeding the floating electrode
   unsigned long long *cir_seen = nullptr;  // absorbed counts already credited
   Tracker *trk = nullptr;                  // surface tracker (optional)
+  void *sources = nullptr;                 // particle sources (source.cu)
 
   // step state
   unsigned long long step = 0;  // steps completed by iskra_step
@@ -354,6 +437,8 @@ int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long lo
 int launch_circuit(Ctx *c, double dt);
 int launch_surface_charge(Ctx *c);  // σ credit of floating-electrode hits (after a push)
 void tracker_destroy(Ctx *c);
+int launch_step_sources(Ctx *c, double dt, uint64_t seed);  // sources sampled every step
+void sources_destroy(Ctx *c);
 int poisson_prepare(Ctx *c);
 bool poisson_df_rho(Ctx *c);   // ρ of the next solve may be formed in double-float
 int sync_rho64(Ctx *c);        // FP64 ρ up to date (particles.cu)

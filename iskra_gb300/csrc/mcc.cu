@@ -80,52 +80,6 @@ void mcc_destroy(Mcc *m) {
   delete m;
 }
 
-// ---- Philox4x32-10 ----------------------------------------------------------
-struct U4 {
-  uint32_t x, y, z, w;
-};
-
-__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
-  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
-  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
-#pragma unroll
-  for (int r = 0; r < 10; r++) {
-    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
-    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
-    k0 += W0;
-    k1 += W1;
-  }
-  return c;
-}
-
-// uniform in [0,1) with 24 random bits
-__device__ __forceinline__ float u01(uint32_t v) { return (float)(v >> 8) * 5.9604644775390625e-08f; }
-
-struct Stream {
-  U4 ctr;
-  uint32_t k0, k1;
-  U4 buf;
-  int left;
-  __device__ float next() {
-    if (left == 0) {
-      buf = philox4x32_10(ctr, k0, k1);
-      ctr.w += 1;
-      left = 4;
-    }
-    uint32_t v = left == 4 ? buf.x : left == 3 ? buf.y : left == 2 ? buf.z : buf.w;
-    left--;
-    return u01(v);
-  }
-  __device__ float normal() {  // Box-Muller (one of the pair)
-    float a = next();
-    float b = next();
-    a = fmaxf(a, 1.0e-12f);
-    float rad = sqrtf(-2.0f * logf(a));
-    return rad * cospif(2.0f * b);
-  }
-};
-
 // ---- kinematics (mcc.jl:53-229) -------------------------------------------
 // euler_angles (mcc.jl:89-106): cosθ = v_z/|v|, sinθ = sqrt(1 - cos²θ),
 // cosϕ = v_x/|v|/sinθ, sinϕ = v_y/|v|/sinθ.  The same angles are formed here

@@ -88,7 +88,8 @@ int launch_circuit(Ctx *c, double dt) {
 
 // queue one PIC step (async; separable Poisson)
 static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocking_solve) {
-  int rc;
+  int rc = launch_step_sources(c, dt, seed);  // sample! of every source (ParticleInCell.jl:104-106)
+  if (rc) return rc;
   if (!c->mccs.empty()) {  // MCC keys read the step counter first
     ISKRA_CUDA(c, launch_pdl(k_step_begin, 1, 1, 0, c->stream, c->d_step));
     ISKRA_CUDA(c, cudaGetLastError());

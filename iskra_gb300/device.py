@@ -140,6 +140,24 @@ class Context:
         self._c(self.lib.iskra_tracker_add_surface(self.h, _ptr(m, _lib.u8p), kind, sigma_dof, area, byref(f)))
         return f.value
 
+    # -- particle sources --
+    def source_create(self, sid, rate, wx, wv, dx=None, dv=None):
+        """MaxwellianSource{2,3}(rate, wx, wv; dx, dv) feeding species sid."""
+        arr = lambda a, n: np.ascontiguousarray(np.broadcast_to(np.asarray(a, float).ravel(), (n,)))
+        wx_, wv_ = arr(wx, 2), arr(wv, 3)
+        dx_ = arr(dx if dx is not None else 0.0, 2)
+        dv_ = arr(dv if dv is not None else 0.0, 3)
+        k = c_int(-1)
+        self._c(self.lib.iskra_source_create(self.h, sid, float(rate), _ptr(wx_), _ptr(dx_), _ptr(wv_), _ptr(dv_),
+                                             byref(k)))
+        return k.value
+
+    def source_sample(self, src, dt, seed=0):
+        self._c(self.lib.iskra_source_sample(self.h, src, dt, seed))
+
+    def source_every_step(self, src, on=True):
+        self._c(self.lib.iskra_source_set_every_step(self.h, src, int(bool(on))))
+
     def tracker_hits(self, surface, sid):
         n = c_int64(0)
         self._c(self.lib.iskra_tracker_hits(self.h, surface, sid, byref(n)))

@@ -68,6 +68,56 @@ def _after_push(part, dims, mode):
     part.ctx.set_boundary(part.sid, modes[0], modes[1])
 
 
+# ---- sources (pic/sources.jl, problem/configuration.jl:89-93) ----------------
+KB = 1.380649e-23
+
+
+class MaxwellianSource:
+    """MaxwellianSource{2,3}(rate, wx, wv; dx, dv) (sources.jl:8-22).  The
+    device object is created when the source is first sampled for a species."""
+
+    def __init__(self, rate, wx, wv, dx=None, dv=None):
+        self.rate = float(rate)
+        self.wx = np.asarray(wx, float).ravel()
+        self.wv = np.asarray(wv, float).ravel()
+        self.dx = np.zeros(2) if dx is None else np.asarray(dx, float).ravel()
+        self.dv = np.zeros(3) if dv is None else np.asarray(dv, float).ravel()
+        self.species = None
+        self.index = None
+
+    def _bind(self, species):
+        if self.index is None:
+            self.species = species
+            self.index = species.ctx.source_create(species.sid, self.rate, self.wx, self.wv, self.dx, self.dv)
+        elif species is not self.species:
+            raise ValueError("a source feeds one species")
+        return self.index
+
+
+def thermal_speed(T, m):
+    """thermal_speed (problem/configuration.jl:80-82): sqrt(2 kB T / m)."""
+    return np.sqrt(2 * KB * T / m)
+
+
+def create_thermalized_beam(species, x, vb, dx=None, T=300.0, rate=1.0):
+    """create_thermalized_beam (problem/configuration.jl:89-93)."""
+    vth = thermal_speed(T, species.m) * np.ones(3)
+    src = MaxwellianSource(rate, x, vth, dx=dx, dv=vb)
+    src.species = species
+    return src
+
+
+def sample(src: MaxwellianSource, species, dt, seed=0):
+    """sample!(src, species, Δt) (sources.jl:24-34) on the device."""
+    k = src._bind(species)
+    species.ctx.source_sample(k, dt, seed)
+
+
+def init(src: MaxwellianSource, species, dt, seed=0):
+    """init(src, species, Δt) (ParticleInCell.jl:47-49)."""
+    sample(src, species, dt, seed)
+
+
 # ---- surfaces (pic/surfaces/build.jl:8-25, circuit_coupling.jl:4-16) --------
 class Surface:
     kind = _lib.SURF_PERIODIC
@@ -229,5 +279,9 @@ def solve(config: Config, dt=1e-5, timesteps=200, seed=0, rtol=1e-8, background=
     ctx = config.grid.device
     if background is not None:
         ctx.set_background(background)
+    for src in config.sources:  # sampled at the start of every step (:104-106)
+        if src.species is None:
+            raise ValueError("a source in config.sources needs its species (create_thermalized_beam)")
+        ctx.source_every_step(src._bind(src.species), True)
     ctx.step(dt, int(timesteps), seed, rtol)
     ctx.sync()

@@ -333,6 +333,39 @@ def tracker_measure(w, e, i, steps, ms_plain):
             "data": "synthetic"}
 
 
+def source_measure(reps=10):
+    """Device particle source (sample! of a MaxwellianSource, pic/sources.jl:
+    24-34): 4M particles appended to an empty species per sample, timed with
+    CUDA events; bytes written per particle 28 (record, cell word, id)."""
+    import torch
+    from iskra_gb300 import _lib
+    from iskra_gb300.device import Context
+    n = NP
+    ctx = Context(NX, NY, DX, DX, (0, 0, 0, 0))
+    sid = ctx.species_create(-QE, ME, 1.0, n)
+    L = (NX - 1) * DX
+    src = ctx.source_create(sid, n / DT, [L, L], [1e5, 1e5, 1e5])
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ts = []
+    for r in range(reps):
+        ctx.upload(sid, np.zeros((0, 2), order="F"), np.zeros((0, 3), order="F"))
+        ctx.sync()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.source_sample(src, DT, seed=r)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b) * 1e-3)
+    assert ctx.count(sid) == n
+    ctx.close()
+    t = float(np.median(ts[2:]))
+    return {"metric": "particles/s", "value": n / t, "unit": "particles/s", "particles_per_sample": n,
+            "ms_per_sample": t * 1e3, "achieved_gbs": 28.0 * n / t / 1e9,
+            "workload": "MaxwellianSource sample! of 4M particles over the 512x512 slab", "data": "synthetic"}
+
+
 def c5_measure():
     """Learned warm start of CG step solves (config C5's method at a reduced
     size): the slab (x Dirichlet 0 / 100 V absorbing, y periodic) at 128^2
@@ -642,6 +675,7 @@ def main():
         line["batched_over_plain"] = line["batched_c4"]["value"] / line["plain_c3"]["value"]
     if rank == 0 and not args.no_tracker:
         line["tracker"] = tracker_measure(w, e, i, min(max(args.steps // 5, 20), 200), ms / args.steps)
+        line["source"] = source_measure()
     if rank == 0 and not args.no_c5:
         line["learned_warm_start_c5"] = c5_measure()
     if rank == 0 and not args.no_cpu_baseline:

@@ -267,6 +267,29 @@ int iskra_mcc_perform(iskra_ctx *ctx, int mid, double dt, uint64_t seed,
 /* Accepted collisions per process since the last call (reset after). */
 int iskra_mcc_counts(iskra_ctx *ctx, int mid, int64_t *counts);
 
+/* ---- DSMC (Chemistry/src/dsmc.jl) ----------------------------------------
+ * DSMC.ElasticCollision(rate, source, target) of dsmc(@reactions ...)
+ * (dsmc.jl:1-13, :140-166) between two kinetic species (source may equal
+ * target): rate is the CrossSection with nodes (g[k], sigma[k]), k < n, g
+ * increasing (cross_section.jl:8-16: linear, flat outside).  *set receives
+ * the set's index. */
+int iskra_dsmc_create(iskra_ctx *ctx, int source, int target, const double *g,
+                      const double *sigma, int n, int *set);
+/* PIC.perform!(dsmc, E, Δt, config) (dsmc.jl:86-138) for one set: per cell
+ * Nc = na Nb Δt σgmax / (Pab + (Wb/Wa) Pba) (x2 for two species) plus the
+ * carried remainder, floor(Nc) random pairs accepted with probability
+ * σ(g) g / σgmax and scattered isotropically in the CM frame
+ * (perform!(::ElasticCollision), :31-84).  Philox keyed by (seed, set,
+ * step, cell).  iskra_step performs every set each step, after the MCC
+ * sets and before the push, keyed by the device step counter. (async) */
+int iskra_dsmc_perform(iskra_ctx *ctx, int set, double dt, uint64_t seed,
+                       uint64_t step);
+/* collisions_remaining (nx*ny FP64) and the accepted collisions of the last
+ * perform! per cell (nx*ny, the "nuDSMC" field); either may be NULL.
+ * Cells are numbered like nodes: the reference's cell (i, j) is entry
+ * (i-1) + nx (j-1). (synchronises) */
+int iskra_dsmc_state(iskra_ctx *ctx, int set, double *remaining, uint32_t *nu);
+
 /* ---- RLC circuit (Circuit/src/Circuit.jl, circuit_coupling.jl) ---------- */
 /* rlc(@netlist ...) with V(t) = amp*sin(2π f t) + dc, coupled to the σ dof
  * of a floating electrode (positive) and a grounded node set (negative), as a

@@ -63,6 +63,9 @@ SIGNATURES = [
     ("iskra_source_create", c_int, [CTX, c_int, c_double, dp, dp, dp, dp, ip]),
     ("iskra_source_sample", c_int, [CTX, c_int, c_double, c_uint64]),
     ("iskra_source_set_every_step", c_int, [CTX, c_int, c_int]),
+    ("iskra_dsmc_create", c_int, [CTX, c_int, c_int, dp, dp, c_int, ip]),
+    ("iskra_dsmc_perform", c_int, [CTX, c_int, c_double, c_uint64, c_uint64]),
+    ("iskra_dsmc_state", c_int, [CTX, c_int, dp, u32p]),
     ("iskra_field_upload_E", c_int, [CTX, dp]),
     ("iskra_field_download", c_int, [CTX, c_int, dp]),
     ("iskra_field_download_async", c_int, [CTX, c_int, dp]),

@@ -92,3 +92,37 @@ def perform(m: MonteCarloCollisions, E, dt, config=None, seed=0):
 
 def collision_counts(m: MonteCarloCollisions):
     return m.ctx.mcc_counts(m.mid, m.N)
+
+
+class DirectSimulationMonteCarlo:
+    """DirectSimulationMonteCarlo (dsmc.jl:15-22) of elastic collisions
+    (DSMC.ElasticCollision, dsmc.jl:1-13) between kinetic species; one device
+    set per collision."""
+
+    def __init__(self, collisions):
+        self.collisions = collisions
+        self.sets = []
+        for r in collisions:
+            if r.products and any(p is not r.source and p is not r.target for p in r.products):
+                raise ValueError("DSMC: only elastic collisions (the reference implements no other perform!)")
+            ctx = r.source.ctx
+            self.sets.append(ctx.dsmc_create(r.source.sid, r.target.sid, r.rate.nodes[:, 0], r.rate.nodes[:, 1]))
+        self.ctx = collisions[0].source.ctx
+        self.step = 0
+
+    def nu(self):
+        """The "nuDSMC" field of the last perform (sum over the collisions)."""
+        return sum(self.ctx.dsmc_state(k)[1].astype(np.int64) for k in self.sets)
+
+
+def dsmc(reactions):
+    """dsmc(@reactions ...) (dsmc.jl:140-166): a Reaction per collision with
+    kinetic source and target species."""
+    return DirectSimulationMonteCarlo(list(reactions))
+
+
+def perform_dsmc(d: DirectSimulationMonteCarlo, E, dt, config=None, seed=0):
+    """PIC.perform!(::DirectSimulationMonteCarlo, E, Δt, config) (dsmc.jl:86-138)."""
+    d.step += 1
+    for k in d.sets:
+        d.ctx.dsmc_perform(k, dt, seed, d.step)

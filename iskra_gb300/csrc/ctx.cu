@@ -265,6 +265,7 @@ int iskra_ctx_destroy(iskra_ctx *h) {
   lws_destroy_ctx(c);
   tracker_destroy(c);
   sources_destroy(c);
+  dsmc_destroy(c);
   invalidate_graphs(c);
   for (auto &s : c->species) {
     for (int b = 0; b < 2; b++) {

@@ -142,6 +142,34 @@ struct Stream {
 };
 
 
+// CrossSection: linear interpolation, flat extrapolation (cross_section.jl:8-14)
+// The bracket e[lo] <= x < e[lo+1] is found by bisection, or for tables on a
+// log-uniform grid from log(x) and then corrected against the table itself
+// (the same bracket either way).
+__device__ __forceinline__ float sigma_at(const float *e, const float *s, int n, float x, int logu, float le0,
+                                          float idl) {
+  if (x <= e[0]) return s[0];
+  if (x >= e[n - 1]) return s[n - 1];
+  int lo;
+  if (logu) {
+    lo = (int)((__logf(x) - le0) * idl);
+    lo = max(0, min(n - 2, lo));
+    while (lo > 0 && e[lo] > x) lo--;
+    while (lo < n - 2 && e[lo + 1] <= x) lo++;
+  } else {
+    lo = 0;
+    int hi = n - 1;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (e[mid] <= x) lo = mid;
+      else hi = mid;
+    }
+  }
+  const int hi = lo + 1;
+  const float t = (x - e[lo]) / (e[hi] - e[lo]);
+  return (1.0f - t) * s[lo] + t * s[hi];
+}
+
 // particle_cell (ParticleInCell.jl:28-35) on the device side of an upload or a
 // source: i0 = floor(x/Δh) (the reference's i - 1, formed without the 1 + ...
 // that can round x just below the far wall onto node nx), the offset rounded
@@ -272,6 +300,7 @@ struct Ctx {
   unsigned long long *cir_seen = nullptr;  // absorbed counts already credited
   Tracker *trk = nullptr;                  // surface tracker (optional)
   void *sources = nullptr;                 // particle sources (source.cu)
+  void *dsmcs = nullptr;                   // DSMC collision sets (dsmc.cu)
 
   // step state
   unsigned long long step = 0;  // steps completed by iskra_step
@@ -439,6 +468,8 @@ int launch_surface_charge(Ctx *c);  // σ credit of floating-electrode hits (aft
 void tracker_destroy(Ctx *c);
 int launch_step_sources(Ctx *c, double dt, uint64_t seed);  // sources sampled every step
 void sources_destroy(Ctx *c);
+int launch_step_dsmc(Ctx *c, double dt, uint64_t seed);     // DSMC sets of a step
+void dsmc_destroy(Ctx *c);
 int poisson_prepare(Ctx *c);
 bool poisson_df_rho(Ctx *c);   // ρ of the next solve may be formed in double-float
 int sync_rho64(Ctx *c);        // FP64 ρ up to date (particles.cu)

@@ -133,34 +133,6 @@ __device__ __forceinline__ void diffuse_reflection(const float v[3], float u1, f
   rotate(sth, cth, sph, cph, sch, cch, seta, ceta, out);
 }
 
-// CrossSection: linear interpolation, flat extrapolation (cross_section.jl:8-14)
-// The bracket e[lo] <= x < e[lo+1] is found by bisection, or for tables on a
-// log-uniform grid from log(x) and then corrected against the table itself
-// (the same bracket either way).
-__device__ __forceinline__ float sigma_at(const float *e, const float *s, int n, float x, int logu, float le0,
-                                          float idl) {
-  if (x <= e[0]) return s[0];
-  if (x >= e[n - 1]) return s[n - 1];
-  int lo;
-  if (logu) {
-    lo = (int)((__logf(x) - le0) * idl);
-    lo = max(0, min(n - 2, lo));
-    while (lo > 0 && e[lo] > x) lo--;
-    while (lo < n - 2 && e[lo + 1] <= x) lo++;
-  } else {
-    lo = 0;
-    int hi = n - 1;
-    while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (e[mid] <= x) lo = mid;
-      else hi = mid;
-    }
-  }
-  const int hi = lo + 1;
-  const float t = (x - e[lo]) / (e[hi] - e[lo]);
-  return (1.0f - t) * s[lo] + t * s[hi];
-}
-
 // warp-aggregated slot reservation: every lane with want=true gets a slot
 __device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsigned int *next_id, uint32_t &nid) {
   const unsigned FULL = 0xffffffffu;

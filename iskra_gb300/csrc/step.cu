@@ -97,9 +97,13 @@ static int queue_step(Ctx *c, double dt, uint64_t seed, double rtol, bool blocki
       rc = launch_mcc(c, m, dt, seed, c->d_step, 0);
       if (rc) return rc;
     }
+    rc = launch_step_dsmc(c, dt, seed);  // the DSMC sets, after the MCC sets (interactions)
+    if (rc) return rc;
     rc = launch_advance_all(c, (float)dt, nullptr, nullptr);
     if (rc) return rc;
   } else {  // the push can advance it (nothing reads it before ρ)
+    rc = launch_step_dsmc(c, dt, seed);
+    if (rc) return rc;
     bool folded = false;
     rc = launch_advance_all(c, (float)dt, c->d_step, &folded);
     if (rc) return rc;

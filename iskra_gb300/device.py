@@ -158,6 +158,24 @@ class Context:
     def source_every_step(self, src, on=True):
         self._c(self.lib.iskra_source_set_every_step(self.h, src, int(bool(on))))
 
+    # -- DSMC --
+    def dsmc_create(self, source, target, g, sigma):
+        g_ = np.ascontiguousarray(g, float)
+        s_ = np.ascontiguousarray(sigma, float)
+        k = c_int(-1)
+        self._c(self.lib.iskra_dsmc_create(self.h, source, target, _ptr(g_), _ptr(s_), len(g_), byref(k)))
+        return k.value
+
+    def dsmc_perform(self, k, dt, seed=0, step=0):
+        self._c(self.lib.iskra_dsmc_perform(self.h, k, dt, seed, step))
+
+    def dsmc_state(self, k):
+        """(collisions_remaining, ν) per cell as (nx, ny) arrays."""
+        rem = np.zeros((self.nx, self.ny), order="F")
+        nu = np.zeros((self.nx, self.ny), dtype=np.uint32, order="F")
+        self._c(self.lib.iskra_dsmc_state(self.h, k, _ptr(rem), _ptr(nu, _lib.u32p)))
+        return rem, nu
+
     def tracker_hits(self, surface, sid):
         n = c_int64(0)
         self._c(self.lib.iskra_tracker_hits(self.h, surface, sid, byref(n)))

@@ -344,7 +344,7 @@ def source_measure(reps=10):
     ctx = Context(NX, NY, DX, DX, (0, 0, 0, 0))
     sid = ctx.species_create(-QE, ME, 1.0, n)
     L = (NX - 1) * DX
-    src = ctx.source_create(sid, n / DT, [L, L], [1e5, 1e5, 1e5])
+    src = ctx.source_create(sid, (n + 0.5) / DT, [L, L], [1e5, 1e5, 1e5])  # floor(rate Δt) = n
     stream = torch.cuda.ExternalStream(ctx.stream)
     ts = []
     for r in range(reps):
@@ -364,6 +364,56 @@ def source_measure(reps=10):
     return {"metric": "particles/s", "value": n / t, "unit": "particles/s", "particles_per_sample": n,
             "ms_per_sample": t * 1e3, "achieved_gbs": 28.0 * n / t / 1e9,
             "workload": "MaxwellianSource sample! of 4M particles over the 512x512 slab", "data": "synthetic"}
+
+
+def dsmc_measure(reps=50):
+    """DSMC perform! on the configuration of problem/05_dsmc.jl: 20x20 nodes of
+    5 cm, 5000 e- and 5000 O (8 m_p) sampled as its start() does (uniform over
+    the domain, thermal O at 300 K, e- at 0.5e6 m/s per in-plane component),
+    cross section 3-6e6 m/s -> [0.01, 0.1, 2.0, 0.01], Δt = 1 ns.  Device time
+    per perform!, pairs tried and collisions accepted per second."""
+    import torch
+    from iskra_gb300 import _lib
+    from iskra_gb300.device import Context
+    n, dh, dt = 20, 0.05, 1e-9
+    L = n * dh
+    kb, mp = 1.3806503e-23, 1.67262192e-27
+    ctx = Context(n, n, dh, dh, (0, 0, 0, 0))
+    e = ctx.species_create(-QE, ME, 1.0, 20000)
+    o = ctx.species_create(0.0, 8 * mp, 1.0, 20000)
+    rng = np.random.default_rng(5)
+    Lg = (n - 1) * dh  # the reference samples over n*Δh, past the last node: kept inside the grid here
+    xe = np.asfortranarray(rng.uniform(0, Lg, (5000, 2)))
+    xo = np.asfortranarray(rng.uniform(0, Lg, (5000, 2)))
+    ve = np.asfortranarray(rng.standard_normal((5000, 3)) * [0.5e6, 0.5e6, 0.0])
+    vth = np.sqrt(2 * kb * 300 / (8 * mp))
+    vo = np.asfortranarray(rng.standard_normal((5000, 3)) * vth)
+    ctx.upload(e, xe, ve)
+    ctx.upload(o, xo, vo)
+    k = ctx.dsmc_create(e, o, [3e6, 4e6, 5e6, 6e6], [0.01, 0.1, 2.0, 0.01])
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    for r in range(3):
+        ctx.dsmc_perform(k, dt, seed=1, step=r)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for r in range(reps):
+        ctx.dsmc_perform(k, dt, seed=1, step=3 + r)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    rem, nu = ctx.dsmc_state(k)
+    ctx.close()
+    # pairs tried per perform! (deterministic from the counts)
+    from_cells = lambda x: np.bincount(np.floor(x[:, 0] / dh).astype(int) + n * np.floor(x[:, 1] / dh).astype(int),
+                                       minlength=n * n)
+    Na, Nb = from_cells(xe), from_cells(xo)
+    nc = Na / (dh * dh) * Nb * dt * (2.0 * 5e6)  # Pab = Pba = 1, two species: x2 / 2
+    pairs = float(np.floor(nc[(Na >= 2) & (Nb >= 2)]).sum())
+    return {"metric": "DSMC pairs tried/s", "value": pairs / (ms * 1e-3), "unit": "pairs/s", "ms_per_perform": ms,
+            "pairs_per_perform": pairs, "accepted_last_perform": int(nu.sum()),
+            "workload": "problem/05_dsmc.jl: 20x20 nodes, 5000 e- + 5000 O, elastic e-O, dt = 1 ns", "data": "synthetic"}
 
 
 def c5_measure():
@@ -676,6 +726,7 @@ def main():
     if rank == 0 and not args.no_tracker:
         line["tracker"] = tracker_measure(w, e, i, min(max(args.steps // 5, 20), 200), ms / args.steps)
         line["source"] = source_measure()
+        line["dsmc_05"] = dsmc_measure()
     if rank == 0 and not args.no_c5:
         line["learned_warm_start_c5"] = c5_measure()
     if rank == 0 and not args.no_cpu_baseline:

@@ -280,7 +280,7 @@ int iskra_dsmc_create(iskra_ctx *ctx, int source, int target, const double *g,
  * carried remainder, floor(Nc) random pairs accepted with probability
  * σ(g) g / σgmax and scattered isotropically in the CM frame
  * (perform!(::ElasticCollision), :31-84).  Philox keyed by (seed, set,
- * step, cell).  iskra_step performs every set each step, after the MCC
+ * step, cell, pair).  iskra_step performs every set each step, after the MCC
  * sets and before the push, keyed by the device step counter. (async) */
 int iskra_dsmc_perform(iskra_ctx *ctx, int set, double dt, uint64_t seed,
                        uint64_t step);

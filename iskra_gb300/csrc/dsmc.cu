@@ -5,14 +5,15 @@
 //
 // Each perform! buckets the live particles of both species by cell (the
 // reference's cache!, :24-29: counts, an exclusive scan, a scatter of slot
-// indices), then one thread per cell sorts its two index lists by particle
-// identifier (so the random picks do not depend on memory order) and
-// runs the reference's loop for the cell in order: Nc from the cell counts
+// indices), then a warp per cell orders its two index lists by particle
+// identifier (so the random picks do not depend on memory order), stages the
+// velocities in shared memory and runs the reference's loop for the cell in
+// order with the warp: Nc from the cell counts
 // and the remainder carried from the last step, floor(Nc) random pairs, each
 // accepted with probability σ(g) g / σgmax and scattered isotropically in
 // the centre-of-mass frame.  Cells hold disjoint particles, so the cells run
 // in parallel without conflicts.  Randomness: Philox keyed by (seed, set,
-// step, cell), a stream per cell.
+// step, cell, pair).
 #include <algorithm>
 #include <cmath>
 #include <new>
@@ -132,19 +133,121 @@ __device__ __forceinline__ void set_vel(const SpeciesDev &s, unsigned p, float3 
   zc[p] = make_float2(v.z, zc[p].y);
 }
 
-// PIC.perform!(dsmc, ...) for one cell (dsmc.jl:103-134), thread per cell.
+// The pairs of one cell in order (dsmc.jl:108-133), by the whole warp:
+// ncol pairs from the id-ordered lists (positions ra < Na, rb < Nb), pair c
+// drawing its own random numbers (Philox keyed by (seed, set, step, cell,
+// c)), accepted with probability σ(g) g / σgmax and scattered by
+// perform!(::ElasticCollision) (dsmc.jl:31-84, vss_inv = 1: an isotropic
+// direction for the relative velocity in the CM frame).  The 32 lanes test
+// 32 consecutive pairs against the current velocities; the first accepted
+// one collides (its lane writes the velocities) and the test resumes after
+// it, so the outcome is that of testing the pairs one by one (acceptance is
+// rare: the 05_dsmc problem accepts ~1 pair in 1500).  A pair of one species
+// draws its second particle among the other Nb - 1 (the reference redraws
+// until they differ, :112-114: the same distribution).  get/set reach the
+// velocities of the r-th particle of each list (shared or global memory).
+// Returns the accepted collisions (on every lane).
+template <class GA, class SA, class GB, class SB>
+__device__ unsigned dsmc_pairs(const DsmcArgs &A, int cell, unsigned long long step, long long ncol, int Na, int Nb,
+                               int lane, GA get_a, SA set_a, GB get_b, SB set_b) {
+  const unsigned FULL = 0xffffffffu;
+  const double Wa = A.w[0], Wb = A.w[1];
+  const float ma = (float)A.m[0], mb = (float)A.m[1];
+  const float mr1 = ma / (ma + mb), mr2 = mb / (ma + mb);
+  const float sgmax = (float)A.sgmax;
+  const float *gt = A.tab, *st = A.tab + A.ntab;
+  const uint32_t k1 = A.k1 ^ (uint32_t)(step >> 32);
+  unsigned accepted = 0;
+  long long c = 0;
+  while (c < ncol) {
+    const long long my = c + lane;
+    bool acc = false;
+    int ra = 0, rb = 0;
+    U4 r0{0, 0, 0, 0}, r1{0, 0, 0, 0};
+    float3 va{0, 0, 0}, vb{0, 0, 0};
+    float g = 0.f;
+    if (my < ncol) {
+      r0 = philox4x32_10(U4{(uint32_t)my, (uint32_t)cell, (uint32_t)step, A.set}, A.k0, k1);
+      r1 = philox4x32_10(U4{(uint32_t)my, (uint32_t)cell, (uint32_t)step, A.set | 0x80000000u}, A.k0, k1);
+      ra = min(Na - 1, (int)(u01(r0.x) * Na));
+      if (A.same) rb = (ra + 1 + min(Nb - 2, (int)(u01(r0.y) * (Nb - 1)))) % Nb;
+      else rb = min(Nb - 1, (int)(u01(r0.y) * Nb));
+      va = get_a(ra);
+      vb = get_b(rb);
+      const float gx = va.x - vb.x, gy = va.y - vb.y, gz = va.z - vb.z;
+      g = sqrtf(gx * gx + gy * gy + gz * gz);
+      const float P = sigma_at(gt, st, A.ntab, g, 0, 0.f, 0.f) * g / sgmax;
+      acc = !(P < u01(r0.z));
+    }
+    const unsigned m = __ballot_sync(FULL, acc);
+    if (m == 0u) {
+      c += 32;
+      continue;
+    }
+    const int f = __ffs(m) - 1;
+    if (lane == f) {
+      const float vcx = mr1 * va.x + mr2 * vb.x, vcy = mr1 * va.y + mr2 * vb.y, vcz = mr1 * va.z + mr2 * vb.z;
+      const float B = 2.0f * u01(r0.w) - 1.0f;
+      const float Aa = sqrtf(fmaxf(1.0f - B * B, 0.0f));
+      float sC, cC;
+      sincospif(2.0f * u01(r1.x), &sC, &cC);
+      const float rx = g * B, ry = g * Aa * cC, rz = g * Aa * sC;
+      if (A.w[0] == A.w[1]) {
+        set_a(ra, make_float3(vcx + mr2 * rx, vcy + mr2 * ry, vcz + mr2 * rz));
+        set_b(rb, make_float3(vcx - mr1 * rx, vcy - mr1 * ry, vcz - mr1 * rz));
+      } else {  // unequal weights (dsmc.jl:72-83)
+        const float u = u01(r1.y);
+        if ((float)(Wb / Wa) > u) set_a(ra, make_float3(vcx + mr2 * rx, vcy + mr2 * ry, vcz + mr2 * rz));
+        if ((float)(Wa / Wb) > u) set_b(rb, make_float3(vcx - mr2 * rx, vcy - mr2 * ry, vcz - mr2 * rz));
+      }
+    }
+    __syncwarp();
+    accepted++;
+    c += f + 1;
+  }
+  return accepted;
+}
+
+// cells whose lists fit are staged in shared memory: the pair loop then
+// waits on shared-memory loads instead of dependent global ones
+constexpr int kDsmcStage = 512;
+struct DsmcShared {
+  float3 va[kDsmcStage], vb[kDsmcStage];      // velocities, id order
+  unsigned sa[kDsmcStage], sb[kDsmcStage];    // slots, id order
+  unsigned tslot[kDsmcStage];                 // a list as scattered
+  uint32_t tid[kDsmcStage];                   // its identifiers
+};
+
+// the list l[0..n) ordered by identifier into out (ids are unique: each
+// element's rank is the number of smaller ids); the warp's lanes share it
+__device__ __forceinline__ void warp_rank_sort(const unsigned *__restrict__ l, int n, const uint32_t *__restrict__ id,
+                                               DsmcShared &sh, unsigned *out, int lane) {
+  for (int e = lane; e < n; e += 32) {
+    sh.tslot[e] = l[e];
+    sh.tid[e] = id[l[e]];
+  }
+  __syncwarp();
+  for (int e = lane; e < n; e += 32) {
+    const uint32_t key = sh.tid[e];
+    int r = 0;
+    for (int q = 0; q < n; q++) r += sh.tid[q] < key;
+    out[r] = sh.tslot[e];
+  }
+  __syncwarp();
+}
+
+// PIC.perform!(dsmc, ...) for one cell (dsmc.jl:103-134), a warp per cell.
 // Cells are numbered like nodes (i0 + nx j0; the reference's (i0+1, j0+1)).
-__global__ void k_dsmc_cells(DsmcArgs A) {
+__global__ void __launch_bounds__(32) k_dsmc_cells(DsmcArgs A) {
   pdl_wait();
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= A.nn) return;
-  A.nu[k] = 0u;
-  const int sa = A.cnt[0][k], Na = A.cnt[0][k + 1] - sa;
-  const int sb = A.cnt[1][k], Nb = A.cnt[1][k + 1] - sb;
-  if (Na < 2 || Nb < 2) return;
-  unsigned *la = A.idx[0] + sa, *lb = A.idx[1] + sb;
-  sort_by_id(la, Na, pick(A.s[0].id[0], A.s[0].id[1], A.s[0].st->cur));
-  if (!A.same) sort_by_id(lb, Nb, pick(A.s[1].id[0], A.s[1].id[1], A.s[1].st->cur));
+  __shared__ DsmcShared sh;
+  const int k = blockIdx.x, lane = threadIdx.x;
+  const int sa0 = A.cnt[0][k], Na = A.cnt[0][k + 1] - sa0;
+  const int sb0 = A.cnt[1][k], Nb = A.cnt[1][k + 1] - sb0;
+  if (Na < 2 || Nb < 2) {
+    if (lane == 0) A.nu[k] = 0u;
+    return;
+  }
   // Nc = na Nb Δt σgmax / (Pab + (Wb/Wa) Pba), doubled for two species,
   // plus the remainder of the last step (dsmc.jl:94-117)
   const double Wa = A.w[0], Wb = A.w[1];
@@ -157,51 +260,50 @@ __global__ void k_dsmc_cells(DsmcArgs A) {
   if (!A.same) Nc *= 2.0;
   Nc += A.remaining[k];
   const double fl = floor(Nc);
-  A.remaining[k] = Nc - fl;
   const long long ncol = (long long)fl;
   const unsigned long long step = A.step ? *A.step : A.step_value;
-  Stream R;
-  R.ctr = U4{(uint32_t)k, A.set, (uint32_t)step, (uint32_t)(step >> 32)};
-  R.k0 = A.k0;
-  R.k1 = A.k1;
-  R.left = 0;
-  const float ma = (float)A.m[0], mb = (float)A.m[1];
-  const float mr1 = ma / (ma + mb), mr2 = mb / (ma + mb);
-  const float sgmax = (float)A.sgmax;
-  const float *gt = A.tab, *st = A.tab + A.ntab;
-  unsigned accepted = 0;
-  for (long long c = 0; c < ncol; c++) {
-    const unsigned s = la[min(Na - 1, (int)(R.next() * Na))];
-    unsigned t = lb[min(Nb - 1, (int)(R.next() * Nb))];
-    if (A.same) {  // a pair of distinct particles (bounded redraws)
-      for (int r = 0; r < 64 && t == s; r++) t = lb[min(Nb - 1, (int)(R.next() * Nb))];
-      if (t == s) continue;
+  const SpeciesDev &S0 = A.s[0], &S1 = A.s[1];
+  const uint32_t *id0 = pick(S0.id[0], S0.id[1], S0.st->cur);
+  const uint32_t *id1 = pick(S1.id[0], S1.id[1], S1.st->cur);
+  unsigned *la = A.idx[0] + sa0, *lb = A.idx[1] + sb0;
+  if (Na <= kDsmcStage && Nb <= kDsmcStage) {
+    warp_rank_sort(la, Na, id0, sh, sh.sa, lane);
+    if (!A.same) warp_rank_sort(lb, Nb, id1, sh, sh.sb, lane);
+    for (int r = lane; r < Na; r += 32) sh.va[r] = vel_of(S0, sh.sa[r]);
+    if (!A.same)
+      for (int r = lane; r < Nb; r += 32) sh.vb[r] = vel_of(S1, sh.sb[r]);
+    __syncwarp();
+    float3 *vb = A.same ? sh.va : sh.vb;
+    auto ga = [&](int r) { return sh.va[r]; };
+    auto sa = [&](int r, float3 v) { sh.va[r] = v; };
+    auto gb = [&](int r) { return vb[r]; };
+    auto sb = [&](int r, float3 v) { vb[r] = v; };
+    const unsigned nacc = dsmc_pairs(A, k, step, ncol, Na, Nb, lane, ga, sa, gb, sb);
+    if (lane == 0) {
+      A.nu[k] = nacc;
+      A.remaining[k] = Nc - fl;
     }
-    const float3 va = vel_of(A.s[0], s), vb = vel_of(A.s[1], t);
-    const float gx = va.x - vb.x, gy = va.y - vb.y, gz = va.z - vb.z;
-    const float g = sqrtf(gx * gx + gy * gy + gz * gz);
-    const float sg = sigma_at(gt, st, A.ntab, g, 0, 0.f, 0.f) * g;
-    const float P = sg / sgmax;
-    if (P < R.next()) continue;
-    // perform!(::ElasticCollision, s, t) (dsmc.jl:31-84), vss_inv = 1: an
-    // isotropic direction for the relative velocity in the CM frame
-    const float vcx = mr1 * va.x + mr2 * vb.x, vcy = mr1 * va.y + mr2 * vb.y, vcz = mr1 * va.z + mr2 * vb.z;
-    const float B = 2.0f * R.next() - 1.0f;
-    const float Aa = sqrtf(fmaxf(1.0f - B * B, 0.0f));
-    float sC, cC;
-    sincospif(2.0f * R.next(), &sC, &cC);
-    const float rx = g * B, ry = g * Aa * cC, rz = g * Aa * sC;
-    if (A.w[0] == A.w[1]) {
-      set_vel(A.s[0], s, make_float3(vcx + mr2 * rx, vcy + mr2 * ry, vcz + mr2 * rz));
-      set_vel(A.s[1], t, make_float3(vcx - mr1 * rx, vcy - mr1 * ry, vcz - mr1 * rz));
-    } else {  // unequal weights (dsmc.jl:72-83)
-      const float u = R.next();
-      if ((float)(Wb / Wa) > u) set_vel(A.s[0], s, make_float3(vcx + mr2 * rx, vcy + mr2 * ry, vcz + mr2 * rz));
-      if ((float)(Wa / Wb) > u) set_vel(A.s[1], t, make_float3(vcx - mr2 * rx, vcy - mr2 * ry, vcz - mr2 * rz));
-    }
-    accepted++;
+    __syncwarp();
+    for (int r = lane; r < Na; r += 32) set_vel(S0, sh.sa[r], sh.va[r]);
+    if (!A.same)
+      for (int r = lane; r < Nb; r += 32) set_vel(S1, sh.sb[r], sh.vb[r]);
+    return;
   }
-  A.nu[k] = accepted;
+  // a crowded cell: lists ordered in place, velocities in global memory
+  if (lane == 0) {
+    sort_by_id(la, Na, id0);
+    if (!A.same) sort_by_id(lb, Nb, id1);
+  }
+  __syncwarp();
+  auto ga = [&](int r) { return vel_of(S0, la[r]); };
+  auto sa = [&](int r, float3 v) { set_vel(S0, la[r], v); };
+  auto gb = [&](int r) { return vel_of(S1, lb[r]); };
+  auto sb = [&](int r, float3 v) { set_vel(S1, lb[r], v); };
+  const unsigned nacc = dsmc_pairs(A, k, step, ncol, Na, Nb, lane, ga, sa, gb, sb);
+  if (lane == 0) {
+    A.nu[k] = nacc;
+    A.remaining[k] = Nc - fl;
+  }
 }
 
 static std::vector<Dsmc *> &dsmc_of(Ctx *c) { return *reinterpret_cast<std::vector<Dsmc *> *>(c->dsmcs); }
@@ -269,7 +371,7 @@ int launch_dsmc(Ctx *c, int k, double dt, uint64_t seed, const unsigned long lon
   A.set = (uint32_t)k;
   A.step = step;
   A.step_value = step_value;
-  ISKRA_CUDA(c, launch_pdl(k_dsmc_cells, (nn + 127) / 128, 128, 0, c->stream, A));
+  ISKRA_CUDA(c, launch_pdl(k_dsmc_cells, nn, 32, 0, c->stream, A));
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }

@@ -177,9 +177,7 @@ __device__ __forceinline__ float sigma_at(const float *e, const float *s, int n,
 // unless that cell does not exist (then the offset stays at 1 - 2^-24), so a
 // download/upload round trip reproduces the state.  Returns the packed cell
 // (i0 | j0 << 16) or -1 outside the grid.
-__device__ __forceinline__ int cell_of_position(double X, double Y, double dx, double dy, int nx, int ny,
-                                                 long long &ux, long long &uy) {
-  const double fx = X / dx, fy = Y / dy;
+__device__ __forceinline__ int cell_of_units(double fx, double fy, int nx, int ny, long long &ux, long long &uy) {
   const double ix = floor(fx), jy = floor(fy);
   long long i0 = (long long)ix, j0 = (long long)jy;
   ux = llrint((fx - ix) * 16777216.0);
@@ -202,6 +200,11 @@ __device__ __forceinline__ int cell_of_position(double X, double Y, double dx, d
   }
   if (i0 < 0 || j0 < 0 || i0 > nx - 2 || j0 > ny - 2) return -1;
   return (int)(i0 | (j0 << 16));
+}
+// the same from a position in metres (f = x / Δh)
+__device__ __forceinline__ int cell_of_position(double X, double Y, double dx, double dy, int nx, int ny,
+                                                 long long &ux, long long &uy) {
+  return cell_of_units(X / dx, Y / dy, nx, ny, ux, uy);
 }
 
 struct Species {

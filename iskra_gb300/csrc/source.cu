@@ -35,9 +35,8 @@ struct SourceArgs {
   SpeciesDev s;
   SourceDev *d;
   long long cap, nmax;    // capacity, floor(rate Δt)
-  double wx[2], dx[2];
+  double wx[2], dx[2];    // in cells: wx / Δh, dx / Δh
   float wv[3], dv[3];
-  double hx, hy;          // Δx, Δy
   int nx, ny;
   uint32_t k0, k1;        // Philox key (seed)
   uint32_t src;           // source index (a counter word)
@@ -75,8 +74,9 @@ __global__ void k_source_fill(SourceArgs A, int *err) {
     const U4 c0 = {(uint32_t)k, (uint32_t)(k >> 32), (uint32_t)step, A.src};
     const U4 r0 = philox4x32_10(c0, A.k0, A.k1);
     const U4 r1 = philox4x32_10(U4{c0.x, c0.y, c0.z, A.src | 0x80000000u}, A.k0, A.k1 ^ (uint32_t)(step >> 32));
-    const double X = (double)u01(r0.x) * A.wx[0] + A.dx[0];
-    const double Y = (double)u01(r0.y) * A.wx[1] + A.dx[1];
+    // x / Δh = U wx / Δh + dx / Δh (FMAs in cell units: no FP64 division here)
+    const double fx = fma((double)u01(r0.x), A.wx[0], A.dx[0]);
+    const double fy = fma((double)u01(r0.y), A.wx[1], A.dx[1]);
     // Box-Muller: two normals from (r0.z, r0.w), one from (r1.x, r1.y)
     const float a0 = fmaxf(u01(r0.z), 1.0e-12f), a1 = fmaxf(u01(r1.x), 1.0e-12f);
     const float rad0 = sqrtf(-2.0f * logf(a0)), rad1 = sqrtf(-2.0f * logf(a1));
@@ -84,7 +84,7 @@ __global__ void k_source_fill(SourceArgs A, int *err) {
     const float g2 = rad1 * cospif(2.0f * u01(r1.y));
     const float vx = fmaf(g0, A.wv[0], A.dv[0]), vy = fmaf(g1, A.wv[1], A.dv[1]), vz = fmaf(g2, A.wv[2], A.dv[2]);
     long long ux, uy;
-    int cell = cell_of_position(X, Y, A.hx, A.hy, A.nx, A.ny, ux, uy);
+    int cell = cell_of_units(fx, fy, A.nx, A.ny, ux, uy);
     if (cell < 0) atomicOr(err, DERR_DOMAIN);
     const long long p = base + k;
     xv[p] = make_float4((float)ux * kOffInv, (float)uy * kOffInv, vx, vy);
@@ -107,16 +107,15 @@ int launch_source(Ctx *c, int src, double dt, uint64_t seed, const unsigned long
   A.cap = sp.cap;
   A.nmax = (long long)std::floor(S.rate * dt);
   if (A.nmax <= 0) return ISKRA_OK;
+  const double h[2] = {c->g.dx, c->g.dy};
   for (int a = 0; a < 2; a++) {
-    A.wx[a] = S.wx[a];
-    A.dx[a] = S.dx[a];
+    A.wx[a] = S.wx[a] / h[a];
+    A.dx[a] = S.dx[a] / h[a];
   }
   for (int a = 0; a < 3; a++) {
     A.wv[a] = (float)S.wv[a];
     A.dv[a] = (float)S.dv[a];
   }
-  A.hx = c->g.dx;
-  A.hy = c->g.dy;
   A.nx = c->nx;
   A.ny = c->ny;
   A.k0 = (uint32_t)seed;

@@ -64,8 +64,8 @@ struct SpeciesDev {            // kernel view of one species (by value)
 };
 
 // Tiles: the push runs one block per tile of kTile x kTile cells over the
-// particles the last sort grouped there, with the E records and the deposit
-// of the tile and a kHalo-cell margin in shared memory.  The sort key of a
+// particles the last sort grouped there, with E at the nodes and the deposit
+// moments of the tile and a kHalo-cell margin in shared memory.  The sort key of a
 // cell is tile-major: tile * kTile^2 + the cell's position in the tile.
 constexpr int kTile = 16;
 constexpr int kTileShift = 4;

@@ -14,9 +14,10 @@
 // exact 48-bit integers.  Over the particles of one cell they sum to
 //   W11 = Σuv,  W10 = 2^24 Σu - Σuv,  W01 = 2^24 Σv - Σuv,
 //   W00 = 2^48 n - 2^24 Σu - 2^24 Σv + Σuv,
-// so a warp reduces the moments (n, Σu, Σv: 32-bit; Σuv: 64-bit) over each run
-// of lanes in the same cell and the run's last lane adds the four node sums
-// with 64-bit integer atomics.  Integer addition is associative: the density
+// so a warp reduces the moments (n, Σu, Σv, Σuv) over each run of lanes in
+// the same cell, the run's last lane adds them to the block's window (16-bit
+// pieces in 32-bit words) and the block adds the window's node sums with
+// 64-bit integer atomics.  Integer addition is associative: the density
 // is bit-identical for any particle order or launch shape.  A node's sum
 // stays below 2^64 while each of its four cells holds at most 16383
 // particles; the per-cell counts are kept alongside and checked by k_finalize.

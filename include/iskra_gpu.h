@@ -361,7 +361,8 @@ int iskra_density_noalloc(const iskra_grid_t *grid, const double *x,
  * Runs with the same seed and initial state follow the same algorithm as a
  * single-run context.  Limits: at most 400 cells per run; separable operator
  * with ny <= 16, no x-periodic wrap, no σ dof (electrodes are Dirichlet,
- * possibly driven); no circuit.  The template context must outlive the
+ * possibly driven); no circuit, surface tracker, particle source or DSMC
+ * set.  The template context must outlive the
  * ensemble; the ensemble uses the template's stream. */
 typedef struct iskra_ens iskra_ens;
 int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t capacity_per_run,

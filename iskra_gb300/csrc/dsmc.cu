@@ -41,7 +41,7 @@ struct DsmcArgs {
   const float *tab;
   int ntab;
   double sgmax, dt, inv_area;   // 1 / (Δx Δy)
-  int nx, ny, nn;
+  int nn;
   bool same;                    // source and target are one species
   double *remaining;
   int *cnt[2], *fill[2];
@@ -354,8 +354,6 @@ int launch_dsmc(Ctx *c, int k, double dt, uint64_t seed, const unsigned long lon
   A.sgmax = d->sgmax;
   A.dt = dt;
   A.inv_area = 1.0 / (c->g.dx * c->g.dy);
-  A.nx = c->nx;
-  A.ny = c->ny;
   A.nn = nn;
   A.same = d->a == d->b;
   A.remaining = d->remaining;

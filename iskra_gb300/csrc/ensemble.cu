@@ -309,6 +309,7 @@ int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t cap_per_run, iskra_ens 
   if (!c->ps) return set_err(c, ISKRA_EINVAL, "template has no Poisson solver");
   if (c->has_circuit) return set_err(c, ISKRA_EINVAL, "ensembles drive electrodes directly (no circuit)");
   if (c->trk) return set_err(c, ISKRA_EINVAL, "ensembles take no surface tracker");
+  if (c->sources || c->dsmcs) return set_err(c, ISKRA_EINVAL, "ensembles take no particle sources or DSMC sets");
   if ((c->nx - 1) * (c->ny - 1) > 400) return set_err(c, ISKRA_EINVAL, "ensemble grids hold at most 400 cells");
   if ((double)cap_per_run * nruns > 2.0e9) return set_err(c, ISKRA_EINVAL, "ensemble store above 2e9 slots");
   iskra_ens *h = new (std::nothrow) iskra_ens();

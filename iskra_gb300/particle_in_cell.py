@@ -138,7 +138,7 @@ class ReflectiveSurface(Surface):
     kind = _lib.SURF_REFLECT
 
 
-@dataclass
+@dataclass(eq=False)  # surfaces compare by identity, as the tracker's keys do
 class FixedPotentialElectrode(Surface):
     """FixedPotentialElectrode (circuit_coupling.jl:4-8): absorbs (:57-63)."""
     phi: float = 0.0
@@ -146,7 +146,7 @@ class FixedPotentialElectrode(Surface):
     kind = _lib.SURF_FIXED
 
 
-@dataclass
+@dataclass(eq=False)
 class FloatingPotentialElectrode(Surface):
     """FloatingPotentialElectrode (circuit_coupling.jl:10-15): absorbs and adds
     q w / area to its σ dof (:45-55)."""

@@ -39,3 +39,33 @@ def test_elastic_collisions_conserve_momentum_and_energy():
     e0 = ma * (va ** 2).sum() + mb * (vb ** 2).sum()
     e1 = ma * (va2 ** 2).sum() + mb * (vb2 ** 2).sum()
     assert np.isclose(e0, e1, rtol=1e-12)
+
+
+def _nc_literal(Na, Nb, Wa, Wb, dx, dy, dt, sgm, same, rem):
+    """dsmc.jl:94-117 transcribed line by line for one cell."""
+    if Wa > Wb:
+        Pab, Pba = Wb / Wa, 1.0
+    else:
+        Pab, Pba = 1.0, Wa / Wb
+    if Na < 2 or Nb < 2:
+        return 0, rem
+    na = Na * Wa / (dx * dy)
+    Nc = na * Nb * dt * sgm
+    Nc /= Pab + (Wb / Wa) * Pba
+    if not same:
+        Nc *= 2
+    Nc += rem
+    return int(np.floor(Nc)), Nc - np.floor(Nc)
+
+
+def test_pairs_and_remaining_match_the_literal_loop():
+    r = np.random.default_rng(7)
+    for same in (False, True):
+        for Wa, Wb in ((1.0, 1.0), (2.0, 0.5), (0.3, 3.0)):
+            Na = r.integers(0, 40, 200)
+            Nb = Na if same else r.integers(0, 40, 200)
+            rem = r.random(200)
+            n, new = do.pairs_and_remaining(Na, Nb, Wa, Wb, 0.05, 0.02, 3e-9, 7e6, same, rem)
+            for k in range(200):
+                nk, rk = _nc_literal(int(Na[k]), int(Nb[k]), Wa, Wb, 0.05, 0.02, 3e-9, 7e6, same, rem[k])
+                assert n[k] == nk and new[k] == rk

@@ -86,3 +86,34 @@ def test_diagonal_crossing_walks_two_edges():
     x, v, ab, hits, _ = _one(tr, [3.8, 3.7], [0.5, 0.5])
     assert not ab[0]
     assert np.allclose(x[0], [4.3, 4.0 - 0.2]) and np.allclose(v[0, :2], [0.5, -0.5])
+
+
+def test_reflection_is_the_mirror_image_and_walls_absorb_escapes():
+    """Known answers from geometry, independent of the walk: with a
+    reflective wall along x = 4 (cell units) and absorbing domain walls, a
+    straight path of less than a cell either stays free, ends at its mirror
+    image about x = 4 with v_x flipped, or leaves the domain and is absorbed."""
+    tr = to.Tracker(10, 10)
+    nodes = np.zeros((10, 10), bool)
+    nodes[4, :] = True
+    f = tr.add(nodes, to.REFLECT)
+    r = np.random.default_rng(3)
+    n = 3000
+    x0 = r.uniform(0.02, 8.98, (n, 2))
+    v = np.column_stack([r.uniform(-0.95, 0.95, (n, 2)), np.zeros(n)])
+    free = x0 + v[:, :2]
+    # keep paths that cross at most one of {x = 4, the walls} and stay away from corners/edges of the decision
+    cross_wall = (np.sign(x0[:, 0] - 4) != np.sign(free[:, 0] - 4))
+    leaves = (free < 0).any(1) | (free > 9).any(1)
+    near = (np.abs(free[:, 0] - 4) < 1e-6) | (np.abs(x0[:, 0] - 4) < 1e-6)
+    keep = ~near & ~(cross_wall & leaves)
+    x, vo, ab, hits, _ = to.advance_tracked(tr, x0[keep], v[keep], 1.0, 1.0, 1.0)
+    cw, lv, fr, v0 = cross_wall[keep], leaves[keep], free[keep], v[keep]
+    # escapes are absorbed by the default walls (surface 0), nothing else is
+    assert np.array_equal(ab, lv) and hits[0] == lv.sum() and hits[f] == 0
+    ok = ~lv
+    mirror = fr.copy()
+    mirror[cw, 0] = 8.0 - fr[cw, 0]
+    assert np.allclose(x[ok], mirror[ok], atol=1e-12)
+    flip = np.where(cw, -1.0, 1.0)
+    assert np.allclose(vo[ok, 0], (flip * v0[:, 0])[ok]) and np.allclose(vo[ok, 1], v0[ok, 1])

@@ -334,16 +334,21 @@ int iskra_kernel_launches(iskra_ctx *ctx, uint64_t *count);
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: a host framework that reserves the GPU's memory up front and
  * forbids later cudaMalloc, or code running while another library holds the
- * stream in capture.  Same result as iskra_density (CIC deposit ./
- * cell_volume, exact int64 fixed-point sums) for the np particles whose
- * positions x (ld x 2, column-major FP64) are in DEVICE memory; the (nx,ny)
- * density goes to n_out (device memory); *flag (device int) is set to 1 when
- * a position lies outside the grid (that particle is skipped), else 0.
+ * stream in capture.  The density of iskra_density (CIC deposit ./
+ * cell_volume on int64 fixed-point sums) for the np particles whose
+ * positions x (ld x 2, column-major FP64) are in DEVICE memory: bit-identical
+ * below 2^15 particles; from 2^15 on each CIC weight is rounded to
+ * 2^(s-48) with s = ceil(log2(np+1)) - 15 so that no node sum can overflow,
+ * i.e. equal within 2^(s-48) relative per particle.  The grid's origin must
+ * be (0,0) as for iskra_ctx_create.  The (nx,ny) density goes to n_out
+ * (device memory); *flag (device int) is set to 1 when a position lies
+ * outside the grid (that particle is skipped), else 0.
  * Allocates nothing: the accumulator is a library-static device array of
  * 2^20 nodes (8 MiB, held on every GPU that loads the library until exit);
  * larger grids return ISKRA_EINVAL.  The first call on a device looks the
  * array's address up (cudaGetSymbolAddress): make that first call before any
- * stream capture.  Each call clears the array it shares with every other
+ * stream capture; the address is cached for the device's primary context,
+ * which must outlive every call (no cudaDeviceReset in between).  Each call clears the array it shares with every other
  * call; calls that overlap on the GPU race.  Asynchronous on `stream`. */
 int iskra_density_noalloc(const iskra_grid_t *grid, const double *x,
                           int64_t np, int64_t ld, double w0, double *n_out,

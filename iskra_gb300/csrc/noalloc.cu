@@ -9,6 +9,7 @@
 // file-scope array below.  That array is part of the library image: every
 // GPU that loads the library holds it (kNoAllocMaxNodes * 8 bytes = 8 MiB)
 // until the process exits.
+#include <atomic>
 #include <cmath>
 
 #include "internal.cuh"
@@ -24,7 +25,11 @@ static __device__ __align__(256) unsigned long long g_noalloc_acc[kNoAllocMaxNod
 
 // Device address of g_noalloc_acc per device, looked up once with that device
 // current (in host code the symbol itself is only a host-side stand-in).
-static unsigned long long *g_acc_addr[kNoAllocMaxDevices] = {};
+// Host threads may call concurrently: each entry is published atomically (two
+// threads racing on the first call both look up the same address).  The
+// cached address belongs to the device's primary context: it assumes that
+// context outlives every call (no cudaDeviceReset between calls).
+static std::atomic<unsigned long long *> g_acc_addr[kNoAllocMaxDevices];
 
 __global__ void __launch_bounds__(256) k_noalloc_deposit(const double *__restrict__ x, long long np, long long ld,
                                                          double dx, double dy, int nx, int ny, int shift,
@@ -86,18 +91,22 @@ extern "C" int iskra_density_noalloc(const iskra_grid_t *grid, const double *x, 
                                      double *n_out, int *flag, uint64_t stream) {
   if (!grid || (!x && np > 0) || !n_out || !flag || np < 0 || ld < np || !(w0 > 0)) return ISKRA_EINVAL;
   if (grid->nx < 2 || grid->ny < 2 || !(grid->dx > 0) || !(grid->dy > 0)) return ISKRA_EINVAL;
+  // particle_cell ignores the origin (ParticleInCell.jl:28-35): like
+  // iskra_ctx_create, only the zero origin is accepted
+  if (grid->ox != 0.0 || grid->oy != 0.0) return ISKRA_EINVAL;
   const long long nn = (long long)grid->nx * grid->ny;
   if (nn > kNoAllocMaxNodes) return ISKRA_EINVAL;  // grid larger than the static accumulator
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return ISKRA_ECUDA;
   if (dev < 0 || dev >= kNoAllocMaxDevices) return ISKRA_EINVAL;
-  if (!g_acc_addr[dev]) {
+  unsigned long long *acc = g_acc_addr[dev].load(std::memory_order_acquire);
+  if (!acc) {
     // one-time set-up for this device (before any stream capture)
     unsigned long long *ptr = nullptr;
     if (cudaGetSymbolAddress((void **)&ptr, g_noalloc_acc) != cudaSuccess || !ptr) return ISKRA_ECUDA;
-    g_acc_addr[dev] = ptr;
+    g_acc_addr[dev].store(ptr, std::memory_order_release);
+    acc = ptr;
   }
-  unsigned long long *acc = g_acc_addr[dev];
   cudaStream_t st = (cudaStream_t)(uintptr_t)stream;
   if (cudaMemsetAsync(acc, 0, (size_t)nn * sizeof(unsigned long long), st) != cudaSuccess) return ISKRA_ECUDA;
   if (cudaMemsetAsync(flag, 0, sizeof(int), st) != cudaSuccess) return ISKRA_ECUDA;

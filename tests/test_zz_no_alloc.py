@@ -59,3 +59,12 @@ def test_density_noalloc_rejects_oversized_grid():
     grid = _lib.Grid(2048, 1024, 1e-4, 1e-4, 0.0, 0.0, (ctypes.c_int32 * 4)(0, 0, 0, 0))
     rc = lib.iskra_density_noalloc(ctypes.byref(grid), None, 0, 0, 1.0, ctypes.c_void_p(8), ctypes.c_void_p(8), 0)
     assert rc == 1  # ISKRA_EINVAL: the grid exceeds the static accumulator; nothing is launched
+
+
+def test_density_noalloc_rejects_grid_origin():
+    """particle_cell ignores the origin, so a grid with one is refused like iskra_ctx_create does."""
+    from iskra_gb300 import _lib
+    lib = _lib.load()
+    grid = _lib.Grid(64, 64, 1e-4, 1e-4, 1e-3, 0.0, (ctypes.c_int32 * 4)(0, 0, 0, 0))
+    rc = lib.iskra_density_noalloc(ctypes.byref(grid), None, 0, 0, 1.0, ctypes.c_void_p(8), ctypes.c_void_p(8), 0)
+    assert rc == 1  # ISKRA_EINVAL before anything is launched

@@ -216,6 +216,17 @@ int iskra_poisson_apply_periodic(iskra_ctx *ctx, int axis);
 int iskra_poisson_add_dof(iskra_ctx *ctx, int *dof);
 /* apply_neumann(ps, nodes, dof) (:235-269). */
 int iskra_poisson_apply_neumann(iskra_ctx *ctx, const uint8_t *nodes, int dof);
+/* apply_neumann(ps, nodes, dof) (:235-269) in units consistent with the
+ * stencil rows and a σ in C/m^2 (the units advance!(::CircuitRLC) and hit!
+ * credit it in, circuit_coupling.jl:35-55): the Gauss law of the electrode
+ * node's half cell, -2/Δx^2 ϕ_i + 2/Δx^2 ϕ_i' + 2/(ε0 Δx) σ = -ρ_i/ε0 (the
+ * reference's edge row divided by Δx, its σ coefficient 2 replaced by
+ * 2/(ε0 Δx)); corner rows divide their σ coefficient by ε0.  The reference's
+ * own rows mix a potential gradient with -ρ/ε0 and an undivided σ, which
+ * drives a floating electrode to tens of kV within a few steps of a
+ * discharge; circuit runs use this form. */
+int iskra_poisson_apply_neumann_gauss(iskra_ctx *ctx, const uint8_t *nodes,
+                                      int dof);
 /* get_rhs(ps, :σ, dof) read / write (:367-370). */
 int iskra_poisson_set_sigma(iskra_ctx *ctx, int dof, double value);
 int iskra_poisson_get_sigma(iskra_ctx *ctx, int dof, double *value);
@@ -266,6 +277,12 @@ int iskra_mcc_perform(iskra_ctx *ctx, int mid, double dt, uint64_t seed,
                       uint64_t step);
 /* Accepted collisions per process since the last call (reset after). */
 int iskra_mcc_counts(iskra_ctx *ctx, int mid, int64_t *counts);
+/* The rate call (process.rate)(ε) of CrossSection (cross_section.jl:8-16:
+ * linear interpolation, flat outside the table) as the MCC kernels evaluate
+ * it -- FP32 table of set mid, process `process` (0-based) -- at n energies
+ * (eV); sigma_out[k] = σ(energies[k]) in m^2.  (synchronises) */
+int iskra_mcc_sigma(iskra_ctx *ctx, int mid, int process,
+                    const double *energies, int64_t n, double *sigma_out);
 
 /* ---- DSMC (Chemistry/src/dsmc.jl) ----------------------------------------
  * DSMC.ElasticCollision(rate, source, target) of dsmc(@reactions ...)

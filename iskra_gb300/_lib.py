@@ -79,6 +79,7 @@ SIGNATURES = [
     ("iskra_poisson_apply_periodic", c_int, [CTX, c_int]),
     ("iskra_poisson_add_dof", c_int, [CTX, ip]),
     ("iskra_poisson_apply_neumann", c_int, [CTX, u8p, c_int]),
+    ("iskra_poisson_apply_neumann_gauss", c_int, [CTX, u8p, c_int]),
     ("iskra_poisson_set_sigma", c_int, [CTX, c_int, c_double]),
     ("iskra_poisson_get_sigma", c_int, [CTX, c_int, dp]),
     ("iskra_poisson_drive_dirichlet", c_int, [CTX, u8p, c_double, c_double, c_double, c_double]),
@@ -90,6 +91,7 @@ SIGNATURES = [
                                  dp, ip]),
     ("iskra_mcc_perform", c_int, [CTX, c_int, c_double, c_uint64, c_uint64]),
     ("iskra_mcc_counts", c_int, [CTX, c_int, i64p]),
+    ("iskra_mcc_sigma", c_int, [CTX, c_int, c_int, dp, c_int64, dp]),
     ("iskra_circuit_create", c_int, [CTX, c_double, c_double, c_double, c_double, c_double, c_double, c_int, u8p,
                                      u8p, c_double, c_double]),
     ("iskra_circuit_advance", c_int, [CTX, c_double]),

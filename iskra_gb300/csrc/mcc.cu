@@ -581,6 +581,14 @@ int ensure_mcc_work(Ctx *c) {
   return ISKRA_OK;
 }
 
+// CrossSection lookups exactly as the MCC kernels make them (FP32 table,
+// sigma_at with the set's log-uniform bracket guess), for a list of energies.
+__global__ void k_mcc_sigma(const float *__restrict__ e, const float *__restrict__ s, int n, int logu, float le0,
+                            float idl, const double *__restrict__ x, long long m, double *__restrict__ out) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x)
+    out[k] = (double)sigma_at(e, s, n, (float)x[k], logu, le0, idl);
+}
+
 int mcc_nproc(Ctx *c, int mid) { return c->mccs[mid]->N; }
 int mcc_src(Ctx *c, int mid) { return c->mccs[mid]->src; }
 int mcc_prod(Ctx *c, int mid) { return c->mccs[mid]->prod; }
@@ -718,6 +726,32 @@ int iskra_mcc_counts(iskra_ctx *h, int mid, int64_t *counts) {
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   for (int k = 0; k < m->N; k++) counts[k] = (int64_t)tmp[k];
   return collect_device_errors(c);
+}
+
+int iskra_mcc_sigma(iskra_ctx *h, int mid, int process, const double *energies, int64_t n, double *sigma_out) {
+  if (!h || (n > 0 && (!energies || !sigma_out)) || n < 0) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (mid < 0 || mid >= (int)c->mccs.size()) return set_err(c, ISKRA_EINVAL, "bad MCC id");
+  Mcc *m = c->mccs[mid];
+  if (process < 0 || process >= m->N) return set_err(c, ISKRA_EINVAL, "bad process index");
+  if (n == 0) return ISKRA_OK;
+  double *d = nullptr;
+  ISKRA_CUDA(c, cudaMalloc(&d, 2 * (size_t)n * sizeof(double)));
+  int rc = ISKRA_OK;
+  cudaError_t e = cudaMemcpyAsync(d, energies, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    const int k = process, len = m->off[k + 1] - m->off[k];
+    const long long blocks = std::min<long long>((n + 255) / 256, 1024);
+    k_mcc_sigma<<<(unsigned)blocks, 256, 0, c->stream>>>(m->eps + m->off[k], m->sig + m->off[k], len, m->logu[k],
+                                                         m->log_e0[k], m->inv_dlog[k], d, n, d + n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(sigma_out, d + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) rc = cuda_check(c, e, "iskra_mcc_sigma");
+  cudaFree(d);
+  return rc;
 }
 
 }  // extern "C"

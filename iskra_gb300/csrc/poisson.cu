@@ -1145,9 +1145,20 @@ static void assemble_dirichlet(Poisson *P, const uint8_t *nodes, double phi0) {
   }
 }
 
-static void assemble_neumann(Poisson *P, const uint8_t *nodes, int dof) {
+// apply_neumann (generalized_poisson.jl:235-269).  gauss = false: the
+// reference's rows exactly.  gauss = true: the same rows in the units of the
+// stencil rows, i.e. the Gauss law of the electrode node's half (edge) or
+// quarter (corner) cell with σ in C/m^2: the edge row is the reference's row
+// divided by Δx with the σ coefficient 2/(ε0 Δx) (the reference's 2/Δx
+// gradient row against a -ρ/ε0 right-hand side and an undivided σ mixes
+// units), the corner row keeps its 1/Δ^2 coefficients and divides the σ
+// coefficient by ε0.
+static void assemble_neumann(Poisson *P, const uint8_t *nodes, int dof, bool gauss) {
   const int nx = P->nx, ny = P->ny;
   const double dx = P->dx, dy = P->dy;
+  const double ge = gauss ? 1.0 / dx : 1.0;               // edge-row scale
+  const double gs = gauss ? 1.0 / (P->eps0 * dx) : 1.0;   // edge-row σ scale
+  const double gc = gauss ? 1.0 / P->eps0 : 1.0;          // corner-row σ scale
   auto N = [&](int i, int j) { return nodes[i + nx * j] != 0; };  // 0-based
   for (int j = 0; j < ny; j++)
     for (int i = 0; i < nx; i++) {
@@ -1163,9 +1174,9 @@ static void assemble_neumann(Poisson *P, const uint8_t *nodes, int dof) {
         const int ip = i == 0 ? i + 1 : i - 1;
         for (int s = 0; s < 7; s++) R[s] = 0.0;
         for (auto &col : P->sig_cols) col[r] = 0.0;
-        R[0] -= 2 * ER(P, i + 1, j + 1) / dx;
-        R[ip == i + 1 ? 2 : 1] += 2 * ER(P, ip + 1, j + 1) / dx;
-        S[r] += 2;
+        R[0] -= 2 * ER(P, i + 1, j + 1) / dx * ge;
+        R[ip == i + 1 ? 2 : 1] += 2 * ER(P, ip + 1, j + 1) / dx * ge;
+        S[r] += 2 * gs;
       }
       if (cc != d) {
         const int ip = i == 0 ? i + 1 : i - 1;
@@ -1177,7 +1188,7 @@ static void assemble_neumann(Poisson *P, const uint8_t *nodes, int dof) {
         R[0] -= 4 * e / (3 * dy * dy);
         R[ip == i + 1 ? 2 : 1] += 4 * e / (3 * dx * dx);
         R[jp == j + 1 ? 4 : 3] += 4 * e / (3 * dy * dy);
-        S[r] += (2.0 / 3.0) * (dx + dy) / (dx * dy);
+        S[r] += (2.0 / 3.0) * (dx + dy) / (dx * dy) * gc;
       }
     }
 }
@@ -2422,7 +2433,17 @@ int iskra_poisson_apply_neumann(iskra_ctx *h, const uint8_t *nodes, int dof) {
   Ctx *c = &h->c;
   if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
   if (dof < 1 || dof > (int)c->ps->sig_b.size()) return set_err(c, ISKRA_EINVAL, "bad σ dof");
-  assemble_neumann(c->ps, nodes, dof);
+  assemble_neumann(c->ps, nodes, dof, false);
+  c->ps->dirty = true;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_apply_neumann_gauss(iskra_ctx *h, const uint8_t *nodes, int dof) {
+  if (!h || !nodes) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  if (dof < 1 || dof > (int)c->ps->sig_b.size()) return set_err(c, ISKRA_EINVAL, "bad σ dof");
+  assemble_neumann(c->ps, nodes, dof, true);
   c->ps->dirty = true;
   return ISKRA_OK;
 }

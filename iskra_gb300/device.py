@@ -248,9 +248,12 @@ class Context:
         self._c(self.lib.iskra_poisson_add_dof(self.h, byref(d)))
         return d.value
 
-    def apply_neumann(self, nodes, dof):
+    def apply_neumann(self, nodes, dof, gauss=False):
+        """apply_neumann; gauss=True: the rows in stencil units with σ in C/m^2
+        (iskra_poisson_apply_neumann_gauss)."""
         m = _mask(nodes, self.nx, self.ny)
-        self._c(self.lib.iskra_poisson_apply_neumann(self.h, _ptr(m, _lib.u8p), dof))
+        f = self.lib.iskra_poisson_apply_neumann_gauss if gauss else self.lib.iskra_poisson_apply_neumann
+        self._c(f(self.h, _ptr(m, _lib.u8p), dof))
 
     def set_sigma(self, dof, value):
         self._c(self.lib.iskra_poisson_set_sigma(self.h, dof, value))
@@ -314,6 +317,13 @@ class Context:
         a = (c_int64 * nproc)()
         self._c(self.lib.iskra_mcc_counts(self.h, mid, a))
         return list(a)
+
+    def mcc_sigma(self, mid, process, energies):
+        """σ of one process at the given energies (eV), as the MCC kernels evaluate it."""
+        e = np.ascontiguousarray(energies, dtype=np.float64)
+        out = np.zeros(len(e))
+        self._c(self.lib.iskra_mcc_sigma(self.h, mid, process, _ptr(e), len(e), _ptr(out)))
+        return out
 
     # -- circuit --
     def circuit_create(self, R, L, C, amp, freq, dc, sigma_dof, pos_nodes, neg_nodes, area, sigma_scale=1.0):

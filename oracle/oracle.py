@@ -380,11 +380,19 @@ class PoissonOracle:
         self.sig_b.append(0.0)
         return len(self.sig_b)
 
-    def apply_neumann(self, nodes, dof):
-        """apply_neumann(ps::PoissonSolver{:xy,2}, nodes, dof) (:235-269)."""
+    def apply_neumann(self, nodes, dof, gauss=False):
+        """apply_neumann(ps::PoissonSolver{:xy,2}, nodes, dof) (:235-269).
+        gauss=True: the same rows in stencil units with σ in C/m^2 -- the edge
+        row divided by Δx with σ coefficient 2/(ε0 Δx), the corner rows' σ
+        coefficient divided by ε0 (the half/quarter-cell Gauss law; the
+        declared consistent form of the library's
+        iskra_poisson_apply_neumann_gauss)."""
         nodes = np.asarray(nodes, dtype=bool)
         nx, ny, er = self.nx, self.ny, self.er
         dx, dy = self.dx, self.dy
+        ge = 1.0 / dx if gauss else 1.0
+        gs = 1.0 / (self.eps0 * dx) if gauss else 1.0
+        gc = 1.0 / self.eps0 if gauss else 1.0
         for (i, j) in zip(*np.nonzero(nodes)):
             a = nodes[i - 1, j] if i > 0 else False
             b = nodes[i + 1, j] if i < nx - 1 else False
@@ -395,9 +403,9 @@ class PoissonOracle:
                 ip_ = i + 1 if i == 0 else i - 1
                 self.C[r, :] = 0.0
                 self.sig_cols[r, :] = 0.0
-                self.C[r, 0] -= 2 * er[i, j] / dx
-                self.C[r, 2 if ip_ == i + 1 else 1] += 2 * er[ip_, j] / dx
-                self.sig_cols[r, dof - 1] += 2
+                self.C[r, 0] -= 2 * er[i, j] / dx * ge
+                self.C[r, 2 if ip_ == i + 1 else 1] += 2 * er[ip_, j] / dx * ge
+                self.sig_cols[r, dof - 1] += 2 * gs
             if c != d:
                 ip_ = i + 1 if i == 0 else i - 1
                 jp_ = j + 1 if c else j - 1
@@ -407,7 +415,7 @@ class PoissonOracle:
                 self.C[r, 0] -= 4 * er[i, j] / (3 * dy ** 2)
                 self.C[r, 2 if ip_ == i + 1 else 1] += 4 * er[i, j] / (3 * dx ** 2)
                 self.C[r, 4 if jp_ == j + 1 else 3] += 4 * er[i, j] / (3 * dy ** 2)
-                self.sig_cols[r, dof - 1] += (2 / 3) * (dx + dy) / (dx * dy)
+                self.sig_cols[r, dof - 1] += (2 / 3) * (dx + dy) / (dx * dy) * gc
 
     def set_sigma(self, dof, value):
         self.sig_b[dof - 1] = value

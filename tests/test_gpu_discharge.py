@@ -6,7 +6,14 @@ discard! in x, wrap! in y.  The GPU runs iskra_step (one CUDA graph per
 step); the oracle runs the reference's loop body (PicOracle) from the same
 initial state with its own random stream.  Compared: accepted collisions per
 process (3.5σ), surviving particle counts and the electron energy
-distribution (L1 distance)."""
+distribution.
+
+The GPU run carries 4x the oracle's macroparticles (weight / 4, the same
+densities), so the oracle's sample dominates the statistical noise.  EEDF
+agreement is stated as the L1 distance between the normalised electron
+energy histograms (16 bins of 2.5 eV on 0-40 eV) and asserted below 0.02
+(the configuration's "EEDF within 2 %"); the L1 expected from sampling
+noise alone, Σ sqrt(2/π) sqrt(p (1-p) (1/n_g + 1/n_o)), is ~0.011 here."""
 import numpy as np
 import pytest
 
@@ -35,9 +42,11 @@ def test_ccp_discharge_statistics(orc, lib):
 
     nx, ny, gap = 129, 2, 0.025
     dx = gap / (nx - 1)
-    n0 = 20000
+    n0, ng0 = 100000, 400000   # oracle / GPU macroparticles per species
     rng = np.random.default_rng(33)
     w = 1e15 * gap * dx / n0
+    wg = 1e15 * gap * dx / ng0
+    r = n0 / ng0               # GPU counts -> oracle scale
 
     def maxwellian(n, T_ev, m):
         x = np.column_stack([rng.uniform(0, gap, n), rng.uniform(0, dx, n)])
@@ -46,6 +55,8 @@ def test_ccp_discharge_statistics(orc, lib):
 
     xe, ve = maxwellian(n0, 4.0, ME)
     xi, vi = maxwellian(n0, 0.03, M_AR)
+    xeg, veg = maxwellian(ng0, 4.0, ME)
+    xig, vig = maxwellian(ng0, 0.03, M_AR)
     eps, el, ex, iz, cx = argon_tables()
     gas_n = np.full((nx, ny), 3.0 / (KB * 300.0))
     dt = 7.4e-11
@@ -56,12 +67,12 @@ def test_ccp_discharge_statistics(orc, lib):
 
     # ---- GPU ----
     ctx = Context(nx, ny, dx, dx)
-    se = ctx.species_create(-QE, ME, w, 4 * n0)
-    si = ctx.species_create(QE, M_AR, w, 4 * n0)
+    se = ctx.species_create(-QE, ME, wg, 4 * ng0)
+    si = ctx.species_create(QE, M_AR, wg, 4 * ng0)
     for s in (se, si):
         ctx.set_boundary(s, lib.BND_DISCARD, lib.BND_WRAP)
-    ctx.upload(se, xe, ve)
-    ctx.upload(si, xi, vi)
+    ctx.upload(se, xeg, veg)
+    ctx.upload(si, xig, vig)
     ctx.poisson_create(EPS0)
     ctx.apply_periodic(1)
     ctx.apply_dirichlet(left, 0.0)
@@ -96,19 +107,19 @@ def test_ccp_discharge_statistics(orc, lib):
     co = np.concatenate([po.counts[0], po.counts[1]]).astype(float)
 
     for k in range(4):
-        sd = np.sqrt(cg[k] + co[k]) + 1.0
-        assert abs(cg[k] - co[k]) <= 3.5 * sd, f"process {k}: gpu {cg[k]} oracle {co[k]}"
+        sd = np.sqrt(r * r * cg[k] + co[k]) + 1.0
+        assert abs(r * cg[k] - co[k]) <= 3.5 * sd, f"process {k}: gpu {cg[k]} (x{r}) oracle {co[k]}"
     ne_o, ni_o = po.species[ie].np, po.species[ii].np
-    assert abs(len(xe_g) - ne_o) <= 0.03 * ne_o, (len(xe_g), ne_o)
-    assert abs(ni_g - ni_o) <= 0.03 * ni_o, (ni_g, ni_o)
+    assert abs(r * len(xe_g) - ne_o) <= 0.03 * ne_o, (len(xe_g), ne_o)
+    assert abs(r * ni_g - ni_o) <= 0.03 * ni_o, (ni_g, ni_o)
     # the driven electrode holds V((n-2)Δt) in both
     assert abs(phi_g[0, 0] - po.phi[0, 0]) <= 1e-9 * amp
     # electron energy distribution: the two runs draw different random
     # streams, so their EEDFs are two samples of one distribution.  Two-sample
-    # chi-square on 32 bins (bins with fewer than 10 pooled counts merged),
-    # plus the L1 distance against its null expectation
+    # chi-square (bins with fewer than 10 pooled counts merged), and the L1
+    # distance, stated and below 2 %, beside its null expectation
     # Σ sqrt(2/π) sqrt(p (1-p) (1/n_g + 1/n_o)).
-    bins = np.linspace(0.0, 40.0, 33)
+    bins = np.linspace(0.0, 40.0, 17)
     eg = 0.5 * ME * np.sum(ve_g ** 2, axis=1) / QE
     eo = 0.5 * ME * np.sum(po.species[ie].v[:ne_o] ** 2, axis=1) / QE
     cg_h = np.histogram(eg, bins)[0].astype(float)
@@ -129,4 +140,7 @@ def test_ccp_discharge_statistics(orc, lib):
     merged_o[-1] += acc_o
     from scipy.stats import chi2_contingency
     pval = chi2_contingency(np.array([merged_g, merged_o]))[1]
-    assert pval > 1e-4 and l1 < 2.0 * l1_null, f"EEDF L1 {l1:.4f} (null {l1_null:.4f}), chi2 p={pval:.2e}"
+    print(f"EEDF L1 {l1:.4f} (sampling-noise expectation {l1_null:.4f}), chi2 p={pval:.2e}; "
+          f"electrons gpu {len(xe_g)} (x{r}) oracle {ne_o}")
+    assert l1 < 0.02, f"EEDF L1 {l1:.4f} (null {l1_null:.4f})"
+    assert pval > 1e-4, f"EEDF chi2 p={pval:.2e}"

@@ -392,3 +392,37 @@ def test_errors_are_reported_not_trapped(lib):
     assert e.value.code == 6  # ENAN
     ctx.sync()  # the context stays usable
     ctx.close()
+
+
+def test_cross_section_lookup_matches_oracle(orc, lib):
+    """CrossSection (cross_section.jl:8-16) as the MCC kernels evaluate it
+    (FP32 table, bracket by log-uniform guess or bisection) against the
+    oracle's FP64 interpolation of the same FP32-rounded table at the same
+    FP32-rounded energies: below the first node, on nodes, between nodes,
+    above the last node; a log-uniform table (1024 nodes), a non-uniform
+    table, a two-node and a one-node table.  |σ_gpu - σ_ref| <= 1e-6 max σ."""
+    nx, ny, dx = 9, 2, 1e-3
+    rng = np.random.default_rng(17)
+    eps_lu = np.logspace(-2, 3, 1024)
+    sig_lu = 3e-20 * (1 + np.sin(np.log(eps_lu)) ** 2)
+    eps_nu = np.sort(rng.uniform(0.05, 500.0, 300))
+    sig_nu = rng.uniform(1e-21, 5e-19, 300)
+    tables = [(eps_lu, sig_lu), (eps_nu, sig_nu), (np.array([1.0, 20.0]), np.array([2e-20, 8e-20])),
+              (np.array([5.0]), np.array([4e-20]))]
+    ctx = make_ctx(nx, ny, dx, dx)
+    se = ctx.species_create(-QE, ME, 1.0, 16)
+    procs = [(lib.MCC_ELASTIC_ISOTROPIC, 0.0, e, s) for e, s in tables]
+    mid, _ = ctx.mcc_create(se, procs, 40 * MP, 300.0, np.full((nx, ny), 1e20))
+    for k, (e, s) in enumerate(tables):
+        lo, hi = e[0], e[-1]
+        probes = np.concatenate([[0.0, lo * 0.5, lo, hi, hi * 2.0, 1e4], e[:: max(1, len(e) // 50)],
+                                 rng.uniform(lo, hi, 2000), np.exp(rng.uniform(np.log(lo), np.log(hi), 2000))])
+        g = ctx.mcc_sigma(mid, k, probes)
+        e32 = e.astype(np.float32).astype(np.float64)
+        s32 = s.astype(np.float32).astype(np.float64)
+        ref = np.array([orc.sigma(e32, s32, float(np.float32(x))) for x in probes])
+        err = np.max(np.abs(g - ref))
+        assert err <= 1e-6 * np.max(s), f"table {k}: max |σ_gpu - σ_ref| {err:.3e} (max σ {np.max(s):.3e})"
+        # flat extrapolation outside the table (cross_section.jl:13)
+        assert g[0] == s32[0] and g[1] == s32[0] and g[4] == s32[-1] and g[5] == s32[-1]
+    ctx.close()

@@ -100,6 +100,7 @@ SIGNATURES = [
     ("iskra_set_sort_every", c_int, [CTX, c_int]),
     ("iskra_autotune_sort", c_int, [CTX, c_double, c_int, c_uint64, c_double, dp, dp]),
     ("iskra_solve_info", c_int, [CTX, ip, dp]),
+    ("iskra_poisson_residual", c_int, [CTX, dp, dp, dp]),
     ("iskra_kernel_launches", c_int, [CTX, POINTER(c_uint64)]),
     ("iskra_density_noalloc", c_int, [POINTER(Grid), c_void_p, c_int64, c_int64, c_double, c_void_p, c_void_p,
                                       c_uint64]),

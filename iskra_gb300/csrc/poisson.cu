@@ -1156,7 +1156,10 @@ static void assemble_dirichlet(Poisson *P, const uint8_t *nodes, double phi0) {
 static void assemble_neumann(Poisson *P, const uint8_t *nodes, int dof, bool gauss) {
   const int nx = P->nx, ny = P->ny;
   const double dx = P->dx, dy = P->dy;
-  const double ge = gauss ? 1.0 / dx : 1.0;               // edge-row scale
+  // edge-row ϕ divisor: Δx (reference), Δx Δx (Gauss form: 2 εr/(Δx Δx)
+  // rounds like the stencil rows' 1/(Δx Δx), so the symmetrising scales stay
+  // exact)
+  const double ge = gauss ? dx * dx : dx;
   const double gs = gauss ? 1.0 / (P->eps0 * dx) : 1.0;   // edge-row σ scale
   const double gc = gauss ? 1.0 / P->eps0 : 1.0;          // corner-row σ scale
   auto N = [&](int i, int j) { return nodes[i + nx * j] != 0; };  // 0-based
@@ -1174,8 +1177,8 @@ static void assemble_neumann(Poisson *P, const uint8_t *nodes, int dof, bool gau
         const int ip = i == 0 ? i + 1 : i - 1;
         for (int s = 0; s < 7; s++) R[s] = 0.0;
         for (auto &col : P->sig_cols) col[r] = 0.0;
-        R[0] -= 2 * ER(P, i + 1, j + 1) / dx * ge;
-        R[ip == i + 1 ? 2 : 1] += 2 * ER(P, ip + 1, j + 1) / dx * ge;
+        R[0] -= 2 * ER(P, i + 1, j + 1) / ge;
+        R[ip == i + 1 ? 2 : 1] += 2 * ER(P, ip + 1, j + 1) / ge;
         S[r] += 2 * gs;
       }
       if (cc != d) {
@@ -2565,6 +2568,42 @@ int iskra_solve_info(iskra_ctx *h, int *iters, double *relres) {
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   if (iters) *iters = c->ps->scal_h->iters;
   if (relres) *relres = c->ps->scal_h->relres;
+  return ISKRA_OK;
+}
+
+int iskra_poisson_residual(iskra_ctx *h, const double *f, const double *phi, double *relres) {
+  if (!h || !f || !phi || !relres) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
+  int rc = poisson_prepare(c);
+  if (rc) return rc;
+  Poisson *P = c->ps;
+  const int nx = P->nx, ny = P->ny, nn = P->nn;
+  // the device copies of the fixed values (driven rows are rewritten there)
+  // and of σ (the circuit and the tracker update it) are authoritative
+  std::vector<double> bfix(nn), sig(P->sig_b.size());
+  ISKRA_CUDA(c, cudaMemcpyAsync(bfix.data(), P->bfix_d, nn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (!sig.empty() && P->sigma_d)
+    ISKRA_CUDA(c, cudaMemcpyAsync(sig.data(), P->sigma_d, std::min<size_t>(sig.size(), P->nsig) * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  double r2 = 0, b2 = 0;
+  for (int r = 0; r < nn; r++) {
+    const int i = r % nx, j = r / nx;
+    const double *R = &P->C[(size_t)r * 7];
+    const int col[7] = {r, i > 0 ? r - 1 : r, i < nx - 1 ? r + 1 : r, j > 0 ? r - nx : r, j < ny - 1 ? r + nx : r,
+                        i == 0 ? r + nx - 1 : (i == nx - 1 ? r - nx + 1 : r),
+                        j == 0 ? r + nx * (ny - 1) : (j == ny - 1 ? r - nx * (ny - 1) : r)};
+    double ax = 0;
+    for (int s = 0; s < 7; s++)
+      if (R[s] != 0.0) ax += R[s] * phi[col[s]];
+    for (size_t k = 0; k < P->sig_cols.size(); k++)
+      if (P->sig_cols[k][r] != 0.0) ax += P->sig_cols[k][r] * sig[k];
+    const double b = P->rho_dof[r] ? f[r] / P->eps0 : bfix[r];
+    r2 += (b - ax) * (b - ax);
+    b2 += b * b;
+  }
+  *relres = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
   return ISKRA_OK;
 }
 

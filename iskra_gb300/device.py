@@ -292,6 +292,14 @@ class Context:
         self._c(self.lib.iskra_solve_info(self.h, byref(it), byref(rr)))
         return it.value, rr.value
 
+    def poisson_residual(self, f, phi):
+        """||b - A ϕ|| / ||b|| of a host potential for the right-hand side f (FP64, host)."""
+        fa = _f64(f, (self.nx, self.ny))
+        pa = _f64(phi, (self.nx, self.ny))
+        rr = c_double()
+        self._c(self.lib.iskra_poisson_residual(self.h, _ptr(fa), _ptr(pa), byref(rr)))
+        return rr.value
+
     # -- MCC --
     def mcc_create(self, src, processes, gas_mass, gas_T, gas_n, gas_q=0.0, product=-1):
         """processes: list of (type, energy, eps_nodes, sigma_nodes)."""

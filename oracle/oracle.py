@@ -390,7 +390,7 @@ class PoissonOracle:
         nodes = np.asarray(nodes, dtype=bool)
         nx, ny, er = self.nx, self.ny, self.er
         dx, dy = self.dx, self.dy
-        ge = 1.0 / dx if gauss else 1.0
+        ge = dx ** 2 if gauss else dx   # edge-row ϕ divisor
         gs = 1.0 / (self.eps0 * dx) if gauss else 1.0
         gc = 1.0 / self.eps0 if gauss else 1.0
         for (i, j) in zip(*np.nonzero(nodes)):
@@ -403,8 +403,8 @@ class PoissonOracle:
                 ip_ = i + 1 if i == 0 else i - 1
                 self.C[r, :] = 0.0
                 self.sig_cols[r, :] = 0.0
-                self.C[r, 0] -= 2 * er[i, j] / dx * ge
-                self.C[r, 2 if ip_ == i + 1 else 1] += 2 * er[ip_, j] / dx * ge
+                self.C[r, 0] -= 2 * er[i, j] / ge
+                self.C[r, 2 if ip_ == i + 1 else 1] += 2 * er[ip_, j] / ge
                 self.sig_cols[r, dof - 1] += 2 * gs
             if c != d:
                 ip_ = i + 1 if i == 0 else i - 1

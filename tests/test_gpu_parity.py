@@ -156,6 +156,14 @@ def _setup_bc(target, kind, nx, ny):
             target.apply_neumann(m1, dof)
             target.set_sigma(dof, 3.0e-6)
         ad(m2, 0.0)
+    elif kind == "neumann_gauss":  # the same floating electrode with the Gauss-law rows (circuit runs)
+        ap(1)
+        dof = target.add_dof() if isdev else target.add_new_dof()
+        m1 = np.zeros((nx, ny), bool); m1[0, :] = True
+        m2 = np.zeros((nx, ny), bool); m2[-1, :] = True
+        target.apply_neumann(m1, dof, gauss=True)
+        target.set_sigma(dof, 3.0e-8)
+        ad(m2, 0.0)
     elif kind == "open_box":  # no periodicity, a Dirichlet blob inside: CG path
         m1 = np.zeros((nx, ny), bool); m1[nx // 3:nx // 3 + 3, ny // 2:ny // 2 + 2] = True
         ad(m1, -20.0)
@@ -164,7 +172,8 @@ def _setup_bc(target, kind, nx, ny):
 
 
 @pytest.mark.parametrize("kind,nx,ny", [("slab", 64, 64), ("slab", 130, 128), ("periodic", 128, 2),
-                                        ("neumann", 257, 2), ("neumann", 33, 16), ("open_box", 31, 23),
+                                        ("neumann", 257, 2), ("neumann", 33, 16), ("neumann_gauss", 257, 2),
+                                        ("neumann_gauss", 64, 32), ("open_box", 31, 23),
                                         ("periodic", 32, 32)])
 def test_poisson_matches_oracle(orc, lib, kind, nx, ny):
     dx = dy = 1e-3
@@ -189,7 +198,7 @@ def test_poisson_matches_oracle(orc, lib, kind, nx, ny):
     E_o = orc.electric_field(phi_o, dx, dy)
     assert np.max(np.abs(E_g - E_o)) <= 1e-6 * np.max(np.abs(E_o))
     sep = ctx.set_method(0)
-    if kind in ("slab", "periodic", "neumann") and (ny & (ny - 1)) == 0:
+    if kind in ("slab", "periodic", "neumann", "neumann_gauss") and (ny & (ny - 1)) == 0:
         assert sep == 0, "separable operator expected to use the FFT/tridiagonal solve"
     ctx.close()
 

@@ -343,11 +343,14 @@ int iskra_autotune_sort(iskra_ctx *ctx, double dt, int trial, uint64_t seed,
                         double rtol, double *scale, double *ms_per_step);
 /* Last Poisson solve: iterations and relative residual (synchronises). */
 int iskra_solve_info(iskra_ctx *ctx, int *iters, double *relres);
-/* Relative residual ||b - A x|| / ||b|| of a host potential phi (nx,ny)
- * against the assembled system of calculate_electric_potential(ps, f)
- * (generalized_poisson.jl:372-378: b[ρ] = f/ε0, fixed rows their values,
- * σ rows the current σ), evaluated in FP64 on the host: the accuracy check
- * of a potential computed elsewhere (another context, an ensemble run). */
+/* Relative residual of a host potential phi (nx,ny) against the assembled
+ * system of calculate_electric_potential(ps, f) (generalized_poisson.jl:
+ * 372-378: b[ρ] = f/ε0, identity rows their values, σ the current σ), as
+ * the solver's tolerance measures it: ||b' - A' ϕ|| / ||b'|| over the
+ * non-identity rows, with the identity rows' values and the σ terms moved
+ * into b'.  Evaluated in FP64 on the host: the accuracy check of a potential
+ * computed elsewhere (another context, an ensemble run).  Singular
+ * (all-periodic) operators are measured without the gauge shift. */
 int iskra_poisson_residual(iskra_ctx *ctx, const double *f, const double *phi,
                            double *relres);
 /* Diagnostic with no reference counterpart: number of kernels iskra_step has

@@ -1,7 +1,9 @@
 // ctx.cu -- context, species store, host<->device conversion, error plumbing.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -63,44 +65,86 @@ int collect_device_errors(Ctx *c) {
 // ---------------------------------------------------------------------------
 // upload / download conversion kernels
 // ---------------------------------------------------------------------------
+// Particle columns of a host array in Julia layout (x, y, vx, vy, vz), each
+// either a device staging copy or the page-locked host array itself, which
+// the kernel reads or writes over NVLink-C2C (no staging pass).
+struct Cols5 {
+  const double *c[5];
+};
+struct OutCols5 {
+  double *c[5];
+};
+
 // particle_cell (ParticleInCell.jl:28-35) on the upload side: f = 1 + x/Δh,
-// i = floor(f), h = f - i, quantised by cell_of_position.
-__global__ void k_upload(const double *__restrict__ st, long long np, double dx, double dy,
-                         int nx, int ny, const uint32_t *__restrict__ ids, float4 *xv,
-                         float2 *zc, uint32_t *id, int *err) {
-  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p >= np) return;
-  double X = st[p], Y = st[p + np];
-  double vx = st[p + 2 * np], vy = st[p + 3 * np], vz = st[p + 4 * np];
-  long long ux, uy;
-  const int c = cell_of_position(X, Y, dx, dy, nx, ny, ux, uy);
-  int cell = -1;
-  bool finite = isfinite(X) && isfinite(Y) && isfinite(vx) && isfinite(vy) && isfinite(vz);
-  if (!finite) {
-    atomicOr(err, DERR_NAN);
-  } else if (c < 0) {
-    atomicOr(err, DERR_DOMAIN);
-  } else {
-    cell = c;
+// i = floor(f), h = f - i, quantised by cell_of_position.  next_id (when
+// given) receives max(id) + 1 of the uploaded identifiers (one atomic per
+// warp).  Each thread converts kConvIlp particles and issues all their loads
+// first: read straight from host memory, the loads cross NVLink-C2C with
+// microseconds of latency, and the bytes in flight set the rate.
+constexpr int kConvIlp = 4;
+
+__global__ void __launch_bounds__(256) k_upload(Cols5 in, long long np, double dx, double dy, int nx, int ny,
+                                                const uint32_t *__restrict__ ids, float4 *xv, float2 *zc,
+                                                uint32_t *id, int *err, unsigned *next_id) {
+  const long long base = (long long)blockIdx.x * blockDim.x * kConvIlp + threadIdx.x;
+  double X[kConvIlp], Y[kConvIlp], VX[kConvIlp], VY[kConvIlp], VZ[kConvIlp];
+  uint32_t I[kConvIlp];
+#pragma unroll
+  for (int u = 0; u < kConvIlp; u++) {
+    const long long p = base + (long long)u * blockDim.x;
+    if (p < np) {
+      X[u] = in.c[0][p];
+      Y[u] = in.c[1][p];
+      VX[u] = in.c[2][p];
+      VY[u] = in.c[3][p];
+      VZ[u] = in.c[4][p];
+      I[u] = ids ? ids[p] : (uint32_t)(p + 1);
+    }
   }
-  xv[p] = make_float4((float)ux * kOffInv, (float)uy * kOffInv, (float)vx, (float)vy);
-  zc[p] = make_float2((float)vz, __int_as_float(cell));
-  id[p] = ids ? ids[p] : (uint32_t)(p + 1);
+  unsigned mx = 0;
+  int flags = 0;
+#pragma unroll
+  for (int u = 0; u < kConvIlp; u++) {
+    const long long p = base + (long long)u * blockDim.x;
+    if (p >= np) continue;
+    long long ux, uy;
+    const int c = cell_of_position(X[u], Y[u], dx, dy, nx, ny, ux, uy);
+    int cell = -1;
+    const bool finite = isfinite(X[u]) && isfinite(Y[u]) && isfinite(VX[u]) && isfinite(VY[u]) && isfinite(VZ[u]);
+    if (!finite) flags |= DERR_NAN;
+    else if (c < 0) flags |= DERR_DOMAIN;
+    else cell = c;
+    xv[p] = make_float4((float)ux * kOffInv, (float)uy * kOffInv, (float)VX[u], (float)VY[u]);
+    zc[p] = make_float2((float)VZ[u], __int_as_float(cell));
+    id[p] = I[u];
+    mx = max(mx, I[u] + 1u);
+  }
+  if (flags) atomicOr(err, flags);
+  if (next_id && ids) {
+    const unsigned m = __reduce_max_sync(0xffffffffu, mx);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(next_id, m);
+  }
 }
 
-__global__ void k_download(double *__restrict__ st, long long np, double dx, double dy,
-                           const float4 *__restrict__ xv, const float2 *__restrict__ zc) {
+__global__ void k_download(OutCols5 out, long long np, double dx, double dy, const float4 *__restrict__ xv,
+                           const float2 *__restrict__ zc, const uint32_t *__restrict__ idd,
+                           uint32_t *__restrict__ id_out) {
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= np) return;
   float4 a = xv[p];
   float2 b = zc[p];
   int cell = __float_as_int(b.y);
   int i0 = cell & 0xffff, j0 = cell >> 16;
-  st[p] = ((double)i0 + (double)a.x) * dx;
-  st[p + np] = ((double)j0 + (double)a.y) * dy;
-  st[p + 2 * np] = a.z;
-  st[p + 3 * np] = a.w;
-  st[p + 4 * np] = b.x;
+  if (out.c[0]) {
+    out.c[0][p] = ((double)i0 + (double)a.x) * dx;
+    out.c[1][p] = ((double)j0 + (double)a.y) * dy;
+  }
+  if (out.c[2]) {
+    out.c[2][p] = a.z;
+    out.c[3][p] = a.w;
+    out.c[4][p] = b.x;
+  }
+  if (id_out) id_out[p] = idd[p];
 }
 
 __global__ void k_upload_E(const double *__restrict__ E, int nx, int ny, float2 *E32, double *E64) {
@@ -129,47 +173,94 @@ static int check_sid(Ctx *c, int sid) {
   return ISKRA_OK;
 }
 
-// Host particle arrays (column-major, leading dimension ld) -> one store
-// segment (buffer 0) through the context's staging buffer; synchronous.
-int upload_particles(Ctx *c, const double *x, const double *v, const uint32_t *id, int64_t np, int64_t ld,
-                     float4 *xv, float2 *zc, uint32_t *idd) {
-  int rc = ensure_stage(c, (size_t)(np > 0 ? np : 1) * (5 * sizeof(double) + sizeof(uint32_t)));
-  if (rc) return rc;
-  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
-  double *st = c->stage;
-  uint32_t *ids = id ? (uint32_t *)(st + 5 * np) : nullptr;
-  for (int k = 0; k < 2 && np > 0; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(st + k * np, x + k * ld, np * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  for (int k = 0; k < 3 && np > 0; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(st + (2 + k) * np, v + k * ld, np * sizeof(double), cudaMemcpyHostToDevice,
-                                  c->stream));
-  if (ids && np > 0)
-    ISKRA_CUDA(c, cudaMemcpyAsync(ids, id, np * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
-  if (np > 0) {
-    const long long B = (np + 255) / 256;
-    k_upload<<<(unsigned)B, 256, 0, c->stream>>>(st, np, c->g.dx, c->g.dy, c->nx, c->ny, ids, xv, zc, idd, c->d_err);
-    ISKRA_CUDA(c, cudaGetLastError());
+// Device address of a host array the GPU can read and write directly
+// (page-locked memory registered with CUDA: cudaHostAlloc, cudaHostRegister,
+// pinned framework tensors), or nullptr (pageable memory: staged copies).
+// On GB300 the kernel then moves the data over NVLink-C2C in the same pass
+// that converts it, instead of a copy into a staging buffer followed by a
+// conversion pass.
+static const void *host_alias(const void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // unregistered pointer: not an error for the caller
+    return nullptr;
   }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return a.devicePointer;
+}
+
+// Host particle arrays (column-major, leading dimension ld) -> one store
+// segment: read directly when every array is page-locked and mapped, else
+// through the context's staging buffer.  next_id (device, optional) receives
+// max(id) + 1 when identifiers are given.  Synchronous: the host arrays are
+// free again on return.
+int upload_particles(Ctx *c, const double *x, const double *v, const uint32_t *id, int64_t np, int64_t ld,
+                     float4 *xv, float2 *zc, uint32_t *idd, unsigned *next_id) {
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (np <= 0) return collect_device_errors(c);
+  const double *hx = (const double *)host_alias(x), *hv = (const double *)host_alias(v);
+  const uint32_t *hid = id ? (const uint32_t *)host_alias(id) : nullptr;
+  Cols5 in{};
+  const uint32_t *ids = nullptr;
+  if (hx && hv && (!id || hid)) {
+    for (int k = 0; k < 2; k++) in.c[k] = hx + k * ld;
+    for (int k = 0; k < 3; k++) in.c[2 + k] = hv + k * ld;
+    ids = hid;
+  } else {
+    int rc = ensure_stage(c, (size_t)np * (5 * sizeof(double) + sizeof(uint32_t)));
+    if (rc) return rc;
+    double *st = c->stage;
+    for (int k = 0; k < 2; k++)
+      ISKRA_CUDA(c, cudaMemcpyAsync(st + k * np, x + k * ld, np * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    for (int k = 0; k < 3; k++)
+      ISKRA_CUDA(c, cudaMemcpyAsync(st + (2 + k) * np, v + k * ld, np * sizeof(double), cudaMemcpyHostToDevice,
+                                    c->stream));
+    if (id) {
+      uint32_t *sid = (uint32_t *)(st + 5 * np);
+      ISKRA_CUDA(c, cudaMemcpyAsync(sid, id, np * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+      ids = sid;
+    }
+    for (int k = 0; k < 5; k++) in.c[k] = st + k * np;
+  }
+  const long long B = (np + 256 * kConvIlp - 1) / (256 * kConvIlp);
+  k_upload<<<(unsigned)B, 256, 0, c->stream>>>(in, np, c->g.dx, c->g.dy, c->nx, c->ny, ids, xv, zc, idd, c->d_err,
+                                               next_id);
+  ISKRA_CUDA(c, cudaGetLastError());
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   return collect_device_errors(c);
 }
 
-// One store segment (np live particles, no holes) -> host arrays; synchronous.
+// One store segment (np live particles, no holes) -> host arrays (x, v, id
+// each optional): written directly when page-locked and mapped, else through
+// the staging buffer; synchronous.
 int download_particles(Ctx *c, const float4 *xv, const float2 *zc, const uint32_t *idd, long long np, double *x,
                        double *v, uint32_t *id, int64_t ld) {
   if (np == 0) return ISKRA_OK;
-  int rc = ensure_stage(c, (size_t)np * 5 * sizeof(double));
-  if (rc) return rc;
+  double *hx = x ? (double *)host_alias(x) : nullptr, *hv = v ? (double *)host_alias(v) : nullptr;
+  uint32_t *hid = id ? (uint32_t *)host_alias(id) : nullptr;
+  const bool direct = (!x || hx) && (!v || hv) && (!id || hid);
+  OutCols5 out{};
+  if (direct) {
+    for (int k = 0; k < 2 && hx; k++) out.c[k] = hx + k * ld;
+    for (int k = 0; k < 3 && hv; k++) out.c[2 + k] = hv + k * ld;
+  } else {
+    int rc = ensure_stage(c, (size_t)np * 5 * sizeof(double));
+    if (rc) return rc;
+    for (int k = 0; k < 5; k++) out.c[k] = c->stage + k * np;
+  }
   const long long B = (np + 255) / 256;
-  k_download<<<(unsigned)B, 256, 0, c->stream>>>(c->stage, np, c->g.dx, c->g.dy, xv, zc);
+  k_download<<<(unsigned)B, 256, 0, c->stream>>>(out, np, c->g.dx, c->g.dy, xv, zc, idd, direct ? hid : nullptr);
   ISKRA_CUDA(c, cudaGetLastError());
-  for (int k = 0; k < 2 && x; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(x + k * ld, c->stage + k * np, np * sizeof(double), cudaMemcpyDeviceToHost,
-                                  c->stream));
-  for (int k = 0; k < 3 && v; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(v + k * ld, c->stage + (2 + k) * np, np * sizeof(double), cudaMemcpyDeviceToHost,
-                                  c->stream));
-  if (id) ISKRA_CUDA(c, cudaMemcpyAsync(id, idd, np * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  if (!direct) {
+    for (int k = 0; k < 2 && x; k++)
+      ISKRA_CUDA(c, cudaMemcpyAsync(x + k * ld, c->stage + k * np, np * sizeof(double), cudaMemcpyDeviceToHost,
+                                    c->stream));
+    for (int k = 0; k < 3 && v; k++)
+      ISKRA_CUDA(c, cudaMemcpyAsync(v + k * ld, c->stage + (2 + k) * np, np * sizeof(double), cudaMemcpyDeviceToHost,
+                                    c->stream));
+    if (id) ISKRA_CUDA(c, cudaMemcpyAsync(id, idd, np * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  }
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   return ISKRA_OK;
 }
@@ -341,8 +432,10 @@ int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t ca
   s.dev.cap = cap;
   size_t nn = (size_t)c->nn;
   for (int b = 0; b < 2; b++) {
-    ISKRA_CUDA(c, cudaMalloc(&s.dev.xv[b], cap * sizeof(float4)));
-    ISKRA_CUDA(c, cudaMalloc(&s.dev.zc[b], cap * sizeof(float2)));
+    // kStorePad slots past the capacity: the push's bulk copies read whole
+    // 32-record stages (and the 16-byte-aligned record below a stage)
+    ISKRA_CUDA(c, cudaMalloc(&s.dev.xv[b], (cap + kStorePad) * sizeof(float4)));
+    ISKRA_CUDA(c, cudaMalloc(&s.dev.zc[b], (cap + kStorePad) * sizeof(float2)));
     ISKRA_CUDA(c, cudaMalloc(&s.dev.id[b], cap * sizeof(uint32_t)));
   }
   ISKRA_CUDA(c, cudaMalloc(&s.dev.st, sizeof(SpeciesState)));
@@ -392,35 +485,14 @@ int iskra_species_upload(iskra_ctx *h, int sid, const double *x, const double *v
       if (wg[p] != s.w0)
         return set_err(c, ISKRA_EINVAL, "per-particle weights must all equal w0 on the device store");
   }
-  int rc = ensure_stage(c, (size_t)(np > 0 ? np : 1) * (5 * sizeof(double) + sizeof(uint32_t)));
-  if (rc) return rc;
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
-  double *st = c->stage;
-  uint32_t *ids = id ? (uint32_t *)(st + 5 * np) : nullptr;
-  for (int k = 0; k < 2 && np > 0; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(st + k * np, x + k * ld, np * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  for (int k = 0; k < 3 && np > 0; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(st + (2 + k) * np, v + k * ld, np * sizeof(double), cudaMemcpyHostToDevice,
-                                  c->stream));
-  if (ids && np > 0)
-    ISKRA_CUDA(c, cudaMemcpyAsync(ids, id, np * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
   SpeciesState st0{};
   st0.np = np;
   st0.cur = 0;
-  uint32_t maxid = (uint32_t)np;
-  if (id)
-    for (int64_t p = 0; p < np; p++) maxid = id[p] > maxid ? id[p] : maxid;
-  st0.next_id = maxid + 1;
+  st0.next_id = (uint32_t)np + 1;  // identifiers 1..np, or max(id) + 1 (raised by the upload kernel)
   ISKRA_CUDA(c, cudaMemcpyAsync(s.dev.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, c->stream));
-  if (np > 0) {
-    int T = 256;
-    long long B = (np + T - 1) / T;
-    k_upload<<<(unsigned)B, T, 0, c->stream>>>(st, np, c->g.dx, c->g.dy, c->nx, c->ny, ids, s.dev.xv[0],
-                                               s.dev.zc[0], s.dev.id[0], c->d_err);
-    ISKRA_CUDA(c, cudaGetLastError());
-  }
-  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));  // staging + host buffers done
-  rc = collect_device_errors(c);
+  unsigned *next_id = (unsigned *)((char *)s.dev.st + offsetof(SpeciesState, next_id));
+  int rc = upload_particles(c, x, v, id, np, ld, s.dev.xv[0], s.dev.zc[0], s.dev.id[0], next_id);
   if (rc) return rc;
   rc = launch_sort(c, sid);
   if (rc) return rc;
@@ -447,21 +519,8 @@ int iskra_species_download(iskra_ctx *h, int sid, double *x, double *v, double *
   if (np_out) *np_out = np;
   if (np > ld) return set_err(c, ISKRA_ECAPACITY, "host arrays too small for the live particles");
   if (np == 0) return ISKRA_OK;
-  rc = ensure_stage(c, (size_t)np * 5 * sizeof(double));
+  rc = download_particles(c, s.dev.xv[st.cur], s.dev.zc[st.cur], s.dev.id[st.cur], np, x, v, id, ld);
   if (rc) return rc;
-  int T = 256;
-  long long B = (np + T - 1) / T;
-  k_download<<<(unsigned)B, T, 0, c->stream>>>(c->stage, np, c->g.dx, c->g.dy, s.dev.xv[st.cur], s.dev.zc[st.cur]);
-  ISKRA_CUDA(c, cudaGetLastError());
-  for (int k = 0; k < 2 && x; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(x + k * ld, c->stage + k * np, np * sizeof(double), cudaMemcpyDeviceToHost,
-                                  c->stream));
-  for (int k = 0; k < 3 && v; k++)
-    ISKRA_CUDA(c, cudaMemcpyAsync(v + k * ld, c->stage + (2 + k) * np, np * sizeof(double),
-                                  cudaMemcpyDeviceToHost, c->stream));
-  if (id)
-    ISKRA_CUDA(c, cudaMemcpyAsync(id, s.dev.id[st.cur], np * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
-  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   if (wg)
     for (long long p = 0; p < np; p++) wg[p] = s.w0;
   return ISKRA_OK;

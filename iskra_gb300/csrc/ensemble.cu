@@ -39,6 +39,12 @@ struct EnsMcc {
   uint2 *keys = nullptr;                 // R
   unsigned long long *counts = nullptr;  // R x N
   int N = 0;
+  MccWork *work = nullptr;               // work list (R x work_cap entries)
+  unsigned long long *nwork = nullptr;   // R
+  // the list is made by the push of the set's source species in the step
+  // before (the first set of each source species); otherwise by a selection
+  // pass at the start of the step
+  bool folded = false;
 };
 
 struct Ens {
@@ -59,9 +65,8 @@ struct Ens {
   double graph_dt = 0;
   cudaGraphExec_t compact_graph = nullptr;
   int compact_every = 32;
-  void *work = nullptr;                   // MCC work list (R x capacity entries)
-  unsigned long long work_cap = 0;
-  unsigned long long *nwork = nullptr;
+  unsigned long long work_cap = 0;        // MCC work-list entries per run and set
+  bool lists_valid = false;               // the folded sets' lists hold the next step's selections
   std::string err;
 };
 
@@ -95,6 +100,12 @@ __global__ void k_runs_state(SpeciesState *st, int R, long long cap, int op) {
 __global__ void k_ens_step_begin(unsigned long long *d_step) {
   pdl_wait();
   *d_step += 1ull;
+}
+
+__global__ void k_zero_u64_runs(unsigned long long *p, int n) {
+  pdl_wait();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0ull;
 }
 
 // Drop discarded particles of every run: live particles move to the other
@@ -162,15 +173,31 @@ static int ens_queue_step(Ens *e, double dt) {
     if (prod >= 0)
       ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[prod].st, R, e->sp[prod].cap, (int)kRunsAppendBegin));
     int rc = launch_mcc_runs(c, m, dt, R, e->sp[src].views, prod >= 0 ? e->sp[prod].views : e->sp[src].views,
-                             e->mcc[m].keys, e->mcc[m].counts, e->E32, e->nn, bpr, e->work, e->nwork, e->work_cap,
-                             e->d_step, e->d_err, st);
+                             e->mcc[m].keys, e->mcc[m].counts, e->E32, e->nn, bpr, e->mcc[m].work, e->mcc[m].nwork,
+                             e->work_cap, e->d_step, e->d_err, st, e->mcc[m].folded ? kMccCollideOnly : kMccBoth);
     if (rc) return ens_err(e, rc, c->err);
     ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[src].st, R, e->sp[src].cap, (int)kRunsAppendEnd));
     if (prod >= 0)
       ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[prod].st, R, e->sp[prod].cap, (int)kRunsAppendEnd));
   }
+  // the pushes make the folded sets' lists for the next step
+  for (int m = 0; m < (int)e->mcc.size(); m++)
+    if (e->mcc[m].folded) ENS_CUDA(e, launch_pdl(k_zero_u64_runs, rb, 128, 0, st, e->mcc[m].nwork, R));
   for (int s = 0; s < (int)e->sp.size(); s++) {
-    int rc = launch_push_runs(c, s, e->sp[s].views, R, e->E32, (float)dt, bpr, e->d_err, st);
+    PushSelect S{};
+    bool sel = false;
+    for (int m = 0; m < (int)e->mcc.size() && !sel; m++) {
+      if (!e->mcc[m].folded || mcc_src(c, m) != s) continue;
+      int rc = mcc_push_select(c, m, dt, &S);
+      if (rc) return ens_err(e, rc, c->err);
+      S.keys = e->mcc[m].keys;
+      S.work = e->mcc[m].work;
+      S.nwork = e->mcc[m].nwork;
+      S.cap_run = e->work_cap;
+      S.d_step = e->d_step;
+      sel = true;
+    }
+    int rc = launch_push_runs(c, s, e->sp[s].views, R, e->E32, (float)dt, bpr, e->d_err, st, sel ? &S : nullptr);
     if (rc) return ens_err(e, rc, c->err);
   }
   FieldRunsHost H{};
@@ -190,6 +217,22 @@ static int ens_queue_step(Ens *e, double dt) {
   H.err = e->d_err;
   int rc = launch_field_runs(c, R, H, st);
   if (rc) return ens_err(e, rc, c->err);
+  return ISKRA_OK;
+}
+
+// The folded sets' work lists for the next step, by a selection pass (after
+// an upload or a compaction moved the particles the last push selected).
+static int ens_queue_select_ahead(Ens *e, double dt) {
+  Ctx *c = e->c;
+  const int bpr = ens_blocks_per_run(e);
+  for (int m = 0; m < (int)e->mcc.size(); m++) {
+    if (!e->mcc[m].folded) continue;
+    const int src = mcc_src(c, m), prod = mcc_prod(c, m);
+    int rc = launch_mcc_runs(c, m, dt, e->R, e->sp[src].views, prod >= 0 ? e->sp[prod].views : e->sp[src].views,
+                             e->mcc[m].keys, e->mcc[m].counts, e->E32, e->nn, bpr, e->mcc[m].work,
+                             e->mcc[m].nwork, e->work_cap, e->d_step, e->d_err, c->stream, kMccSelectAhead);
+    if (rc) return ens_err(e, rc, c->err);
+  }
   return ISKRA_OK;
 }
 
@@ -260,6 +303,8 @@ static void ens_free(Ens *e) {
   for (auto &m : e->mcc) {
     cudaFree(m.keys);
     cudaFree(m.counts);
+    cudaFree(m.work);
+    cudaFree(m.nwork);
   }
   cudaFree(e->rho);
   cudaFree(e->x);
@@ -267,8 +312,6 @@ static void ens_free(Ens *e) {
   cudaFree(e->amp);
   cudaFree(e->d_step);
   cudaFree(e->d_err);
-  cudaFree(e->work);
-  cudaFree(e->nwork);
   if (e->h_err) cudaFreeHost(e->h_err);
   *e = Ens{};  // detached: every later call but destroy fails
 }
@@ -390,8 +433,15 @@ int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t cap_per_run, iskra_ens 
   }
   if (!c->mccs.empty()) {
     e->work_cap = (unsigned long long)cap_per_run;  // per run segment
-    ENS_ALLOC(e->work, R * e->work_cap * mcc_work_entry_bytes());
-    ENS_ALLOC(e->nwork, R * sizeof(unsigned long long));
+    std::vector<bool> src_folded(c->species.size(), false);
+    for (int m = 0; m < (int)e->mcc.size(); m++) {
+      ENS_ALLOC(e->mcc[m].work, R * e->work_cap * mcc_work_entry_bytes());
+      ENS_ALLOC(e->mcc[m].nwork, R * sizeof(unsigned long long));
+      cudaMemset(e->mcc[m].nwork, 0, R * sizeof(unsigned long long));
+      const int src = mcc_src(c, m);
+      e->mcc[m].folded = !src_folded[src];
+      src_folded[src] = true;
+    }
   }
   ENS_ALLOC(e->d_step, sizeof(unsigned long long));
   cudaMemset(e->d_step, 0, sizeof(unsigned long long));
@@ -448,6 +498,7 @@ int iskra_ens_upload(iskra_ens *h, int run, int sid, const double *x, const doub
   if (np < 0 || np > q.cap) return ens_err(e, ISKRA_ECAPACITY, "np exceeds the run capacity");
   if (np > 0 && (!x || !v || ld < np)) return ens_err(e, ISKRA_EINVAL, "bad particle arrays");
   const size_t off = (size_t)run * q.cap;
+  e->lists_valid = false;  // new particles: the next step selects from scratch
   int rc = upload_particles(e->c, x, v, id, np, ld, q.xv[0] + off, q.zc[0] + off, q.id[0] + off);
   if (rc) return ens_err(e, rc, e->c->err);
   SpeciesState s0{};
@@ -474,6 +525,7 @@ int iskra_ens_count(iskra_ens *h, int run, int sid, int64_t *np) {
     if (rc) return rc;
   }
   ENS_CUDA(e, cudaGraphLaunch(e->compact_graph, e->c->stream));
+  e->lists_valid = false;  // the particles moved
   SpeciesState s{};
   ENS_CUDA(e, cudaMemcpyAsync(&s, e->sp[sid].st + run, sizeof(s), cudaMemcpyDeviceToHost, e->c->stream));
   ENS_CUDA(e, cudaStreamSynchronize(e->c->stream));
@@ -506,12 +558,14 @@ int iskra_ens_step(iskra_ens *h, double dt, int nsteps) {
   Ens *e = &h->e;
   if (!(dt > 0) || nsteps < 0) return ens_err(e, ISKRA_EINVAL, "bad dt / nsteps");
   if (nsteps == 0) return ISKRA_OK;
+  if (!e->keys_valid) e->lists_valid = false;  // selections drawn with other keys
   int rc = ens_update_keys(e);
   if (rc) return rc;
   if (e->graph && e->graph_dt != dt) {
     cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;
   }
+  if (e->graph_dt != dt) e->lists_valid = false;  // selections drawn for another Δt
   if (!e->graph) {
     rc = ens_capture(e, &e->graph, [&]() { return ens_queue_step(e, dt); });
     if (rc) return rc;
@@ -522,10 +576,17 @@ int iskra_ens_step(iskra_ens *h, double dt, int nsteps) {
     if (rc) return rc;
   }
   for (int n = 0; n < nsteps; n++) {
+    if (!e->lists_valid) {
+      rc = ens_queue_select_ahead(e, dt);
+      if (rc) return rc;
+      e->lists_valid = true;
+    }
     ENS_CUDA(e, cudaGraphLaunch(e->graph, e->c->stream));
     e->step++;
-    if (e->compact_every > 0 && e->step % e->compact_every == 0)
+    if (e->compact_every > 0 && e->step % e->compact_every == 0) {
       ENS_CUDA(e, cudaGraphLaunch(e->compact_graph, e->c->stream));
+      e->lists_valid = false;  // the particles moved
+    }
   }
   return ISKRA_OK;
 }

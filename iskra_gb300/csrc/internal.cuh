@@ -29,6 +29,9 @@ constexpr int kMaxSpecies = 8;
 // most kMaxCell particles per cell the sum stays below 4 * 16383 * 2^48 < 2^64.
 constexpr unsigned kMaxCell = 16383;
 constexpr int kMaxMcc = 8;
+// slots allocated past a species' capacity in its record arrays (whole-stage
+// bulk copies of the push may read up to 33 records past a slice's end)
+constexpr int kStorePad = 64;
 
 // device error flags (bitmask in Ctx::d_err)
 enum : int {
@@ -114,6 +117,20 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
+// MCC work-list entry (mcc.cu): a selected particle's record as the
+// collision pass needs it -- a = {hx, hy, vx, vy}, b = {vz bits, cell, id,
+// slot} -- one 32-byte sector.
+struct __align__(16) MccWork {
+  float4 a;
+  uint4 b;
+};
+__device__ __forceinline__ MccWork mcc_entry(float4 a, float2 b, uint32_t pid, uint32_t slot) {
+  MccWork e;
+  e.a = a;
+  e.b = make_uint4(__float_as_uint(b.x), __float_as_uint(b.y), pid, slot);
+  return e;
+}
+
 // uniform in [0,1) with 24 random bits
 __device__ __forceinline__ float u01(uint32_t v) { return (float)(v >> 8) * 5.9604644775390625e-08f; }
 
@@ -139,6 +156,41 @@ struct Stream {
     float rad = sqrtf(-2.0f * logf(a));
     return rad * cospif(2.0f * b);
   }
+};
+
+// The MCC random stream of one particle in one step (mcc.cu): Philox keyed by
+// the set's key, counter (particle id, step, draw).
+__device__ __forceinline__ Stream particle_stream(uint32_t pid, unsigned long long step, uint2 key) {
+  Stream R;
+  R.ctr = U4{pid, (uint32_t)step, (uint32_t)(step >> 32), 0u};
+  R.k0 = key.x;
+  R.k1 = key.y;
+  R.left = 0;
+  return R;
+}
+
+// selections ~ Poisson(lam) by inversion (bounded): the stream's first draw
+__device__ __forceinline__ int draw_selections(Stream &R, float lam, float expl) {
+  const float u = R.next();
+  float pk = expl, cdf = expl;
+  int nsel = 0;
+  while (u > cdf && nsel < 16) {
+    nsel++;
+    pk *= lam / nsel;
+    cdf += pk;
+  }
+  return nsel;
+}
+
+// Selection for the next MCC step folded into an ensemble push (k_push_runs):
+// per run, the set's key, its work list segment and counter.
+struct PushSelect {
+  float lam;                    // N maxPt of the MCC set
+  const uint2 *keys;            // R
+  MccWork *work;                // R x cap_run
+  unsigned long long *nwork;    // R
+  unsigned long long cap_run;
+  const unsigned long long *d_step;  // the current step (entries are for step + 1)
 };
 
 
@@ -431,15 +483,20 @@ struct FieldRunsHost {
 };
 int launch_field_runs(Ctx *c, int R, FieldRunsHost &H, cudaStream_t st);
 int upload_particles(Ctx *c, const double *x, const double *v, const uint32_t *id, int64_t np, int64_t ld,
-                     float4 *xv, float2 *zc, uint32_t *idd);
+                     float4 *xv, float2 *zc, uint32_t *idd, unsigned *next_id = nullptr);
 int download_particles(Ctx *c, const float4 *xv, const float2 *zc, const uint32_t *idd, long long np, double *x,
                        double *v, uint32_t *id, int64_t ld);
 int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float2 *E2, float dt, int blocks_per_run,
-                     int *err, cudaStream_t st);
+                     int *err, cudaStream_t st, const PushSelect *sel = nullptr);
+// phases of an MCC launch over runs: selection then collisions; collisions
+// only (the work list was made by the previous step's push); selection only,
+// for the step after the device step counter's (a list made before a step)
+enum { kMccBoth = 0, kMccCollideOnly = 1, kMccSelectAhead = 2 };
 int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, const SpeciesDev *prod,
                     const uint2 *keys, unsigned long long *counts, const float2 *E32, int nn, int blocks_per_run,
                     void *work, unsigned long long *nwork, unsigned long long cap_work,
-                    const unsigned long long *d_step, int *err, cudaStream_t st);
+                    const unsigned long long *d_step, int *err, cudaStream_t st, int phases = kMccBoth);
+int mcc_push_select(Ctx *c, int mid, double dt, PushSelect *S);
 size_t mcc_work_entry_bytes();
 int ensure_mcc_work(Ctx *c);
 void ensembles_detach(Ctx *c);
@@ -486,6 +543,60 @@ struct WarmArgs {
   unsigned fixed_bit;
 };
 bool poisson_warm_args(Ctx *c, WarmArgs *w);
+__device__ __forceinline__ void warm_node(const WarmArgs &W, bool hist, int k) {
+  const float2 xa = W.xd[k];
+  if (hist && !(W.cls[k] & W.fixed_bit)) W.xd[k] = df_add(make_float2(2.f * xa.x, 2.f * xa.y), df_neg(W.xh[k]));
+  W.xh[k] = xa;
+}
+
+// Density of every species and ρ = Σ q n at one node in double-float
+// (kinetic.jl:53, RegularGrids.jl:26-38, ParticleInCell.jl:118-122): the
+// int64 node sums of the species whose deposit is unconsumed are turned into
+// densities (and cleared), the others' stored densities enter as they are.
+struct FinalizeDfArgs {
+  int ns;
+  unsigned long long *acc[kMaxSpecies];
+  unsigned *cnt[kMaxSpecies];
+  float2 *n[kMaxSpecies];
+  float2 scale[kMaxSpecies];  // w0 * 2^-48
+  float2 q[kMaxSpecies];
+  int consume[kMaxSpecies];
+};
+__device__ __forceinline__ void finalize_df_node(const FinalizeDfArgs &A, const float2 *__restrict__ vol_inv,
+                                                 const float2 *__restrict__ bg, float2 *__restrict__ rho, int k,
+                                                 int &flags) {
+  const float2 vi = vol_inv[k];
+  float2 r = bg ? bg[k] : make_float2(0.f, 0.f);
+  unsigned long long a[kMaxSpecies];
+  unsigned cn[kMaxSpecies];
+  float2 nold[kMaxSpecies];
+#pragma unroll
+  for (int s = 0; s < kMaxSpecies; s++) {
+    if (s >= A.ns) break;
+    if (A.consume[s]) {
+      a[s] = A.acc[s][k];
+      cn[s] = A.cnt[s][k];
+    } else {
+      nold[s] = A.n[s][k];
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < kMaxSpecies; s++) {
+    if (s >= A.ns) break;
+    float2 n;
+    if (A.consume[s]) {
+      if (cn[s] > kMaxCell) flags |= DERR_OVERFLOW;
+      n = df_mul(df_mul(df_from_u64(a[s]), A.scale[s]), vi);
+      A.n[s][k] = n;
+      A.acc[s][k] = 0ull;
+      A.cnt[s][k] = 0u;
+    } else {
+      n = nold[s];
+    }
+    r = df_add(r, df_mul(n, A.q[s]));
+  }
+  rho[k] = r;
+}
 int launch_step_density(Ctx *c);  // ρ of a graph step (with the fused warm start)
 void poisson_destroy(Poisson *p);
 void mcc_destroy(Mcc *m);

@@ -153,49 +153,27 @@ __device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsi
 }
 
 // ---- two-phase null-collision step --------------------------------------
-// Phase 1 (k_mcc_select, every live particle): the particle's first draw
-// gives its number of selections c ~ Poisson(N maxPt); particles with c > 0
-// go to a work list (run, slot, c).  Phase 2 (k_mcc_collide, the work list
-// only): each entry replays its particle's stream past that draw and runs
-// the c selections -- the k choice, acceptance test and kinematics -- in
-// order.  With N maxPt ~ 0.1 a warp of phase 2 holds 32 colliding particles
-// instead of the ~3 a single pass over all particles would.
-struct MccWork {
-  uint32_t slot;
-  uint32_t nsel;
-};
-
-constexpr int kSelChunk = 2048;  // particles per block pass of k_mcc_select
-
-__device__ __forceinline__ Stream particle_stream(uint32_t pid, unsigned long long step, uint2 key) {
-  Stream R;
-  R.ctr = U4{pid, (uint32_t)step, (uint32_t)(step >> 32), 0u};
-  R.k0 = key.x;
-  R.k1 = key.y;
-  R.left = 0;
-  return R;
-}
-
-// selections ~ Poisson(lam) by inversion (bounded)
-__device__ __forceinline__ int draw_selections(Stream &R, float lam, float expl) {
-  const float u = R.next();
-  float pk = expl, cdf = expl;
-  int nsel = 0;
-  while (u > cdf && nsel < 16) {
-    nsel++;
-    pk *= lam / nsel;
-    cdf += pk;
-  }
-  return nsel;
-}
+// Phase 1 (k_mcc_select, every live particle; in ensembles the push of the
+// step before, k_push_runs): the particle's first draw gives its number of
+// selections c ~ Poisson(N maxPt); particles with c > 0 go to a work list
+// as their whole record (MccWork: position, velocity, cell, id, slot).
+// Phase 2 (k_mcc_collide, the work list only): each entry replays its
+// particle's stream (the first draw gives c again) and runs the c selections
+// -- the k choice, acceptance test and kinematics -- in order, then writes
+// the changed velocity back to the particle's slot.  With N maxPt ~ 0.1 a
+// warp of phase 2 holds 32 colliding particles instead of the ~3 a single
+// pass over all particles would, and it reads them as one contiguous
+// 32-byte entry each instead of three scattered records.
+constexpr int kSelChunk = 1024;  // particles per block pass of k_mcc_select
 
 // Phase 1 over the particles of run blockIdx.y (R = 1 for a single context):
 // a block collects the selected particles of a chunk in shared memory and
 // appends them to its run's segment [r cap_run, ...) of the work list with
-// one atomic on the run's counter nwork[r].
+// one atomic on the run's counter nwork[r].  step_ahead = 1 draws for the
+// step after the device counter's (a list built before the step begins).
 __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict__ src, float lam, uint2 key1,
                                                     const uint2 *__restrict__ keys,
-                                                    const unsigned long long *__restrict__ d_step,
+                                                    const unsigned long long *__restrict__ d_step, int step_ahead,
                                                     MccWork *__restrict__ work, unsigned long long *__restrict__ nwork,
                                                     unsigned long long cap_run, int *err) {
   pdl_wait();
@@ -209,9 +187,10 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
   const int lane = threadIdx.x & 31;
   const long long np = s.st->np;
   const int cur = s.st->cur;
+  const float4 *__restrict__ xv = pick(s.xv[0], s.xv[1], cur);
   const float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
   const uint32_t *__restrict__ ids = pick(s.id[0], s.id[1], cur);
-  const unsigned long long step = *d_step;
+  const unsigned long long step = *d_step + (unsigned long long)step_ahead;
   const float expl = __expf(-lam);
   MccWork *__restrict__ seg = work + (size_t)r * cap_run;
   int flags = 0;
@@ -221,9 +200,15 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
     for (int i = threadIdx.x; i < kSelChunk; i += blockDim.x) {
       const long long p = c0 + i;
       int nsel = 0;
-      if (p < np && __float_as_int(zc[p].y) >= 0) {
-        Stream R = particle_stream(ids[p], step, key);
-        nsel = draw_selections(R, lam, expl);
+      float2 b = make_float2(0.f, 0.f);
+      uint32_t pid = 0;
+      if (p < np) {
+        b = zc[p];
+        if (__float_as_int(b.y) >= 0) {
+          pid = ids[p];
+          Stream R = particle_stream(pid, step, key);
+          nsel = draw_selections(R, lam, expl);
+        }
       }
       const unsigned m = __ballot_sync(FULL, nsel > 0);
       if (!m) continue;
@@ -231,7 +216,7 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
       unsigned at = 0;
       if (lane == leader) at = atomicAdd(&cnt, (unsigned)__popc(m));
       at = __shfl_sync(FULL, at, leader) + __popc(m & ((1u << lane) - 1u));
-      if (nsel > 0) buf[at] = MccWork{(uint32_t)p, (uint32_t)nsel};
+      if (nsel > 0) buf[at] = mcc_entry(xv[p], b, pid, (uint32_t)p);
     }
     __syncthreads();
     if (threadIdx.x == 0) base = atomicAdd(nwork + r, (unsigned long long)cnt);
@@ -290,10 +275,10 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
     const bool act = w < nw;
     int nsel = 0;
     long long p = 0;
+    MccWork e{};
     if (act) {
-      const MccWork e = seg[w];
-      p = e.slot;
-      nsel = (int)e.nsel;
+      e = seg[w];
+      p = e.b.w;
     }
     bool ion_child = false;
     float cv[3] = {0, 0, 0};
@@ -303,12 +288,12 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
     float2 b = make_float2(0, 0);
     int cell = -1;
     if (act) {
-      b = zc[p];
-      cell = __float_as_int(b.y);
-      a = xv[p];
-      const uint32_t pid = pick(s.id[0], s.id[1], cur)[p];
+      a = e.a;
+      b = make_float2(__uint_as_float(e.b.x), __uint_as_float(e.b.y));
+      cell = (int)e.b.y;
+      const uint32_t pid = e.b.z;
       Stream R = particle_stream(pid, step, keys ? keys[r] : make_uint2(M.key0, M.key1));
-      (void)draw_selections(R, M.lam, expl);  // the phase-1 draw
+      nsel = draw_selections(R, M.lam, expl);  // the phase-1 draw again: its count
       v[0] = a.z;
       v[1] = a.w;
       v[2] = b.x;
@@ -501,14 +486,17 @@ static int mcc_params(Ctx *c, int mid, double dt, uint64_t seed, MccDev &M) {
 static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const SpeciesDev *src, const SpeciesDev *prod,
                             const uint2 *keys, unsigned long long *counts, const float2 *E, int nn, int select_blocks,
                             MccWork *work, unsigned long long *nwork, unsigned long long cap_work,
-                            const unsigned long long *d_step, int *err, cudaStream_t st) {
+                            const unsigned long long *d_step, int *err, cudaStream_t st, int phases = kMccBoth) {
   Mcc *m = c->mccs[mid];
   const int ntab = m->off[m->N];
   const size_t smem = (size_t)2 * ntab * sizeof(float);
   const uint2 key1 = make_uint2(M.key0, M.key1);
-  ISKRA_CUDA(c, launch_pdl(k_zero_u64, (R + 255) / 256, 256, 0, st, nwork, R));
-  ISKRA_CUDA(c, launch_pdl(k_mcc_select, dim3(select_blocks, R), 256, 0, st, src, M.lam, key1, keys, d_step, work, nwork,
-                           cap_work, err));
+  if (phases != kMccCollideOnly) {
+    ISKRA_CUDA(c, launch_pdl(k_zero_u64, (R + 255) / 256, 256, 0, st, nwork, R));
+    ISKRA_CUDA(c, launch_pdl(k_mcc_select, dim3(select_blocks, R), 256, 0, st, src, M.lam, key1, keys, d_step,
+                             phases == kMccSelectAhead ? 1 : 0, work, nwork, cap_work, err));
+  }
+  if (phases == kMccSelectAhead) return ISKRA_OK;
   const int collide_blocks = R == 1 ? c->num_sms * 8 : select_blocks;
   ISKRA_CUDA(c, launch_pdl(k_mcc_collide, dim3(collide_blocks, R), 256, smem, st, src, prod, (int)(m->prod >= 0), M,
                            keys, counts, E, nn, c->nx, d_step, (const MccWork *)work, (const unsigned long long *)nwork,
@@ -554,12 +542,22 @@ int launch_mcc(Ctx *c, int mid, double dt, uint64_t seed, const unsigned long lo
 int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, const SpeciesDev *prod,
                     const uint2 *keys, unsigned long long *counts, const float2 *E32, int nn, int blocks_per_run,
                     void *work, unsigned long long *nwork, unsigned long long cap_work,
-                    const unsigned long long *d_step, int *err, cudaStream_t st) {
+                    const unsigned long long *d_step, int *err, cudaStream_t st, int phases) {
   MccDev M;
   int rc = mcc_params(c, mid, dt, 0, M);
   if (rc) return rc;
   return queue_mcc_phases(c, mid, M, R, src, prod, keys, counts, E32, nn, blocks_per_run, (MccWork *)work, nwork,
-                          cap_work, d_step, err, st);
+                          cap_work, d_step, err, st, phases);
+}
+
+// The selection draw of MCC set mid for time step dt, for a push that makes
+// the set's next work list (keys, list and counters are the caller's).
+int mcc_push_select(Ctx *c, int mid, double dt, PushSelect *S) {
+  MccDev M;
+  int rc = mcc_params(c, mid, dt, 0, M);
+  if (rc) return rc;
+  S->lam = M.lam;
+  return ISKRA_OK;
 }
 
 size_t mcc_work_entry_bytes() { return sizeof(MccWork); }

@@ -257,9 +257,23 @@ struct PushShared {
 // Shared memory of a tile block: the warps' record rings, E at the window's
 // nodes (a cell's four corner fields are four 8-byte loads; 3.5 KB instead
 // of 12.8 KB of per-cell records) and the window moments.
+// ISKRA_PUSH_BULK=1 fills the rings with TMA bulk copies instead of per-lane
+// cp.async: measured on GB300 (512x512 slab, 300 steps, interleaved runs) at
+// 0.1580 ms per step against 0.1500 (k_push2 at 56.4-57.1 % of HBM against
+// 62.6-62.7 %): the per-warp mbarrier round trip on every 32-record stage
+// costs more than the L1 instructions it saves.  Kept as a build option.
+#ifndef ISKRA_PUSH_BULK
+#define ISKRA_PUSH_BULK 0
+#endif
+#if ISKRA_PUSH_BULK
+constexpr int kRbStage = 34;  // {vz, cell} records of a stage from the 16-byte boundary at or below its first slot
+#else
+constexpr int kRbStage = 32;
+#endif
 struct TileShared {
-  float4 ra[ISKRA_PUSH_THREADS / 32][kStages][32];  // staged records {hx, hy, vx, vy}
-  float2 rb[ISKRA_PUSH_THREADS / 32][kStages][32];  // staged records {vz, cell}
+  float4 ra[ISKRA_PUSH_THREADS / 32][kStages][32];        // staged records {hx, hy, vx, vy}
+  float2 rb[ISKRA_PUSH_THREADS / 32][kStages][kRbStage];  // staged records {vz, cell}
+  unsigned long long bar[ISKRA_PUSH_THREADS / 32][kStages];  // stage mbarriers (bulk-copy ring)
   float2 ne[kWinN * kWinN];
   unsigned mom[kMoms][kWinCells];
   unsigned char trk[kWinCells];  // track! flags of the window cells (with a surface tracker)
@@ -276,6 +290,52 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// ---- bulk-copy ring (TMA 1-D copies, mbarrier completion) ----
+// A stage of a warp's ring is filled by two cp.async.bulk copies issued by
+// lane 0 -- the stage's 32 {hx, hy, vx, vy} records (512 B) and its {vz,
+// cell} records from the 16-byte boundary at or below the first slot (34
+// records, 272 B) -- which complete on the stage's mbarrier with their byte
+// count.  The copies run on the TMA unit: no per-lane LSU instruction and no
+// L1 pass for the streamed particle records.  Source: this GPU's own memory;
+// no multicast.
+constexpr unsigned kMbarSpins = 1u << 20;  // polls of one stage before DERR_TIMEOUT
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bulk_stage(unsigned long long *bar, float4 *dst_a, float2 *dst_b, const float4 *src_a,
+                                           const float2 *src_b) {
+  const unsigned b = smem_u32(bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(512u + 16u * (kRbStage / 2))
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 512, [%2];" ::"r"(
+                   smem_u32(dst_a)),
+               "l"(src_a), "r"(b)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst_b)),
+               "l"(src_b), "r"(8u * kRbStage), "r"(b)
+               : "memory");
+}
+
+// waits for the phase `parity` of a stage; false after `spins` polls
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, unsigned spins) {
+  const unsigned b = smem_u32(bar);
+  for (unsigned it = 0; it < spins; it++) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(b), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
 }
 
 // E records (corner fields) of window cell (la, lb)
@@ -346,10 +406,11 @@ template <bool PUSH, int MX, int MY, bool WIN, bool TRK = false, class SH>
 __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restrict__ zc, long long p, bool valid,
                                         float4 a, float2 b, const float2 *__restrict__ E2, const SH &sh,
                                         int ox, int oy, int ww, int wh, const PushParams &P, unsigned ab[4],
-                                        int &flags, Moments &m) {
+                                        int &flags, Moments &m, float4 *out_a = nullptr, float2 *out_b = nullptr) {
   const int nx = P.nx;
   int key = -1;
   m = Moments{0u, 0u, 0u, 0u};
+  if (out_b) *out_b = make_float2(0.f, __int_as_float(-1));  // (no live particle unless pushed below)
   if (valid) {
     int cell = __float_as_int(b.y);
     if (cell >= 0) {
@@ -413,6 +474,10 @@ __device__ __forceinline__ int push_one(float4 *__restrict__ xv, float2 *__restr
         }
         __stcs(xv + p, make_float4(hx, hy, vx, vy));
         __stcs(zc + p, make_float2(b.x, __int_as_float(cell)));
+        if (out_a) {  // the pushed record, for a caller that selects it for the next MCC step
+          *out_a = make_float4(hx, hy, vx, vy);
+          *out_b = make_float2(b.x, __int_as_float(cell));
+        }
       }
       if (cell >= 0) {
         const int la = i0 - ox, lb = j0 - oy;
@@ -457,9 +522,11 @@ template <bool PUSH, int MX, int MY, bool WIN, bool TRK = false, class SH>
 __device__ __forceinline__ void push_warp(const SpeciesDev &s, float4 *__restrict__ xv, float2 *__restrict__ zc,
                                           long long p, bool valid, float4 a, float2 b,
                                           const float2 *__restrict__ E2, SH &sh, int ox, int oy, int ww,
-                                          int wh, const PushParams &P, unsigned ab[4], int &flags) {
+                                          int wh, const PushParams &P, unsigned ab[4], int &flags,
+                                          float4 *out_a = nullptr, float2 *out_b = nullptr) {
   Moments m;
-  const int key = push_one<PUSH, MX, MY, WIN, TRK>(xv, zc, p, valid, a, b, E2, sh, ox, oy, ww, wh, P, ab, flags, m);
+  const int key = push_one<PUSH, MX, MY, WIN, TRK>(xv, zc, p, valid, a, b, E2, sh, ox, oy, ww, wh, P, ab, flags, m,
+                                                   out_a, out_b);
   deposit_warp<WIN>(s, sh, key, m, P.nx);
 }
 
@@ -509,6 +576,48 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
       const int cnt = (int)max(0LL, min(end, w0 + slice) - w0);
       float4 *__restrict__ xw = xv + w0;
       float2 *__restrict__ zw = zc + w0;
+#if ISKRA_PUSH_BULK
+      // {vz, cell} stages start at the 16-byte boundary at or below their
+      // first slot: w0 + o has the parity of `begin` (slices and stages are
+      // multiples of 32 slots)
+      const int sft = (int)(begin & 1);
+      if (lane == 0) {
+#pragma unroll
+        for (int d = 0; d < kStages; d++) mbar_init(&sh.bar[wib][d], 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      }
+      __syncwarp();
+      if (lane == 0) {  // prologue: the first kStages - 1 iterations' records in flight
+#pragma unroll
+        for (int d = 0; d < kStages - 1; d++)
+          if (32 * d < cnt) bulk_stage(&sh.bar[wib][d], sh.ra[wib][d], sh.rb[wib][d], xw + 32 * d, zw + 32 * d - sft);
+      }
+      unsigned phase = 0u;  // bit st: parity of stage st's next completion
+      int st = 0;           // stage of the current iteration
+      for (int o = 0; o < cnt; o += 32) {
+        __syncwarp();  // every lane has read the stage refilled next (one iteration ago)
+        {
+          const int q = o + 32 * (kStages - 1);
+          const int sn = st == 0 ? kStages - 1 : st - 1;
+          if (lane == 0 && q < cnt) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the reads precede the copy's writes
+            bulk_stage(&sh.bar[wib][sn], sh.ra[wib][sn], sh.rb[wib][sn], xw + q, zw + q - sft);
+          }
+        }
+        // bounded: a stage that never completes is flagged and its records
+        // skipped; the later stages are still waited for (each bounded), so
+        // no copy is in flight when the block leaves the ring
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sh.bar[wib][st], (phase >> st) & 1u, kMbarSpins));
+        if (!ok) flags |= DERR_TIMEOUT;
+        phase ^= 1u << st;
+        const float4 a = sh.ra[wib][st][lane];
+        const float2 b = sh.rb[wib][st][lane + sft];
+        st = st + 1 == kStages ? 0 : st + 1;
+        push_warp<PUSH, MX, MY, true, TRK>(s, xw, zw, o + lane, ok && o + lane < cnt, a, b, E2, sh, ox, oy, kWin,
+                                           kWin, P, ab, flags);
+      }
+      __syncthreads();
+#else
       // prologue: the first kStages - 1 iterations' records in flight
 #pragma unroll
       for (int d = 0; d < kStages - 1; d++) {
@@ -533,6 +642,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
       }
       cp_async_wait<0>();
       __syncthreads();
+#endif
       // node sums from the moments of the up to four window cells around each node
       for (int t = threadIdx.x; t < kWinN * kWinN; t += blockDim.x) {
         const int a = t % kWinN, b = t / kWinN;
@@ -814,16 +924,6 @@ __global__ void k_finalize(FinalizeArgs A, const double *__restrict__ vol_inv, c
 // ~1/64 of its FP32 rate): the int64 sums split exactly into three FP32
 // pieces, products by two-product FMA; ρ and the densities to ~2^-48
 // relative, written as double-float pairs (FP64 copies on download).
-struct FinalizeDfArgs {
-  int ns;
-  unsigned long long *acc[kMaxSpecies];
-  unsigned *cnt[kMaxSpecies];
-  float2 *n[kMaxSpecies];
-  float2 scale[kMaxSpecies];  // w0 * 2^-48
-  float2 q[kMaxSpecies];
-  int consume[kMaxSpecies];
-};
-
 // WARM: the step solve's warm start on the same nodes (ϕ <- 2ϕ_n - ϕ_(n-1)
 // on free rows once the history is valid; the last block marks it valid)
 template <bool WARM>
@@ -834,42 +934,8 @@ __global__ void k_finalize_df(FinalizeDfArgs A, const float2 *__restrict__ vol_i
   const bool hist = WARM && *W.hist != 0;
   int flags = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-    const float2 vi = vol_inv[k];
-    float2 r = bg ? bg[k] : make_float2(0.f, 0.f);
-    unsigned long long a[kMaxSpecies];
-    unsigned cn[kMaxSpecies];
-    float2 nold[kMaxSpecies];
-#pragma unroll
-    for (int s = 0; s < kMaxSpecies; s++) {
-      if (s >= A.ns) break;
-      if (A.consume[s]) {
-        a[s] = A.acc[s][k];
-        cn[s] = A.cnt[s][k];
-      } else {
-        nold[s] = A.n[s][k];
-      }
-    }
-#pragma unroll
-    for (int s = 0; s < kMaxSpecies; s++) {
-      if (s >= A.ns) break;
-      float2 n;
-      if (A.consume[s]) {
-        if (cn[s] > kMaxCell) flags |= DERR_OVERFLOW;
-        n = df_mul(df_mul(df_from_u64(a[s]), A.scale[s]), vi);
-        A.n[s][k] = n;
-        A.acc[s][k] = 0ull;
-        A.cnt[s][k] = 0u;
-      } else {
-        n = nold[s];
-      }
-      r = df_add(r, df_mul(n, A.q[s]));
-    }
-    rho[k] = r;
-    if (WARM) {
-      const float2 xa = W.xd[k];
-      if (hist && !(W.cls[k] & W.fixed_bit)) W.xd[k] = df_add(make_float2(2.f * xa.x, 2.f * xa.y), df_neg(W.xh[k]));
-      W.xh[k] = xa;
-    }
+    finalize_df_node(A, vol_inv, bg, rho, k, flags);
+    if (WARM) warm_node(W, hist, k);
   }
   if (flags) atomicOr(err, flags);
   if (WARM) {
@@ -989,6 +1055,7 @@ static int finalize(Ctx *c, bool with_rho, bool step = false) {
 
 int launch_charge_density(Ctx *c) { return finalize(c, true); }
 int launch_step_density(Ctx *c) { return finalize(c, true, true); }
+
 
 // ---------------------------------------------------------------------------
 // E = -∇ϕ  (generalized_poisson.jl:398-410)
@@ -1216,10 +1283,18 @@ int launch_sort(Ctx *c, int sid) {
 // run's particles (any order), deposits into shared memory and adds the
 // node sums to the run's accumulator.
 // ---------------------------------------------------------------------------
-template <int MX, int MY>
+//
+// SEL: the species is the source of an MCC set, and the push also makes the
+// set's work list for the next step -- each pushed particle that stays draws
+// its selection count for step + 1 from its own stream (the draw
+// k_mcc_select would make at the start of that step: nothing changes the
+// particle in between) and, when selected, its new record goes to the run's
+// list.  The next step's collision pass then starts without a selection pass
+// over all particles.
+template <int MX, int MY, bool SEL>
 __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(const SpeciesDev *__restrict__ runs,
                                                                           const float2 *__restrict__ E2, int nnode,
-                                                                          PushParams P, int *err) {
+                                                                          PushParams P, int *err, PushSelect S) {
   pdl_wait();
   __shared__ PushShared sh;
   const unsigned FULL = 0xffffffffu;
@@ -1241,6 +1316,11 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   float2 *__restrict__ zc = pick(s.zc[0], s.zc[1], cur);
   unsigned ab[4] = {0, 0, 0, 0};
   int flags = 0;
+  const uint32_t *__restrict__ ids = pick(s.id[0], s.id[1], cur);
+  const unsigned long long step1 = SEL ? *S.d_step + 1ull : 0ull;
+  const uint2 key = SEL ? S.keys[r] : make_uint2(0u, 0u);
+  const float expl = __expf(-S.lam);  // as k_mcc_select and k_mcc_collide form it
+  MccWork *__restrict__ seg = SEL ? S.work + (size_t)r * S.cap_run : nullptr;
   const long long warp = (long long)blockIdx.x * nwb + wib, nwarps = (long long)gridDim.x * nwb;
   for (long long base = warp * 32; base < np; base += nwarps * 32) {
     const long long p = base + lane;
@@ -1251,7 +1331,30 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
       a = ld_stream(xv + p);
       b = ld_stream(zc + p);
     }
-    push_warp<true, MX, MY, true>(s, xv, zc, p, v, a, b, E2, sh, 0, 0, cx, cy, P, ab, flags);
+    float4 na;
+    float2 nb;
+    push_warp<true, MX, MY, true>(s, xv, zc, p, v, a, b, E2, sh, 0, 0, cx, cy, P, ab, flags, SEL ? &na : nullptr,
+                                  SEL ? &nb : nullptr);
+    if (SEL) {
+      int nsel = 0;
+      uint32_t pid = 0;
+      if (v && __float_as_int(nb.y) >= 0) {
+        pid = ids[p];
+        Stream R = particle_stream(pid, step1, key);
+        nsel = draw_selections(R, S.lam, expl);
+      }
+      const unsigned m = __ballot_sync(FULL, nsel > 0);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        unsigned long long at = 0;
+        if (lane == leader) at = atomicAdd(S.nwork + r, (unsigned long long)__popc(m));
+        at = __shfl_sync(FULL, at, leader) + __popc(m & ((1u << lane) - 1u));
+        if (nsel > 0) {
+          if (at < S.cap_run) seg[at] = mcc_entry(na, nb, pid, (uint32_t)p);
+          else flags |= DERR_CAPACITY;
+        }
+      }
+    }
   }
   __syncthreads();
   const int wn = cx + 1;
@@ -1285,7 +1388,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
 
 // Ensemble push of one species (runs: device array of R run views).
 int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float2 *E2, float dt, int blocks_per_run,
-                     int *err, cudaStream_t st) {
+                     int *err, cudaStream_t st, const PushSelect *sel) {
   Species &s = c->species[sid];
   if ((c->nx - 1) * (c->ny - 1) > kWinCells) return set_err(c, ISKRA_EINVAL, "ensemble grid larger than one window");
   PushParams P{};  // no surface tracker in ensembles
@@ -1299,11 +1402,13 @@ int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float
   P.tiles_x = 0;
   const int nnode = c->nn;
   const dim3 grid(blocks_per_run, R);
+  const PushSelect S = sel ? *sel : PushSelect{};
 #define ISKRA_PUSH_RUNS_CASE(MX, MY)                                                                           \
   if (P.mode_x == MX && P.mode_y == MY) {                                                                       \
-    cudaFuncSetAttribute(k_push_runs<MX, MY>, cudaFuncAttributePreferredSharedMemoryCarveout,                   \
+    auto kern = sel ? k_push_runs<MX, MY, true> : k_push_runs<MX, MY, false>;                                   \
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                                  \
                          (int)cudaSharedmemCarveoutMaxShared);                                                  \
-    ISKRA_CUDA(c, launch_pdl(k_push_runs<MX, MY>, grid, 256, 0, st, runs, E2, nnode, P, err));                 \
+    ISKRA_CUDA(c, launch_pdl(kern, grid, 256, 0, st, runs, E2, nnode, P, err, S));                             \
     return ISKRA_OK;                                                                                            \
   }
   ISKRA_PUSH_RUNS_CASE(0, 0) ISKRA_PUSH_RUNS_CASE(0, 1) ISKRA_PUSH_RUNS_CASE(0, 2)

@@ -525,32 +525,17 @@ __device__ __forceinline__ void efield_df5(float2 xk, float2 xw, float2 xe, floa
 // the pass is bound by memory latency, not bandwidth.  In a step graph the
 // FIRST pass writes no E (a correction nearly always follows); when it meets
 // rtol already, the next pass, otherwise skipped, writes E instead.
+// The node loop of k_residual_df over nodes k0, k0 + stride, ... < nn
+// (partial norms in a2, b2).
 template <bool FIRST, bool EOUT>
-__global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__restrict__ x,
-                                                     const double *__restrict__ rho, const float2 *__restrict__ rho_df,
-                                                     float2 nie_df, double neg_inv_eps0,
-                                                     float2 *__restrict__ bd, PoissonScal *sc, float *__restrict__ r32,
-                                                     double *__restrict__ part, int nn, int singular, double rtol2,
-                                                     EOut eo, SweepLoop loop) {
-  pdl_wait();
-  __shared__ double sh[40];
-  __shared__ RowClass cls_sh[kSmemClasses];
-  __shared__ int last;
+__device__ __forceinline__ void residual_df_nodes(const OpView &op, const RowClass *__restrict__ CT,
+                                                  const float2 *__restrict__ x, const double *__restrict__ rho,
+                                                  const float2 *__restrict__ rho_df, float2 nie_df,
+                                                  double neg_inv_eps0, float2 *__restrict__ bd,
+                                                  float *__restrict__ r32, int nn, int singular, double lam,
+                                                  const EOut &eo, int k0, int stride, double &a2, double &b2) {
   const int nx = op.nx, ny = op.ny;
-  if (!FIRST && sc->done) {
-    if (!EOUT || !sc->e_pending) return;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-      const int j = k / nx, i = k - j * nx;
-      const int w = i > 0 ? k - 1 : k + nx - 1, e = i < nx - 1 ? k + 1 : k - nx + 1;
-      const int s = j > 0 ? k - nx : k + nx * (ny - 1), n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
-      efield_df5(x[k], x[w], x[e], x[s], x[n], k, i, j, nx, ny, eo);
-    }
-    return;
-  }
-  const RowClass *__restrict__ CT = stage_classes(op, cls_sh);
-  const double lam = singular ? sc->lambda : 0.0;
-  double a2 = 0, b2 = 0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+  for (int k = k0; k < nn; k += stride) {
     const int j = k / nx, i = k - j * nx;
     const int w = i > 0 ? k - 1 : k + nx - 1;
     const int e = i < nx - 1 ? k + 1 : k - nx + 1;
@@ -617,6 +602,50 @@ __global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__
     const double rv = (double)resf;
     a2 = fma(rv, rv, a2);
   }
+}
+
+// E = -∇ϕ of the double-float ϕ at every node (a converged first residual
+// wrote none)
+__device__ __forceinline__ void efield_df_nodes(const float2 *__restrict__ x, int nx, int ny, int nn,
+                                                const EOut &eo, int k0, int stride) {
+  for (int k = k0; k < nn; k += stride) {
+    const int j = k / nx, i = k - j * nx;
+    const int w = i > 0 ? k - 1 : k + nx - 1, e = i < nx - 1 ? k + 1 : k - nx + 1;
+    const int s = j > 0 ? k - nx : k + nx * (ny - 1), n = j < ny - 1 ? k + nx : k - nx * (ny - 1);
+    efield_df5(x[k], x[w], x[e], x[s], x[n], k, i, j, nx, ny, eo);
+  }
+}
+
+// Residual pass of the separable solver on the double-float ϕ: the stencil
+// A x is summed in double-float arithmetic (FP32 pipes); the FIRST pass forms
+// b (FP64, then split) for the free rows into bd and the rhs norm, later
+// passes reuse bd.  Scaled FP32 residual to r32, E (EOUT), convergence test
+// as k_residual (norms in FP64).  A node's loads (its row class, ϕ at the
+// five stencil nodes, b) are all issued before its branch on the row class:
+// the pass is bound by memory latency, not bandwidth.  In a step graph the
+// FIRST pass writes no E (a correction nearly always follows); when it meets
+// rtol already, the next pass, otherwise skipped, writes E instead.
+template <bool FIRST, bool EOUT>
+__global__ void __launch_bounds__(256) k_residual_df(OpView op, const float2 *__restrict__ x,
+                                                     const double *__restrict__ rho, const float2 *__restrict__ rho_df,
+                                                     float2 nie_df, double neg_inv_eps0,
+                                                     float2 *__restrict__ bd, PoissonScal *sc, float *__restrict__ r32,
+                                                     double *__restrict__ part, int nn, int singular, double rtol2,
+                                                     EOut eo, SweepLoop loop) {
+  pdl_wait();
+  __shared__ double sh[40];
+  __shared__ RowClass cls_sh[kSmemClasses];
+  __shared__ int last;
+  const int k0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  if (!FIRST && sc->done) {
+    if (EOUT && sc->e_pending) efield_df_nodes(x, op.nx, op.ny, nn, eo, k0, stride);
+    return;
+  }
+  const RowClass *__restrict__ CT = stage_classes(op, cls_sh);
+  const double lam = singular ? sc->lambda : 0.0;
+  double a2 = 0, b2 = 0;
+  residual_df_nodes<FIRST, EOUT>(op, CT, x, rho, rho_df, nie_df, neg_inv_eps0, bd, r32, nn, singular, lam, eo, k0,
+                                 stride, a2, b2);
   finish_norms<FIRST>(sc, part, a2, b2, rtol2, loop, sh, &last);
 }
 
@@ -677,15 +706,14 @@ __device__ void fft_columns(float2 *buf, int TP, int N, int S, int logN, const f
 }
 
 // r (nx, ny) -> spec[i K + k], k = 0..N/2: forward FFT along y of the 2 TP
-// columns of this block, two per complex transform
-__global__ void __launch_bounds__(256) k_fft_fwd(const float *__restrict__ r, int nx, int N, int logN, int TP,
-                                                 const float2 *__restrict__ tw, float2 *__restrict__ spec,
-                                                 const PoissonScal *__restrict__ sc) {
-  pdl_wait();
-  extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
-  if (sc->done) return;
+// columns of work item `item` (columns 2 TP item ...), two per complex
+// transform.  fbuf: TP columns of stride N + 1, then N/2 twiddles.  Ends with
+// a block barrier (the next item may reuse fbuf).
+__device__ __forceinline__ void fft_fwd_item(int item, const float *__restrict__ r, int nx, int N, int logN, int TP,
+                                             const float2 *__restrict__ tw, float2 *__restrict__ spec,
+                                             float2 *fbuf) {
   const int S = N + 1, W = 2 * TP, K = (N >> 1) + 1;
-  const int i0 = blockIdx.x * W;
+  const int i0 = item * W;
   float2 *tws = fbuf + TP * S;
   for (int t = threadIdx.x; t < (N >> 1); t += blockDim.x) tws[t] = __ldg(tw + t);
   for (int t = threadIdx.x; t < W * N; t += blockDim.x) {
@@ -704,6 +732,16 @@ __global__ void __launch_bounds__(256) k_fft_fwd(const float *__restrict__ r, in
     if (ia < nx) spec[(size_t)ia * K + k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
     if (ia + 1 < nx) spec[(size_t)(ia + 1) * K + k] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
   }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_fft_fwd(const float *__restrict__ r, int nx, int N, int logN, int TP,
+                                                 const float2 *__restrict__ tw, float2 *__restrict__ spec,
+                                                 const PoissonScal *__restrict__ sc) {
+  pdl_wait();
+  extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
+  if (sc->done) return;
+  fft_fwd_item(blockIdx.x, r, nx, N, logN, TP, tw, spec, fbuf);
 }
 
 // Per Fourier mode and real/imaginary part (one thread each): Thomas forward
@@ -780,31 +818,33 @@ __global__ void __launch_bounds__(64) k_tridiag(float *__restrict__ spec, int nx
 // contiguously (fwd: nf (α, γ) pairs, back: nb (a/b, c/b) pairs, backb: nb
 // 1/b, then 1/b of the last row), and the block stages them in shared memory
 // with the data in one pass, so the 2L dependent levels run on shared memory
-// only.
-__global__ void __launch_bounds__(256) k_tridiag_cr(float *__restrict__ spec, int nx, int K, int G, int L, int nf,
-                                                    int nb, const float2 *__restrict__ fwd,
-                                                    const float2 *__restrict__ back, const float *__restrict__ backb,
-                                                    const float *__restrict__ top, const float *__restrict__ q,
-                                                    const float *__restrict__ gk, int cyclic, int pin0,
-                                                    const PoissonScal *__restrict__ sc) {
-  pdl_wait();
-  extern __shared__ float fsh[];  // data [col][nx] (col = 2 (k - k0) + part), then per mode fwd, back, backb
-  if (sc->done) return;
-  const int k0 = blockIdx.x * G;
+// only.  Work item `item` takes modes G item ...; ends with a block barrier.
+struct CrArgs {
+  float *spec;
+  int nx, K, G, L, nf, nb;
+  const float2 *fwd, *back;
+  const float *backb, *top, *q, *gk;
+  int cyclic, pin0;
+};
+
+__device__ __forceinline__ void cr_item(int item, const CrArgs &A, float *fsh) {
+  const int nx = A.nx, K = A.K, G = A.G, L = A.L, nf = A.nf, nb = A.nb;
+  float *__restrict__ spec = A.spec;
+  const int k0 = item * G;
   const int g = min(G, K - k0), ncol = 2 * g;
   float2 *cf = reinterpret_cast<float2 *>(fsh + 2 * G * nx);  // [g][nf]
   float2 *cb = cf + (size_t)G * nf;                            // [g][nb]
   float *cbb = reinterpret_cast<float *>(cb + (size_t)G * nb);  // [g][nb]
-  for (int t = threadIdx.x; t < g * nf; t += blockDim.x) cf[t] = __ldg(fwd + (size_t)k0 * nf + t);
+  for (int t = threadIdx.x; t < g * nf; t += blockDim.x) cf[t] = __ldg(A.fwd + (size_t)k0 * nf + t);
   for (int t = threadIdx.x; t < g * nb; t += blockDim.x) {
-    cb[t] = __ldg(back + (size_t)k0 * nb + t);
-    cbb[t] = __ldg(backb + (size_t)k0 * nb + t);
+    cb[t] = __ldg(A.back + (size_t)k0 * nb + t);
+    cbb[t] = __ldg(A.backb + (size_t)k0 * nb + t);
   }
   for (int t = threadIdx.x; t < nx * ncol; t += blockDim.x) {
     const int i = t / ncol, col = t - i * ncol;
     const int k = k0 + (col >> 1);
     float v = spec[((size_t)i * K + k) * 2 + (col & 1)];
-    if (pin0 >= 0 && k == 0 && i == pin0) v = 0.f;  // pinned row of the singular mode
+    if (A.pin0 >= 0 && k == 0 && i == A.pin0) v = 0.f;  // pinned row of the singular mode
     fsh[col * nx + i] = v;
   }
   __syncthreads();
@@ -825,7 +865,7 @@ __global__ void __launch_bounds__(256) k_tridiag_cr(float *__restrict__ spec, in
     __syncthreads();
   }
   const int topr = (1 << L) - 1;
-  for (int col = threadIdx.x; col < ncol; col += blockDim.x) fsh[col * nx + topr] *= __ldg(top + k0 + (col >> 1));
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) fsh[col * nx + topr] *= __ldg(A.top + k0 + (col >> 1));
   __syncthreads();
   for (int l = L - 1; l >= 0; l--) {
     const int s = 1 << l, ecnt = ((nx >> l) + 1) >> 1;
@@ -848,22 +888,27 @@ __global__ void __launch_bounds__(256) k_tridiag_cr(float *__restrict__ spec, in
     const int k = k0 + (col >> 1);
     const float *dc = fsh + col * nx;
     float v = dc[i];
-    if (cyclic && !(k == 0 && pin0 >= 0)) v -= (dc[0] + gk[K + k] * dc[nx - 1]) * gk[k] * q[(size_t)i * K + k];
+    if (A.cyclic && !(k == 0 && A.pin0 >= 0)) v -= (dc[0] + A.gk[K + k] * dc[nx - 1]) * A.gk[k] * A.q[(size_t)i * K + k];
     spec[((size_t)i * K + k) * 2 + (col & 1)] = v;
   }
+  __syncthreads();
 }
 
-// spec -> δ (nx, ny) by the inverse of k_fft_fwd; x += δ on free rows
-template <bool DF>
-__global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict__ spec, int nx, int N, int logN,
-                                                        int TP, const float2 *__restrict__ tw,
-                                                        const uint16_t *__restrict__ cls, float2 *__restrict__ xd,
-                                                        double *__restrict__ x64, const PoissonScal *__restrict__ sc) {
+__global__ void __launch_bounds__(256) k_tridiag_cr(CrArgs A, const PoissonScal *__restrict__ sc) {
   pdl_wait();
-  extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
+  extern __shared__ float fsh[];  // data [col][nx] (col = 2 (k - k0) + part), then per mode fwd, back, backb
   if (sc->done) return;
+  cr_item(blockIdx.x, A, fsh);
+}
+
+// spec -> δ (nx, ny) by the inverse of k_fft_fwd for work item `item`; x +=
+// δ on free rows.  Ends with a block barrier.
+template <bool DF>
+__device__ __forceinline__ void fft_inv_item(int item, const float2 *__restrict__ spec, int nx, int N, int logN,
+                                             int TP, const float2 *__restrict__ tw, const uint16_t *__restrict__ cls,
+                                             float2 *__restrict__ xd, double *__restrict__ x64, float2 *fbuf) {
   const int S = N + 1, W = 2 * TP, K = (N >> 1) + 1;
-  const int i0 = blockIdx.x * W;
+  const int i0 = item * W;
   float2 *tws = fbuf + TP * S;
   for (int t = threadIdx.x; t < (N >> 1); t += blockDim.x) tws[t] = __ldg(tw + t);
   // the update's ϕ values and row classes, fetched before the transform
@@ -930,6 +975,18 @@ __global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict
       }
     }
   }
+  __syncthreads();
+}
+
+template <bool DF>
+__global__ void __launch_bounds__(256) k_fft_inv_update(const float2 *__restrict__ spec, int nx, int N, int logN,
+                                                        int TP, const float2 *__restrict__ tw,
+                                                        const uint16_t *__restrict__ cls, float2 *__restrict__ xd,
+                                                        double *__restrict__ x64, const PoissonScal *__restrict__ sc) {
+  pdl_wait();
+  extern __shared__ float2 fbuf[];  // TP columns of stride S, then N/2 twiddles
+  if (sc->done) return;
+  fft_inv_item<DF>(blockIdx.x, spec, nx, N, logN, TP, tw, cls, xd, x64, fbuf);
 }
 
 // mean-zero projection of x over nodes (singular case)
@@ -1760,6 +1817,26 @@ static int fft_smem_attr(Ctx *c, int N) {
   return ISKRA_OK;
 }
 
+static CrArgs cr_args(Poisson *P, int G) {
+  CrArgs A;
+  A.spec = (float *)P->spec;
+  A.nx = P->nx;
+  A.K = P->K;
+  A.G = G;
+  A.L = P->cr_levels;
+  A.nf = P->cr_nf;
+  A.nb = P->cr_nb;
+  A.fwd = P->cr_fwd;
+  A.back = P->cr_back;
+  A.backb = P->cr_backb;
+  A.top = P->cr_top;
+  A.q = P->q;
+  A.gk = P->gk;
+  A.cyclic = (int)P->cyclic;
+  A.pin0 = P->pin_k0;
+  return A;
+}
+
 // Launch shape of the separable correction.
 struct SepShape {
   int TP, fb, G;
@@ -1861,10 +1938,8 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
       ISKRA_CUDA(c, launch_pdl(k_fft_fwd, sh.fb, 256, sh.smem, st, (const float *)P->r32, P->nx, N, P->logN, sh.TP,
                                (const float2 *)P->tw, P->spec, sc));
       if (sh.G) {
-        ISKRA_CUDA(c, launch_pdl(k_tridiag_cr, (K + sh.G - 1) / sh.G, 256, cr_smem(P, sh.G), st, (float *)P->spec,
-                                 P->nx, K, sh.G, P->cr_levels, P->cr_nf, P->cr_nb, (const float2 *)P->cr_fwd,
-                                 (const float2 *)P->cr_back, (const float *)P->cr_backb, (const float *)P->cr_top,
-                                 (const float *)P->q, (const float *)P->gk, (int)P->cyclic, P->pin_k0, sc));
+        ISKRA_CUDA(c, launch_pdl(k_tridiag_cr, (K + sh.G - 1) / sh.G, 256, cr_smem(P, sh.G), st, cr_args(P, sh.G),
+                                 sc));
       } else {
         ISKRA_CUDA(c, launch_pdl(k_tridiag, (2 * K + 63) / 64, 64, 0, st, (float *)P->spec, P->nx, K,
                                  (const float *)P->low, (const float *)P->inv, (const float *)P->cp,
@@ -2587,20 +2662,37 @@ int iskra_poisson_residual(iskra_ctx *h, const double *f, const double *phi, dou
     ISKRA_CUDA(c, cudaMemcpyAsync(sig.data(), P->sigma_d, std::min<size_t>(sig.size(), P->nsig) * sizeof(double),
                                   cudaMemcpyDeviceToHost, c->stream));
   ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  // identity rows (Dirichlet values, driven rows): known values, moved to
+  // the right-hand side as the solver does; the norms run over the others
+  auto identity = [&](int r) {
+    const double *R = &P->C[(size_t)r * 7];
+    if (R[0] != 1.0) return false;
+    for (int q = 1; q < 7; q++)
+      if (R[q] != 0.0) return false;
+    for (const auto &col : P->sig_cols)
+      if (col[r] != 0.0) return false;
+    return true;
+  };
+  std::vector<char> fixed(nn);
+  for (int r = 0; r < nn; r++) fixed[r] = identity(r);
   double r2 = 0, b2 = 0;
   for (int r = 0; r < nn; r++) {
+    if (fixed[r]) continue;
     const int i = r % nx, j = r / nx;
     const double *R = &P->C[(size_t)r * 7];
     const int col[7] = {r, i > 0 ? r - 1 : r, i < nx - 1 ? r + 1 : r, j > 0 ? r - nx : r, j < ny - 1 ? r + nx : r,
                         i == 0 ? r + nx - 1 : (i == nx - 1 ? r - nx + 1 : r),
                         j == 0 ? r + nx * (ny - 1) : (j == ny - 1 ? r - nx * (ny - 1) : r)};
-    double ax = 0;
-    for (int s = 0; s < 7; s++)
-      if (R[s] != 0.0) ax += R[s] * phi[col[s]];
+    double afree = 0, known = 0;
+    for (int q = 0; q < 7; q++) {
+      if (R[q] == 0.0) continue;
+      if (fixed[col[q]]) known += R[q] * phi[col[q]];
+      else afree += R[q] * phi[col[q]];
+    }
     for (size_t k = 0; k < P->sig_cols.size(); k++)
-      if (P->sig_cols[k][r] != 0.0) ax += P->sig_cols[k][r] * sig[k];
-    const double b = P->rho_dof[r] ? f[r] / P->eps0 : bfix[r];
-    r2 += (b - ax) * (b - ax);
+      if (P->sig_cols[k][r] != 0.0) known += P->sig_cols[k][r] * sig[k];
+    const double b = (P->rho_dof[r] ? f[r] / P->eps0 : bfix[r]) - known;
+    r2 += (b - afree) * (b - afree);
     b2 += b * b;
   }
   *relres = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);

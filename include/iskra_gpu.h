@@ -252,8 +252,12 @@ int iskra_poisson_solve_host(iskra_ctx *ctx, const double *f, double rtol,
  * (default; either way the solve iterates to the same tolerance). */
 int iskra_poisson_set_warm_start(iskra_ctx *ctx, int mode);
 /* Solver method: 0 = automatic (the exact FFT(y)/tridiagonal(x) solve when
- * the assembled operator is separable, else CG), 1 = CG with Jacobi scaling
- * only.  Returns the method in effect through *active when non-NULL. */
+ * the assembled operator is separable, else CG preconditioned by a geometric
+ * multigrid V-cycle, or CG with Jacobi scaling when the operator is singular),
+ * 1 = CG with Jacobi scaling only, 2 = multigrid-preconditioned CG even for
+ * a separable operator.  Every method iterates to the same FP64 relative
+ * residual.  Returns the method in effect through *active when non-NULL
+ * (0 separable, 1 Jacobi CG, 2 multigrid CG). */
 int iskra_poisson_set_method(iskra_ctx *ctx, int method, int *active);
 
 /* ---- Monte Carlo collisions (Chemistry/src/mcc.jl) ----------------------- */

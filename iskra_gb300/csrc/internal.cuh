@@ -278,6 +278,13 @@ struct Species {
 struct Poisson;                // poisson.cu
 struct Mcc;                    // mcc.cu
 struct Lws;                    // lws.cu (learned warm start of CG solves)
+struct Mg;                     // multigrid.cu (V-cycle preconditioner of CG solves)
+int mg_build(struct Ctx *c, int nx, int ny, const std::vector<double> &s0, const std::vector<double> &sW,
+             const std::vector<double> &sE, const std::vector<double> &sS, const std::vector<double> &sN,
+             const std::vector<char> &free_row, int per_x, int per_y, Mg **out);
+int mg_queue_cycle(struct Ctx *c, Mg *m, const double *r, double *z, const int *skip);
+int mg_levels(const Mg *m);
+void mg_destroy(Mg *m);
 struct CircuitDev {            // device-resident circuit state (FP64)
   double R, L, C, amp, freq, dc, area, scale;
   double t, i, q, vext;

@@ -75,7 +75,10 @@ struct Poisson {
   std::vector<DriveGroup> drives;
   std::vector<double> er;       // (nx+1)*(ny+1) ones
   bool dirty = true;
-  int method = 0;               // 0 auto, 1 CG
+  int method = 0;               // 0 auto, 1 CG (Jacobi), 2 CG with the multigrid preconditioner
+  Mg *mg = nullptr;             // multigrid hierarchy of a non-separable operator (multigrid.cu)
+  cudaGraphExec_t pcg_graph = nullptr;  // one multigrid-CG iteration (~70 kernels), replayed
+  double pcg_graph_rtol = 0;
   // ---- device representation ----
   bool separable = false, singular = false, cyclic = false;
   int nclass = 0;
@@ -136,6 +139,8 @@ constexpr int kPartials = 1024;
 
 void poisson_destroy(Poisson *p) {
   if (!p) return;
+  mg_destroy(p->mg);
+  if (p->pcg_graph) cudaGraphExecDestroy(p->pcg_graph);
   cudaFree(p->cls);
   cudaFree(p->classes);
   cudaFree(p->bfix_d);
@@ -1027,13 +1032,18 @@ __global__ void k_cg_init(OpView op, const double *__restrict__ r, double *__res
     v += r[k] * zz;
   }
   double t = block_sum(v, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = t;
+  if (threadIdx.x == 0) part[2 * kPartials + blockIdx.x] = t;  // summed by k_cg_rz0
 }
 
+// rz of the iteration is held in sc->rz; the kernel that forms the next one
+// stores it in sc->rz_new and this kernel (one per iteration, which reads
+// neither) moves it to sc->rz: no block of a kernel reads a scalar another
+// block of the same kernel writes.
 __global__ void k_cg_ap(OpView op, const double *__restrict__ p, double *__restrict__ ap, double *__restrict__ part,
-                        int nn, const PoissonScal *__restrict__ sc) {
+                        int nn, PoissonScal *__restrict__ sc) {
   __shared__ double sh[40];
   if (sc->done) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc->rz = sc->rz_new;
   double v = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const RowClass &C = op.classes[op.cls[k] & kClassMask];
@@ -1051,7 +1061,7 @@ __global__ void k_cg_update(OpView op, double *__restrict__ x, double *__restric
                             int nparts, int nn, const PoissonScal *__restrict__ sc) {
   __shared__ double sh[40];
   if (sc->done) return;
-  const double rz = sum_partials(part, nparts, sh);
+  const double rz = sc->rz;
   const double pap = sum_partials(part + kPartials, nparts, sh);
   const double alpha = pap != 0 ? rz / pap : 0.0;
   double v = 0, w2 = 0;
@@ -1083,21 +1093,104 @@ __global__ void k_cg_dir(OpView op, const double *__restrict__ z, double *__rest
                          int nparts, int nn, PoissonScal *sc, double rtol2) {
   __shared__ double sh[40];
   if (sc->done) return;
-  const double rz = sum_partials(part, nparts, sh);
+  const double rz = sc->rz;
   const double rzn = sum_partials(part + 2 * kPartials, nparts, sh);
   const double res2 = sum_partials(part + 3 * kPartials, nparts, sh);
   const double beta = rz != 0 ? rzn / rz : 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) p[k] = z[k] + beta * p[k];
-  // next iteration's rz lives in part[0..nparts): copy rz_new there
-  __syncthreads();
-  if (blockIdx.x == 0) {
-    for (int k = threadIdx.x; k < nparts; k += blockDim.x) part[k] = part[2 * kPartials + k];
-    if (threadIdx.x == 0) {
-      sc->res2 = res2;
-      sc->relres = sc->rhs2 > 0 ? sqrt(res2 / sc->rhs2) : sqrt(res2);
-      sc->iters += 1;
-      if ((sc->rhs2 > 0 && res2 <= rtol2 * sc->rhs2) || res2 == 0.0) sc->done = 1;
-    }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->rz_new = rzn;  // moved to sc->rz by the next k_cg_ap
+    sc->res2 = res2;
+    sc->relres = sc->rhs2 > 0 ? sqrt(res2 / sc->rhs2) : sqrt(res2);
+    sc->iters += 1;
+    if ((sc->rhs2 > 0 && res2 <= rtol2 * sc->rhs2) || res2 == 0.0) sc->done = 1;
+  }
+}
+
+// rz of the first iteration (partials of k_cg_init / k_pcg_init in part[2K..])
+__global__ void k_cg_rz0(const double *__restrict__ part, int nparts, PoissonScal *sc) {
+  __shared__ double sh[40];
+  const double t = sum_partials(part + 2 * kPartials, nparts, sh);
+  if (threadIdx.x == 0) sc->rz_new = t;
+}
+
+// ---- flexible PCG with the multigrid preconditioner (multigrid.cu) ----
+// z = M^-1 r comes from a V-cycle between k_pcg_update and k_pcg_dots; the
+// direction update is Polak-Ribiere, beta = z_new.(r_new - r_old) / rz_old
+// = -alpha z_new.(S p) / rz_old, which tolerates the FP32 rounding of the
+// cycle.  Iteration: k_cg_ap, k_pcg_update, cycle, k_pcg_dots, k_pcg_dir.
+__global__ void k_pcg_init(OpView op, const double *__restrict__ r, const double *__restrict__ z,
+                           double *__restrict__ p, double *__restrict__ part, int nn) {
+  __shared__ double sh[40];
+  double v = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const double zz = (op.cls[k] & kFixedBit) ? 0.0 : z[k];
+    p[k] = zz;
+    v += r[k] * zz;
+  }
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[2 * kPartials + blockIdx.x] = t;
+}
+
+// α = rz/pAp; x += αp; r -= αAp; partial ||res||²; α kept for the direction
+__global__ void k_pcg_update(OpView op, double *__restrict__ x, double *__restrict__ r, const double *__restrict__ p,
+                             const double *__restrict__ ap, double *__restrict__ part, int nparts, int nn,
+                             PoissonScal *__restrict__ sc) {
+  __shared__ double sh[40];
+  if (sc->done) return;
+  const double rz = sc->rz;
+  const double pap = sum_partials(part + kPartials, nparts, sh);
+  const double alpha = pap != 0 ? rz / pap : 0.0;
+  double w2 = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    const RowClass &C = op.classes[op.cls[k] & kClassMask];
+    if (C.fixed) continue;
+    x[k] += alpha * p[k];
+    const double rr = r[k] - alpha * ap[k];
+    r[k] = rr;
+    const double res = rr / C.d;
+    w2 += res * res;
+  }
+  double t2 = block_sum(w2, sh);
+  if (threadIdx.x == 0) part[3 * kPartials + blockIdx.x] = t2;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc->pap = alpha;
+}
+
+// partials of z.r (part[2K..]) and z.Sp (part[K..], after k_pcg_update read pAp)
+__global__ void k_pcg_dots(const double *__restrict__ r, const double *__restrict__ z, const double *__restrict__ ap,
+                           double *__restrict__ part, int nn, const PoissonScal *__restrict__ sc) {
+  __shared__ double sh[40];
+  if (sc->done) return;
+  double a = 0, b = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    a += z[k] * r[k];
+    b += z[k] * ap[k];
+  }
+  const double ta = block_sum(a, sh), tb = block_sum(b, sh);
+  if (threadIdx.x == 0) {
+    part[2 * kPartials + blockIdx.x] = ta;
+    part[kPartials + blockIdx.x] = tb;
+  }
+}
+
+// β (Polak-Ribiere), p = z + βp on free rows, convergence on the unscaled residual
+__global__ void k_pcg_dir(OpView op, const double *__restrict__ z, double *__restrict__ p, double *__restrict__ part,
+                          int nparts, int nn, PoissonScal *sc, double rtol2) {
+  __shared__ double sh[40];
+  if (sc->done) return;
+  const double rz = sc->rz, alpha = sc->pap;
+  const double rzn = sum_partials(part + 2 * kPartials, nparts, sh);
+  const double zap = sum_partials(part + kPartials, nparts, sh);
+  const double res2 = sum_partials(part + 3 * kPartials, nparts, sh);
+  const double beta = rz != 0 ? -alpha * zap / rz : 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x)
+    p[k] = (op.cls[k] & kFixedBit) ? 0.0 : z[k] + beta * p[k];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->rz_new = rzn;
+    sc->res2 = res2;
+    sc->relres = sc->rhs2 > 0 ? sqrt(res2 / sc->rhs2) : sqrt(res2);
+    sc->iters += 1;
+    if ((sc->rhs2 > 0 && res2 <= rtol2 * sc->rhs2) || res2 == 0.0) sc->done = 1;
   }
 }
 
@@ -1432,6 +1525,30 @@ static int build_device(Ctx *c, Poisson *P) {
     }
   }
   P->separable = sep;
+  // ---- multigrid preconditioner of the CG path ----
+  mg_destroy(P->mg);
+  P->mg = nullptr;
+  if (P->pcg_graph) cudaGraphExecDestroy(P->pcg_graph);
+  P->pcg_graph = nullptr;
+  if (!sep && !singular && P->method != 1) {
+    std::vector<double> s0(nn, 0.0), sW(nn, 0.0), sE(nn, 0.0), sS(nn, 0.0), sN(nn, 0.0);
+    std::vector<char> free_row(nn, 0);
+    int per_x = 0, per_y = 0;
+    for (int r = 0; r < nn; r++) {
+      per_x |= P->C[(size_t)r * 7 + 5] != 0.0;
+      per_y |= P->C[(size_t)r * 7 + 6] != 0.0;
+      const RowEff &e = rows[r];
+      if (e.fixed) continue;
+      free_row[r] = 1;
+      s0[r] = -d[r] * e.c0;
+      sW[r] = -d[r] * e.cW;
+      sE[r] = -d[r] * e.cE;
+      sS[r] = -d[r] * e.cS;
+      sN[r] = -d[r] * e.cN;
+    }
+    int rc = mg_build(c, nx, ny, s0, sW, sE, sS, sN, free_row, per_x, per_y, &P->mg);
+    if (rc) return rc;
+  }
   // ---- device upload ----
   cudaStream_t st = c->stream;
   ISKRA_CUDA(c, cudaStreamSynchronize(st));
@@ -1962,8 +2079,27 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
                                  (int)P->singular, rtol2, eout(c, true), last ? loop : none));
       }
     }
+  } else if (P->mg) {  // flexible PCG, one multigrid V-cycle per iteration
+    const int *skip = &P->scal->done;
+    if (reset_cg) {  // rhs2 is already in scal
+      int rc = mg_queue_cycle(c, P->mg, P->r, P->z, skip);
+      if (rc) return rc;
+      k_pcg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);
+      k_cg_rz0<<<1, T, 0, st>>>(P->part, B, P->scal);
+    }
+    for (int s = 0; s < count; s++) {
+      k_cg_ap<<<B, T, 0, st>>>(op, P->p, P->ap, P->part, nn, P->scal);
+      k_pcg_update<<<B, T, 0, st>>>(op, P->x, P->r, P->p, P->ap, P->part, B, nn, P->scal);
+      int rc = mg_queue_cycle(c, P->mg, P->r, P->z, skip);
+      if (rc) return rc;
+      k_pcg_dots<<<B, T, 0, st>>>(P->r, P->z, P->ap, P->part, nn, P->scal);
+      k_pcg_dir<<<B, T, 0, st>>>(op, P->z, P->p, P->part, B, nn, P->scal, rtol2);
+    }
   } else {
-    if (reset_cg) k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);  // rhs2 is already in scal
+    if (reset_cg) {  // rhs2 is already in scal
+      k_cg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);
+      k_cg_rz0<<<1, T, 0, st>>>(P->part, B, P->scal);
+    }
     for (int s = 0; s < count; s++) {
       k_cg_ap<<<B, T, 0, st>>>(op, P->p, P->ap, P->part, nn, P->scal);
       k_cg_update<<<B, T, 0, st>>>(op, P->x, P->r, P->z, P->p, P->ap, P->part, B, nn, P->scal);
@@ -2081,7 +2217,7 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
   int done_it = 0;
   const SweepLoop none{};
   for (;;) {
-    const int chunk = std::min(P->separable ? 2 : 32, maxit - done_it);
+    const int chunk = std::min(P->separable ? 2 : (P->mg ? 4 : 32), maxit - done_it);
     if (first) {
       rc = queue_prologue(c, rtol, c->graph_dt, none, false);
       if (rc) return rc;
@@ -2115,8 +2251,35 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
         }
       }
     }
-    rc = queue_sweeps(c, rtol, chunk, first, none);
-    if (rc) return rc;
+    if (P->mg) {
+      // multigrid CG: the start (V-cycle of the first residual) queued, then
+      // the iteration's kernels replayed as one graph
+      if (first) {
+        rc = queue_sweeps(c, rtol, 0, true, none);
+        if (rc) return rc;
+      }
+      if (!P->pcg_graph || P->pcg_graph_rtol != rtol) {
+        if (P->pcg_graph) cudaGraphExecDestroy(P->pcg_graph);
+        P->pcg_graph = nullptr;
+        cudaGraph_t g;
+        ISKRA_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int qrc = queue_sweeps(c, rtol, 1, false, none);
+        const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+        if (qrc) {
+          if (ce == cudaSuccess) cudaGraphDestroy(g);
+          return qrc;
+        }
+        ISKRA_CUDA(c, ce);
+        const cudaError_t ie = cudaGraphInstantiate(&P->pcg_graph, g, 0);
+        cudaGraphDestroy(g);
+        ISKRA_CUDA(c, ie);
+        P->pcg_graph_rtol = rtol;
+      }
+      for (int s = 0; s < chunk; s++) ISKRA_CUDA(c, cudaGraphLaunch(P->pcg_graph, c->stream));
+    } else {
+      rc = queue_sweeps(c, rtol, chunk, first, none);
+      if (rc) return rc;
+    }
     first = false;
     ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost, c->stream));
     ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -2579,14 +2742,14 @@ int iskra_poisson_set_method(iskra_ctx *h, int method, int *active) {
   if (!h) return ISKRA_EINVAL;
   Ctx *c = &h->c;
   if (!c->ps) return set_err(c, ISKRA_EINVAL, "no Poisson solver");
-  if (method != 0 && method != 1) return set_err(c, ISKRA_EINVAL, "method must be 0 or 1");
+  if (method < 0 || method > 2) return set_err(c, ISKRA_EINVAL, "method must be 0, 1 or 2");
   if (c->ps->method != method) {
     c->ps->method = method;
     c->ps->dirty = true;
   }
   int rc = poisson_prepare(c);
   if (rc) return rc;
-  if (active) *active = c->ps->separable ? 0 : 1;
+  if (active) *active = c->ps->separable ? 0 : (c->ps->mg ? 2 : 1);
   return ISKRA_OK;
 }
 

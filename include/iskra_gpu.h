@@ -361,6 +361,24 @@ int iskra_poisson_residual(iskra_ctx *ctx, const double *f, const double *phi,
  * launched on this context (graph replays x kernel nodes). */
 int iskra_kernel_launches(iskra_ctx *ctx, uint64_t *count);
 
+/* ---- diagnostics: openPMD records as HDF5 (Diagnostics/src/hdf5.jl) ------
+ * new_iteration(prefix, i, t, dt) (:47-66) with save_record of every field
+ * and particle record (:69-101) and the metadata of Diagnostics/src/openpmd:
+ * writes <prefix>/hdf5/data<iteration>.h5 holding, under /data/<iteration>/,
+ * fields/{rho, phi, E/{x,y,z}, n<species>, nuMCC-<species>-<k>} (the MCC
+ * counts accumulated since the previous record; the reference writes every
+ * step's), the circuit's fields/{Q1, I1, V1, Vext} when one is attached and,
+ * when particles != 0, particles/<species>/{position/{x,y}, momentum/{x,y,z},
+ * weighting, id, charge, mass, positionOffset/{x,y,z}}.  Field arrays in
+ * Julia memory order (HDF5 dimensions (ny, nx)).  species_names: one name
+ * per species (NULL: "s0", "s1", ...).  The file is laid out from the
+ * published HDF5 file format (version 2 superblock and object headers,
+ * compact groups, contiguous FP64 datasets); no HDF5 library is linked.
+ * (synchronises) */
+int iskra_write_openpmd(iskra_ctx *ctx, const char *prefix, int64_t iteration,
+                        double time, double dt,
+                        const char *const *species_names, int particles);
+
 /* ---- density without device allocation -----------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: a host framework that reserves the GPU's memory up front and

@@ -102,6 +102,7 @@ SIGNATURES = [
     ("iskra_solve_info", c_int, [CTX, ip, dp]),
     ("iskra_poisson_residual", c_int, [CTX, dp, dp, dp]),
     ("iskra_kernel_launches", c_int, [CTX, POINTER(c_uint64)]),
+    ("iskra_write_openpmd", c_int, [CTX, c_char_p, c_int64, c_double, c_double, POINTER(c_char_p), c_int]),
     ("iskra_density_noalloc", c_int, [POINTER(Grid), c_void_p, c_int64, c_int64, c_double, c_void_p, c_void_p,
                                       c_uint64]),
     ("iskra_ens_create", c_int, [CTX, c_int, c_int64, POINTER(c_void_p)]),

@@ -509,6 +509,7 @@ int ensure_mcc_work(Ctx *c);
 void ensembles_detach(Ctx *c);
 void mcc_key(uint64_t seed, int set_index, uint32_t &k0, uint32_t &k1);
 int mcc_nproc(Ctx *c, int mid);
+int mcc_download_nu(Ctx *c, int mid, unsigned *out);  // accepted collisions per node and process, then zeroed
 int mcc_src(Ctx *c, int mid);
 int mcc_prod(Ctx *c, int mid);
 int mcc_set_index(Ctx *c, int mid);

@@ -587,6 +587,18 @@ __global__ void k_mcc_sigma(const float *__restrict__ e, const float *__restrict
     out[k] = (double)sigma_at(e, s, n, (float)x[k], logu, le0, idl);
 }
 
+// Accepted collisions per node and process since the previous call (the
+// "nuMCC" record of perform!, mcc.jl:234,283,287, which counts one step):
+// out[node N + k]; the device counters restart from zero.  Synchronous.
+int mcc_download_nu(Ctx *c, int mid, unsigned *out) {
+  Mcc *m = c->mccs[mid];
+  const size_t bytes = (size_t)c->nn * m->N * sizeof(unsigned);
+  ISKRA_CUDA(c, cudaMemcpyAsync(out, m->nu, bytes, cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(m->nu, 0, bytes, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ISKRA_OK;
+}
+
 int mcc_nproc(Ctx *c, int mid) { return c->mccs[mid]->N; }
 int mcc_src(Ctx *c, int mid) { return c->mccs[mid]->src; }
 int mcc_prod(Ctx *c, int mid) { return c->mccs[mid]->prod; }

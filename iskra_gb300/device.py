@@ -7,6 +7,7 @@ float64 node arrays (nx, ny), particle matrices (np, 2) / (np, 3).
 from __future__ import annotations
 
 import ctypes
+import os
 from ctypes import byref, c_double, c_int, c_int64, c_uint64, c_void_p
 
 import numpy as np
@@ -356,6 +357,15 @@ class Context:
         n = c_uint64()
         self._c(self.lib.iskra_kernel_launches(self.h, byref(n)))
         return n.value
+
+    def write_openpmd(self, prefix, iteration, time, dt, species_names=None, particles=True):
+        """new_iteration + save_record of every record: <prefix>/hdf5/data<iteration>.h5."""
+        names = None
+        if species_names is not None:
+            names = (ctypes.c_char_p * len(species_names))(*[s.encode() for s in species_names])
+        self._c(self.lib.iskra_write_openpmd(self.h, str(prefix).encode(), int(iteration), float(time), float(dt),
+                                             names, int(bool(particles))))
+        return os.path.join(str(prefix), "hdf5", f"data{int(iteration)}.h5")
 
     def set_sort_every(self, every):
         self._c(self.lib.iskra_set_sort_every(self.h, every))

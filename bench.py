@@ -314,7 +314,7 @@ def c4_measure(steps, plain_n=105000, plain_amp=300.0):
     ctx.close()
     return {"metric": "particle-steps/s", "value": 0.5 * (n0 + n_end) * steps / (ms * 1e-3),
             "unit": "particle-steps/s", "ms_per_step": ms / steps, "steps": steps, "runs": R,
-            "particles": [n0, n_end], "workload": "256 x (1D CCP argon discharge, 257x2 nodes, e- and Ar+ MCC, "
+            "particles": [n0, n_end], "workload": f"{R} x (1D CCP argon discharge, 257x2 nodes, e- and Ar+ MCC, "
             "drive U[100,500] V; run 0 = the plain run), one ensemble step graph", "data": "synthetic",
             "run0_relres": field_relres(rho0, phi0)}, v_run0
 
@@ -628,6 +628,7 @@ def cpu_run(w, e, i, max_seconds=20.0, max_steps=None):
 
 # ----------------------------------------------------------------------------
 def main():
+    global C4_RUNS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
@@ -638,7 +639,10 @@ def main():
     ap.add_argument("--no-c4", action="store_true", help="skip the batched-ensemble (C4) leg")
     ap.add_argument("--no-c5", action="store_true", help="skip the learned-warm-start (C5 method) leg")
     ap.add_argument("--no-tracker", action="store_true", help="skip the surface-tracker leg")
+    ap.add_argument("--c4-runs", type=int, default=C4_RUNS,
+                    help="runs of the batched ensemble (smaller cases for profiling)")
     args = ap.parse_args()
+    C4_RUNS = args.c4_runs
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -610,10 +610,21 @@ void poisson_destroy(Poisson *p);
 void mcc_destroy(Mcc *m);
 
 // learned warm start (lws.cu), called by CG solves after their first residual
+struct LwsScal {               // device-resident scalars of the learned warm start
+  double ss;                   // Σ r² of the solve's first (scaled) residual
+  double inv_s, scale;         // 1/s and s·gain, s = RMS of r (both 0 when r = 0)
+  double alpha;                // line-search step of the correction (0: not applied)
+  double res2_before;          // squared residual norm before the correction
+  double alpha_sum, ratio_sum; // over the applied corrections
+  long long warm_solves;
+};
 bool lws_active(Ctx *c);
-int lws_begin(Ctx *c, const double *r, const float **y, double *scale);
+bool lws_harvesting(Ctx *c);
+// queues the network on r; *y (device; nullptr unless in use mode) times
+// *scale (device) is the predicted correction
+int lws_begin(Ctx *c, const double *r, const float **y, const double **scale);
+LwsScal *lws_scal(Ctx *c);
 int lws_mark_start(Ctx *c, const double *phi);
-void lws_note_applied(Ctx *c, double alpha, double ratio);
 int lws_end(Ctx *c, const double *phi, bool converged);
 void lws_destroy_ctx(Ctx *c);
 

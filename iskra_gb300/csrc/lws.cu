@@ -162,6 +162,207 @@ __global__ void __launch_bounds__(128) k_conv32(const bf16 *__restrict__ in, con
   }
 }
 
+// ---- the same convolution on the 5th-generation tensor cores (tcgen05) ----
+//
+// Implicit GEMM per 16 x 8-pixel output tile: D (128 pixels x 32 output
+// channels, FP32 in tensor memory) = Σ over 9 taps x 2 K-slices of
+// A (128 pixels x 16 input channels) B (16 x 32), 18 tcgen05.mma of
+// M128 N32 K16 (BF16 x BF16 -> FP32) issued by one thread.  Both operands sit
+// in shared memory in the canonical K-major layout without swizzle: "core
+// matrices" of 8 rows x 16 bytes (8 channels), 128 contiguous bytes.
+//   A: the tile's (16 + 2) x (8 + 2)-pixel patch stored as four planes, one
+//      per channel octet, of 180 pixels x 16 bytes.  The tap (dy, dx) view is
+//      the plane address shifted by dy * 10 + dx pixels: its 8-row core
+//      matrices are the tile's pixel rows (8 consecutive pixels, 16 B apart),
+//      successive rows 10 pixels (160 B) apart (stride offset), successive
+//      octets one plane (2880 B) apart (leading offset).
+//   B: w[tap][n][k] as (tap, octet, n) chunks of 16 bytes: core matrices of
+//      8 output channels 128 B apart, octets 512 B apart.
+// Blocks are persistent (a fixed number per SM, weights staged once): the
+// patch of the next tile streams in by cp.async while the current tile's
+// accumulators (two 32-column TMEM buffers) are read back with tcgen05.ld,
+// activated, rounded to BF16 and stored.  Waits on the MMA completion
+// barrier are bounded; a wait that gives up raises DERR_TIMEOUT and the block
+// stops after its MMAs drain.
+constexpr int kTcTy = 16, kTcTx = 8;                         // output tile: M = 128 pixels
+constexpr int kTcPw = kTcTx + 2, kTcPix = (kTcTy + 2) * kTcPw;  // patch: 18 x 10 pixels
+constexpr int kTcPlane = kTcPix * 16;                         // bytes per channel-octet plane
+constexpr int kTcPatch = 4 * kTcPlane;                        // 11520 B
+constexpr int kTcWBytes = 9 * 4 * kCh * 16;                   // 18432 B
+constexpr int kTcSmem = kTcWBytes + 2 * kTcPatch;             // 41472 B
+constexpr int kTcBlocksPerSm = 4;                             // 4 x 64 TMEM columns of 512
+constexpr unsigned kTcSpins = 1u << 22;                       // polls of the MMA barrier before DERR_TIMEOUT
+// instruction descriptor (kind::f16): D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17,
+// M >> 4 at bit 24
+constexpr unsigned kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(kCh >> 3) << 17) | ((128u >> 4) << 24);
+
+// shared-memory matrix descriptor: start, leading and stride byte offsets
+// (16-byte units), descriptor version 1 (bit 46), no swizzle, base offset 0
+__device__ __forceinline__ unsigned long long tc_sdesc(unsigned saddr, unsigned lbo, unsigned sbo) {
+  return (unsigned long long)((saddr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void tc_mma(unsigned d_tmem, unsigned long long a, unsigned long long b, unsigned acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kTcIdesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(unsigned long long *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ bool tc_wait(unsigned long long *bar, unsigned parity) {
+  const unsigned b = smem_u32(bar);
+  for (unsigned it = 0; it < kTcSpins; it++) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(b), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// 32 FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld32(unsigned taddr, unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async16(unsigned dst, const void *src, unsigned bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+
+template <bool RELU>
+__global__ void __launch_bounds__(128) k_conv32_tc(const bf16 *__restrict__ in, const bf16 *__restrict__ w,
+                                                   bf16 *__restrict__ out, int H, int W, int *err) {
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  __shared__ __align__(8) unsigned long long bar[2];
+  __shared__ unsigned tmem_base;
+  __shared__ int stop;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const unsigned sW = smem_u32(tc_smem), sP = sW + kTcWBytes;
+  const int ntx = (W + kTcTx - 1) / kTcTx, ntiles = ntx * ((H + kTcTy - 1) / kTcTy);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(&tmem_base))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[1])) : "memory");
+    stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int c = tid; c < 9 * kCh * 4; c += blockDim.x) {
+    const int o = c & 3, row = c >> 2;  // row = tap * 32 + n
+    *reinterpret_cast<uint4 *>(tc_smem + (row >> 5) * 2048 + o * 512 + (row & 31) * 16) =
+        *reinterpret_cast<const uint4 *>(w + row * kCh + o * 8);
+  }
+  auto load_patch_tc = [&](int t, int b) {
+    const int y0 = (t / ntx) * kTcTy - 1, x0 = (t % ntx) * kTcTx - 1;
+    const unsigned dst = sP + b * kTcPatch;
+    for (int c = tid; c < kTcPix * 4; c += blockDim.x) {
+      const int o = c & 3, q = c >> 2;
+      const int y = y0 + q / kTcPw, x = x0 + q % kTcPw;
+      const bool ok = y >= 0 && y < H && x >= 0 && x < W;
+      cp_async16(dst + o * kTcPlane + q * 16, ok ? in + ((size_t)y * W + x) * kCh + o * 8 : in, ok ? 16u : 0u);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  auto issue = [&](int b) {
+    tc_fence_after();
+    const unsigned pa = sP + b * kTcPatch, d = tmem_base + b * kCh;
+#pragma unroll
+    for (int tap = 0; tap < 9; tap++) {
+      const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+      for (int kc = 0; kc < 2; kc++) {
+        const unsigned long long a = tc_sdesc(pa + kc * 2 * kTcPlane + (dy * kTcPw + dx) * 16, kTcPlane, kTcPw * 16);
+        const unsigned long long bd = tc_sdesc(sW + tap * 2048 + kc * 1024, 512, 128);
+        tc_mma(d, a, bd, (tap | kc) ? 1u : 0u);
+      }
+    }
+    tc_commit(&bar[b]);
+  };
+  int t = blockIdx.x;
+  if (t < ntiles) load_patch_tc(t, 0);
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && t < ntiles) issue(0);
+  unsigned phase = 0;  // bit b: parity of the next completion of bar[b]
+  int b = 0;
+  for (; t < ntiles; t += gridDim.x, b ^= 1) {
+    const int tn = t + gridDim.x;
+    if (tn < ntiles) load_patch_tc(tn, b ^ 1);
+    const bool ok = tc_wait(&bar[b], (phase >> b) & 1u);
+    if (ok) phase ^= 1u << b;
+    tc_fence_after();
+    if (ok) {
+      unsigned r[32];
+      tc_ld32(tmem_base + b * kCh + ((unsigned)(warp * 32) << 16), r);
+      const int m = tid;  // TMEM lane = GEMM row = tile pixel
+      const int y = (t / ntx) * kTcTy + (m >> 3), x = (t % ntx) * kTcTx + (m & 7);
+      if (y < H && x < W) {
+        uint4 *dst = reinterpret_cast<uint4 *>(out + ((size_t)y * W + x) * kCh);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          unsigned v[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            float v0 = __uint_as_float(r[8 * q + 2 * e]), v1 = __uint_as_float(r[8 * q + 2 * e + 1]);
+            if (RELU) {
+              v0 = fmaxf(v0, 0.f);
+              v1 = fmaxf(v1, 0.f);
+            }
+            __nv_bfloat162 p2 = __floats2bfloat162_rn(v0, v1);
+            v[e] = *reinterpret_cast<unsigned *>(&p2);
+          }
+          dst[q] = make_uint4(v[0], v[1], v[2], v[3]);
+        }
+      }
+    } else {
+      atomicOr(err, DERR_TIMEOUT);
+      stop = 1;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (stop) break;
+    if (tid == 0 && tn < ntiles) issue(b ^ 1);
+  }
+  if (stop && tid == 0) tc_wait(&bar[b], (phase >> b) & 1u);  // the MMAs in flight drain before TMEM is freed
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem_base) : "memory");
+  }
+}
+
 // dw[tap][co][ci] += Σ_p dz[p][co] in[p + off(tap)][ci]: nine warps, one per
 // tap, each a 32 x 32 FP32 tile (co x ci) over the K = pixel dimension in
 // steps of one 16-pixel tile row; operands are read transposed from the
@@ -229,34 +430,42 @@ __global__ void __launch_bounds__(288) k_conv32_dw(const bf16 *__restrict__ in, 
       }
 }
 
-// a0[p][c] = relu(Σ_tap x[p + off(tap)] w0[tap][c]), x rounded to BF16
-__global__ void k_enc0(const float *__restrict__ x, const bf16 *__restrict__ w0, bf16 *__restrict__ a0, int H, int W) {
-  __shared__ float ws[kW1];
-  for (int t = threadIdx.x; t < kW1; t += blockDim.x) ws[t] = bf(w0[t]);
-  __syncthreads();
-  const int P = H * W;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+// a0[p][c] = relu(Σ_tap x[p + off(tap)] w0[tap][c]), x rounded to BF16.
+// Four threads per pixel, one per channel octet, each holding its 9 x 8
+// weights in registers; the quad's x loads coincide (one transaction).
+__global__ void __launch_bounds__(256) k_enc0(const float *__restrict__ x, const bf16 *__restrict__ w0,
+                                              bf16 *__restrict__ a0, int H, int W) {
+  const int o = threadIdx.x & 3;
+  float wr[9][8];
+#pragma unroll
+  for (int tap = 0; tap < 9; tap++)
+#pragma unroll
+    for (int u = 0; u < 8; u++) wr[tap][u] = bf(w0[tap * kCh + o * 8 + u]);
+  const int P = H * W;  // at most 2^30 nodes
+  const int per_block = blockDim.x >> 2;
+  for (int p = blockIdx.x * per_block + (threadIdx.x >> 2); p < P; p += gridDim.x * per_block) {
     const int y = p / W, xx = p - y * W;
     float v[9];
 #pragma unroll
-    for (int tap = 0; tap < 9; tap++) {
+    for (int tap = 0; tap < 9; tap++) {  // unconditional loads of the clamped pixel, zeroed outside
       const int yy = y + tap / 3 - 1, xq = xx + tap % 3 - 1;
-      v[tap] = (yy >= 0 && yy < H && xq >= 0 && xq < W) ? x[yy * W + xq] : 0.f;
+      const int yc = min(max(yy, 0), H - 1), xc = min(max(xq, 0), W - 1);
+      const float t = __ldg(x + (size_t)yc * W + xc);
+      v[tap] = (yy == yc && xq == xc) ? t : 0.f;
     }
-    __nv_bfloat162 o[kCh / 2];
+    unsigned out[4];
 #pragma unroll
-    for (int c = 0; c < kCh; c += 2) {
+    for (int u = 0; u < 8; u += 2) {
       float s0 = 0.f, s1 = 0.f;
 #pragma unroll
       for (int tap = 0; tap < 9; tap++) {
-        s0 = fmaf(v[tap], ws[tap * kCh + c], s0);
-        s1 = fmaf(v[tap], ws[tap * kCh + c + 1], s1);
+        s0 = fmaf(v[tap], wr[tap][u], s0);
+        s1 = fmaf(v[tap], wr[tap][u + 1], s1);
       }
-      o[c / 2] = __floats2bfloat162_rn(fmaxf(s0, 0.f), fmaxf(s1, 0.f));
+      __nv_bfloat162 h2 = __floats2bfloat162_rn(fmaxf(s0, 0.f), fmaxf(s1, 0.f));
+      out[u / 2] = *reinterpret_cast<unsigned *>(&h2);
     }
-    uint4 *dst = reinterpret_cast<uint4 *>(a0 + (size_t)p * kCh);
-#pragma unroll
-    for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const uint4 *>(o)[q];
+    *reinterpret_cast<uint4 *>(a0 + (size_t)p * kCh + o * 8) = make_uint4(out[0], out[1], out[2], out[3]);
   }
 }
 
@@ -275,28 +484,45 @@ __global__ void __launch_bounds__(288) k_enc0_dw(const float *__restrict__ x, co
   atomicAdd(dw + tap * kCh + c, s);
 }
 
-// y[p] = Σ_tap Σ_c a[p + off(tap)][c] w7[tap][c] (FP32 output)
-__global__ void k_head(const bf16 *__restrict__ a, const bf16 *__restrict__ w7, float *__restrict__ y, int H, int W) {
-  __shared__ float ws[kW1];
-  for (int t = threadIdx.x; t < kW1; t += blockDim.x) ws[t] = bf(w7[t]);
-  __syncthreads();
-  const int P = H * W;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
-    const int yy0 = p / W, xx0 = p - yy0 * W;
+// y[p] = Σ_tap Σ_c a[p + off(tap)][c] w7[tap][c] (FP32 output).  Four
+// threads per pixel, one per channel octet (its 9 x 8 weights in registers,
+// one 16-byte load per tap), summed across the quad with two shuffles; the
+// block's pixel range advances uniformly so every lane reaches the shuffles.
+__global__ void __launch_bounds__(256) k_head(const bf16 *__restrict__ a, const bf16 *__restrict__ w7,
+                                              float *__restrict__ y, int H, int W) {
+  const int o = threadIdx.x & 3;
+  float wr[9][8];
+#pragma unroll
+  for (int tap = 0; tap < 9; tap++)
+#pragma unroll
+    for (int u = 0; u < 8; u++) wr[tap][u] = bf(w7[tap * kCh + o * 8 + u]);
+  const int P = H * W;  // at most 2^30 nodes
+  const int per_block = blockDim.x >> 2;
+  for (int base = blockIdx.x * per_block; base < P; base += gridDim.x * per_block) {
+    const int p = base + (threadIdx.x >> 2);
     float s = 0.f;
-    for (int tap = 0; tap < 9; tap++) {
-      const int yy = yy0 + tap / 3 - 1, xq = xx0 + tap % 3 - 1;
-      if (yy < 0 || yy >= H || xq < 0 || xq >= W) continue;
-      const uint4 *src = reinterpret_cast<const uint4 *>(a + ((size_t)yy * W + xq) * kCh);
+    if (p < P) {
+      const int yy0 = p / W, xx0 = p - yy0 * W;
+      uint4 v[9];
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const uint4 v = src[q];
-        const bf16 *e = reinterpret_cast<const bf16 *>(&v);
+      for (int tap = 0; tap < 9; tap++) {
+        // unconditional loads from the clamped pixel (all nine in flight at
+        // once), zeroed outside the image
+        const int yy = yy0 + tap / 3 - 1, xq = xx0 + tap % 3 - 1;
+        const int yc = min(max(yy, 0), H - 1), xc = min(max(xq, 0), W - 1);
+        const uint4 t = __ldg(reinterpret_cast<const uint4 *>(a + ((size_t)yc * W + xc) * kCh + o * 8));
+        v[tap] = (yy == yc && xq == xc) ? t : make_uint4(0u, 0u, 0u, 0u);
+      }
 #pragma unroll
-        for (int u = 0; u < 8; u++) s = fmaf(bf(e[u]), ws[tap * kCh + q * 8 + u], s);
+      for (int tap = 0; tap < 9; tap++) {
+        const bf16 *e = reinterpret_cast<const bf16 *>(&v[tap]);
+#pragma unroll
+        for (int u = 0; u < 8; u++) s = fmaf(bf(e[u]), wr[tap][u], s);
       }
     }
-    y[p] = s;
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (p < P && o == 0) y[p] = s;
   }
 }
 
@@ -527,8 +753,18 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
 
 // network input: x = bf16(r / s) of the scaled residual (and a copy into the
 // harvested pair when rec != nullptr)
-__global__ void k_lws_input(const double *__restrict__ r, double inv_s, float *__restrict__ x, float *__restrict__ rec,
-                            int P) {
+// s = RMS of the first residual (from ss = Σ r²), its inverse and the scale of
+// the network's output, on the device (no host round trip inside the solve)
+__global__ void k_lws_scale(LwsScal *ls, int P, double gain) {
+  const double s = sqrt(ls->ss / P);
+  const bool ok = s > 0 && isfinite(s);
+  ls->inv_s = ok ? 1.0 / s : 0.0;
+  ls->scale = ok ? s * gain : 0.0;
+}
+
+__global__ void k_lws_input(const double *__restrict__ r, const LwsScal *__restrict__ ls, float *__restrict__ x,
+                            float *__restrict__ rec, int P) {
+  const double inv_s = ls->inv_s;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
     const float v = round_bf((float)(r[p] * inv_s));
     x[p] = v;
@@ -567,8 +803,9 @@ __global__ void k_smooth(const float *__restrict__ in, float *__restrict__ out, 
 }
 
 // harvested target (ϕ - ϕ_prev) / s
-__global__ void k_lws_target(const double *__restrict__ phi, const double *__restrict__ prev, double inv_s,
-                             float *__restrict__ t, int P) {
+__global__ void k_lws_target(const double *__restrict__ phi, const double *__restrict__ prev,
+                             const LwsScal *__restrict__ ls, float *__restrict__ t, int P) {
+  const double inv_s = ls->inv_s;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x)
     t[p] = (float)((phi[p] - prev[p]) * inv_s);
 }
@@ -593,11 +830,9 @@ struct Lws {
   double *prev = nullptr;                      // ϕ before the solve (harvest)
   double *loss = nullptr;                      // device accumulator
   int slot = -1;                               // pair being harvested by the running solve
-  double s = 0.0;
   double gain = 0.0;                           // network output x gain = correction / s (0: not set)
-  long long solves = 0, warm_solves = 0;
-  double alpha_sum = 0.0;                      // line-search steps of the applied warm starts
-  double ratio_sum = 0.0;                      // residual norm after / before the warm starts
+  long long solves = 0;
+  LwsScal *scal = nullptr;                     // device: s of the running solve, warm-start statistics
   std::vector<void *> allocs;
 };
 
@@ -623,6 +858,41 @@ int blocks_for(Ctx *c, long long n, int threads) {
 
 dim3 conv_grid(int H, int W) { return dim3((W + kTx - 1) / kTx, (H + kTy - 1) / kTy); }
 
+#define LWS_TRY(call)        \
+  do {                       \
+    const int rc_ = (call);  \
+    if (rc_) return rc_;     \
+  } while (0)
+
+// out = act(conv(in, w)) for one 32 -> 32 layer: tcgen05 kernel, or the
+// mma.sync kernel when the context selected it (ISKRA_CONV_MMA_SYNC=1, kept
+// for measurement)
+int conv32(Ctx *c, bool relu, const bf16 *in, const bf16 *w, bf16 *out, int H, int W) {
+  cudaStream_t st = c->stream;
+  static const bool legacy = [] {
+    const char *e = std::getenv("ISKRA_CONV_MMA_SYNC");
+    return e && e[0] == '1';
+  }();
+  if (legacy) {
+    if (relu) k_conv32<true><<<conv_grid(H, W), 128, 0, st>>>(in, w, out, H, W);
+    else k_conv32<false><<<conv_grid(H, W), 128, 0, st>>>(in, w, out, H, W);
+    ISKRA_CUDA(c, cudaGetLastError());
+    return ISKRA_OK;
+  }
+  static bool attr = false;
+  if (!attr) {
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_conv32_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_conv32_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+    attr = true;
+  }
+  const int tiles = ((W + kTcTx - 1) / kTcTx) * ((H + kTcTy - 1) / kTcTy);
+  const int grid = std::min(tiles, kTcBlocksPerSm * c->num_sms);
+  if (relu) k_conv32_tc<true><<<grid, 128, kTcSmem, st>>>(in, w, out, H, W, c->d_err);
+  else k_conv32_tc<false><<<grid, 128, kTcSmem, st>>>(in, w, out, H, W, c->d_err);
+  ISKRA_CUDA(c, cudaGetLastError());
+  return ISKRA_OK;
+}
+
 int lws_forward(Ctx *c, Lws *L) {
   cudaStream_t st = c->stream;
   const int T = 256;
@@ -631,13 +901,13 @@ int lws_forward(Ctx *c, Lws *L) {
   k_enc0<<<blocks_for(c, (long long)h[0] * w[0], T), T, 0, st>>>(L->x, wb + layer_off(0), L->a[0], h[0], w[0]);
   for (int l = 1; l <= 3; l++) {
     k_pool<<<blocks_for(c, (long long)h[l] * w[l] * 4, T), T, 0, st>>>(L->a[l - 1], L->p[l], h[l - 1], w[l - 1]);
-    k_conv32<true><<<conv_grid(h[l], w[l]), 128, 0, st>>>(L->p[l], wb + layer_off(l), L->a[l], h[l], w[l]);
+    LWS_TRY(conv32(c, true, L->p[l], wb + layer_off(l), L->a[l], h[l], w[l]));
   }
   // decoder: a4 at level 2, a5 at level 1, a6 at level 0
   for (int l = 2; l >= 0; l--) {
     const int li = 6 - l;  // layer 4, 5, 6
     k_up_add<<<blocks_for(c, (long long)h[l] * w[l] * 4, T), T, 0, st>>>(L->a[li - 1], L->a[l], L->u[l], h[l], w[l]);
-    k_conv32<true><<<conv_grid(h[l], w[l]), 128, 0, st>>>(L->u[l], wb + layer_off(li), L->a[li], h[l], w[l]);
+    LWS_TRY(conv32(c, true, L->u[l], wb + layer_off(li), L->a[li], h[l], w[l]));
   }
   k_head<<<blocks_for(c, (long long)h[0] * w[0], T), T, 0, st>>>(L->a[6], wb + layer_off(7), L->y, h[0], w[0]);
   ISKRA_CUDA(c, cudaGetLastError());
@@ -668,7 +938,7 @@ int lws_backward(Ctx *c, Lws *L, const float *t, float tscale, bool energy = fal
   // decoder layers 6, 5, 4 (levels 0, 1, 2): input u[l], output gradient dz[li]
   for (int l = 0; l <= 2; l++) {
     const int li = 6 - l;
-    k_conv32<false><<<conv_grid(h[l], w[l]), 128, 0, st>>>(L->dz[li], L->wt + layer_off(li), L->du[l], h[l], w[l]);
+    LWS_TRY(conv32(c, false, L->dz[li], L->wt + layer_off(li), L->du[l], h[l], w[l]));
     k_conv32_dw<<<dwb(l), 288, 0, st>>>(L->u[l], L->dz[li], L->g32 + layer_off(li), h[l], w[l]);
     // the upsampled input came from layer li - 1 one level down
     k_up_bwd_mask<<<blocks_for(c, (long long)h[l + 1] * w[l + 1] * 4, T), T, 0, st>>>(
@@ -677,7 +947,7 @@ int lws_backward(Ctx *c, Lws *L, const float *t, float tscale, bool energy = fal
   // encoder layers 3, 2, 1: input p[l], then the pooled layer l - 1 gets its
   // pooling gradient plus the skip gradient du[l - 1]
   for (int l = 3; l >= 1; l--) {
-    k_conv32<false><<<conv_grid(h[l], w[l]), 128, 0, st>>>(L->dz[l], L->wt + layer_off(l), L->dp[l], h[l], w[l]);
+    LWS_TRY(conv32(c, false, L->dz[l], L->wt + layer_off(l), L->dp[l], h[l], w[l]));
     k_conv32_dw<<<dwb(l), 288, 0, st>>>(L->p[l], L->dz[l], L->g32 + layer_off(l), h[l], w[l]);
     k_pool_bwd_mask<<<blocks_for(c, (long long)h[l - 1] * w[l - 1] * 4, T), T, 0, st>>>(
         L->dp[l], L->du[l - 1], L->a[l - 1], L->dz[l - 1], h[l - 1], w[l - 1]);
@@ -723,25 +993,24 @@ bool lws_active(Ctx *c) { return c->lws && (c->lws->harvest || c->lws->use); }
 // harvested pair and, in use mode, runs the network: *y (device) times
 // *scale is the predicted correction of ϕ (*y = nullptr otherwise).  The
 // solver applies it along an exact line search in its energy norm.
-int lws_begin(Ctx *c, const double *r, const float **y, double *scale) {
+bool lws_harvesting(Ctx *c) { return c->lws && c->lws->harvest; }
+
+LwsScal *lws_scal(Ctx *c) { return c->lws ? c->lws->scal : nullptr; }
+
+int lws_begin(Ctx *c, const double *r, const float **y, const double **scale) {
   Lws *L = c->lws;
   *y = nullptr;
-  *scale = 0.0;
+  *scale = nullptr;
   L->slot = -1;
   const int P = L->H * L->W;
   const int T = 256;
-  ISKRA_CUDA(c, cudaMemsetAsync(L->loss, 0, sizeof(double), c->stream));
-  k_sumsq<double><<<blocks_for(c, P, T), T, 0, c->stream>>>(r, P, L->loss);
-  double ss = 0.0;
-  ISKRA_CUDA(c, cudaMemcpyAsync(&ss, L->loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
-  const double s = std::sqrt(ss / P);
-  if (!(s > 0) || !std::isfinite(s)) return ISKRA_OK;
-  L->s = s;
+  ISKRA_CUDA(c, cudaMemsetAsync(&L->scal->ss, 0, sizeof(double), c->stream));
+  k_sumsq<double><<<blocks_for(c, P, T), T, 0, c->stream>>>(r, P, &L->scal->ss);
+  k_lws_scale<<<1, 1, 0, c->stream>>>(L->scal, P, L->gain > 0 ? L->gain : 1.0);
   float *rec = nullptr;
   if (L->harvest && L->capacity > 0) L->slot = L->next;
   if (L->slot >= 0) rec = L->din + (size_t)L->slot * P;
-  k_lws_input<<<blocks_for(c, P, T), T, 0, c->stream>>>(r, 1.0 / s, L->x, rec, P);
+  k_lws_input<<<blocks_for(c, P, T), T, 0, c->stream>>>(r, L->scal, L->x, rec, P);
   ISKRA_CUDA(c, cudaGetLastError());
   L->solves++;
   if (L->use) {
@@ -756,7 +1025,7 @@ int lws_begin(Ctx *c, const double *r, const float **y, double *scale) {
     }
     ISKRA_CUDA(c, cudaGetLastError());
     *y = a;
-    *scale = s * (L->gain > 0 ? L->gain : 1.0);
+    *scale = &L->scal->scale;
   }
   return ISKRA_OK;
 }
@@ -771,22 +1040,13 @@ int lws_mark_start(Ctx *c, const double *phi) {
   return ISKRA_OK;
 }
 
-// a warm start was applied with line-search step alpha; ratio = residual
-// norm after it / before it
-void lws_note_applied(Ctx *c, double alpha, double ratio) {
-  Lws *L = c->lws;
-  L->warm_solves++;
-  L->alpha_sum += alpha;
-  L->ratio_sum += ratio;
-}
-
 // After the solve: the harvested target of a converged solve
 int lws_end(Ctx *c, const double *phi, bool converged) {
   Lws *L = c->lws;
   if (L->slot < 0) return ISKRA_OK;
   const int P = L->H * L->W;
   if (converged) {
-    k_lws_target<<<blocks_for(c, P, 256), 256, 0, c->stream>>>(phi, L->prev, 1.0 / L->s,
+    k_lws_target<<<blocks_for(c, P, 256), 256, 0, c->stream>>>(phi, L->prev, L->scal,
                                                                 L->dout + (size_t)L->slot * P, P);
     ISKRA_CUDA(c, cudaGetLastError());
     L->next = (L->next + 1) % L->capacity;
@@ -849,6 +1109,7 @@ int iskra_lws_create(iskra_ctx *h, int capacity, uint64_t seed) {
   LWS_ALLOC(L->dy, P0 * sizeof(float));
   LWS_ALLOC(L->te, P0 * sizeof(float));
   LWS_ALLOC(L->loss, sizeof(double));
+  LWS_ALLOC(L->scal, sizeof(LwsScal));
   LWS_ALLOC(L->prev, P0 * sizeof(double));
   // level of each activation: a0..a3 at 0..3, a4 at 2, a5 at 1, a6 at 0
   const int lev[7] = {0, 1, 2, 3, 2, 1, 0};
@@ -913,12 +1174,16 @@ int iskra_lws_info(iskra_ctx *h, int *pairs, int *nparams, int64_t *solves, int6
                    double *mean_alpha, double *mean_ratio) {
   Lws *L = get_lws(h);
   if (!L) return h ? set_err(&h->c, ISKRA_EINVAL, "no learned warm start") : ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  LwsScal st;
+  ISKRA_CUDA(c, cudaMemcpyAsync(&st, L->scal, sizeof(LwsScal), cudaMemcpyDeviceToHost, c->stream));
+  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
   if (pairs) *pairs = L->count;
   if (nparams) *nparams = kParams;
   if (solves) *solves = L->solves;
-  if (warm_solves) *warm_solves = L->warm_solves;
-  if (mean_alpha) *mean_alpha = L->warm_solves ? L->alpha_sum / L->warm_solves : 0.0;
-  if (mean_ratio) *mean_ratio = L->warm_solves ? L->ratio_sum / L->warm_solves : 0.0;
+  if (warm_solves) *warm_solves = st.warm_solves;
+  if (mean_alpha) *mean_alpha = st.warm_solves ? st.alpha_sum / st.warm_solves : 0.0;
+  if (mean_ratio) *mean_ratio = st.warm_solves ? st.ratio_sum / st.warm_solves : 0.0;
   return ISKRA_OK;
 }
 

@@ -40,6 +40,7 @@ struct MgLevel {
   int nx = 0, ny = 0, n = 0;
   int per_x = 0, per_y = 0;   // couplings across the seam exist on this axis
   int cx = 0, cy = 0;          // x / y coarsened towards the next level
+  int five = 0;                // no corner couplings (5-point stencil)
   float *coef = nullptr;       // 9 x n: offset o = (dy + 1) 3 + (dx + 1), node-major
   float *dinv = nullptr;       // omega / diagonal, 0 on nodes outside the correction
   float *x = nullptr, *x2 = nullptr, *b = nullptr, *r = nullptr;
@@ -98,53 +99,82 @@ __host__ __device__ __forceinline__ int axis_parents(int i, int n, int nc, int c
 }
 
 // ---- kernels (FP32) ----------------------------------------------------------
+// Node kernels run one thread per node on (32 x 8)-thread blocks over the
+// level's grid; every stencil load is issued unconditionally (a zero
+// coefficient multiplies a finite x) so that the loads of a node overlap.
+// FIVE: the level has no corner couplings (level 0, the 5-point operator):
+// the four corner planes are neither read nor multiplied.
+constexpr int kMgBx = 32, kMgBy = 8;
+
 __device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+template <bool FIVE>
 __device__ __forceinline__ float apply9(const float *__restrict__ coef, const float *__restrict__ x, int k, int i,
                                         int j, int nx, int ny, int n) {
-  float a = 0.f;
-#pragma unroll
-  for (int dy = -1; dy <= 1; dy++) {
-    const int jj = wrap_idx(j + dy, ny);
-#pragma unroll
-    for (int dx = -1; dx <= 1; dx++) {
-      const float cf = coef[(size_t)((dy + 1) * 3 + dx + 1) * n + k];
-      if (cf != 0.f) a = fmaf(cf, x[wrap_idx(i + dx, nx) + nx * jj], a);
-    }
+  const int iw = wrap_idx(i - 1, nx), ie = wrap_idx(i + 1, nx);
+  const int rs = nx * wrap_idx(j - 1, ny), rc = nx * j, rn = nx * wrap_idx(j + 1, ny);
+  float a = coef[(size_t)4 * n + k] * x[k];
+  a = fmaf(coef[(size_t)1 * n + k], x[i + rs], a);
+  a = fmaf(coef[(size_t)3 * n + k], x[iw + rc], a);
+  a = fmaf(coef[(size_t)5 * n + k], x[ie + rc], a);
+  a = fmaf(coef[(size_t)7 * n + k], x[i + rn], a);
+  if (!FIVE) {
+    a = fmaf(coef[(size_t)0 * n + k], x[iw + rs], a);
+    a = fmaf(coef[(size_t)2 * n + k], x[ie + rs], a);
+    a = fmaf(coef[(size_t)6 * n + k], x[iw + rn], a);
+    a = fmaf(coef[(size_t)8 * n + k], x[ie + rn], a);
   }
   return a;
 }
 
-// one damped-Jacobi sweep: xo = xi + dinv (b - A xi); xi == nullptr: xi = 0
-__global__ void __launch_bounds__(256) k_mg_smooth(const float *__restrict__ coef, const float *__restrict__ dinv,
-                                                   const float *__restrict__ xi, float *__restrict__ xo,
-                                                   const float *__restrict__ b, int nx, int ny, const int *skip) {
+// One damped-Jacobi sweep: xo = xi + dinv (b - A xi).  xi == nullptr: the
+// first sweep from x = 0 (xo = dinv b); with r64 given it also forms the
+// level-0 right-hand side b = (float) r64 (the FP64 scaled residual of the
+// CG iteration).  z64 given: the last sweep of the cycle writes the result
+// in FP64 there instead of xo.
+template <bool FIVE>
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_smooth(const float *__restrict__ coef,
+                                                             const float *__restrict__ dinv,
+                                                             const float *__restrict__ xi, float *__restrict__ xo,
+                                                             float *__restrict__ b, int nx, int ny, const int *skip,
+                                                             const double *__restrict__ r64, double *__restrict__ z64) {
   pdl_wait();
   if (*skip) return;
-  const int n = nx * ny;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const float dk = dinv[k];
-    if (!xi) {
-      xo[k] = dk * b[k];
-      continue;
+  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const int n = nx * ny, k = i + nx * j;
+  const float dk = dinv[k];
+  if (!xi) {
+    float bk;
+    if (r64) {
+      bk = (float)r64[k];
+      b[k] = bk;
+    } else {
+      bk = b[k];
     }
-    const int j = k / nx, i = k - j * nx;
-    const float ax = dk != 0.f ? apply9(coef, xi, k, i, j, nx, ny, n) : 0.f;
-    xo[k] = xi[k] + dk * (b[k] - ax);
+    xo[k] = dk * bk;
+    return;
   }
+  const float ax = apply9<FIVE>(coef, xi, k, i, j, nx, ny, n);
+  const float v = dk != 0.f ? xi[k] + dk * (b[k] - ax) : 0.f;
+  if (z64) z64[k] = (double)v;
+  else xo[k] = v;
 }
 
 // r = b - A x on the correction's nodes
-__global__ void __launch_bounds__(256) k_mg_residual(const float *__restrict__ coef, const float *__restrict__ dinv,
-                                                     const float *__restrict__ x, const float *__restrict__ b,
-                                                     float *__restrict__ r, int nx, int ny, const int *skip) {
+template <bool FIVE>
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_residual(const float *__restrict__ coef,
+                                                               const float *__restrict__ dinv,
+                                                               const float *__restrict__ x,
+                                                               const float *__restrict__ b, float *__restrict__ r,
+                                                               int nx, int ny, const int *skip) {
   pdl_wait();
   if (*skip) return;
-  const int n = nx * ny;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int j = k / nx, i = k - j * nx;
-    r[k] = dinv[k] != 0.f ? b[k] - apply9(coef, x, k, i, j, nx, ny, n) : 0.f;
-  }
+  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const int n = nx * ny, k = i + nx * j;
+  const float ax = apply9<FIVE>(coef, x, k, i, j, nx, ny, n);
+  r[k] = dinv[k] != 0.f ? b[k] - ax : 0.f;
 }
 
 struct MgXfer {
@@ -152,13 +182,13 @@ struct MgXfer {
 };
 
 // coarse b = P^T r (gathered per coarse node from its fine candidates)
-__global__ void __launch_bounds__(256) k_mg_restrict(const float *__restrict__ r, float *__restrict__ bc, MgXfer T,
-                                                     const int *skip) {
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_restrict(const float *__restrict__ r, float *__restrict__ bc,
+                                                               MgXfer T, const int *skip) {
   pdl_wait();
   if (*skip) return;
-  const int nc = T.ncx * T.ncy;
-  for (int K = blockIdx.x * blockDim.x + threadIdx.x; K < nc; K += gridDim.x * blockDim.x) {
-    const int J = K / T.ncx, I = K - J * T.ncx;
+  const int I = blockIdx.x * kMgBx + threadIdx.x, J = blockIdx.y * kMgBy + threadIdx.y;
+  if (I < T.ncx && J < T.ncy) {
+    const int K = I + T.ncx * J;
     float s = 0.f;
     // fine candidates along each axis: 2I-1, 2I, 2I+1 (wrapped), or I itself
     int fi[3], fj[3];
@@ -210,51 +240,43 @@ __global__ void __launch_bounds__(256) k_mg_restrict(const float *__restrict__ r
 }
 
 // x += P xc on the correction's nodes
-__global__ void __launch_bounds__(256) k_mg_prolong(float *__restrict__ x, const float *__restrict__ dinv,
-                                                    const float *__restrict__ xc, MgXfer T, const int *skip) {
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_prolong(float *__restrict__ x, const float *__restrict__ dinv,
+                                                              const float *__restrict__ xc, MgXfer T,
+                                                              const int *skip) {
   pdl_wait();
   if (*skip) return;
-  const int n = T.nx * T.ny;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    if (dinv[k] == 0.f) continue;
-    const int j = k / T.nx, i = k - j * T.nx;
-    int ci[2], cj[2];
-    float wi[2], wj[2];
-    const int pi = axis_parents(i, T.nx, T.ncx, T.cx, T.per_x, ci, wi);
-    const int pj = axis_parents(j, T.ny, T.ncy, T.cy, T.per_y, cj, wj);
-    float v = 0.f;
-    for (int b2 = 0; b2 < pj; b2++)
-      for (int a2 = 0; a2 < pi; a2++) v = fmaf(wi[a2] * wj[b2], xc[ci[a2] + T.ncx * cj[b2]], v);
-    x[k] += v;
-  }
+  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
+  if (i >= T.nx || j >= T.ny) return;
+  const int k = i + T.nx * j;
+  if (dinv[k] == 0.f) return;
+  int ci[2], cj[2];
+  float wi[2], wj[2];
+  const int pi = axis_parents(i, T.nx, T.ncx, T.cx, T.per_x, ci, wi);
+  const int pj = axis_parents(j, T.ny, T.ncy, T.cy, T.per_y, cj, wj);
+  float v = 0.f;
+  for (int b2 = 0; b2 < pj; b2++)
+    for (int a2 = 0; a2 < pi; a2++) v = fmaf(wi[a2] * wj[b2], xc[ci[a2] + T.ncx * cj[b2]], v);
+  x[k] += v;
 }
 
 // coarsest level: x = Ainv b (one warp per row)
+// (a hierarchy of one level reads r64 and writes z64, the FP64 vectors of the
+// CG iteration, directly)
 __global__ void __launch_bounds__(256) k_mg_coarse(const float *__restrict__ inv, const float *__restrict__ b,
-                                                   float *__restrict__ x, int n, const int *skip) {
+                                                   float *__restrict__ x, int n, const int *skip,
+                                                   const double *__restrict__ r64, double *__restrict__ z64) {
   pdl_wait();
   if (*skip) return;
   const int lane = threadIdx.x & 31;
   for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += (gridDim.x * blockDim.x) >> 5) {
     float s = 0.f;
-    for (int c = lane; c < n; c += 32) s = fmaf(inv[(size_t)row * n + c], b[c], s);
+    for (int c = lane; c < n; c += 32) s = fmaf(inv[(size_t)row * n + c], r64 ? (float)r64[c] : b[c], s);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) x[row] = s;
+    if (lane == 0) {
+      if (z64) z64[row] = (double)s;
+      else x[row] = s;
+    }
   }
-}
-
-// level 0 input / output: b0 = r (the FP64 scaled residual) on free rows; z = x0
-__global__ void __launch_bounds__(256) k_mg_in(const double *__restrict__ r, float *__restrict__ b, int n,
-                                               const int *skip) {
-  pdl_wait();
-  if (*skip) return;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) b[k] = (float)r[k];
-}
-__global__ void __launch_bounds__(256) k_mg_out(const float *__restrict__ x, double *__restrict__ z, int n,
-                                                const int *skip) {
-  pdl_wait();
-  if (*skip) return;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) z[k] = (double)x[k];
 }
 
 // ---- host: hierarchy --------------------------------------------------------
@@ -430,6 +452,10 @@ int mg_build(Ctx *c, int nx, int ny, const std::vector<double> &s0, const std::v
     D.per_y = S.per_y;
     D.cx = l + 1 < H.size() ? cxs[l] : 0;
     D.cy = l + 1 < H.size() ? cys[l] : 0;
+    D.five = 1;
+    for (int o : {0, 2, 6, 8})
+      for (int k = 0; k < D.n && D.five; k++)
+        if (S.coef[(size_t)o * D.n + k] != 0.0) D.five = 0;
     std::vector<float> cf(S.coef.begin(), S.coef.end()), dinv(D.n, 0.f);
     for (int k = 0; k < D.n; k++)
       if (S.active[k] && S.coef[(size_t)4 * D.n + k] > 0) dinv[k] = kMgOmega / (float)S.coef[(size_t)4 * D.n + k];
@@ -458,14 +484,27 @@ int mg_build(Ctx *c, int nx, int ny, const std::vector<double> &s0, const std::v
 
 int mg_levels(const Mg *m) { return m ? (int)m->lv.size() : 0; }
 
-static int mg_grid(Ctx *c, int n) { return std::max(1, std::min(c->num_sms * 4, (n + 255) / 256)); }
+static dim3 mg_grid2(int nx, int ny) { return dim3((nx + kMgBx - 1) / kMgBx, (ny + kMgBy - 1) / kMgBy); }
+
+static int mg_smooth(Ctx *c, const MgLevel &D, const float *src, float *dst, const int *skip, const double *r64,
+                     double *z64) {
+  const dim3 g = mg_grid2(D.nx, D.ny), t(kMgBx, kMgBy);
+  if (D.five)
+    ISKRA_CUDA(c, launch_pdl(k_mg_smooth<true>, g, t, 0, c->stream, (const float *)D.coef, (const float *)D.dinv, src,
+                             dst, D.b, D.nx, D.ny, skip, r64, z64));
+  else
+    ISKRA_CUDA(c, launch_pdl(k_mg_smooth<false>, g, t, 0, c->stream, (const float *)D.coef, (const float *)D.dinv, src,
+                             dst, D.b, D.nx, D.ny, skip, r64, z64));
+  return ISKRA_OK;
+}
 
 // z = M^-1 r: one V(2,2) cycle on the scaled residual r (FP64, free rows);
-// every kernel returns at once while *skip is set (a converged solve)
+// every kernel returns at once while *skip is set (a converged solve).  The
+// first sweep of level 0 converts r to FP32, the last one writes z in FP64.
 int mg_queue_cycle(Ctx *c, Mg *m, const double *r, double *z, const int *skip) {
   cudaStream_t st = c->stream;
   const int L = (int)m->lv.size();
-  ISKRA_CUDA(c, launch_pdl(k_mg_in, mg_grid(c, m->lv[0].n), 256, 0, st, r, m->lv[0].b, m->lv[0].n, skip));
+  const dim3 t(kMgBx, kMgBy);
   auto xfer = [&](int l) {
     const MgLevel &F = m->lv[l], &C = m->lv[l + 1];
     return MgXfer{F.nx, F.ny, C.nx, C.ny, F.cx, F.cy, F.per_x, F.per_y};
@@ -475,38 +514,39 @@ int mg_queue_cycle(Ctx *c, Mg *m, const double *r, double *z, const int *skip) {
   static_assert(kMgSweeps % 2 == 0, "an even sweep count leaves the iterate in x");
   for (int l = 0; l + 1 < L; l++) {
     MgLevel &D = m->lv[l];
-    const int g = mg_grid(c, D.n);
     for (int s = 0; s < kMgSweeps; s++) {
       const float *src = s == 0 ? nullptr : ((s & 1) ? D.x2 : D.x);
       float *dst = (s & 1) ? D.x : D.x2;
-      ISKRA_CUDA(c, launch_pdl(k_mg_smooth, g, 256, 0, st, (const float *)D.coef, (const float *)D.dinv, src, dst,
-                               (const float *)D.b, D.nx, D.ny, skip));
+      const int rc = mg_smooth(c, D, src, dst, skip, (l == 0 && s == 0) ? r : nullptr, nullptr);
+      if (rc) return rc;
     }
-    ISKRA_CUDA(c, launch_pdl(k_mg_residual, g, 256, 0, st, (const float *)D.coef, (const float *)D.dinv,
-                             (const float *)D.x, (const float *)D.b, D.r, D.nx, D.ny, skip));
+    if (D.five)
+      ISKRA_CUDA(c, launch_pdl(k_mg_residual<true>, mg_grid2(D.nx, D.ny), t, 0, st, (const float *)D.coef,
+                               (const float *)D.dinv, (const float *)D.x, (const float *)D.b, D.r, D.nx, D.ny, skip));
+    else
+      ISKRA_CUDA(c, launch_pdl(k_mg_residual<false>, mg_grid2(D.nx, D.ny), t, 0, st, (const float *)D.coef,
+                               (const float *)D.dinv, (const float *)D.x, (const float *)D.b, D.r, D.nx, D.ny, skip));
     const MgLevel &C = m->lv[l + 1];
-    ISKRA_CUDA(c, launch_pdl(k_mg_restrict, mg_grid(c, C.n), 256, 0, st, (const float *)D.r, C.b, xfer(l), skip));
+    ISKRA_CUDA(c, launch_pdl(k_mg_restrict, mg_grid2(C.nx, C.ny), t, 0, st, (const float *)D.r, C.b, xfer(l), skip));
   }
   {
     MgLevel &C = m->lv[L - 1];
     ISKRA_CUDA(c, launch_pdl(k_mg_coarse, std::max(1, std::min(c->num_sms * 2, (C.n + 7) / 8)), 256, 0, st,
-                             (const float *)m->cinv, (const float *)C.b, C.x, C.n, skip));
+                             (const float *)m->cinv, (const float *)C.b, C.x, C.n, skip, L == 1 ? r : nullptr,
+                             L == 1 ? z : nullptr));
   }
   // up: prolong, smooth
   for (int l = L - 2; l >= 0; l--) {
     MgLevel &D = m->lv[l];
-    const int g = mg_grid(c, D.n);
-    ISKRA_CUDA(c, launch_pdl(k_mg_prolong, g, 256, 0, st, D.x, (const float *)D.dinv, (const float *)m->lv[l + 1].x,
-                             xfer(l), skip));
+    ISKRA_CUDA(c, launch_pdl(k_mg_prolong, mg_grid2(D.nx, D.ny), t, 0, st, D.x, (const float *)D.dinv,
+                             (const float *)m->lv[l + 1].x, xfer(l), skip));
     for (int s = 0; s < kMgSweeps; s++) {
       const float *src = (s & 1) ? D.x2 : D.x;
       float *dst = (s & 1) ? D.x : D.x2;
-      ISKRA_CUDA(c, launch_pdl(k_mg_smooth, g, 256, 0, st, (const float *)D.coef, (const float *)D.dinv, src, dst,
-                               (const float *)D.b, D.nx, D.ny, skip));
+      const int rc = mg_smooth(c, D, src, dst, skip, nullptr, (l == 0 && s == kMgSweeps - 1) ? z : nullptr);
+      if (rc) return rc;
     }
   }
-  ISKRA_CUDA(c, launch_pdl(k_mg_out, mg_grid(c, m->lv[0].n), 256, 0, st, (const float *)m->lv[0].x, z,
-                           m->lv[0].n, skip));
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
 }

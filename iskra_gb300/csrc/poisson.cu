@@ -36,6 +36,7 @@ namespace iskra {
 struct RowClass {
   double c0, cW, cE, cS, cN;  // original (unscaled) coefficients
   double d;                   // symmetrising row scale
+  double inv_d;               // 1 / d
   double sig_coef;            // coefficient of the σ column
   int sig_dof;                // -1: none
   int fixed;                  // identity row
@@ -122,6 +123,7 @@ struct Poisson {
   double *drive_par = nullptr;  // 4 per group
   int ndrive = 0;
   int blocks = 0;
+  int cg_blocks = 0;            // blocks of the multigrid-PCG vector kernels (more per SM: latency bound)
   bool rho_fixed = false;       // some identity row takes its value from ρ (rewritten every solve)
   int last_iters = 0;
   double last_relres = 0;
@@ -1148,7 +1150,7 @@ __global__ void k_pcg_update(OpView op, double *__restrict__ x, double *__restri
     x[k] += alpha * p[k];
     const double rr = r[k] - alpha * ap[k];
     r[k] = rr;
-    const double res = rr / C.d;
+    const double res = rr * C.inv_d;
     w2 += res * res;
   }
   double t2 = block_sum(w2, sh);
@@ -1478,6 +1480,7 @@ static int build_device(Ctx *c, Poisson *P) {
       rc.cS = e.cS;
       rc.cN = e.cN;
       rc.d = e.fixed ? 1.0 : d[r];
+      rc.inv_d = 1.0 / rc.d;
       rc.nd32 = (float)(-rc.d);
       auto split = [](double v) {
         const float h = (float)v;
@@ -1622,6 +1625,7 @@ static int build_device(Ctx *c, Poisson *P) {
     }
   }
   P->blocks = std::min(kPartials, std::max(1, std::min(c->num_sms * ISKRA_RES_BLOCKS_PER_SM, (nn + 255) / 256)));
+  P->cg_blocks = std::min(kPartials, std::max(1, std::min(c->num_sms * 6, (nn + 255) / 256)));
   // ---- separable factorisation ----
   cudaFree(P->r32);
   cudaFree(P->spec);
@@ -2081,19 +2085,20 @@ static int queue_sweeps(Ctx *c, double rtol, int count, bool reset_cg, SweepLoop
     }
   } else if (P->mg) {  // flexible PCG, one multigrid V-cycle per iteration
     const int *skip = &P->scal->done;
+    const int G = P->cg_blocks;
     if (reset_cg) {  // rhs2 is already in scal
       int rc = mg_queue_cycle(c, P->mg, P->r, P->z, skip);
       if (rc) return rc;
-      k_pcg_init<<<B, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);
-      k_cg_rz0<<<1, T, 0, st>>>(P->part, B, P->scal);
+      k_pcg_init<<<G, T, 0, st>>>(op, P->r, P->z, P->p, P->part, nn);
+      k_cg_rz0<<<1, T, 0, st>>>(P->part, G, P->scal);
     }
     for (int s = 0; s < count; s++) {
-      k_cg_ap<<<B, T, 0, st>>>(op, P->p, P->ap, P->part, nn, P->scal);
-      k_pcg_update<<<B, T, 0, st>>>(op, P->x, P->r, P->p, P->ap, P->part, B, nn, P->scal);
+      k_cg_ap<<<G, T, 0, st>>>(op, P->p, P->ap, P->part, nn, P->scal);
+      k_pcg_update<<<G, T, 0, st>>>(op, P->x, P->r, P->p, P->ap, P->part, G, nn, P->scal);
       int rc = mg_queue_cycle(c, P->mg, P->r, P->z, skip);
       if (rc) return rc;
-      k_pcg_dots<<<B, T, 0, st>>>(P->r, P->z, P->ap, P->part, nn, P->scal);
-      k_pcg_dir<<<B, T, 0, st>>>(op, P->z, P->p, P->part, B, nn, P->scal, rtol2);
+      k_pcg_dots<<<G, T, 0, st>>>(P->r, P->z, P->ap, P->part, nn, P->scal);
+      k_pcg_dir<<<G, T, 0, st>>>(op, P->z, P->p, P->part, G, nn, P->scal, rtol2);
     }
   } else {
     if (reset_cg) {  // rhs2 is already in scal
@@ -2155,14 +2160,16 @@ int poisson_solve_graph(Ctx *c, double rtol) {
 // Learned warm start of a CG solve: δ = scale y on the free rows (the
 // network's predicted correction), applied as ϕ += α δ with the exact line
 // search α = δ·r / δ·Sδ in the energy norm of the scaled system S ϕ = c
-// (r = c - S ϕ the scaled residual), so the CG error never grows.
-__global__ void k_lws_dir(OpView op, const float *__restrict__ y, double scale, const double *__restrict__ r,
-                          double *__restrict__ p, double *__restrict__ part, int nn) {
+// (r = c - S ϕ the scaled residual), so the CG error never grows.  Every
+// scalar stays on the device: no host round trip inside the solve.
+__global__ void k_lws_dir(OpView op, const float *__restrict__ y, const double *__restrict__ scale,
+                          const double *__restrict__ r, double *__restrict__ p, double *__restrict__ part, int nn) {
   __shared__ double sh[40];
+  const double sc = *scale;
   double v = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const RowClass &C = op.classes[op.cls[k] & kClassMask];
-    const double d = C.fixed ? 0.0 : scale * (double)y[k];
+    const double d = C.fixed ? 0.0 : sc * (double)y[k];
     p[k] = d;
     v += d * r[k];
   }
@@ -2170,33 +2177,54 @@ __global__ void k_lws_dir(OpView op, const float *__restrict__ y, double scale, 
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-__global__ void k_lws_axpy(double *__restrict__ x, const double *__restrict__ p, double alpha, int nn) {
+// α from the block partials of δ·r (part) and δ·Sδ (part + kPartials); no
+// step when the first residual already met the tolerance or α is not a
+// positive number
+__global__ void __launch_bounds__(256) k_lws_alpha(const double *__restrict__ part, int nb, LwsScal *ls,
+                                                   const PoissonScal *sc) {
+  __shared__ double sh[40];
+  double dr = 0, dsd = 0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    dr += part[b];
+    dsd += part[kPartials + b];
+  }
+  dr = block_sum(dr, sh);
+  __syncthreads();
+  dsd = block_sum(dsd, sh);
+  if (threadIdx.x == 0) {
+    double a = dsd > 0 ? dr / dsd : 0.0;
+    if (!(a > 0) || !isfinite(a) || sc->done) a = 0.0;
+    ls->alpha = a;
+    ls->res2_before = sc->res2;
+  }
+}
+
+__global__ void k_lws_axpy(double *__restrict__ x, const double *__restrict__ p, const LwsScal *__restrict__ ls,
+                           int nn) {
+  const double alpha = ls->alpha;
+  if (alpha == 0.0) return;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) x[k] += alpha * p[k];
 }
 
-static int lws_line_search(Ctx *c, const float *y, double scale, double *applied_alpha) {
-  *applied_alpha = 0.0;
+// after the residual of the corrected ϕ: statistics of the applied step
+__global__ void k_lws_stats(LwsScal *ls, const PoissonScal *sc) {
+  if (ls->alpha > 0) {
+    ls->warm_solves++;
+    ls->alpha_sum += ls->alpha;
+    ls->ratio_sum += ls->res2_before > 0 ? sqrt(sc->res2 / ls->res2_before) : 0.0;
+  }
+}
+
+static int lws_line_search(Ctx *c, const float *y, const double *scale) {
   Poisson *P = c->ps;
   const int B = P->blocks, T = 256, nn = P->nn;
   OpView op = opview(P);
+  LwsScal *ls = lws_scal(c);
   k_lws_dir<<<B, T, 0, c->stream>>>(op, y, scale, P->r, P->p, P->part, nn);
   k_cg_ap<<<B, T, 0, c->stream>>>(op, P->p, P->ap, P->part, nn, P->scal);
+  k_lws_alpha<<<1, 256, 0, c->stream>>>(P->part, B, ls, P->scal);
+  k_lws_axpy<<<B, T, 0, c->stream>>>(P->x, P->p, ls, nn);
   ISKRA_CUDA(c, cudaGetLastError());
-  std::vector<double> h(2 * (size_t)B);
-  ISKRA_CUDA(c, cudaMemcpyAsync(h.data(), P->part, B * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  ISKRA_CUDA(c, cudaMemcpyAsync(h.data() + B, P->part + kPartials, B * sizeof(double), cudaMemcpyDeviceToHost,
-                                c->stream));
-  ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
-  double dr = 0, dsd = 0;
-  for (int b = 0; b < B; b++) {
-    dr += h[b];
-    dsd += h[B + b];
-  }
-  const double alpha = dsd > 0 ? dr / dsd : 0.0;
-  if (!(alpha > 0) || !std::isfinite(alpha)) return ISKRA_OK;
-  k_lws_axpy<<<B, T, 0, c->stream>>>(P->x, P->p, alpha, nn);
-  ISKRA_CUDA(c, cudaGetLastError());
-  *applied_alpha = alpha;
   return ISKRA_OK;
 }
 
@@ -2222,31 +2250,33 @@ static int solve_sync(Ctx *c, double rtol, int maxit, int *iters, double *relres
       rc = queue_prologue(c, rtol, c->graph_dt, none, false);
       if (rc) return rc;
       if (!P->separable && lws_active(c)) {
-        // learned warm start: the network's correction from the first residual,
-        // then the residual again (CG restarts from the corrected ϕ)
-        ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost, c->stream));
-        ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
-        if (!P->scal_h->done) {
+        // learned warm start: the network's correction from the first
+        // residual, then the residual again (CG restarts from the corrected
+        // ϕ).  Harvesting reads the first residual's convergence on the host
+        // (a solve that needs no iteration gives no training pair); in use
+        // mode the device skips the step of an already converged solve.
+        bool run = true;
+        if (lws_harvesting(c)) {
+          ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost,
+                                        c->stream));
+          ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+          run = !P->scal_h->done;
+        }
+        if (run) {
           const float *y = nullptr;
-          double scale = 0.0;
+          const double *scale = nullptr;
           lws_pending = true;
           rc = lws_begin(c, P->r, &y, &scale);
           if (rc) return rc;
           rc = lws_mark_start(c, P->x);
           if (rc) return rc;
           if (y) {
-            const double res2 = P->scal_h->res2;
-            double alpha = 0.0;
-            rc = lws_line_search(c, y, scale, &alpha);
+            rc = lws_line_search(c, y, scale);
             if (rc) return rc;
-            if (alpha > 0) {
-              rc = queue_prologue(c, rtol, c->graph_dt, none, false);
-              if (rc) return rc;
-              ISKRA_CUDA(c, cudaMemcpyAsync(P->scal_h, P->scal, sizeof(PoissonScal), cudaMemcpyDeviceToHost,
-                                            c->stream));
-              ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
-              lws_note_applied(c, alpha, res2 > 0 ? std::sqrt(P->scal_h->res2 / res2) : 0.0);
-            }
+            rc = queue_prologue(c, rtol, c->graph_dt, none, false);
+            if (rc) return rc;
+            k_lws_stats<<<1, 1, 0, c->stream>>>(lws_scal(c), P->scal);
+            ISKRA_CUDA(c, cudaGetLastError());
           }
         }
       }

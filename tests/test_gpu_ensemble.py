@@ -189,14 +189,21 @@ def eedf_l1(ve_a, ve_b):
 def test_ensemble_runs_match_oracle(orc, lib):
     """Ensemble runs against the FP64 oracle's loop body (PicOracle) directly:
     two runs of the batched discharge (drive amplitudes 200 V and 400 V),
-    400 steps.  Each ensemble run carries 4x the oracle's macroparticles
-    (weight / 4, the same densities).  Per run: accepted collisions per
+    400 steps, each ensemble run from the same initial particles as its
+    oracle run (the same macroparticle count: with four times the particles
+    at a quarter of the weight, the 400 V run's ionization and excitation
+    counts fell 2.5-9 % below the oracle's, ~3σ, the smaller numerical
+    heating of the finer sampling).  Per run: accepted collisions per
     process within 3.5σ, surviving counts within 3 %, EEDF L1 below 0.02
-    (the configuration's 2 %; its sampling-noise expectation is ~0.011)."""
-    R, n0, ng0, steps = 2, 100000, 400000, 400
+    (the configuration's 2 %; the sampling-noise expectation is printed)."""
+    R, n0, steps = 2, 100000, 400
     amps = [200.0, 400.0]
-    r_ = n0 / ng0
-    tmpl, ens, _, (se, si, me_, mi_), _ = make_ensemble(lib, R, ng0, amps)
+    r_ = 1.0
+    tmpl, ens, _, (se, si, me_, mi_), _ = make_ensemble(lib, R, n0, amps)
+    for r in range(R):
+        (xe, ve), (xi, vi) = initial_state(90 + r, n0)
+        ens.upload(r, se, xe, ve)
+        ens.upload(r, si, xi, vi)
     ens.step(DT, steps)
     ens.sync()
     eps, el, ex, iz, cx = argon_tables()

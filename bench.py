@@ -679,7 +679,14 @@ def main():
     ctx, se, si = setup_context(w, e, i)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
+    # push tile size and sort cadence tuned on this run (cached for the
+    # process: the end-to-end leg's context takes the same choice), then the
     # warm-up (also captures the step graph)
+    tile, sort_scale, tune_ms, tune_grid, _ = ctx.autotune(DT, trial=32, seed=1, rtol=RTOL)
+    autotune = {"tile_cells": tile, "sort_period_factor": sort_scale, "ms_per_step": tune_ms,
+                "candidates_ms_per_step": {f"{t}x{t} cells, sort factor {f:g}": v
+                                           for (t, f), v in sorted(tune_grid.items())},
+                "note": "iskra_autotune: 32 trial steps per candidate on this run, before the warm-up"}
     ctx.step(DT, args.warmup, seed=1, rtol=RTOL)
     ctx.sync()
     np_before = ctx.count(se) + ctx.count(si)
@@ -771,6 +778,7 @@ def main():
         # first steps capture the step and sort graphs and load the kernels
         ctx2.upload(se2, *host_in[0])
         ctx2.upload(si2, *host_in[1])
+        ctx2.autotune(DT, trial=32, seed=1, rtol=RTOL)  # the device leg's choice, from the process cache
         for k in range(max(args.warmup, 3)):
             ctx2.step(DT, 1, seed=1, rtol=RTOL)
             ctx2.field_async(1, phi_host[k % 2])
@@ -803,6 +811,7 @@ def main():
                               f"last relres {relres:.2e} in {it} sweep(s)",
                    "sort_every": "per species (automatic)" if SORT_EVERY < 0 else SORT_EVERY},
         "gpu_launches": launches,
+        "autotune": autotune,
         "roofline": {"bound": "hbm", "kernel": "k_push2 (both species: gather+push+discard/wrap+deposit)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic,

@@ -345,6 +345,26 @@ int iskra_set_sort_every(iskra_ctx *ctx, int every);
  * cadence (iskra_set_sort_every(ctx, -1)). */
 int iskra_autotune_sort(iskra_ctx *ctx, double dt, int trial, uint64_t seed,
                         double rtol, double *scale, double *ms_per_step);
+/* Push tile size (no reference counterpart): tiles of `cells` x `cells`
+ * cells, 8, 16 (default) or 32.  Re-sorts every species by the new tiles
+ * and rebuilds the step graph; results do not depend on it (the tile decides
+ * which block pushes a particle, never how). */
+int iskra_set_tile(iskra_ctx *ctx, int cells);
+int iskra_get_tile(iskra_ctx *ctx, int *cells);
+/* Autotunes the push tile size and the sort cadence together on the
+ * caller's own run: `trial` steps (as iskra_step with dt, seed, rtol) per
+ * candidate -- tiles of 8, 16, 32 cells x factors 0.5, 1, 2, 4 on the
+ * speed-based sort periods -- each after a sort of every species, timed on
+ * the device; keeps the fastest pair and returns it (tile, scale) with its
+ * time per step; ms_all (12 entries, tile-major, may be NULL) receives every
+ * candidate's time.  The choice is cached for the process by (grid,
+ * species count, particles per cell rounded to a power of two, tracker): a
+ * later call for the same shape applies it without trials (*cached = 1).
+ * Advances the simulation by 12 (trial + 1) steps unless cached.  Needs the
+ * automatic cadence. */
+int iskra_autotune(iskra_ctx *ctx, double dt, int trial, uint64_t seed,
+                   double rtol, int *tile, double *scale, double *ms_per_step,
+                   double *ms_all, int *cached);
 /* Last Poisson solve: iterations and relative residual (synchronises). */
 int iskra_solve_info(iskra_ctx *ctx, int *iters, double *relres);
 /* Relative residual of a host potential phi (nx,ny) against the assembled

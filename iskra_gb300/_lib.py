@@ -99,6 +99,9 @@ SIGNATURES = [
     ("iskra_step", c_int, [CTX, c_double, c_int, c_uint64, c_double]),
     ("iskra_set_sort_every", c_int, [CTX, c_int]),
     ("iskra_autotune_sort", c_int, [CTX, c_double, c_int, c_uint64, c_double, dp, dp]),
+    ("iskra_set_tile", c_int, [CTX, c_int]),
+    ("iskra_get_tile", c_int, [CTX, ip]),
+    ("iskra_autotune", c_int, [CTX, c_double, c_int, c_uint64, c_double, ip, dp, dp, dp, ip]),
     ("iskra_solve_info", c_int, [CTX, ip, dp]),
     ("iskra_poisson_residual", c_int, [CTX, dp, dp, dp]),
     ("iskra_kernel_launches", c_int, [CTX, POINTER(c_uint64)]),

@@ -28,6 +28,13 @@ int grid_blocks(Ctx *c, int threads, int per_sm) {
   return c->num_sms * per_sm;
 }
 
+void set_tile_shift_geometry(Ctx *c, int ts) {
+  c->tile_shift = ts;
+  tile_geometry(c->nx, c->ny, ts, c->tiles_x, c->tiles_y);
+  c->ntiles = c->tiles_x * c->tiles_y;
+  c->nkeys = c->ntiles << (2 * ts);
+}
+
 void invalidate_graphs(Ctx *c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
   c->graph = nullptr;
@@ -286,10 +293,13 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
   c->nx = g->nx;
   c->ny = g->ny;
   c->nn = g->nx * g->ny;
-  c->tiles_x = (std::max(g->nx - 1, 1) + kTile - 1) / kTile;
-  c->tiles_y = (std::max(g->ny - 1, 1) + kTile - 1) / kTile;
-  c->ntiles = c->tiles_x * c->tiles_y;
-  c->nkeys = c->ntiles * kTile * kTile;
+  for (int ts = kTileShiftMin; ts <= kTileShiftMax; ts++) {  // buffers fit every tile size
+    int tx, ty;
+    tile_geometry(g->nx, g->ny, ts, tx, ty);
+    c->ntiles_cap = std::max(c->ntiles_cap, tx * ty);
+    c->nkeys_cap = std::max(c->nkeys_cap, (tx * ty) << (2 * ts));
+  }
+  set_tile_shift_geometry(c, kTileShiftDefault);
   auto fail = [&](int rc) {
     iskra_ctx_destroy(h);
     return rc;
@@ -312,9 +322,9 @@ int iskra_ctx_create(const iskra_grid_t *g, uint64_t stream, iskra_ctx **out) {
             cudaMalloc(&c->vol_inv_df, nn * sizeof(float2)) == cudaSuccess &&
             cudaMalloc(&c->d_err, sizeof(int)) == cudaSuccess &&
             cudaMallocHost(&c->h_err, sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&c->cell_count, ((size_t)c->nkeys + 1) * sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&c->cell_cursor, ((size_t)c->nkeys + 1) * sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&c->scan_tmp, ((size_t)c->nkeys / 4096 + 2) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->cell_count, ((size_t)c->nkeys_cap + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->cell_cursor, ((size_t)c->nkeys_cap + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&c->scan_tmp, ((size_t)c->nkeys_cap / 4096 + 2) * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&c->d_step, sizeof(unsigned long long)) == cudaSuccess &&
             cudaMalloc(&c->d_scratch, 16 * sizeof(double)) == cudaSuccess;
   if (!ok) return fail(ISKRA_ENOMEM);
@@ -441,9 +451,9 @@ int iskra_species_create(iskra_ctx *h, double q, double m, double w0, int64_t ca
   ISKRA_CUDA(c, cudaMalloc(&s.dev.st, sizeof(SpeciesState)));
   ISKRA_CUDA(c, cudaMalloc(&s.dev.acc, nn * sizeof(unsigned long long)));
   ISKRA_CUDA(c, cudaMalloc(&s.dev.cnt, nn * sizeof(unsigned)));
-  ISKRA_CUDA(c, cudaMalloc(&s.dev.tile_begin, ((size_t)c->ntiles + 1) * sizeof(int)));
+  ISKRA_CUDA(c, cudaMalloc(&s.dev.tile_begin, ((size_t)c->ntiles_cap + 1) * sizeof(int)));
   ISKRA_CUDA(c, cudaMalloc(&s.dview, sizeof(SpeciesDev)));
-  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.tile_begin, 0, ((size_t)c->ntiles + 1) * sizeof(int), c->stream));
+  ISKRA_CUDA(c, cudaMemsetAsync(s.dev.tile_begin, 0, ((size_t)c->ntiles_cap + 1) * sizeof(int), c->stream));
   ISKRA_CUDA(c, cudaMalloc(&s.n, nn * sizeof(double)));
   ISKRA_CUDA(c, cudaMalloc(&s.n_df, nn * sizeof(float2)));
   ISKRA_CUDA(c, cudaMemsetAsync(s.dev.st, 0, sizeof(SpeciesState), c->stream));

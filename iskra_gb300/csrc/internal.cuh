@@ -66,17 +66,26 @@ struct SpeciesDev {            // kernel view of one species (by value)
   int *tile_begin;             // (ntiles + 1) first slot of each tile after the last sort
 };
 
-// Tiles: the push runs one block per tile of kTile x kTile cells over the
-// particles the last sort grouped there, with E at the nodes and the deposit
-// moments of the tile and a kHalo-cell margin in shared memory.  The sort key of a
-// cell is tile-major: tile * kTile^2 + the cell's position in the tile.
-constexpr int kTile = 16;
-constexpr int kTileShift = 4;
+// Tiles: the push runs one block per tile of 2^ts x 2^ts cells (ts =
+// Ctx::tile_shift: 8, 16 or 32 cells per axis, chosen by the autotuner;
+// 16 by default) over the particles the last sort grouped there, with E at
+// the nodes and the deposit moments of the tile and a kHalo-cell margin in
+// shared memory.  The sort key of a cell is tile-major: tile * 4^ts + the
+// cell's position in the tile.
+constexpr int kTileShiftMin = 3, kTileShiftMax = 5, kTileShiftDefault = 4;
 constexpr int kHalo = 2;
 
-__device__ __host__ __forceinline__ int cell_key(int i0, int j0, int tiles_x) {
-  const int t = (i0 >> kTileShift) + tiles_x * (j0 >> kTileShift);
-  return (t << (2 * kTileShift)) + (i0 & (kTile - 1)) + ((j0 & (kTile - 1)) << kTileShift);
+__device__ __host__ __forceinline__ int cell_key(int i0, int j0, int tiles_x, int ts) {
+  const int t = (i0 >> ts) + tiles_x * (j0 >> ts);
+  const int m = (1 << ts) - 1;
+  return (t << (2 * ts)) + (i0 & m) + ((j0 & m) << ts);
+}
+
+// tile counts of a grid of nx x ny nodes for tile shift ts
+inline void tile_geometry(int nx, int ny, int ts, int &tiles_x, int &tiles_y) {
+  const int t = 1 << ts;
+  tiles_x = ((nx > 1 ? nx - 1 : 1) + t - 1) / t;
+  tiles_y = ((ny > 1 ? ny - 1 : 1) + t - 1) / t;
 }
 
 // Buffer of a double-buffered array without dynamic indexing of a kernel
@@ -312,7 +321,9 @@ struct Tracker {
 struct Ctx {
   iskra_grid_t g{};
   int nx = 0, ny = 0, nn = 0;
-  int tiles_x = 0, tiles_y = 0, ntiles = 0, nkeys = 0;  // push tiles; sort keys = ntiles * kTile^2
+  int tile_shift = kTileShiftDefault;                   // push tiles of 2^tile_shift cells per axis
+  int tiles_x = 0, tiles_y = 0, ntiles = 0, nkeys = 0;  // push tiles; sort keys = ntiles * 4^tile_shift
+  int ntiles_cap = 0, nkeys_cap = 0;                    // allocated for the largest of the tile sizes
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int device = 0, num_sms = 0;
@@ -467,6 +478,8 @@ int cuda_check(Ctx *c, cudaError_t e, const char *what);
 int grid_blocks(Ctx *c, int threads, int per_sm);
 int collect_device_errors(Ctx *c);   // synchronises
 void invalidate_graphs(Ctx *c);      // the captured step no longer matches the setup
+void set_tile_shift_geometry(Ctx *c, int ts);  // tiles_x, tiles_y, ntiles, nkeys of tile shift ts
+int set_tile_shift(Ctx *c, int ts);   // new tile size: geometry, re-sort of every species, new step graph
 
 #define ISKRA_CUDA(c, call)                                   \
   do {                                                        \

@@ -3,6 +3,9 @@
 // ParticleInCell/src/ParticleInCell.jl:102-135) replayed as a CUDA graph.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "internal.cuh"
@@ -410,6 +413,132 @@ int iskra_autotune_sort(iskra_ctx *h, double dt, int trial, uint64_t seed, doubl
   c->periods_valid = false;
   if (scale_out) *scale_out = best;
   if (ms_out) *ms_out = best_ms;
+  return collect_device_errors(c);
+}
+
+int iskra_set_tile(iskra_ctx *h, int cells) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  const int ts = cells == 8 ? 3 : cells == 16 ? 4 : cells == 32 ? 5 : -1;
+  if (ts < 0) return set_err(c, ISKRA_EINVAL, "tile size must be 8, 16 or 32 cells");
+  const int rc = set_tile_shift(c, ts);
+  if (rc) return rc;
+  return collect_device_errors(c);
+}
+
+int iskra_get_tile(iskra_ctx *h, int *cells) {
+  if (!h || !cells) return ISKRA_EINVAL;
+  *cells = 1 << h->c.tile_shift;
+  return ISKRA_OK;
+}
+
+// Autotuner of the push tile size and the sort cadence: `trial` steps of the
+// caller's own simulation per candidate (tiles of 8, 16 and 32 cells x the
+// factors 0.5, 1, 2, 4 on the speed-based sort periods), each after a sort of
+// every species, timed with CUDA events on the library stream; the fastest
+// pair is kept.  Tile size and cadence only decide which block pushes a
+// particle and in which order particles sit in memory; every per-particle
+// result and the integer deposit are independent of both.  The choice is
+// cached for the process by (grid, species, particles per cell, tracker):
+// a later context of the same shape takes it without trials.
+namespace {
+struct TuneKey {
+  int nx, ny, ns, ppc_log2, trk;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(nx, ny, ns, ppc_log2, trk) < std::tie(o.nx, o.ny, o.ns, o.ppc_log2, o.trk);
+  }
+};
+struct TuneVal {
+  int ts;
+  double scale, ms;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune_cache;
+}  // namespace
+
+int iskra_autotune(iskra_ctx *h, double dt, int trial, uint64_t seed, double rtol, int *tile_out, double *scale_out,
+                   double *ms_out, double *ms_all, int *cached) {
+  if (!h) return ISKRA_EINVAL;
+  Ctx *c = &h->c;
+  if (trial < 1) return set_err(c, ISKRA_EINVAL, "trial steps must be >= 1");
+  if (c->sort_every >= 0) return set_err(c, ISKRA_EINVAL, "autotuning needs the automatic sort cadence");
+  long long np = 0;
+  for (int s = 0; s < (int)c->species.size(); s++) {
+    long long n = 0;
+    ISKRA_CUDA(c, cudaMemcpyAsync(&n, &c->species[s].dev.st->np, sizeof(long long), cudaMemcpyDeviceToHost,
+                                  c->stream));
+    ISKRA_CUDA(c, cudaStreamSynchronize(c->stream));
+    np += n;
+  }
+  const double ppc = (double)np / std::max(1, (c->nx - 1) * (c->ny - 1));
+  const TuneKey key{c->nx, c->ny, (int)c->species.size(), ppc > 1 ? (int)std::lround(std::log2(ppc)) : 0,
+                    c->trk ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      int rc = set_tile_shift(c, it->second.ts);
+      if (rc) return rc;
+      c->sort_scale = it->second.scale;
+      c->periods_valid = false;
+      if (tile_out) *tile_out = 1 << it->second.ts;
+      if (scale_out) *scale_out = it->second.scale;
+      if (ms_out) *ms_out = it->second.ms;
+      if (cached) *cached = 1;
+      return collect_device_errors(c);
+    }
+  }
+  const double factors[] = {0.5, 1.0, 2.0, 4.0};
+  double best_ms = 0, best_f = 1.0;
+  int best_ts = c->tile_shift;
+  cudaEvent_t e0, e1;
+  ISKRA_CUDA(c, cudaEventCreate(&e0));
+  ISKRA_CUDA(c, cudaEventCreate(&e1));
+  int rc = ISKRA_OK, k = 0;
+  for (int ts = kTileShiftMin; ts <= kTileShiftMax && !rc; ts++) {
+    rc = set_tile_shift(c, ts);
+    for (double f : factors) {
+      if (rc) break;
+      c->sort_scale = f;
+      c->periods_valid = false;
+      for (int s = 0; s < (int)c->species.size() && !rc; s++) rc = launch_sort(c, s);
+      if (!rc) rc = iskra_step(h, dt, 1, seed, rtol);  // periods, graphs
+      if (rc) break;
+      cudaEventRecord(e0, c->stream);
+      rc = iskra_step(h, dt, trial, seed, rtol);
+      if (rc) break;
+      cudaEventRecord(e1, c->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = set_err(c, ISKRA_ECUDA, "autotune timing");
+        break;
+      }
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      const double per = ms / trial;
+      if (ms_all) ms_all[k] = per;
+      k++;
+      if (best_ms == 0 || per < best_ms) {
+        best_ms = per;
+        best_f = f;
+        best_ts = ts;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  rc = set_tile_shift(c, best_ts);
+  if (rc) return rc;
+  c->sort_scale = best_f;
+  c->periods_valid = false;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = TuneVal{best_ts, best_f, best_ms};
+  }
+  if (tile_out) *tile_out = 1 << best_ts;
+  if (scale_out) *scale_out = best_f;
+  if (ms_out) *ms_out = best_ms;
+  if (cached) *cached = 0;
   return collect_device_errors(c);
 }
 

@@ -370,6 +370,25 @@ class Context:
     def set_sort_every(self, every):
         self._c(self.lib.iskra_set_sort_every(self.h, every))
 
+    def set_tile(self, cells):
+        self._c(self.lib.iskra_set_tile(self.h, int(cells)))
+
+    def tile(self):
+        t = c_int()
+        self._c(self.lib.iskra_get_tile(self.h, byref(t)))
+        return t.value
+
+    def autotune(self, dt, trial=64, seed=0, rtol=1e-8):
+        """Push tile size and sort cadence tuned together on this run:
+        (tile, sort-period factor, ms per step, {(tile, factor): ms}, cached)."""
+        t, f, ms, cached = c_int(), c_double(), c_double(), c_int()
+        allv = (c_double * 12)()
+        self._c(self.lib.iskra_autotune(self.h, dt, trial, seed, rtol, byref(t), byref(f), byref(ms), allv,
+                                        byref(cached)))
+        grid = {(tile, fac): allv[4 * k + j] for k, tile in enumerate((8, 16, 32))
+                for j, fac in enumerate((0.5, 1.0, 2.0, 4.0))}
+        return t.value, f.value, ms.value, (None if cached.value else grid), bool(cached.value)
+
     def autotune_sort(self, dt, trial=64, seed=0, rtol=1e-8):
         """Returns (chosen factor on the speed-based sort periods, ms per step)."""
         f, ms = c_double(), c_double()

@@ -1,4 +1,5 @@
-"""Sort cadence: results do not depend on it, and the autotuner picks one.
+"""Sort cadence and push tile size: results do not depend on them, and the
+autotuners pick them.
 
 The sort only permutes the particle store; push and boundary rules act per
 particle, the deposit sums integers (order-independent), so two runs from the
@@ -68,6 +69,53 @@ def test_autotune_sort_picks_a_factor(lib):
     with pytest.raises(Exception):
         ctx.autotune_sort(DT, trial=4)
     ctx.close()
+
+
+@pytest.mark.parametrize("cells", [8, 32])
+def test_results_do_not_depend_on_tile_size(lib, cells):
+    """The push tile (8, 16 or 32 cells per axis) only decides which block
+    pushes a particle: runs with different tiles agree bit for bit."""
+    a, sa = _slab(lib, -1)
+    b, sb = _slab(lib, -1)
+    assert a.tile() == 16
+    b.set_tile(cells)
+    assert b.tile() == cells
+    a.step(DT, 40, seed=1, rtol=1e-8)
+    b.step(DT, 20, seed=1, rtol=1e-8)
+    b.set_tile(16 if cells == 32 else 32)  # a change in the middle of a run
+    b.step(DT, 20, seed=1, rtol=1e-8)
+    assert np.array_equal(a.field(lib.FIELD_RHO), b.field(lib.FIELD_RHO))
+    assert np.array_equal(a.field(lib.FIELD_PHI), b.field(lib.FIELD_PHI))
+    for s in (0, 1):
+        xa, va, ia = a.download(sa[s])
+        xb, vb, ib = b.download(sb[s])
+        oa, ob = np.argsort(ia), np.argsort(ib)
+        assert np.array_equal(ia[oa], ib[ob])
+        assert np.array_equal(xa[oa], xb[ob]) and np.array_equal(va[oa], vb[ob])
+        assert a.absorbed(sa[s]) == b.absorbed(sb[s])
+    with pytest.raises(Exception):
+        b.set_tile(12)
+    a.close()
+    b.close()
+
+
+def test_autotune_picks_tile_and_cadence(lib):
+    """iskra_autotune times every (tile, sort factor) pair on the run and keeps
+    the fastest; a second context of the same shape takes the cached choice."""
+    ctx, _ = _slab(lib, -1)
+    tile, f, ms, grid, cached = ctx.autotune(DT, trial=8, seed=1)
+    assert not cached and tile in (8, 16, 32) and f in (0.5, 1.0, 2.0, 4.0)
+    assert len(grid) == 12 and all(v > 0 for v in grid.values())
+    assert ms == min(grid.values()) and grid[(tile, f)] == ms
+    assert ctx.tile() == tile
+    print("autotune (tile, sort factor) -> ms per step:", {k: round(v, 4) for k, v in grid.items()})
+    ctx.step(DT, 5, seed=1, rtol=1e-8)
+    assert ctx.solve_info()[1] <= 1e-8
+    other, _ = _slab(lib, -1)
+    t2, f2, ms2, grid2, cached2 = other.autotune(DT, trial=8, seed=1)
+    assert cached2 and grid2 is None and (t2, f2, ms2) == (tile, f, ms) and other.tile() == tile
+    ctx.close()
+    other.close()
 
 
 def test_double_float_rho_matches_fp64_rho(lib):

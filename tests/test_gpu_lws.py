@@ -4,9 +4,12 @@
   (oracle/lws_oracle.py, same BF16 rounding points, FP64 sums): the GPU sums
   in FP32, so values differ by about one BF16 rounding per stored tensor;
   tolerances 2 % on y and the loss, 3 % (relative L2) on the gradient;
-* training on pairs the simulation harvests lowers the loss, and a
-  warm-started CG solve needs fewer iterations than the plain one at the same
-  tolerance (the physics is unchanged: the same residual test ends both).
+* training on pairs the simulation harvests lowers the loss on pairs it did
+  not see; the warm start removes most of a solve's starting residual, and CG,
+  iterated to the same tolerance (the physics is unchanged: the same residual
+  test ends both), needs no more iterations than from the extrapolated start
+  -- on Jacobi CG it needs about as many: the smooth error modes, which a
+  local network barely reduces, set the count.
 """
 import numpy as np
 import pytest
@@ -79,7 +82,7 @@ def _steps(ctx, k):
     return np.array(its, float)
 
 
-def test_lws_training_and_warm_start_gain(lib):
+def test_lws_training_and_warm_start(lib):
     ctx = _slab_cg(lib)
     ctx.lws_create(512, seed=5)
     _steps(ctx, 300)                       # past the sheath-forming transient
@@ -107,6 +110,8 @@ def test_lws_training_and_warm_start_gain(lib):
     # warm-started solves: the network's correction (line search in the energy
     # norm) removes most of the starting residual, and CG, iterated to the
     # same tolerance, needs no more iterations than from the extrapolated ϕ
+    # (Jacobi CG on this slab; the 1024^2 multigrid-CG measurement is the
+    # bench's learned_warm_start_c5)
     use, plain = [], []
     for _ in range(2):
         ctx.lws_set_mode(use=True, smooth=0)
@@ -121,5 +126,8 @@ def test_lws_training_and_warm_start_gain(lib):
     use, plain = np.concatenate(use), np.concatenate(plain)
     print(f"CG iterations per step: {use.mean():.2f} warm-started by the network, {plain.mean():.2f} from the "
           f"extrapolated start; starting residual ratio {ratio:.3f}")
-    assert use.mean() <= 1.05 * plain.mean(), (use.mean(), plain.mean())
+    # measured 117.2-118.4 against 118.2 iterations: the network removes ~87 %
+    # of the starting residual, CG still needs as many iterations (the smooth
+    # modes set the count); no loss beyond the window-to-window noise
+    assert use.mean() <= 1.02 * plain.mean(), (use.mean(), plain.mean())
     ctx.close()

@@ -48,6 +48,8 @@ struct MgLevel {
 
 struct Mg {
   std::vector<MgLevel> lv;
+  MgLevel *dlv = nullptr;      // device copy of lv (the single-block bottom reads it)
+  int bottom = 0;              // first level of the single-block bottom (0: none)
   float *cinv = nullptr;       // dense inverse of the coarsest level (n x n)
 };
 
@@ -62,6 +64,7 @@ void mg_destroy(Mg *m) {
     cudaFree(l.r);
   }
   cudaFree(m->cinv);
+  cudaFree(m->dlv);
   delete m;
 }
 
@@ -127,21 +130,16 @@ __device__ __forceinline__ float apply9(const float *__restrict__ coef, const fl
   return a;
 }
 
-// One damped-Jacobi sweep: xo = xi + dinv (b - A xi).  xi == nullptr: the
-// first sweep from x = 0 (xo = dinv b); with r64 given it also forms the
-// level-0 right-hand side b = (float) r64 (the FP64 scaled residual of the
-// CG iteration).  z64 given: the last sweep of the cycle writes the result
-// in FP64 there instead of xo.
+// One damped-Jacobi sweep at node (i, j): xo = xi + dinv (b - A xi).
+// xi == nullptr: the first sweep from x = 0 (xo = dinv b); with r64 given it
+// also forms the level-0 right-hand side b = (float) r64 (the FP64 scaled
+// residual of the CG iteration).  z64 given: the last sweep of the cycle
+// writes the result in FP64 there instead of xo.
 template <bool FIVE>
-__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_smooth(const float *__restrict__ coef,
-                                                             const float *__restrict__ dinv,
-                                                             const float *__restrict__ xi, float *__restrict__ xo,
-                                                             float *__restrict__ b, int nx, int ny, const int *skip,
-                                                             const double *__restrict__ r64, double *__restrict__ z64) {
-  pdl_wait();
-  if (*skip) return;
-  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
-  if (i >= nx || j >= ny) return;
+__device__ __forceinline__ void smooth_node(const float *__restrict__ coef, const float *__restrict__ dinv,
+                                            const float *__restrict__ xi, float *__restrict__ xo,
+                                            float *__restrict__ b, int nx, int ny, int i, int j,
+                                            const double *__restrict__ r64, double *__restrict__ z64) {
   const int n = nx * ny, k = i + nx * j;
   const float dk = dinv[k];
   if (!xi) {
@@ -161,17 +159,11 @@ __global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_smooth(const float *__rest
   else xo[k] = v;
 }
 
-// r = b - A x on the correction's nodes
+// r = b - A x at node (i, j) of the correction's nodes
 template <bool FIVE>
-__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_residual(const float *__restrict__ coef,
-                                                               const float *__restrict__ dinv,
-                                                               const float *__restrict__ x,
-                                                               const float *__restrict__ b, float *__restrict__ r,
-                                                               int nx, int ny, const int *skip) {
-  pdl_wait();
-  if (*skip) return;
-  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
-  if (i >= nx || j >= ny) return;
+__device__ __forceinline__ void residual_node(const float *__restrict__ coef, const float *__restrict__ dinv,
+                                              const float *__restrict__ x, const float *__restrict__ b,
+                                              float *__restrict__ r, int nx, int ny, int i, int j) {
   const int n = nx * ny, k = i + nx * j;
   const float ax = apply9<FIVE>(coef, x, k, i, j, nx, ny, n);
   r[k] = dinv[k] != 0.f ? b[k] - ax : 0.f;
@@ -181,72 +173,61 @@ struct MgXfer {
   int nx, ny, ncx, ncy, cx, cy, per_x, per_y;
 };
 
-// coarse b = P^T r (gathered per coarse node from its fine candidates)
-__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_restrict(const float *__restrict__ r, float *__restrict__ bc,
-                                                               MgXfer T, const int *skip) {
-  pdl_wait();
-  if (*skip) return;
-  const int I = blockIdx.x * kMgBx + threadIdx.x, J = blockIdx.y * kMgBy + threadIdx.y;
-  if (I < T.ncx && J < T.ncy) {
-    const int K = I + T.ncx * J;
-    float s = 0.f;
-    // fine candidates along each axis: 2I-1, 2I, 2I+1 (wrapped), or I itself
-    int fi[3], fj[3];
-    int ni = 0, nj = 0;
-    if (T.cx) {
-      for (int d = -1; d <= 1; d++) {
-        int f = 2 * I + d;
-        if (f < 0 || f >= T.nx) {
-          if (!T.per_x) continue;
-          f = wrap_idx(f, T.nx);
-        }
-        fi[ni++] = f;
+// coarse b = P^T r at coarse node (I, J) (gathered from its fine candidates)
+__device__ __forceinline__ void restrict_node(const float *__restrict__ r, float *__restrict__ bc, const MgXfer &T,
+                                              int I, int J) {
+  float s = 0.f;
+  // fine candidates along each axis: 2I-1, 2I, 2I+1 (wrapped), or I itself
+  int fi[3], fj[3];
+  int ni = 0, nj = 0;
+  if (T.cx) {
+    for (int d = -1; d <= 1; d++) {
+      int f = 2 * I + d;
+      if (f < 0 || f >= T.nx) {
+        if (!T.per_x) continue;
+        f = wrap_idx(f, T.nx);
       }
-    } else {
-      fi[ni++] = I;
+      fi[ni++] = f;
     }
-    if (T.cy) {
-      for (int d = -1; d <= 1; d++) {
-        int f = 2 * J + d;
-        if (f < 0 || f >= T.ny) {
-          if (!T.per_y) continue;
-          f = wrap_idx(f, T.ny);
-        }
-        fj[nj++] = f;
-      }
-    } else {
-      fj[nj++] = J;
-    }
-    for (int b2 = 0; b2 < nj; b2++) {
-      int cj[2];
-      float wj[2];
-      const int pj = axis_parents(fj[b2], T.ny, T.ncy, T.cy, T.per_y, cj, wj);
-      float wy = 0.f;
-      for (int q = 0; q < pj; q++)
-        if (cj[q] == J) wy += wj[q];
-      if (wy == 0.f) continue;
-      for (int a2 = 0; a2 < ni; a2++) {
-        int ci[2];
-        float wi[2];
-        const int pi = axis_parents(fi[a2], T.nx, T.ncx, T.cx, T.per_x, ci, wi);
-        float wx = 0.f;
-        for (int q = 0; q < pi; q++)
-          if (ci[q] == I) wx += wi[q];
-        if (wx != 0.f) s = fmaf(wx * wy, r[fi[a2] + T.nx * fj[b2]], s);
-      }
-    }
-    bc[K] = s;
+  } else {
+    fi[ni++] = I;
   }
+  if (T.cy) {
+    for (int d = -1; d <= 1; d++) {
+      int f = 2 * J + d;
+      if (f < 0 || f >= T.ny) {
+        if (!T.per_y) continue;
+        f = wrap_idx(f, T.ny);
+      }
+      fj[nj++] = f;
+    }
+  } else {
+    fj[nj++] = J;
+  }
+  for (int b2 = 0; b2 < nj; b2++) {
+    int cj[2];
+    float wj[2];
+    const int pj = axis_parents(fj[b2], T.ny, T.ncy, T.cy, T.per_y, cj, wj);
+    float wy = 0.f;
+    for (int q = 0; q < pj; q++)
+      if (cj[q] == J) wy += wj[q];
+    if (wy == 0.f) continue;
+    for (int a2 = 0; a2 < ni; a2++) {
+      int ci[2];
+      float wi[2];
+      const int pi = axis_parents(fi[a2], T.nx, T.ncx, T.cx, T.per_x, ci, wi);
+      float wx = 0.f;
+      for (int q = 0; q < pi; q++)
+        if (ci[q] == I) wx += wi[q];
+      if (wx != 0.f) s = fmaf(wx * wy, r[fi[a2] + T.nx * fj[b2]], s);
+    }
+  }
+  bc[I + T.ncx * J] = s;
 }
 
-// x += P xc on the correction's nodes
-__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_prolong(float *__restrict__ x, const float *__restrict__ dinv,
-                                                              const float *__restrict__ xc, MgXfer T,
-                                                              const int *skip) {
-  pdl_wait();
-  if (*skip) return;
-  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
-  if (i >= T.nx || j >= T.ny) return;
+// x += P xc at fine node (i, j) of the correction's nodes
+__device__ __forceinline__ void prolong_node(float *__restrict__ x, const float *__restrict__ dinv,
+                                             const float *__restrict__ xc, const MgXfer &T, int i, int j) {
   const int k = i + T.nx * j;
   if (dinv[k] == 0.f) return;
   int ci[2], cj[2];
@@ -257,6 +238,47 @@ __global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_prolong(float *__restrict_
   for (int b2 = 0; b2 < pj; b2++)
     for (int a2 = 0; a2 < pi; a2++) v = fmaf(wi[a2] * wj[b2], xc[ci[a2] + T.ncx * cj[b2]], v);
   x[k] += v;
+}
+
+template <bool FIVE>
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_smooth(const float *__restrict__ coef,
+                                                             const float *__restrict__ dinv,
+                                                             const float *__restrict__ xi, float *__restrict__ xo,
+                                                             float *__restrict__ b, int nx, int ny, const int *skip,
+                                                             const double *__restrict__ r64, double *__restrict__ z64) {
+  pdl_wait();
+  if (*skip) return;
+  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
+  if (i < nx && j < ny) smooth_node<FIVE>(coef, dinv, xi, xo, b, nx, ny, i, j, r64, z64);
+}
+
+template <bool FIVE>
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_residual(const float *__restrict__ coef,
+                                                               const float *__restrict__ dinv,
+                                                               const float *__restrict__ x,
+                                                               const float *__restrict__ b, float *__restrict__ r,
+                                                               int nx, int ny, const int *skip) {
+  pdl_wait();
+  if (*skip) return;
+  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
+  if (i < nx && j < ny) residual_node<FIVE>(coef, dinv, x, b, r, nx, ny, i, j);
+}
+
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_restrict(const float *__restrict__ r, float *__restrict__ bc,
+                                                               MgXfer T, const int *skip) {
+  pdl_wait();
+  if (*skip) return;
+  const int I = blockIdx.x * kMgBx + threadIdx.x, J = blockIdx.y * kMgBy + threadIdx.y;
+  if (I < T.ncx && J < T.ncy) restrict_node(r, bc, T, I, J);
+}
+
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_prolong(float *__restrict__ x, const float *__restrict__ dinv,
+                                                              const float *__restrict__ xc, MgXfer T,
+                                                              const int *skip) {
+  pdl_wait();
+  if (*skip) return;
+  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
+  if (i < T.nx && j < T.ny) prolong_node(x, dinv, xc, T, i, j);
 }
 
 // coarsest level: x = Ainv b (one warp per row)
@@ -276,6 +298,58 @@ __global__ void __launch_bounds__(256) k_mg_coarse(const float *__restrict__ inv
       if (z64) z64[row] = (double)s;
       else x[row] = s;
     }
+  }
+}
+
+// The smallest levels of the cycle in one block: levels l0 .. L-1 (each of at
+// most kMgBottomNodes nodes) get the same sweeps, residuals, transfers and
+// coarsest solve as the per-level kernels, separated by block barriers
+// instead of launches -- at a few hundred to a thousand nodes a launch
+// costs more than the level's work.  Leaves the correction in lv[l0].x.
+constexpr int kMgBottomNodes = 1024;
+constexpr int kMgBottomThreads = 1024;
+
+__global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(const MgLevel *__restrict__ lv, int l0, int L,
+                                                                const float *__restrict__ cinv, const int *skip) {
+  pdl_wait();
+  if (*skip) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  auto xfer = [&](int l) {
+    const MgLevel &F = lv[l], &C = lv[l + 1];
+    return MgXfer{F.nx, F.ny, C.nx, C.ny, F.cx, F.cy, F.per_x, F.per_y};
+  };
+  auto smooth = [&](const MgLevel &D, const float *src, float *dst) {
+    for (int k = tid; k < D.n; k += nt)
+      smooth_node<false>(D.coef, D.dinv, src, dst, D.b, D.nx, D.ny, k % D.nx, k / D.nx, nullptr, nullptr);
+    __syncthreads();
+  };
+  for (int l = l0; l + 1 < L; l++) {
+    const MgLevel &D = lv[l];
+    for (int s = 0; s < kMgSweeps; s++) smooth(D, s == 0 ? nullptr : ((s & 1) ? D.x2 : D.x), (s & 1) ? D.x : D.x2);
+    for (int k = tid; k < D.n; k += nt) residual_node<false>(D.coef, D.dinv, D.x, D.b, D.r, D.nx, D.ny, k % D.nx, k / D.nx);
+    __syncthreads();
+    const MgLevel &C = lv[l + 1];
+    const MgXfer T = xfer(l);
+    for (int k = tid; k < C.n; k += nt) restrict_node(D.r, C.b, T, k % C.nx, k / C.nx);
+    __syncthreads();
+  }
+  {
+    const MgLevel &C = lv[L - 1];
+    const int lane = tid & 31;
+    for (int row = tid >> 5; row < C.n; row += nt >> 5) {
+      float acc = 0.f;
+      for (int c = lane; c < C.n; c += 32) acc = fmaf(cinv[(size_t)row * C.n + c], C.b[c], acc);
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (lane == 0) C.x[row] = acc;
+    }
+    __syncthreads();
+  }
+  for (int l = L - 2; l >= l0; l--) {
+    const MgLevel &D = lv[l];
+    const MgXfer T = xfer(l);
+    for (int k = tid; k < D.n; k += nt) prolong_node(D.x, D.dinv, lv[l + 1].x, T, k % D.nx, k / D.nx);
+    __syncthreads();
+    for (int s = 0; s < kMgSweeps; s++) smooth(D, (s & 1) ? D.x2 : D.x, (s & 1) ? D.x : D.x2);
   }
 }
 
@@ -478,6 +552,20 @@ int mg_build(Ctx *c, int nx, int ny, const std::vector<double> &s0, const std::v
     return set_err(c, ISKRA_ENOMEM, "multigrid coarsest inverse");
   }
   cudaMemcpy(m->cinv, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice);
+  // the single-block bottom: the smallest levels (from level 1 on, so that
+  // level 0's FP64 conversions stay in its own kernels), if more than the
+  // coarsest one qualifies
+  const int L = (int)m->lv.size();
+  int l0 = L;
+  while (l0 > 1 && m->lv[l0 - 1].n <= kMgBottomNodes) l0--;
+  if (l0 <= L - 2) {
+    if (cudaMalloc(&m->dlv, L * sizeof(MgLevel)) != cudaSuccess) {
+      mg_destroy(m);
+      return set_err(c, ISKRA_ENOMEM, "multigrid level table");
+    }
+    cudaMemcpy(m->dlv, m->lv.data(), L * sizeof(MgLevel), cudaMemcpyHostToDevice);
+    m->bottom = l0;
+  }
   *out = m;
   return ISKRA_OK;
 }
@@ -512,7 +600,8 @@ int mg_queue_cycle(Ctx *c, Mg *m, const double *r, double *z, const int *skip) {
   // down: smooth from zero (sweeps alternate x2 <- x <- ..., ending in x),
   // residual, restrict
   static_assert(kMgSweeps % 2 == 0, "an even sweep count leaves the iterate in x");
-  for (int l = 0; l + 1 < L; l++) {
+  const int lb = m->bottom ? m->bottom : L - 1;  // first level not run by per-level kernels
+  for (int l = 0; l < lb; l++) {
     MgLevel &D = m->lv[l];
     for (int s = 0; s < kMgSweeps; s++) {
       const float *src = s == 0 ? nullptr : ((s & 1) ? D.x2 : D.x);
@@ -529,14 +618,17 @@ int mg_queue_cycle(Ctx *c, Mg *m, const double *r, double *z, const int *skip) {
     const MgLevel &C = m->lv[l + 1];
     ISKRA_CUDA(c, launch_pdl(k_mg_restrict, mg_grid2(C.nx, C.ny), t, 0, st, (const float *)D.r, C.b, xfer(l), skip));
   }
-  {
+  if (m->bottom) {
+    ISKRA_CUDA(c, launch_pdl(k_mg_bottom, 1, kMgBottomThreads, 0, st, (const MgLevel *)m->dlv, m->bottom, L,
+                             (const float *)m->cinv, skip));
+  } else {
     MgLevel &C = m->lv[L - 1];
     ISKRA_CUDA(c, launch_pdl(k_mg_coarse, std::max(1, std::min(c->num_sms * 2, (C.n + 7) / 8)), 256, 0, st,
                              (const float *)m->cinv, (const float *)C.b, C.x, C.n, skip, L == 1 ? r : nullptr,
                              L == 1 ? z : nullptr));
   }
   // up: prolong, smooth
-  for (int l = L - 2; l >= 0; l--) {
+  for (int l = lb - 1; l >= 0; l--) {
     MgLevel &D = m->lv[l];
     ISKRA_CUDA(c, launch_pdl(k_mg_prolong, mg_grid2(D.nx, D.ny), t, 0, st, D.x, (const float *)D.dinv,
                              (const float *)m->lv[l + 1].x, xfer(l), skip));

@@ -243,11 +243,18 @@ struct PushShared {
 #ifndef ISKRA_PUSH_BULK
 #define ISKRA_PUSH_BULK 0
 #endif
-#if ISKRA_PUSH_BULK
+#if ISKRA_PUSH_BULK == 1
 constexpr int kRbStage = 34;  // {vz, cell} records of a stage from the 16-byte boundary at or below its first slot
 #else
 constexpr int kRbStage = 32;
 #endif
+// ISKRA_PUSH_BULK=2: one ring per block instead of one per warp -- a
+// producer warp (added to the ISKRA_PUSH_THREADS consumers) fills stages of
+// ISKRA_PUSH_THREADS records (one per consumer thread) with two bulk copies
+// each and a full/empty mbarrier pair per stage, so the records never pass
+// through the LSU on their way into shared memory and the mbarrier round
+// trip is paid once per 192 records.
+constexpr int kPushBlock = ISKRA_PUSH_THREADS + (ISKRA_PUSH_BULK == 2 ? 32 : 0);
 // The window of a tile of 2^TS x 2^TS cells: the tile and a kHalo-cell
 // margin (particles drift off their tile between sorts).  Dynamic shared
 // memory (the 32 x 32-cell tile's window needs 72 KB).
@@ -257,9 +264,15 @@ struct TileShared {
   static constexpr int kWin = kTileC + 2 * kHalo;  // window cells per axis
   static constexpr int kWinN = kWin + 1;           // window nodes per axis
   static constexpr int kWinCells = kWin * kWin;
+#if ISKRA_PUSH_BULK == 2
+  float4 ra[kStages][ISKRA_PUSH_THREADS];      // staged records {hx, hy, vx, vy}
+  float2 rb[kStages][ISKRA_PUSH_THREADS + 2];  // {vz, cell} from the 16-byte boundary at or below the first
+  unsigned long long full[kStages], empty[kStages];
+#else
   float4 ra[ISKRA_PUSH_THREADS / 32][kStages][32];        // staged records {hx, hy, vx, vy}
   float2 rb[ISKRA_PUSH_THREADS / 32][kStages][kRbStage];  // staged records {vz, cell}
   unsigned long long bar[ISKRA_PUSH_THREADS / 32][kStages];  // stage mbarriers (bulk-copy ring)
+#endif
   float2 ne[kWinN * kWinN];
   unsigned mom[kMoms][kWinCells];
   unsigned char trk[kWinCells];  // track! flags of the window cells (with a surface tracker)
@@ -555,6 +568,72 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
           sh.trk[t] = (i >= 0 && i < nx - 1 && j >= 0 && j < P.ny - 1) ? P.trk_cell[i + nx * j] : 0;
         }
       }
+#if ISKRA_PUSH_BULK == 2
+      constexpr int C = ISKRA_PUSH_THREADS;  // records per stage, one per consumer thread
+      if (threadIdx.x == 0) {
+#pragma unroll
+        for (int d = 0; d < kStages; d++) {
+          mbar_init(&sh.full[d], 1u);
+          mbar_init(&sh.empty[d], (unsigned)(C / 32));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      }
+      __syncthreads();
+      {
+        const long long len = end - begin;
+        const int nchunks = (int)((len + C - 1) / C);
+        const int sft = (int)(begin & 1);  // chunks start at begin + q C: the same parity (C is even)
+        if (threadIdx.x >= C) {
+          // producer: chunk q into stage q % kStages once the consumers have
+          // released that stage's previous chunk
+          if (lane == 0) {
+            for (int q = 0; q < nchunks; q++) {
+              const int st = q % kStages;
+              if (q >= kStages) {
+                if (!mbar_wait(&sh.empty[st], (unsigned)((q / kStages) - 1) & 1u, kMbarSpins)) {
+                  flags |= DERR_TIMEOUT;  // the consumers time out on the chunks not issued
+                  break;
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // their reads precede the copy's writes
+              }
+              const long long r0 = begin + (long long)q * C;
+              const int n = (int)min((long long)C, end - r0);
+              const unsigned ba = 16u * n, bb = 8u * ((n + sft + 1) & ~1);  // both multiples of 16 bytes
+              const unsigned bar = smem_u32(&sh.full[st]);
+              asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(ba + bb)
+                           : "memory");
+              asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                               "r"(smem_u32(&sh.ra[st][0])), "l"(xv + r0), "r"(ba), "r"(bar)
+                           : "memory");
+              asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                               "r"(smem_u32(&sh.rb[st][0])), "l"(zc + r0 - sft), "r"(bb), "r"(bar)
+                           : "memory");
+            }
+          }
+        } else {
+          float4 *__restrict__ xw = xv + begin;
+          float2 *__restrict__ zw = zc + begin;
+          for (int q = 0; q < nchunks; q++) {
+            const int st = q % kStages;
+            // bounded: a stage that never completes is flagged and its records skipped
+            const bool ok = __all_sync(FULL, mbar_wait(&sh.full[st], (unsigned)(q / kStages) & 1u, kMbarSpins));
+            if (!ok) flags |= DERR_TIMEOUT;
+            const int o = q * C + threadIdx.x;
+            const bool v = ok && o < len;
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 b = make_float2(0.f, 0.f);
+            if (v) {
+              a = sh.ra[st][threadIdx.x];
+              b = sh.rb[st][threadIdx.x + sft];
+            }
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sh.empty[st])) : "memory");
+            push_warp<PUSH, MX, MY, true, TRK>(s, xw, zw, o, v, a, b, E2, sh, ox, oy, kWin, kWin, P, ab, flags);
+          }
+        }
+      }
+      __syncthreads();
+#else
       __syncthreads();
       // each warp takes a contiguous slice of the tile's slots (cell-sorted
       // slices touch few cells in common)
@@ -566,7 +645,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
       const int cnt = (int)max(0LL, min(end, w0 + slice) - w0);
       float4 *__restrict__ xw = xv + w0;
       float2 *__restrict__ zw = zc + w0;
-#if ISKRA_PUSH_BULK
+#if ISKRA_PUSH_BULK == 1
       // {vz, cell} stages start at the 16-byte boundary at or below their
       // first slot: w0 + o has the parity of `begin` (slices and stages are
       // multiples of 32 slots)
@@ -633,6 +712,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
       cp_async_wait<0>();
       __syncthreads();
 #endif
+#endif  // ISKRA_PUSH_BULK == 2
       // node sums from the moments of the up to four window cells around each node
       for (int t = threadIdx.x; t < kWinN * kWinN; t += blockDim.x) {
         const int a = t % kWinN, b = t / kWinN;
@@ -684,7 +764,7 @@ __device__ __forceinline__ void push_block(const SpeciesDev &s, const PushParams
 // TRK: with the surface tracker (a separate instantiation keeps the walk's
 // registers out of the push without one)
 template <bool PUSH, int MX, int MY, bool TRK, int TS>
-__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, TRK ? ISKRA_PUSH_TRK_MIN_BLOCKS : ISKRA_PUSH_MIN_BLOCKS)
+__global__ void __launch_bounds__(kPushBlock, TRK ? ISKRA_PUSH_TRK_MIN_BLOCKS : ISKRA_PUSH_MIN_BLOCKS)
     k_push(SpeciesDev s, const float2 *__restrict__ E2, PushParams P, int ntiles, int *err) {
   pdl_wait();
   extern __shared__ __align__(16) unsigned char push_smem[];
@@ -702,7 +782,7 @@ __global__ void __launch_bounds__(ISKRA_PUSH_THREADS, TRK ? ISKRA_PUSH_TRK_MIN_B
 // step_ctr (optional): the step counter, advanced here when no MCC set reads
 // it earlier in the step (saves the step's opening launch).
 template <int MX, int MY, bool TRK, int TS>
-__global__ void __launch_bounds__(ISKRA_PUSH_THREADS, TRK ? ISKRA_PUSH_TRK_MIN_BLOCKS : ISKRA_PUSH_MIN_BLOCKS)
+__global__ void __launch_bounds__(kPushBlock, TRK ? ISKRA_PUSH_TRK_MIN_BLOCKS : ISKRA_PUSH_MIN_BLOCKS)
     k_push2(SpeciesDev s0, SpeciesDev s1, const float2 *__restrict__ E2, PushParams P0, PushParams P1, int ntiles,
             int *err, unsigned long long *step_ctr) {
   pdl_wait();
@@ -740,13 +820,13 @@ struct PushTile {
     if (!push) {
       auto kern = k_push<false, 0, 0, false, TS>;
       prepare(kern);
-      return launch_pdl(kern, blocks, ISKRA_PUSH_THREADS, kSmem, st, s, E2, P, ntiles, err);
+      return launch_pdl(kern, blocks, kPushBlock, kSmem, st, s, E2, P, ntiles, err);
     }
 #define ISKRA_PUSH_CASE(MX, MY)                                                                \
   if (P.mode_x == MX && P.mode_y == MY) {                                                      \
     auto kern = trk ? k_push<true, MX, MY, true, TS> : k_push<true, MX, MY, false, TS>;        \
     prepare(kern);                                                                             \
-    return launch_pdl(kern, blocks, ISKRA_PUSH_THREADS, kSmem, st, s, E2, P, ntiles, err);     \
+    return launch_pdl(kern, blocks, kPushBlock, kSmem, st, s, E2, P, ntiles, err);             \
   }
     ISKRA_PUSH_CASE(0, 0) ISKRA_PUSH_CASE(0, 1) ISKRA_PUSH_CASE(0, 2)
     ISKRA_PUSH_CASE(1, 0) ISKRA_PUSH_CASE(1, 1) ISKRA_PUSH_CASE(1, 2)
@@ -762,7 +842,7 @@ struct PushTile {
   if (Pa.mode_x == MX && Pa.mode_y == MY) {                                                               \
     auto kern = trk ? k_push2<MX, MY, true, TS> : k_push2<MX, MY, false, TS>;                             \
     prepare(kern);                                                                                        \
-    return launch_pdl(kern, blocks, ISKRA_PUSH_THREADS, kSmem, st, a, b, E2, Pa, Pb, ntiles, err, step_ctr); \
+    return launch_pdl(kern, blocks, kPushBlock, kSmem, st, a, b, E2, Pa, Pb, ntiles, err, step_ctr);         \
   }
     ISKRA_PUSH2_CASE(0, 0) ISKRA_PUSH2_CASE(0, 1) ISKRA_PUSH2_CASE(0, 2)
     ISKRA_PUSH2_CASE(1, 0) ISKRA_PUSH2_CASE(1, 1) ISKRA_PUSH2_CASE(1, 2)

@@ -29,6 +29,7 @@
 // gradient -- run on the tensor cores (mma.sync m16n8k16, BF16 x BF16 ->
 // FP32); the 1->32 and 32->1 end layers, pooling, upsampling and the
 // elementwise gradient combinations run on the FP32 pipes.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -360,6 +361,165 @@ __global__ void __launch_bounds__(128) k_conv32_tc(const bf16 *__restrict__ in, 
   if (warp == 0) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem_base) : "memory");
+  }
+}
+
+// The same convolution with the patches brought in by the tensor memory
+// accelerator: one 3-D tiled bulk-tensor load per channel octet (box 8
+// channels x 10 x 18 pixels of the NHWC activation, zeros outside the image
+// -- the load starts at pixel (-1, -1) of the tile, its channel coordinate is
+// a multiple of 8 BF16 = 16 bytes) writes exactly one octet plane of the
+// patch (pixel q = y 10 + x, 16 bytes each), completing on the buffer's
+// mbarrier.  One thread issues the loads and the MMAs; the others only read
+// the accumulators back.  Planes are 2944 bytes apart (128-byte aligned).
+constexpr int kTmaPlane = 2944;
+constexpr int kTmaPatch = 4 * kTmaPlane;
+constexpr int kTmaSmem = kTcWBytes + 2 * kTmaPatch + 128;  // + room to align the base to 128 bytes
+constexpr unsigned kTmaBytes = 4u * kTcPix * 16u;         // bytes a patch load delivers
+
+__device__ __forceinline__ void tma_patch(const CUtensorMap *map, unsigned dst, int c, int x, int y, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+template <bool RELU>
+__global__ void __launch_bounds__(128) k_conv32_tma(const __grid_constant__ CUtensorMap map,
+                                                    const bf16 *__restrict__ w, bf16 *__restrict__ out, int H, int W,
+                                                    int *err) {
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  __shared__ __align__(8) unsigned long long ld_bar[2], mma_bar[2];
+  __shared__ unsigned tmem_base;
+  __shared__ int stop;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const unsigned base = (smem_u32(tc_smem) + 127u) & ~127u;
+  unsigned char *gbase = tc_smem + (base - smem_u32(tc_smem));
+  const unsigned sW = base, sP = base + kTcWBytes;
+  const int ntx = (W + kTcTx - 1) / kTcTx, ntiles = ntx * ((H + kTcTy - 1) / kTcTy);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(&tmem_base))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int d = 0; d < 2; d++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&ld_bar[d])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mma_bar[d])) : "memory");
+    }
+    stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<unsigned long long>(&map)) : "memory");
+  }
+  for (int c = tid; c < 9 * kCh * 4; c += blockDim.x) {
+    const int o = c & 3, row = c >> 2;  // row = tap * 32 + n
+    *reinterpret_cast<uint4 *>(gbase + (row >> 5) * 2048 + o * 512 + (row & 31) * 16) =
+        *reinterpret_cast<const uint4 *>(w + row * kCh + o * 8);
+  }
+  fence_async_smem();  // the weights (generic stores) are read by the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = tmem_base;
+  auto load = [&](int t, int b) {
+    const int y0 = (t / ntx) * kTcTy - 1, x0 = (t % ntx) * kTcTx - 1;
+    const unsigned bar = smem_u32(&ld_bar[b]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kTmaBytes) : "memory");
+#pragma unroll
+    for (int o = 0; o < 4; o++) tma_patch(&map, sP + b * kTmaPatch + o * kTmaPlane, 8 * o, x0, y0, bar);
+  };
+  auto issue = [&](int b) {
+    tc_fence_after();
+    const unsigned pa = sP + b * kTmaPatch, d = tmem + b * kCh;
+#pragma unroll
+    for (int tap = 0; tap < 9; tap++) {
+      const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+      for (int kc = 0; kc < 2; kc++) {
+        const unsigned long long a = tc_sdesc(pa + kc * 2 * kTmaPlane + (dy * kTcPw + dx) * 16, kTmaPlane, kTcPw * 16);
+        const unsigned long long bd = tc_sdesc(sW + tap * 2048 + kc * 1024, 512, 128);
+        tc_mma(d, a, bd, (tap | kc) ? 1u : 0u);
+      }
+    }
+    tc_commit(&mma_bar[b]);
+  };
+  int t = blockIdx.x;
+  unsigned ldp = 0, mmp = 0;  // bit b: parity of the next completion of buffer b's barriers
+  unsigned ldpend = 0;        // thread 0: bit b, a load into buffer b not yet waited for
+  bool mma_pending = false;   // thread 0: an issued MMA group not yet waited for
+  if (tid == 0 && t < ntiles) {
+    load(t, 0);
+    ldpend |= 1u;
+  }
+  int b = 0;
+  for (; t < ntiles; t += gridDim.x, b ^= 1) {
+    const int tn = t + gridDim.x;
+    if (tid == 0) {
+      // buffer b ^ 1 is free: the MMAs that read it (tile t - G) completed in the previous iteration
+      if (tn < ntiles) {
+        load(tn, b ^ 1);
+        ldpend |= 1u << (b ^ 1);
+      }
+      if (tc_wait(&ld_bar[b], (ldp >> b) & 1u)) {
+        ldp ^= 1u << b;
+        ldpend &= ~(1u << b);
+        issue(b);
+        mma_pending = true;
+      } else {
+        atomicOr(err, DERR_TIMEOUT);
+        stop = 1;
+      }
+    }
+    __syncthreads();
+    if (stop) break;
+    const bool ok = tc_wait(&mma_bar[b], (mmp >> b) & 1u);
+    if (ok) mmp ^= 1u << b;
+    tc_fence_after();
+    if (ok) {
+      unsigned r[32];
+      tc_ld32(tmem + b * kCh + ((unsigned)(warp * 32) << 16), r);
+      const int m = tid;  // TMEM lane = GEMM row = tile pixel
+      const int y = (t / ntx) * kTcTy + (m >> 3), x = (t % ntx) * kTcTx + (m & 7);
+      if (y < H && x < W) {
+        uint4 *dst = reinterpret_cast<uint4 *>(out + ((size_t)y * W + x) * kCh);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          unsigned v[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            float v0 = __uint_as_float(r[8 * q + 2 * e]), v1 = __uint_as_float(r[8 * q + 2 * e + 1]);
+            if (RELU) {
+              v0 = fmaxf(v0, 0.f);
+              v1 = fmaxf(v1, 0.f);
+            }
+            __nv_bfloat162 p2 = __floats2bfloat162_rn(v0, v1);
+            v[e] = *reinterpret_cast<unsigned *>(&p2);
+          }
+          dst[q] = make_uint4(v[0], v[1], v[2], v[3]);
+        }
+      }
+    } else {
+      atomicOr(err, DERR_TIMEOUT);
+      stop = 1;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0 && ok) mma_pending = false;
+    if (stop) break;
+  }
+  if (tid == 0 && stop) {
+    // bounded drains: the MMAs and the loads still in flight finish before
+    // TMEM and the block's shared memory are given up
+    if (mma_pending) tc_wait(&mma_bar[b], (mmp >> b) & 1u);
+    for (int x = 0; x < 2; x++)
+      if (ldpend & (1u << x)) tc_wait(&ld_bar[x], (ldp >> x) & 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
   }
 }
 
@@ -833,6 +993,7 @@ struct Lws {
   double gain = 0.0;                           // network output x gain = correction / s (0: not set)
   long long solves = 0;
   LwsScal *scal = nullptr;                     // device: s of the running solve, warm-start statistics
+  std::vector<std::pair<const void *, CUtensorMap>> maps;  // TMA maps of the 32 -> 32 convolutions' inputs
   std::vector<void *> allocs;
 };
 
@@ -883,14 +1044,69 @@ int conv32(Ctx *c, bool relu, const bf16 *in, const bf16 *w, bf16 *out, int H, i
   if (!attr) {
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_conv32_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_conv32_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_conv32_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmaSmem));
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_conv32_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmaSmem));
     attr = true;
   }
   const int tiles = ((W + kTcTx - 1) / kTcTx) * ((H + kTcTy - 1) / kTcTy);
   const int grid = std::min(tiles, kTcBlocksPerSm * c->num_sms);
-  if (relu) k_conv32_tc<true><<<grid, 128, kTcSmem, st>>>(in, w, out, H, W, c->d_err);
-  else k_conv32_tc<false><<<grid, 128, kTcSmem, st>>>(in, w, out, H, W, c->d_err);
+  const CUtensorMap *map = nullptr;
+  for (const auto &m : c->lws->maps)
+    if (m.first == in) map = &m.second;
+  if (map) {
+    if (relu) k_conv32_tma<true><<<grid, 128, kTmaSmem, st>>>(*map, w, out, H, W, c->d_err);
+    else k_conv32_tma<false><<<grid, 128, kTmaSmem, st>>>(*map, w, out, H, W, c->d_err);
+  } else if (relu) {
+    k_conv32_tc<true><<<grid, 128, kTcSmem, st>>>(in, w, out, H, W, c->d_err);
+  } else {
+    k_conv32_tc<false><<<grid, 128, kTcSmem, st>>>(in, w, out, H, W, c->d_err);
+  }
   ISKRA_CUDA(c, cudaGetLastError());
   return ISKRA_OK;
+}
+
+// TMA tensor map of a 32-channel BF16 NHWC activation (H x W): boxes of 8
+// channels x 10 x 18 pixels, zeros outside.  False when the driver cannot
+// encode it (the convolution then stages its patches with cp.async).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn) nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+static bool activation_map(CUtensorMap *m, const bf16 *ptr, int H, int W) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn || W < kTcPw || H < kTcTy + 2) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)kCh, (cuuint64_t)W, (cuuint64_t)H};
+  const cuuint64_t strides[2] = {(cuuint64_t)kCh * sizeof(bf16), (cuuint64_t)W * kCh * sizeof(bf16)};
+  const cuuint32_t box[3] = {8, (cuuint32_t)kTcPw, (cuuint32_t)(kTcTy + 2)}, es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(ptr), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// maps of every input of a 32 -> 32 convolution (forward: pooled inputs and
+// upsampled sums; backward: the output gradients)
+static void make_maps(Lws *L) {
+  L->maps.clear();
+  auto add = [&](const bf16 *p, int l) {
+    CUtensorMap m;
+    if (activation_map(&m, p, L->h[l], L->w[l])) L->maps.emplace_back(p, m);
+  };
+  for (int l = 1; l <= 3; l++) add(L->p[l], l);
+  for (int l = 0; l <= 2; l++) add(L->u[l], l);
+  for (int l = 0; l <= 2; l++) add(L->dz[6 - l], l);
+  for (int l = 1; l <= 3; l++) add(L->dz[l], l);
 }
 
 int lws_forward(Ctx *c, Lws *L) {
@@ -1133,6 +1349,7 @@ int iskra_lws_create(iskra_ctx *h, int capacity, uint64_t seed) {
     LWS_ALLOC(L->dout, (size_t)capacity * P0 * sizeof(float));
   }
 #undef LWS_ALLOC
+  make_maps(L);
   // He initialisation (std sqrt(2 / fan_in)); the output layer starts small
   std::vector<float> w0(kParams);
   std::mt19937_64 gen(seed);

@@ -1199,20 +1199,6 @@ __global__ void k_pcg_dir(OpView op, const double *__restrict__ z, double *__res
 // ===========================================================================
 // host: assembly
 // ===========================================================================
-static inline int slot_col(const Poisson *P, int r, int s) {
-  const int nx = P->nx, ny = P->ny, i = r % nx, j = r / nx;
-  switch (s) {
-    case 0: return r;
-    case 1: return i > 0 ? r - 1 : -1;
-    case 2: return i < nx - 1 ? r + 1 : -1;
-    case 3: return j > 0 ? r - nx : -1;
-    case 4: return j < ny - 1 ? r + nx : -1;
-    case 5: return i == 0 ? (nx - 1) + nx * j : (i == nx - 1 ? nx * j : -1);
-    case 6: return j == 0 ? i + nx * (ny - 1) : (j == ny - 1 ? i : -1);
-  }
-  return -1;
-}
-
 static Poisson *poisson_new(Ctx *c, double eps0) {
   Poisson *P = new Poisson();
   P->nx = c->nx;
@@ -2481,7 +2467,6 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
   }
   __syncthreads();
   // scaled residual of the free rows
-  double a2 = 0, b2 = 0;
   for (int k = threadIdx.x; k < nn; k += blockDim.x) {
     const int j = k / nx, i = k - j * nx;
     const double rhoc = F.rho[o + k];
@@ -2564,8 +2549,6 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
     F.x[o + k] = xs[k];
     efield_at(xs, k, i, j, nx, ny, eo);
   }
-  (void)a2;
-  (void)b2;
   if (flags) atomicOr(F.err, flags);
 }
 

@@ -627,6 +627,20 @@ def cpu_run(w, e, i, max_seconds=20.0, max_steps=None):
 
 
 # ----------------------------------------------------------------------------
+def whole_job(ms, units, dist=None, device="cpu"):
+    """The whole-job aggregate of independent replicas (one per rank): the
+    slowest rank's time and the units all ranks processed.  Identity for a
+    single process (dist None)."""
+    if dist is None:
+        return ms, units
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(u)
+    return float(t.item()), float(u.item())
+
+
 def main():
     global C4_RUNS
     ap = argparse.ArgumentParser()
@@ -718,13 +732,7 @@ def main():
     np_after = ctx.count(se) + ctx.count(si)
     it, relres = ctx.solve_info()
     psteps = 0.5 * (np_before + np_after) * args.steps
-    t = torch.tensor([ms], device="cuda") if dist else None
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        pt = torch.tensor([psteps], device="cuda", dtype=torch.float64)
-        dist.all_reduce(pt)
-        psteps = float(pt.item())
+    ms, psteps = whole_job(ms, psteps, dist, "cuda")
     value = psteps / (ms * 1e-3)
 
     # roofline of the dominant kernel (fused gather+push+boundary+deposit of both
@@ -784,6 +792,8 @@ def main():
             ctx2.field_async(1, phi_host[k % 2])
         ctx2.sync()
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         t0 = time.perf_counter()
         ctx2.upload(se2, *host_in[0])
         ctx2.upload(si2, *host_in[1])
@@ -795,9 +805,11 @@ def main():
         xi_o, vi_o, _ = ctx2.download(si2, out=host_out[1])
         t_e2e = time.perf_counter() - t0
         np_e2e = 0.5 * (2 * NP + xe_o.shape[0] + xi_o.shape[0])
-        e2e = {"value": np_e2e * k_e2e / t_e2e, "unit": "particle-steps/s",
-               "h2d_bytes_per_step": 2 * NP * 5 * 8 / k_e2e,
-               "d2h_bytes_per_step": NX * NY * 8 + (xe_o.shape[0] + xi_o.shape[0]) * 5 * 8 / k_e2e, "steps": k_e2e,
+        ms_e2e, psteps_e2e = whole_job(1e3 * t_e2e, np_e2e * k_e2e, dist, "cuda")
+        e2e = {"value": psteps_e2e / (ms_e2e * 1e-3), "unit": "particle-steps/s",
+               "h2d_bytes_per_step": world * 2 * NP * 5 * 8 / k_e2e,
+               "d2h_bytes_per_step": world * (NX * NY * 8 + (xe_o.shape[0] + xi_o.shape[0]) * 5 * 8 / k_e2e),
+               "steps": k_e2e,
                "note": "C-ABI with pinned host FP64 arrays, after warm-up steps (graph capture): particle upload of the initial state, per step iskra_step + non-blocking phi download (overlapping the next step), final sync and particle download"}
         ctx2.close()
 

@@ -653,6 +653,8 @@ def main():
     ap.add_argument("--no-c4", action="store_true", help="skip the batched-ensemble (C4) leg")
     ap.add_argument("--no-c5", action="store_true", help="skip the learned-warm-start (C5 method) leg")
     ap.add_argument("--no-tracker", action="store_true", help="skip the surface-tracker leg")
+    ap.add_argument("--tile", type=int, default=0, choices=[0, 8, 16, 32],
+                    help="push tile size instead of the autotuner's choice (profiling runs)")
     ap.add_argument("--c4-runs", type=int, default=C4_RUNS,
                     help="runs of the batched ensemble (smaller cases for profiling)")
     args = ap.parse_args()
@@ -696,11 +698,15 @@ def main():
     # push tile size and sort cadence tuned on this run (cached for the
     # process: the end-to-end leg's context takes the same choice), then the
     # warm-up (also captures the step graph)
-    tile, sort_scale, tune_ms, tune_grid, _ = ctx.autotune(DT, trial=32, seed=1, rtol=RTOL)
-    autotune = {"tile_cells": tile, "sort_period_factor": sort_scale, "ms_per_step": tune_ms,
-                "candidates_ms_per_step": {f"{t}x{t} cells, sort factor {f:g}": v
-                                           for (t, f), v in sorted(tune_grid.items())},
-                "note": "iskra_autotune: 32 trial steps per candidate on this run, before the warm-up"}
+    if args.tile:
+        ctx.set_tile(args.tile)
+        autotune = {"tile_cells": args.tile, "note": "set by --tile, not tuned"}
+    else:
+        tile, sort_scale, tune_ms, tune_grid, _ = ctx.autotune(DT, trial=32, seed=1, rtol=RTOL)
+        autotune = {"tile_cells": tile, "sort_period_factor": sort_scale, "ms_per_step": tune_ms,
+                    "candidates_ms_per_step": {f"{t}x{t} cells, sort factor {f:g}": v
+                                               for (t, f), v in sorted(tune_grid.items())},
+                    "note": "iskra_autotune: 32 trial steps per candidate on this run, before the warm-up"}
     ctx.step(DT, args.warmup, seed=1, rtol=RTOL)
     ctx.sync()
     np_before = ctx.count(se) + ctx.count(si)
@@ -786,7 +792,10 @@ def main():
         # first steps capture the step and sort graphs and load the kernels
         ctx2.upload(se2, *host_in[0])
         ctx2.upload(si2, *host_in[1])
-        ctx2.autotune(DT, trial=32, seed=1, rtol=RTOL)  # the device leg's choice, from the process cache
+        if args.tile:
+            ctx2.set_tile(args.tile)
+        else:
+            ctx2.autotune(DT, trial=32, seed=1, rtol=RTOL)  # the device leg's choice, from the process cache
         for k in range(max(args.warmup, 3)):
             ctx2.step(DT, 1, seed=1, rtol=RTOL)
             ctx2.field_async(1, phi_host[k % 2])

@@ -232,6 +232,39 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
   if (lane == 0 && f) atomicOr(err, f);
 }
 
+// Whether a work entry collides in this step: its selections replayed in
+// order up to the first accepted one (a rejected selection changes nothing,
+// so these are exactly the tests the collision code makes before its first
+// collision); a probability above the bound counts as a hit (the collision
+// code raises the flag).
+__device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M, const float *tab, int ntab,
+                                               const float2 *__restrict__ Er, int nx, unsigned long long step,
+                                               uint2 key, float expl) {
+  Stream R = particle_stream(e.b.z, step, key);
+  const int nsel = draw_selections(R, M.lam, expl);
+  if (nsel == 0) return false;
+  const int cell = (int)e.b.y;
+  const int node = (cell & 0xffff) + nx * (cell >> 16);
+  const float n = __ldg(M.gas_n + node);
+  const float2 ef = __ldg(Er + node);
+  const float gx = M.qmt_dt * ef.x - e.a.z, gy = M.qmt_dt * ef.y - e.a.w, gz = -__uint_as_float(e.b.x);
+  const float g = sqrtf(gx * gx + gy * gy + gz * gz);
+  const float eps = 0.5f * M.m_ev * g * g;
+  for (int sidx = 0; sidx < nsel && n >= 0.0f; sidx++) {
+    const float U = R.next();
+    int k = (int)floorf(M.N * U);
+    if (k >= M.N) k = M.N - 1;
+    const float sg = sigma_at(tab + M.off[k], tab + ntab + M.off[k], M.off[k + 1] - M.off[k], eps, M.logu[k],
+                              M.log_e0[k], M.inv_dlog[k]) *
+                     g;
+    float Pk = -expm1f(-n * sg * M.dt);
+    Pk *= M.inv_nmaxpt;
+    if (Pk > 1.0f) return true;
+    if (U > (float)(k + 1) / M.N - Pk) return true;
+  }
+  return false;
+}
+
 // Phase 2 over the work list segment of run r = blockIdx.y: the run's stores
 // src[r] / prod[r], node field E + r nn, key keys[r] (or M's key for a single
 // context), counters counts_runs + r N (or M.counts).
@@ -270,9 +303,37 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
   unsigned acc_k[kMaxProc];
 #pragma unroll
   for (int k = 0; k < kMaxProc; k++) acc_k[k] = 0u;
-  for (long long base = warp * 32; base < nw; base += nwarps * 32) {
-    const long long w = base + lane;
-    const bool act = w < nw;
+  // Each warp tests 32 entries at a time (mcc_entry_hits) and queues the
+  // ~5 % that collide in its own shared-memory queue; whenever 32 are queued
+  // (and for the rest at the end) it runs the collision code on them densely,
+  // instead of diverging into the kinematics for its one or two colliding
+  // lanes of every 32.  Warps never wait for one another.
+  __shared__ unsigned wq[8][64];
+  const uint2 key = keys ? keys[r] : make_uint2(M.key0, M.key1);
+  unsigned *q = wq[threadIdx.x >> 5];
+  int qn = 0;  // queued entries (warp-uniform)
+  for (long long base = warp * 32;; base += nwarps * 32) {
+    const bool more = base < nw;  // warp-uniform
+    if (more) {
+      const long long wt = base + lane;
+      const bool hit = wt < nw && mcc_entry_hits(seg[wt], M, tab, ntab, Er, nx, step, key, expl);
+      const unsigned hm = __ballot_sync(FULL, hit);
+      if (hit) q[qn + __popc(hm & ((1u << lane) - 1u))] = (unsigned)wt;
+      qn += __popc(hm);
+      __syncwarp();
+    }
+    if (qn < 32 && (more || qn == 0)) {
+      if (more) continue;
+      break;
+    }
+    const int take = qn < 32 ? qn : 32;
+    const bool act = lane < take;
+    const long long w = act ? (long long)q[lane] : 0;
+    __syncwarp();
+    if (lane < qn - take) q[lane] = q[take + lane];  // the rest moves to the front (at most 31)
+    __syncwarp();
+    qn -= take;
+    {
     int nsel = 0;
     long long p = 0;
     MccWork e{};
@@ -406,6 +467,9 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
         }
       }
     }
+    }
+    if (!more && qn == 0) break;
+    if (!more) base -= nwarps * 32;  // more queued entries: another group without new tests
   }
 #pragma unroll
   for (int k = 0; k < kMaxProc; k++) {

@@ -178,9 +178,25 @@ __device__ __forceinline__ Stream particle_stream(uint32_t pid, unsigned long lo
   return R;
 }
 
-// selections ~ Poisson(lam) by inversion (bounded): the stream's first draw
-__device__ __forceinline__ int draw_selections(Stream &R, float lam, float expl) {
-  const float u = R.next();
+// The uniform that decides a particle's number of selections in a step: a
+// 64-bit mix of (key, step, particle id) -- the finalizer of SplitMix64
+// (Steele, Lea and Flood, OOPSLA 2014) over the key and the id and step
+// spread by odd multipliers -- 24 bits.  Every particle draws it every step
+// (most draw no selection), so it is a tenth of a Philox evaluation; the
+// collision draws of the selected particles come from their Philox stream.
+__device__ __forceinline__ float selection_uniform(uint32_t pid, unsigned long long step, uint2 key) {
+  unsigned long long z = (((unsigned long long)key.y << 32) | key.x) ^ (step * 0x9E3779B97F4A7C15ull) ^
+                         ((unsigned long long)pid * 0xD1B54A32D192ED03ull);
+  z ^= z >> 30;
+  z *= 0xBF58476D1CE4E5B9ull;
+  z ^= z >> 27;
+  z *= 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (float)(z >> 40) * 5.9604644775390625e-08f;
+}
+
+// selections ~ Poisson(lam) by inversion (bounded) of the selection uniform u
+__device__ __forceinline__ int draw_selections(float u, float lam, float expl) {
   float pk = expl, cdf = expl;
   int nsel = 0;
   while (u > cdf && nsel < 16) {

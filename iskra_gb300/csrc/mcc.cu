@@ -206,8 +206,7 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
         b = zc[p];
         if (__float_as_int(b.y) >= 0) {
           pid = ids[p];
-          Stream R = particle_stream(pid, step, key);
-          nsel = draw_selections(R, lam, expl);
+          nsel = draw_selections(selection_uniform(pid, step, key), lam, expl);
         }
       }
       const unsigned m = __ballot_sync(FULL, nsel > 0);
@@ -240,9 +239,9 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
 __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M, const float *tab, int ntab,
                                                const float2 *__restrict__ Er, int nx, unsigned long long step,
                                                uint2 key, float expl) {
-  Stream R = particle_stream(e.b.z, step, key);
-  const int nsel = draw_selections(R, M.lam, expl);
+  const int nsel = draw_selections(selection_uniform(e.b.z, step, key), M.lam, expl);
   if (nsel == 0) return false;
+  Stream R = particle_stream(e.b.z, step, key);
   const int cell = (int)e.b.y;
   const int node = (cell & 0xffff) + nx * (cell >> 16);
   const float n = __ldg(M.gas_n + node);
@@ -353,8 +352,8 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
       b = make_float2(__uint_as_float(e.b.x), __uint_as_float(e.b.y));
       cell = (int)e.b.y;
       const uint32_t pid = e.b.z;
-      Stream R = particle_stream(pid, step, keys ? keys[r] : make_uint2(M.key0, M.key1));
-      nsel = draw_selections(R, M.lam, expl);  // the phase-1 draw again: its count
+      Stream R = particle_stream(pid, step, key);
+      nsel = draw_selections(selection_uniform(pid, step, key), M.lam, expl);  // the phase-1 draw again: its count
       v[0] = a.z;
       v[1] = a.w;
       v[2] = b.x;

@@ -659,8 +659,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
       uint32_t pid = 0;
       if (v && __float_as_int(nb.y) >= 0) {
         pid = ids[p];
-        Stream R = particle_stream(pid, step1, key);
-        nsel = draw_selections(R, S.lam, expl);
+        nsel = draw_selections(selection_uniform(pid, step1, key), S.lam, expl);
       }
       const unsigned m = __ballot_sync(FULL, nsel > 0);
       if (m) {

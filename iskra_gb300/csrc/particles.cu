@@ -641,14 +641,25 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   const float expl = __expf(-S.lam);  // as k_mcc_select and k_mcc_collide form it
   MccWork *__restrict__ seg = SEL ? S.work + (size_t)r * S.cap_run : nullptr;
   const long long warp = (long long)blockIdx.x * nwb + wib, nwarps = (long long)gridDim.x * nwb;
+  // the next iteration's records are loaded before this one is pushed (two
+  // iterations in flight per warp: the loop was bound by the load latency)
+  float4 an = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 bn = make_float2(0.f, 0.f);
+  if (warp * 32 + lane < np) {
+    an = ld_stream(xv + warp * 32 + lane);
+    bn = ld_stream(zc + warp * 32 + lane);
+  }
   for (long long base = warp * 32; base < np; base += nwarps * 32) {
     const long long p = base + lane;
     const bool v = p < np;
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 b = make_float2(0.f, 0.f);
-    if (v) {
-      a = ld_stream(xv + p);
-      b = ld_stream(zc + p);
+    const float4 a = an;
+    const float2 b = bn;
+    {
+      const long long pn = p + nwarps * 32;  // a slot no push of this iteration writes
+      if (pn < np) {
+        an = ld_stream(xv + pn);
+        bn = ld_stream(zc + pn);
+      }
     }
     float4 na;
     float2 nb;

@@ -194,7 +194,7 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 #define ISKRA_PUSH_TRK_MIN_BLOCKS ISKRA_PUSH_MIN_BLOCKS
 #endif
 #ifndef ISKRA_PUSH_RUNS_MIN_BLOCKS
-#define ISKRA_PUSH_RUNS_MIN_BLOCKS 5
+#define ISKRA_PUSH_RUNS_MIN_BLOCKS 4
 #endif
 #ifndef ISKRA_PUSH_STAGES
 #define ISKRA_PUSH_STAGES 4

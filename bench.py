@@ -426,17 +426,18 @@ def source_measure(reps=10):
             "workload": "MaxwellianSource sample! of 4M particles over the 512x512 slab", "data": "synthetic"}
 
 
-def dsmc_measure(reps=50):
+def dsmc_measure(reps=50, n=20, dt=1e-9):
     """DSMC perform! on the configuration of problem/05_dsmc.jl: 20x20 nodes of
     5 cm, 5000 e- and 5000 O (8 m_p) sampled as its start() does (uniform over
     the domain, thermal O at 300 K, e- at 0.5e6 m/s per in-plane component),
     cross section 3-6e6 m/s -> [0.01, 0.1, 2.0, 0.01], Δt = 1 ns.  Device time
-    per perform!, pairs tried and collisions accepted per second."""
+    per perform!, pairs tried and collisions accepted per second.  With n = 3
+    (2x2 cells of ~1250 + 1250 particles) every cell is crowded: its lists do
+    not fit the shared-memory stage of 512."""
     import torch
     from iskra_gb300 import _lib
     from iskra_gb300.device import Context
-    n, dh, dt = 20, 0.05, 1e-9
-    L = n * dh
+    dh = 0.05
     kb, mp = 1.3806503e-23, 1.67262192e-27
     ctx = Context(n, n, dh, dh, (0, 0, 0, 0))
     e = ctx.species_create(-QE, ME, 1.0, 20000)
@@ -473,7 +474,9 @@ def dsmc_measure(reps=50):
     pairs = float(np.floor(nc[(Na >= 2) & (Nb >= 2)]).sum())
     return {"metric": "DSMC pairs tried/s", "value": pairs / (ms * 1e-3), "unit": "pairs/s", "ms_per_perform": ms,
             "pairs_per_perform": pairs, "accepted_last_perform": int(nu.sum()),
-            "workload": "problem/05_dsmc.jl: 20x20 nodes, 5000 e- + 5000 O, elastic e-O, dt = 1 ns", "data": "synthetic"}
+            "max_particles_per_cell": int(max(Na.max(), Nb.max())),
+            "workload": f"problem/05_dsmc.jl: {n}x{n} nodes, 5000 e- + 5000 O, elastic e-O, dt = {dt:g} s",
+            "data": "synthetic"}
 
 
 def c5_measure(n=1024, npart=1 << 25, pre=40, window=20, harvest=160, train=(600, 600, 600)):
@@ -862,6 +865,7 @@ def main():
         line["tracker"] = tracker_measure(w, e, i, min(max(args.steps // 5, 20), 200), ms / args.steps)
         line["source"] = source_measure()
         line["dsmc_05"] = dsmc_measure()
+        line["dsmc_crowded"] = dsmc_measure(reps=10, n=3, dt=1e-12)
     if rank == 0 and not args.no_c5:
         line["learned_warm_start_c5"] = c5_measure()
     if rank == 0 and not args.no_cpu_baseline:

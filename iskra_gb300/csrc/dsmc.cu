@@ -32,6 +32,7 @@ struct Dsmc {
   int *cnt = nullptr;           // [2][nn + 1] per-cell counts, then exclusive offsets
   int *fill = nullptr;          // [2][nn] scatter cursors
   unsigned *idx[2] = {nullptr, nullptr};  // slot indices by cell, per species
+  unsigned *ord[2] = {nullptr, nullptr};  // the lists of crowded cells in identifier order
   unsigned *nu = nullptr;       // accepted collisions per cell, last perform! (the "nuDSMC" field)
 };
 
@@ -45,7 +46,7 @@ struct DsmcArgs {
   bool same;                    // source and target are one species
   double *remaining;
   int *cnt[2], *fill[2];
-  unsigned *idx[2];
+  unsigned *idx[2], *ord[2];
   unsigned *nu;
   uint32_t k0, k1, set;
   const unsigned long long *step;
@@ -105,19 +106,6 @@ __global__ void k_dsmc_scatter(SpeciesDev s, int nx, const int *__restrict__ sta
 // a cell's slots ordered by particle identifier (insertion sort: cells hold
 // few particles), so the picks depend neither on the order the scatter wrote
 // them in nor on where the sort left the particles in memory
-__device__ __forceinline__ void sort_by_id(unsigned *a, int n, const uint32_t *__restrict__ id) {
-  for (int i = 1; i < n; i++) {
-    const unsigned v = a[i];
-    const uint32_t kv = id[v];
-    int j = i - 1;
-    while (j >= 0 && id[a[j]] > kv) {
-      a[j + 1] = a[j];
-      j--;
-    }
-    a[j + 1] = v;
-  }
-}
-
 __device__ __forceinline__ float3 vel_of(const SpeciesDev &s, unsigned p) {
   const int cur = s.st->cur;
   const float4 a = pick(s.xv[0], s.xv[1], cur)[p];
@@ -211,7 +199,7 @@ __device__ unsigned dsmc_pairs(const DsmcArgs &A, int cell, unsigned long long s
 // cells whose lists fit are staged in shared memory: the pair loop then
 // waits on shared-memory loads instead of dependent global ones
 constexpr int kDsmcStage = 512;
-struct DsmcShared {
+struct __align__(16) DsmcShared {  // 16-byte aligned: tid is read as uint4
   float3 va[kDsmcStage], vb[kDsmcStage];      // velocities, id order
   unsigned sa[kDsmcStage], sb[kDsmcStage];    // slots, id order
   unsigned tslot[kDsmcStage];                 // a list as scattered
@@ -232,6 +220,34 @@ __device__ __forceinline__ void warp_rank_sort(const unsigned *__restrict__ l, i
     int r = 0;
     for (int q = 0; q < n; q++) r += sh.tid[q] < key;
     out[r] = sh.tslot[e];
+  }
+  __syncwarp();
+}
+
+// The same order for a list of any length, into global memory: each lane
+// ranks one element of every 32 against all ids, staged through shared
+// memory kDsmcStage at a time (n²/32 shared-memory compares per lane, no
+// dependent global loads).
+__device__ void warp_rank_sort_long(const unsigned *__restrict__ l, int n, const uint32_t *__restrict__ id,
+                                    DsmcShared &sh, unsigned *__restrict__ out, int lane) {
+  for (int g = 0; g < n; g += 32) {
+    const int e = g + lane;
+    const unsigned slot = e < n ? l[e] : 0u;
+    const uint32_t key = e < n ? id[slot] : 0u;
+    int r = 0;
+    for (int c0 = 0; c0 < n; c0 += kDsmcStage) {
+      const int m = min(kDsmcStage, n - c0);
+      __syncwarp();
+      for (int q = lane; q < m; q += 32) sh.tid[q] = id[l[c0 + q]];
+      __syncwarp();
+      int q = 0;
+      for (; q + 4 <= m; q += 4) {
+        const uint4 t = *reinterpret_cast<const uint4 *>(sh.tid + q);
+        r += (t.x < key) + (t.y < key) + (t.z < key) + (t.w < key);
+      }
+      for (; q < m; q++) r += sh.tid[q] < key;
+    }
+    if (e < n) out[r] = slot;
   }
   __syncwarp();
 }
@@ -289,12 +305,20 @@ __global__ void __launch_bounds__(32) k_dsmc_cells(DsmcArgs A) {
       for (int r = lane; r < Nb; r += 32) set_vel(S1, sh.sb[r], sh.vb[r]);
     return;
   }
-  // a crowded cell: lists ordered in place, velocities in global memory
-  if (lane == 0) {
-    sort_by_id(la, Na, id0);
-    if (!A.same) sort_by_id(lb, Nb, id1);
+  // a crowded cell: lists ranked into identifier order in global memory,
+  // velocities in global memory
+  {
+    unsigned *oa = A.ord[0] + sa0;
+    warp_rank_sort_long(la, Na, id0, sh, oa, lane);
+    la = oa;
+    if (!A.same) {
+      unsigned *ob = A.ord[1] + sb0;
+      warp_rank_sort_long(lb, Nb, id1, sh, ob, lane);
+      lb = ob;
+    } else {
+      lb = oa;
+    }
   }
-  __syncwarp();
   auto ga = [&](int r) { return vel_of(S0, la[r]); };
   auto sa = [&](int r, float3 v) { set_vel(S0, la[r], v); };
   auto gb = [&](int r) { return vel_of(S1, lb[r]); };
@@ -315,6 +339,8 @@ static void dsmc_free(Dsmc *d) {
   cudaFree(d->fill);
   cudaFree(d->idx[0]);
   if (d->idx[1] != d->idx[0]) cudaFree(d->idx[1]);
+  cudaFree(d->ord[0]);
+  if (d->ord[1] != d->ord[0]) cudaFree(d->ord[1]);
   cudaFree(d->nu);
   delete d;
 }
@@ -363,6 +389,8 @@ int launch_dsmc(Ctx *c, int k, double dt, uint64_t seed, const unsigned long lon
   A.fill[1] = d->fill + (A.same ? 0 : (size_t)nn);
   A.idx[0] = d->idx[0];
   A.idx[1] = A.same ? d->idx[0] : d->idx[1];
+  A.ord[0] = d->ord[0];
+  A.ord[1] = A.same ? d->ord[0] : d->ord[1];
   A.nu = d->nu;
   A.k0 = (uint32_t)seed;
   A.k1 = (uint32_t)(seed >> 32) ^ 0xD5AC0000u;
@@ -424,9 +452,15 @@ int iskra_dsmc_create(iskra_ctx *h, int source, int target, const double *g, con
             cudaMalloc(&d->cnt, 2 * (nn + 1) * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&d->fill, 2 * nn * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&d->idx[0], (size_t)std::max(1LL, A.cap) * sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc(&d->ord[0], (size_t)std::max(1LL, A.cap) * sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc(&d->nu, nn * sizeof(unsigned)) == cudaSuccess;
-  if (ok && source != target) ok = cudaMalloc(&d->idx[1], (size_t)std::max(1LL, B.cap) * sizeof(unsigned)) == cudaSuccess;
-  else d->idx[1] = d->idx[0];
+  if (ok && source != target)
+    ok = cudaMalloc(&d->idx[1], (size_t)std::max(1LL, B.cap) * sizeof(unsigned)) == cudaSuccess &&
+         cudaMalloc(&d->ord[1], (size_t)std::max(1LL, B.cap) * sizeof(unsigned)) == cudaSuccess;
+  if (source == target) {
+    d->idx[1] = d->idx[0];
+    d->ord[1] = d->ord[0];
+  }
   if (!ok) {
     dsmc_free(d);
     return set_err(c, ISKRA_ENOMEM, "out of device memory for DSMC");

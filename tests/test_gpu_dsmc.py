@@ -118,3 +118,78 @@ def test_dsmc_in_step_graph(lib):
     e1 = ME * (_vel(ctx, a)[1] ** 2).sum() + 8 * MP * (_vel(ctx, b)[1] ** 2).sum()
     assert np.isclose(e0, e1, rtol=1e-4)  # uncharged species: no field work
     ctx.close()
+
+
+@pytest.mark.parametrize("same", [False, True])
+def test_dsmc_crowded_cells(lib, same):
+    """Cells with more lists than shared memory stages (above 512 particles)
+    take the global-memory path: remainder against the oracle, accepted
+    collisions against the oracle's own random run, momentum and energy
+    conserved, and the result reproducible (independent of the order in
+    which the cell lists were scattered)."""
+    from iskra_gb300.device import Context
+    n, d, dt = 3, 0.05, 5e-13  # 2x2 cells
+    r = np.random.default_rng(11)
+    na, nb = 3000, 2400
+
+    def pos(m):
+        c = r.integers(0, n - 1, (m, 2))
+        return np.asfortranarray((c + r.uniform(0.05, 0.95, (m, 2))) * d)
+
+    xa, xb = pos(na), pos(nb)
+    va = np.asfortranarray(r.normal(0, 2.5e6, (na, 3)))
+    vb = np.asfortranarray(r.normal(0, 3e3, (nb, 3)))
+    ma, mb = ME, (ME if same else 8 * MP)
+
+    def make():
+        ctx = Context(n, n, d, d, (0, 0, 0, 0))
+        a = ctx.species_create(0.0, ma, 1.0, 2 * na)
+        ctx.set_boundary(a, lib.BND_WRAP, lib.BND_WRAP)
+        ctx.upload(a, xa, va, ids=np.arange(na, dtype=np.uint32))
+        b = a
+        if not same:
+            b = ctx.species_create(0.0, mb, 1.0, 2 * nb)
+            ctx.set_boundary(b, lib.BND_WRAP, lib.BND_WRAP)
+            ctx.upload(b, xb, vb, ids=np.arange(nb, dtype=np.uint32))
+        return ctx, a, b, ctx.dsmc_create(a, b, G, S)
+
+    ctx, a, b, k = make()
+    x0a, v0a = _vel(ctx, a)
+    x0b, v0b = _vel(ctx, b)
+    counts = np.bincount((x0a[:, 0] // d).astype(int) + 2 * (x0a[:, 1] // d).astype(int), minlength=4)
+    assert counts.min() > 512
+    rem = np.zeros(n * n)
+    acc_gpu = acc_orc = 0
+    va_o, vb_o = v0a.copy(), v0b.copy()
+    for step in range(2):
+        ctx.dsmc_perform(k, dt, seed=7, step=step)
+        rem_g, nu_g = ctx.dsmc_state(k)
+        va_o, vb_o, rem, nu_o = do.perform(x0a, va_o, x0b, vb_o, ma, mb, 1.0, 1.0, G, S, (n, n, d, d), dt, rem,
+                                           same=same, rng=np.random.default_rng(100 + step))
+        assert np.allclose(rem_g.ravel(order="F"), rem, rtol=0, atol=1e-9)
+        acc_gpu += int(nu_g.sum())
+        acc_orc += int(nu_o.sum())
+    assert acc_orc > 200
+    assert abs(acc_gpu - acc_orc) < 6 * np.sqrt(acc_orc) + 10, (acc_gpu, acc_orc)
+    _, v1a = _vel(ctx, a)
+    _, v1b = _vel(ctx, b)
+    ctx.close()
+    if same:
+        p0, p1 = ma * v0a.sum(0), ma * v1a.sum(0)
+        e0, e1 = ma * (v0a ** 2).sum(), ma * (v1a ** 2).sum()
+        scale = ma * np.abs(v0a).sum()
+    else:
+        p0, p1 = ma * v0a.sum(0) + mb * v0b.sum(0), ma * v1a.sum(0) + mb * v1b.sum(0)
+        e0, e1 = ma * (v0a ** 2).sum() + mb * (v0b ** 2).sum(), ma * (v1a ** 2).sum() + mb * (v1b ** 2).sum()
+        scale = ma * np.abs(v0a).sum() + mb * np.abs(v0b).sum()
+    assert np.all(np.abs(p1 - p0) < 1e-5 * scale)
+    assert np.isclose(e0, e1, rtol=1e-5)
+    assert not np.array_equal(v0a, v1a)
+    # the same perform! again on a fresh context: bit-identical
+    ctx, a, b, k = make()
+    ctx.dsmc_perform(k, dt, seed=7, step=0)
+    ctx.dsmc_perform(k, dt, seed=7, step=1)
+    assert np.array_equal(_vel(ctx, a)[1], v1a)
+    if not same:
+        assert np.array_equal(_vel(ctx, b)[1], v1b)
+    ctx.close()

@@ -40,7 +40,7 @@ struct EnsMcc {
   unsigned long long *counts = nullptr;  // R x N
   int N = 0;
   MccWork *work = nullptr;               // work list (R x work_cap entries)
-  unsigned long long *nwork = nullptr;   // R
+  unsigned long long *nwork = nullptr;   // R counters, kNworkStride apart
   // the list is made by the push of the set's source species in the step
   // before (the first set of each source species); otherwise by a selection
   // pass at the start of the step
@@ -105,7 +105,7 @@ __global__ void k_ens_step_begin(unsigned long long *d_step) {
 __global__ void k_zero_u64_runs(unsigned long long *p, int n) {
   pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = 0ull;
+  if (i < n) p[(size_t)i * kNworkStride] = 0ull;
 }
 
 // Drop discarded particles of every run: live particles move to the other
@@ -436,8 +436,8 @@ int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t cap_per_run, iskra_ens 
     std::vector<bool> src_folded(c->species.size(), false);
     for (int m = 0; m < (int)e->mcc.size(); m++) {
       ENS_ALLOC(e->mcc[m].work, R * e->work_cap * mcc_work_entry_bytes());
-      ENS_ALLOC(e->mcc[m].nwork, R * sizeof(unsigned long long));
-      cudaMemset(e->mcc[m].nwork, 0, R * sizeof(unsigned long long));
+      ENS_ALLOC(e->mcc[m].nwork, (size_t)R * kNworkStride * sizeof(unsigned long long));
+      cudaMemset(e->mcc[m].nwork, 0, (size_t)R * kNworkStride * sizeof(unsigned long long));
       const int src = mcc_src(c, m);
       e->mcc[m].folded = !src_folded[src];
       src_folded[src] = true;

@@ -44,7 +44,10 @@ enum : int {
   DERR_OVERFLOW = 64,
 };
 
-struct SpeciesState {          // device-resident, written by kernels
+// device-resident, written by kernels; one 128-byte line each, so that the
+// states of an ensemble's runs (an array) do not share lines between the
+// runs' atomics
+struct alignas(128) SpeciesState {
   long long np;                // slots in use (live + discarded holes)
   int cur;                     // active buffer of the double-buffered store
   int pad;
@@ -207,13 +210,18 @@ __device__ __forceinline__ int draw_selections(float u, float lam, float expl) {
   return nsel;
 }
 
+// The runs' work-list counters lie a 128-byte line apart: every warp of a
+// run reserves list positions on its run's counter, and counters that share
+// a line serialise in one L2 slice.
+constexpr int kNworkStride = 16;
+
 // Selection for the next MCC step folded into an ensemble push (k_push_runs):
 // per run, the set's key, its work list segment and counter.
 struct PushSelect {
   float lam;                    // N maxPt of the MCC set
   const uint2 *keys;            // R
   MccWork *work;                // R x cap_run
-  unsigned long long *nwork;    // R
+  unsigned long long *nwork;    // R counters, kNworkStride apart
   unsigned long long cap_run;
   const unsigned long long *d_step;  // the current step (entries are for step + 1)
 };

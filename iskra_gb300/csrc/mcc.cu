@@ -9,10 +9,12 @@
 // times (the per-particle law of drawing Nc times with replacement, whose
 // mean is N*maxPt per step including the carried remainder), and each
 // selection runs the reference's k-choice, acceptance test and kinematics on
-// that particle in order.  Randomness comes from Philox4x32-10 (Salmon,
+// that particle in order.  Randomness: the selection count from the
+// SplitMix64 finalizer (Steele, Lea, Flood, OOPSLA 2014) of (set key, step,
+// particle id); the draws of each selection from Philox4x32-10 (Salmon,
 // Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11)
-// keyed by (seed, set) with counter (particle id, step, selection, draw), so
-// the result does not depend on the particle order in memory.  Differences
+// keyed by (seed, set) with counter (particle id, step, draw), so the result
+// does not depend on the particle order in memory.  Differences
 // from the reference, both statistical only: particles created by ionisation
 // in this step are not selected again in the same step (the reference re-reads
 // np after each draw), and the number of draws per step is Poisson instead of
@@ -50,6 +52,7 @@ struct MccDev {
   uint32_t key0, key1;
   int logu[kMaxProc];    // table energies log-uniform: O(1) bracket guess
   float log_e0[kMaxProc], inv_dlog[kMaxProc];
+  int staged;            // some table is not log-uniform: the collision pass stages the tables in shared memory
 };
 
 struct Mcc {
@@ -154,11 +157,11 @@ __device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsi
 
 // ---- two-phase null-collision step --------------------------------------
 // Phase 1 (k_mcc_select, every live particle; in ensembles the push of the
-// step before, k_push_runs): the particle's first draw gives its number of
+// step before, k_push_runs): the particle's hash uniform gives its number of
 // selections c ~ Poisson(N maxPt); particles with c > 0 go to a work list
 // as their whole record (MccWork: position, velocity, cell, id, slot).
 // Phase 2 (k_mcc_collide, the work list only): each entry replays its
-// particle's stream (the first draw gives c again) and runs the c selections
+// particle's count (the hash gives c again) and runs the c selections
 // -- the k choice, acceptance test and kinematics -- in order, then writes
 // the changed velocity back to the particle's slot.  With N maxPt ~ 0.1 a
 // warp of phase 2 holds 32 colliding particles instead of the ~3 a single
@@ -169,7 +172,7 @@ constexpr int kSelChunk = 1024;  // particles per block pass of k_mcc_select
 // Phase 1 over the particles of run blockIdx.y (R = 1 for a single context):
 // a block collects the selected particles of a chunk in shared memory and
 // appends them to its run's segment [r cap_run, ...) of the work list with
-// one atomic on the run's counter nwork[r].  step_ahead = 1 draws for the
+// one atomic on the run's counter nwork[r kNworkStride].  step_ahead = 1 draws for the
 // step after the device counter's (a list built before the step begins).
 __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict__ src, float lam, uint2 key1,
                                                     const uint2 *__restrict__ keys,
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
       if (nsel > 0) buf[at] = mcc_entry(xv[p], b, pid, (uint32_t)p);
     }
     __syncthreads();
-    if (threadIdx.x == 0) base = atomicAdd(nwork + r, (unsigned long long)cnt);
+    if (threadIdx.x == 0) base = atomicAdd(nwork + (size_t)r * kNworkStride, (unsigned long long)cnt);
     __syncthreads();
     for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) {
       const unsigned long long at = base + i;
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(256) k_mcc_select(const SpeciesDev *__restrict
 // so these are exactly the tests the collision code makes before its first
 // collision); a probability above the bound counts as a hit (the collision
 // code raises the flag).
-__device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M, const float *tab, int ntab,
+__device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M, const float *te, const float *ts,
                                                const float2 *__restrict__ Er, int nx, unsigned long long step,
                                                uint2 key, float expl) {
   const int nsel = draw_selections(selection_uniform(e.b.z, step, key), M.lam, expl);
@@ -253,7 +256,7 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
     const float U = R.next();
     int k = (int)floorf(M.N * U);
     if (k >= M.N) k = M.N - 1;
-    const float sg = sigma_at(tab + M.off[k], tab + ntab + M.off[k], M.off[k + 1] - M.off[k], eps, M.logu[k],
+    const float sg = sigma_at(te + M.off[k], ts + M.off[k], M.off[k + 1] - M.off[k], eps, M.logu[k],
                               M.log_e0[k], M.inv_dlog[k]) *
                      g;
     float Pk = -expm1f(-n * sg * M.dt);
@@ -267,7 +270,14 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
 // Phase 2 over the work list segment of run r = blockIdx.y: the run's stores
 // src[r] / prod[r], node field E + r nn, key keys[r] (or M's key for a single
 // context), counters counts_runs + r N (or M.counts).
-__global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restrict__ src,
+// Blocks of 256 threads per SM asked of the register allocator: 3 (80
+// registers, a few bytes spilled) against 2 (102 registers): 245 against
+// 283 us per electron pass of a 128-run ensemble, which waits on the
+// dependent loads of each entry (its node's gas density and field).
+#ifndef ISKRA_MCC_COLLIDE_MIN_BLOCKS
+#define ISKRA_MCC_COLLIDE_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_collide(const SpeciesDev *__restrict__ src,
                                                      const SpeciesDev *__restrict__ prod, int has_prod, MccDev M,
                                                      const uint2 *__restrict__ keys, unsigned long long *counts_runs,
                                                      const float2 *__restrict__ E, int nn, int nx,
@@ -278,15 +288,22 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
   pdl_wait();
   extern __shared__ float tab[];
   const unsigned FULL = 0xffffffffu;
-  const int ntab = M.off[M.N];
-  for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
-    tab[t] = M.eps[t];
-    tab[ntab + t] = M.sig[t];
+  // log-uniform tables take O(1) lookups, read through the caches; others
+  // (binary search) are staged in shared memory
+  const float *te = M.eps, *ts = M.sig;
+  if (M.staged) {
+    const int ntab = M.off[M.N];
+    for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
+      tab[t] = M.eps[t];
+      tab[ntab + t] = M.sig[t];
+    }
+    __syncthreads();
+    te = tab;
+    ts = tab + ntab;
   }
-  __syncthreads();
   const unsigned long long step = *d_step;
   const int r = blockIdx.y;
-  const long long nw = (long long)min(nwork[r], cap_run);
+  const long long nw = (long long)min(nwork[(size_t)r * kNworkStride], cap_run);
   const MccWork *__restrict__ seg = work + (size_t)r * cap_run;
   const float expl = __expf(-M.lam);
   int flags = 0;
@@ -315,7 +332,7 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
     const bool more = base < nw;  // warp-uniform
     if (more) {
       const long long wt = base + lane;
-      const bool hit = wt < nw && mcc_entry_hits(seg[wt], M, tab, ntab, Er, nx, step, key, expl);
+      const bool hit = wt < nw && mcc_entry_hits(seg[wt], M, te, ts, Er, nx, step, key, expl);
       const unsigned hm = __ballot_sync(FULL, hit);
       if (hit) q[qn + __popc(hm & ((1u << lane) - 1u))] = (unsigned)wt;
       qn += __popc(hm);
@@ -370,7 +387,7 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
         const float gx = tvx - v[0], gy = tvy - v[1], gz = -v[2];
         const float g = sqrtf(gx * gx + gy * gy + gz * gz);
         const float eps = 0.5f * M.m_ev * g * g;
-        const float sg = sigma_at(tab + M.off[k], tab + ntab + M.off[k], M.off[k + 1] - M.off[k], eps, M.logu[k],
+        const float sg = sigma_at(te + M.off[k], ts + M.off[k], M.off[k + 1] - M.off[k], eps, M.logu[k],
                                   M.log_e0[k], M.inv_dlog[k]) *
                          g;
         float Pk = -expm1f(-n * sg * M.dt);
@@ -480,9 +497,9 @@ __global__ void __launch_bounds__(256) k_mcc_collide(const SpeciesDev *__restric
   if (lane == 0 && f) atomicOr(err, f);
 }
 
-__global__ void k_zero_u64(unsigned long long *p, int n) {
+__global__ void k_zero_u64(unsigned long long *p, int n, int stride) {
   pdl_wait();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0ull;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[(size_t)i * stride] = 0ull;
 }
 
 // Appends reserve slots from np_new so that np (the loop bound of the running
@@ -535,10 +552,12 @@ static int mcc_params(Ctx *c, int mid, double dt, uint64_t seed, MccDev &M) {
   M.counts = m->counts;
   M.nu = m->nu;
   mcc_key(seed, m->set_index, M.key0, M.key1);
+  M.staged = 0;
   for (int k = 0; k < m->N; k++) {
     M.logu[k] = m->logu[k];
     M.log_e0[k] = m->log_e0[k];
     M.inv_dlog[k] = m->inv_dlog[k];
+    if (!m->logu[k]) M.staged = 1;
   }
   return ISKRA_OK;
 }
@@ -552,10 +571,10 @@ static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const Speci
                             const unsigned long long *d_step, int *err, cudaStream_t st, int phases = kMccBoth) {
   Mcc *m = c->mccs[mid];
   const int ntab = m->off[m->N];
-  const size_t smem = (size_t)2 * ntab * sizeof(float);
+  const size_t smem = M.staged ? (size_t)2 * ntab * sizeof(float) : 0;
   const uint2 key1 = make_uint2(M.key0, M.key1);
   if (phases != kMccCollideOnly) {
-    ISKRA_CUDA(c, launch_pdl(k_zero_u64, (R + 255) / 256, 256, 0, st, nwork, R));
+    ISKRA_CUDA(c, launch_pdl(k_zero_u64, (R + 255) / 256, 256, 0, st, nwork, R, kNworkStride));
     ISKRA_CUDA(c, launch_pdl(k_mcc_select, dim3(select_blocks, R), 256, 0, st, src, M.lam, key1, keys, d_step,
                              phases == kMccSelectAhead ? 1 : 0, work, nwork, cap_work, err));
   }

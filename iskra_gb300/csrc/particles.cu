@@ -610,6 +610,22 @@ int launch_sort(Ctx *c, int sid) {
 // particle in between) and, when selected, its new record goes to the run's
 // list.  The next step's collision pass then starts without a selection pass
 // over all particles.
+// Appends a warp's n <= 32 buffered work-list entries to its run's list
+// (counter cnt, segment seg of cap entries).
+__device__ __forceinline__ void flush_entries(const MccWork *buf, int n, unsigned long long *cnt,
+                                              MccWork *__restrict__ seg, unsigned long long cap, int &flags) {
+  const int lane = threadIdx.x & 31;
+  __syncwarp();  // the entries are in buf
+  unsigned long long at = 0;
+  if (lane == 0) at = atomicAdd(cnt, (unsigned long long)n);
+  at = __shfl_sync(0xffffffffu, at, 0) + (unsigned)lane;
+  if (lane < n) {
+    if (at < cap) seg[at] = buf[lane];
+    else flags |= DERR_CAPACITY;
+  }
+  __syncwarp();  // buf may be written again
+}
+
 template <int MX, int MY, bool SEL>
 __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(const SpeciesDev *__restrict__ runs,
                                                                           const float2 *__restrict__ E2, int nnode,
@@ -645,20 +661,31 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   // iterations in flight per warp: the loop was bound by the load latency)
   float4 an = make_float4(0.f, 0.f, 0.f, 0.f);
   float2 bn = make_float2(0.f, 0.f);
+  uint32_t idn = 0;  // the identifier, which the selection draw needs
+  // A warp's selected entries gather in its shared-memory buffer and go to
+  // the run's list 32 at a time: one reservation (an atomic on the run's
+  // counter, which every warp of the run shares) per 32 entries instead of
+  // one per iteration, and 1 KB contiguous stores.  nbuf: entries buffered
+  // (warp-uniform, < 32 between iterations).
+  __shared__ MccWork wbuf[8][64];
+  int nbuf = 0;
   if (warp * 32 + lane < np) {
     an = ld_stream(xv + warp * 32 + lane);
     bn = ld_stream(zc + warp * 32 + lane);
+    if (SEL) idn = ids[warp * 32 + lane];
   }
   for (long long base = warp * 32; base < np; base += nwarps * 32) {
     const long long p = base + lane;
     const bool v = p < np;
     const float4 a = an;
     const float2 b = bn;
+    const uint32_t idc = idn;
     {
       const long long pn = p + nwarps * 32;  // a slot no push of this iteration writes
       if (pn < np) {
         an = ld_stream(xv + pn);
         bn = ld_stream(zc + pn);
+        if (SEL) idn = ids[pn];
       }
     }
     float4 na;
@@ -669,22 +696,21 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
       int nsel = 0;
       uint32_t pid = 0;
       if (v && __float_as_int(nb.y) >= 0) {
-        pid = ids[p];
+        pid = idc;
         nsel = draw_selections(selection_uniform(pid, step1, key), S.lam, expl);
       }
       const unsigned m = __ballot_sync(FULL, nsel > 0);
-      if (m) {
-        const int leader = __ffs(m) - 1;
-        unsigned long long at = 0;
-        if (lane == leader) at = atomicAdd(S.nwork + r, (unsigned long long)__popc(m));
-        at = __shfl_sync(FULL, at, leader) + __popc(m & ((1u << lane) - 1u));
-        if (nsel > 0) {
-          if (at < S.cap_run) seg[at] = mcc_entry(na, nb, pid, (uint32_t)p);
-          else flags |= DERR_CAPACITY;
-        }
+      if (nsel > 0) wbuf[wib][nbuf + __popc(m & ((1u << lane) - 1u))] = mcc_entry(na, nb, pid, (uint32_t)p);
+      nbuf += __popc(m);
+      if (nbuf >= 32) {
+        flush_entries(wbuf[wib], 32, S.nwork + (size_t)r * kNworkStride, seg, S.cap_run, flags);
+        nbuf -= 32;
+        if (lane < nbuf) wbuf[wib][lane] = wbuf[wib][32 + lane];
+        __syncwarp();
       }
     }
   }
+  if (SEL && nbuf) flush_entries(wbuf[wib], nbuf, S.nwork + (size_t)r * kNworkStride, seg, S.cap_run, flags);
   __syncthreads();
   const int wn = cx + 1;
   for (int t = threadIdx.x; t < (cx + 1) * (cy + 1); t += blockDim.x) {

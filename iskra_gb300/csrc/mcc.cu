@@ -277,6 +277,10 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
 #ifndef ISKRA_MCC_COLLIDE_MIN_BLOCKS
 #define ISKRA_MCC_COLLIDE_MIN_BLOCKS 3
 #endif
+// ensembles: collision-pass blocks per run = the push's blocks per run / this
+#ifndef ISKRA_MCC_COLLIDE_SPLIT
+#define ISKRA_MCC_COLLIDE_SPLIT 1
+#endif
 __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_collide(const SpeciesDev *__restrict__ src,
                                                      const SpeciesDev *__restrict__ prod, int has_prod, MccDev M,
                                                      const uint2 *__restrict__ keys, unsigned long long *counts_runs,
@@ -579,7 +583,7 @@ static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const Speci
                              phases == kMccSelectAhead ? 1 : 0, work, nwork, cap_work, err));
   }
   if (phases == kMccSelectAhead) return ISKRA_OK;
-  const int collide_blocks = R == 1 ? c->num_sms * 8 : select_blocks;
+  const int collide_blocks = R == 1 ? c->num_sms * 8 : std::max(1, select_blocks / ISKRA_MCC_COLLIDE_SPLIT);
   ISKRA_CUDA(c, launch_pdl(k_mcc_collide, dim3(collide_blocks, R), 256, smem, st, src, prod, (int)(m->prod >= 0), M,
                            keys, counts, E, nn, c->nx, d_step, (const MccWork *)work, (const unsigned long long *)nwork,
                            cap_work, err));

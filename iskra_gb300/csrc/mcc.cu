@@ -277,9 +277,13 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
 #ifndef ISKRA_MCC_COLLIDE_MIN_BLOCKS
 #define ISKRA_MCC_COLLIDE_MIN_BLOCKS 3
 #endif
-// ensembles: collision-pass blocks per run = the push's blocks per run / this
+// Ensembles: collision-pass blocks per run = the push's blocks per run / this.
+// A block's setup (run views, step, key) is a chain of dependent loads, and
+// with the push's count each warp ran only ~4 rounds of 32 entries: 2 gives
+// 218 against 241 us per electron pass of a 128-run ensemble (4: 252, 8: 389,
+// the largest runs' blocks then set the pass's length).
 #ifndef ISKRA_MCC_COLLIDE_SPLIT
-#define ISKRA_MCC_COLLIDE_SPLIT 1
+#define ISKRA_MCC_COLLIDE_SPLIT 2
 #endif
 __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_collide(const SpeciesDev *__restrict__ src,
                                                      const SpeciesDev *__restrict__ prod, int has_prod, MccDev M,

@@ -757,7 +757,7 @@ int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float
   P.mode_y = s.bnd[1];
   P.tiles_x = 0;
   const int nnode = c->nn;
-  const dim3 grid(blocks_per_run, R);
+  const dim3 grid(std::max(1, blocks_per_run * ISKRA_PUSH_RUNS_SCALE8 / 8), R);
   const PushSelect S = sel ? *sel : PushSelect{};
 #define ISKRA_PUSH_RUNS_CASE(MX, MY)                                                                           \
   if (P.mode_x == MX && P.mode_y == MY) {                                                                       \

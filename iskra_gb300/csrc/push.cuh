@@ -196,6 +196,10 @@ __device__ __forceinline__ int apply_boundary(int &i, int P) {
 #ifndef ISKRA_PUSH_RUNS_MIN_BLOCKS
 #define ISKRA_PUSH_RUNS_MIN_BLOCKS 4
 #endif
+// ensemble push blocks per run = the ensemble's blocks per run × this / 8
+#ifndef ISKRA_PUSH_RUNS_SCALE8
+#define ISKRA_PUSH_RUNS_SCALE8 8
+#endif
 #ifndef ISKRA_PUSH_STAGES
 #define ISKRA_PUSH_STAGES 4
 #endif

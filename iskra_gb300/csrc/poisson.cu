@@ -129,8 +129,10 @@ struct Poisson {
   double last_relres = 0;
   // FP64 Thomas factors of the separable operator (host copy; uploaded on
   // demand for the ensemble field solve)
-  std::vector<double> lo64, inv64, cp64;
-  double *lo64_d = nullptr, *inv64_d = nullptr, *cp64_d = nullptr;
+  // FP64 cyclic-reduction coefficients of the ensemble field solve, packed:
+  // fwd (K nf pairs), back (K nb pairs), backb (K nb), top (K)
+  std::vector<double> cr64;
+  double *cr64_d = nullptr;
 };
 
 constexpr int kPartials = 1024;
@@ -158,9 +160,7 @@ void poisson_destroy(Poisson *p) {
   cudaFree(p->part);
   cudaFree(p->scal);
   if (p->scal_h) cudaFreeHost(p->scal_h);
-  cudaFree(p->lo64_d);
-  cudaFree(p->inv64_d);
-  cudaFree(p->cp64_d);
+  cudaFree(p->cr64_d);
   cudaFree(p->r32);
   cudaFree(p->spec);
   cudaFree(p->tw);
@@ -1775,13 +1775,13 @@ static int build_device(Ctx *c, Poisson *P) {
       const double ang = -2.0 * M_PI * m / N;
       tw[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
-    P->lo64 = lo;
-    P->inv64 = inv;
-    P->cp64 = cpv;
-    cudaFree(P->lo64_d);
-    cudaFree(P->inv64_d);
-    cudaFree(P->cp64_d);
-    P->lo64_d = P->inv64_d = P->cp64_d = nullptr;
+    P->cr64.clear();
+    for (const double2 &v : cr_fwd) P->cr64.insert(P->cr64.end(), {v.x, v.y});
+    for (const double2 &v : cr_back) P->cr64.insert(P->cr64.end(), {v.x, v.y});
+    P->cr64.insert(P->cr64.end(), cr_backb.begin(), cr_backb.end());
+    P->cr64.insert(P->cr64.end(), cr_top.begin(), cr_top.end());
+    cudaFree(P->cr64_d);
+    P->cr64_d = nullptr;
     const std::vector<float> lo32 = f32(lo), up32 = f32(upv), inv32 = f32(inv), cp32 = f32(cpv), gk32 = f32(gkv),
                              q32 = f32(qv), backb32 = f32(cr_backb), top32 = f32(cr_top);
     const std::vector<float2> fwd32 = f32x2(cr_fwd), back32 = f32x2(cr_back);
@@ -2394,10 +2394,13 @@ int poisson_solve_blocking(Ctx *c, double rtol, int maxit) {
 // Ensemble field solve: one block per run forms ρ from the run's deposit,
 // sets the fixed rows (drive amplitudes per run), and solves the separable
 // operator directly in FP64 -- residual of the previous potential, DFT along
-// y (N <= 16, direct), one Thomas sweep per Fourier mode along x with the
-// host's FP64 factors staged in shared memory, inverse DFT -- then writes E.
-// The same operator and algorithm as one FP64 sweep of the single-run solver,
-// which is exact to rounding.
+// y (N <= 16, direct), cyclic reduction along x per Fourier mode with the
+// host's FP64 coefficients (the single-run solver's, staged in shared memory
+// while ρ is formed), inverse DFT -- then writes E.  The same operator as one
+// FP64 sweep of the single-run solver, exact to rounding.  Cyclic reduction
+// takes 2 log2(nx) dependent levels where a Thomas sweep takes 2 nx dependent
+// FP64 steps on one thread per mode (on GB300, whose FP64 rate is ~1/64 of
+// FP32, that chain was 2/3 of the kernel).
 // ---------------------------------------------------------------------------
 struct FieldRuns {
   int ns;
@@ -2415,27 +2418,34 @@ struct FieldRuns {
   int ndrive_nodes;
   const unsigned long long *d_step;
   double dt, neg_inv_eps0;
-  const double *lo, *inv, *cp;           // FP64 Thomas factors
+  const double *cr;                      // packed FP64 cyclic-reduction coefficients
+  int ncr, L, nf, nb, pin0;              // their count, levels, rows per mode; pinned row of mode 0 (or -1)
   int N, K;
   float idx2, idx1, idy2, idy1;
   int *err;
 };
 
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+
 __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
-  pdl_wait();
-  extern __shared__ double fsm[];
+  extern __shared__ __align__(16) double fsm[];
   __shared__ RowClass cls_sh[kSmemClasses];
   __shared__ double twc[16], tws[16];  // cos, sin of 2π m/N
-  const int nx = op.nx, ny = op.ny, nn = nx * ny, N = F.N, K = F.K;
+  const int nx = op.nx, ny = op.ny, nn = nx * ny, N = F.N, K = F.K, ncol = 2 * K;
+  // xs, rs: nn each; dsp: column col = 2 k + part of the spectrum (nx each);
+  // crs: the coefficients (2 nn + 2 nx K is even: 16-byte aligned pairs)
+  double *xs = fsm, *rs = xs + nn, *dsp = rs + nn, *crs = dsp + (size_t)ncol * nx;
+  // the coefficients do not depend on the previous kernel: staged before it ends
+  for (int t = threadIdx.x; t < F.ncr; t += blockDim.x) cp_async8(crs + t, F.cr + t);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  pdl_wait();
   if (threadIdx.x < N) sincospi(2.0 * threadIdx.x / N, &tws[threadIdx.x], &twc[threadIdx.x]);
-  double *xs = fsm, *rs = xs + nn, *spec = rs + nn, *sinv = spec + 2 * nx * K, *scp = sinv + nx * K;
   const int r = blockIdx.x;
   const size_t o = (size_t)r * nn;
   const RowClass *__restrict__ CT = stage_classes(op, cls_sh);
-  for (int t = threadIdx.x; t < nx * K; t += blockDim.x) {
-    sinv[t] = F.inv[t];
-    scp[t] = F.cp[t];
-  }
   int flags = 0;
   // ρ from the run's deposit (consumed); ϕ of the previous step
   for (int k = threadIdx.x; k < nn; k += blockDim.x) {
@@ -2489,7 +2499,8 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
     rs[k] = -C.d * (b - ax);
   }
   __syncthreads();
-  // DFT along y: spec[i][k] = Σ_j r[i, j] e^{-2πi jk/N}
+  // DFT along y: column 2k (real) and 2k+1 (imaginary) of mode k,
+  // Σ_j r[i, j] e^{-2πi jk/N}; the pinned row of mode 0 is zero
   for (int t = threadIdx.x; t < nx * K; t += blockDim.x) {
     const int i = t / K, k = t - i * K;
     double re = 0, im = 0;
@@ -2499,29 +2510,52 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
       re += v * twc[m];
       im -= v * tws[m];
     }
-    spec[2 * t] = re;
-    spec[2 * t + 1] = im;
+    if (k == 0 && i == F.pin0) re = im = 0.0;
+    dsp[(2 * k) * nx + i] = re;
+    dsp[(2 * k + 1) * nx + i] = im;
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
-  // Thomas per mode and part (sequential along x)
-  if (threadIdx.x < 2 * K) {
-    const int k = threadIdx.x >> 1, part = threadIdx.x & 1;
-    const bool real_mode = k == 0 || 2 * k == N;
-    if (!(part && real_mode)) {
-      double y = 0.0;
-      for (int i = 0; i < nx; i++) {
-        const double a = i > 0 ? F.lo[i] : 0.0;
-        y = (spec[2 * (i * K + k) + part] - a * y) * sinv[i * K + k];
-        spec[2 * (i * K + k) + part] = y;
-      }
-      double xn = y;
-      for (int i = nx - 2; i >= 0; i--) {
-        xn = spec[2 * (i * K + k) + part] - scp[i * K + k] * xn;
-        spec[2 * (i * K + k) + part] = xn;
-      }
+  // cyclic reduction (the single-run solver's levels, in FP64)
+  const double2 *fwd = reinterpret_cast<const double2 *>(crs);
+  const double2 *back = fwd + (size_t)K * F.nf;
+  const double *backb = reinterpret_cast<const double *>(back + (size_t)K * F.nb);
+  const double *top = backb + (size_t)K * F.nb;
+  int Fo = 0, Bo = 0;
+  for (int l = 0; l < F.L; l++) {
+    const int s = 1 << l, cnt = nx >> (l + 1);
+    for (int t = threadIdx.x; t < cnt * ncol; t += blockDim.x) {
+      const int m = t / ncol, col = t - m * ncol;
+      const int i = (m + 1) * 2 * s - 1;
+      const double2 ag = fwd[(size_t)(col >> 1) * F.nf + Fo + m];
+      double *dc = dsp + (size_t)col * nx;
+      double v = dc[i] - ag.x * dc[i - s];
+      if (i + s < nx) v -= ag.y * dc[i + s];
+      dc[i] = v;
     }
+    Fo += cnt;
+    Bo += ((nx >> l) + 1) >> 1;
+    __syncthreads();
   }
+  const int topr = (1 << F.L) - 1;
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) dsp[(size_t)col * nx + topr] *= top[col >> 1];
   __syncthreads();
+  for (int l = F.L - 1; l >= 0; l--) {
+    const int s = 1 << l, ecnt = ((nx >> l) + 1) >> 1;
+    Bo -= ecnt;
+    for (int t = threadIdx.x; t < ecnt * ncol; t += blockDim.x) {
+      const int m = t / ncol, col = t - m * ncol;
+      const int j = (2 * m + 1) * s - 1;
+      const size_t q = (size_t)(col >> 1) * F.nb + Bo + m;
+      const double2 rr = back[q];
+      double *dc = dsp + (size_t)col * nx;
+      double x = backb[q] * dc[j];
+      if (j - s >= 0) x -= rr.x * dc[j - s];
+      if (j + s < nx) x -= rr.y * dc[j + s];
+      dc[j] = x;
+    }
+    __syncthreads();
+  }
   // inverse DFT (Hermitian spectrum) and update of the free rows
   for (int k = threadIdx.x; k < nn; k += blockDim.x) {
     if (op.cls[k] & kFixedBit) continue;
@@ -2529,8 +2563,8 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
     double v = 0;
     for (int m = 0; m < N; m++) {
       const int mm = m < K ? m : N - m;
-      const double re = spec[2 * (i * K + mm)];
-      const double im = m < K ? spec[2 * (i * K + mm) + 1] : -spec[2 * (i * K + mm) + 1];
+      const double re = dsp[(2 * mm) * nx + i];
+      const double im = m < K ? dsp[(2 * mm + 1) * nx + i] : -dsp[(2 * mm + 1) * nx + i];
       const int q = (j * m) % N;
       v += re * twc[q] - im * tws[q];
     }
@@ -2561,7 +2595,7 @@ int launch_field_runs(Ctx *c, int R, FieldRunsHost &H, cudaStream_t st) {
   if (!P->separable || P->cyclic || P->singular || P->N > 16 || P->nsig > 0 || P->rho_fixed)
     return set_err(c, ISKRA_EINVAL, "ensemble field solve needs a separable, non-periodic-x operator with ny <= 16");
   const int nx = P->nx, K = P->K, nn = P->nn;
-  if (!P->lo64_d) return set_err(c, ISKRA_EINVAL, "FP64 factors not uploaded (poisson_upload_fp64)");
+  if (!P->cr64_d) return set_err(c, ISKRA_EINVAL, "FP64 factors not uploaded (poisson_upload_fp64)");
   FieldRuns F{};
   F.ns = H.ns;
   for (int s = 0; s < H.ns; s++) {
@@ -2584,9 +2618,12 @@ int launch_field_runs(Ctx *c, int R, FieldRunsHost &H, cudaStream_t st) {
   F.d_step = H.d_step;
   F.dt = H.dt;
   F.neg_inv_eps0 = -1.0 / P->eps0;
-  F.lo = P->lo64_d;
-  F.inv = P->inv64_d;
-  F.cp = P->cp64_d;
+  F.cr = P->cr64_d;
+  F.ncr = (int)P->cr64.size();
+  F.L = P->cr_levels;
+  F.nf = P->cr_nf;
+  F.nb = P->cr_nb;
+  F.pin0 = P->pin_k0;
   F.N = P->N;
   F.K = K;
   const EOut e = eout(c, true);
@@ -2595,7 +2632,7 @@ int launch_field_runs(Ctx *c, int R, FieldRunsHost &H, cudaStream_t st) {
   F.idy2 = e.idy2;
   F.idy1 = e.idy1;
   F.err = H.err;
-  const size_t smem = (2 * (size_t)nn + 4 * (size_t)nx * K) * sizeof(double);
+  const size_t smem = (2 * (size_t)nn + 2 * (size_t)nx * K + P->cr64.size()) * sizeof(double);
   if (smem > 200 * 1024) return set_err(c, ISKRA_EINVAL, "ensemble grid too large for the per-run field solve");
   ISKRA_CUDA(c, cudaFuncSetAttribute(k_field_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   ISKRA_CUDA(c, launch_pdl(k_field_runs, R, 256, smem, st, opview(P), F));
@@ -2608,14 +2645,9 @@ int poisson_upload_fp64(Ctx *c) {
   if (rc) return rc;
   Poisson *P = c->ps;
   if (!P->separable) return set_err(c, ISKRA_EINVAL, "ensemble field solve needs a separable operator");
-  if (P->lo64_d) return ISKRA_OK;
-  const int nx = P->nx, K = P->K;
-  ISKRA_CUDA(c, cudaMalloc(&P->lo64_d, nx * sizeof(double)));
-  ISKRA_CUDA(c, cudaMalloc(&P->inv64_d, (size_t)nx * K * sizeof(double)));
-  ISKRA_CUDA(c, cudaMalloc(&P->cp64_d, (size_t)nx * K * sizeof(double)));
-  ISKRA_CUDA(c, cudaMemcpy(P->lo64_d, P->lo64.data(), nx * sizeof(double), cudaMemcpyHostToDevice));
-  ISKRA_CUDA(c, cudaMemcpy(P->inv64_d, P->inv64.data(), (size_t)nx * K * sizeof(double), cudaMemcpyHostToDevice));
-  ISKRA_CUDA(c, cudaMemcpy(P->cp64_d, P->cp64.data(), (size_t)nx * K * sizeof(double), cudaMemcpyHostToDevice));
+  if (P->cr64_d) return ISKRA_OK;
+  ISKRA_CUDA(c, cudaMalloc(&P->cr64_d, std::max<size_t>(1, P->cr64.size()) * sizeof(double)));
+  ISKRA_CUDA(c, cudaMemcpy(P->cr64_d, P->cr64.data(), P->cr64.size() * sizeof(double), cudaMemcpyHostToDevice));
   return ISKRA_OK;
 }
 

@@ -580,6 +580,8 @@ static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const Speci
   Mcc *m = c->mccs[mid];
   const int ntab = m->off[m->N];
   const size_t smem = M.staged ? (size_t)2 * ntab * sizeof(float) : 0;
+  if (smem > 48 * 1024)  // tables of up to kMaxTable nodes
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_mcc_collide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint2 key1 = make_uint2(M.key0, M.key1);
   if (phases != kMccCollideOnly) {
     ISKRA_CUDA(c, launch_pdl(k_zero_u64, (R + 255) / 256, 256, 0, st, nwork, R, kNworkStride));

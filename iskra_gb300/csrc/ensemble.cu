@@ -435,7 +435,7 @@ int iskra_ens_create(iskra_ctx *tmpl, int nruns, int64_t cap_per_run, iskra_ens 
     e->work_cap = (unsigned long long)cap_per_run;  // per run segment
     std::vector<bool> src_folded(c->species.size(), false);
     for (int m = 0; m < (int)e->mcc.size(); m++) {
-      ENS_ALLOC(e->mcc[m].work, R * e->work_cap * mcc_work_entry_bytes());
+      ENS_ALLOC(e->mcc[m].work, mcc_work_bytes(R, e->work_cap));
       ENS_ALLOC(e->mcc[m].nwork, (size_t)R * kNworkStride * sizeof(unsigned long long));
       cudaMemset(e->mcc[m].nwork, 0, (size_t)R * kNworkStride * sizeof(unsigned long long));
       const int src = mcc_src(c, m);

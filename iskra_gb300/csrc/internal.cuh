@@ -541,7 +541,9 @@ int launch_mcc_runs(Ctx *c, int mid, double dt, int R, const SpeciesDev *src, co
                     void *work, unsigned long long *nwork, unsigned long long cap_work,
                     const unsigned long long *d_step, int *err, cudaStream_t st, int phases = kMccBoth);
 int mcc_push_select(Ctx *c, int mid, double dt, PushSelect *S);
-size_t mcc_work_entry_bytes();
+// bytes of a work list of R runs x cap entries: the entries, then one hit bit
+// per entry (k_mcc_test -> k_mcc_collide)
+size_t mcc_work_bytes(size_t R, size_t cap);
 int ensure_mcc_work(Ctx *c);
 void ensembles_detach(Ctx *c);
 void mcc_key(uint64_t seed, int set_index, uint32_t &k0, uint32_t &k1);

@@ -168,6 +168,8 @@ __device__ __forceinline__ long long warp_reserve(bool want, long long *np, unsi
 // pass over all particles would, and it reads them as one contiguous
 // 32-byte entry each instead of three scattered records.
 constexpr int kSelChunk = 1024;  // particles per block pass of k_mcc_select
+// words of hit bits per run (one bit per work-list entry), after the entries
+__host__ __device__ __forceinline__ size_t hit_words(size_t cap) { return (cap + 31) / 32; }
 
 // Phase 1 over the particles of run blockIdx.y (R = 1 for a single context):
 // a block collects the selected particles of a chunk in shared memory and
@@ -285,6 +287,49 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
 #ifndef ISKRA_MCC_COLLIDE_SPLIT
 #define ISKRA_MCC_COLLIDE_SPLIT 2
 #endif
+// Phase 2a over the work-list segment of run r = blockIdx.y: each warp
+// tests 32 entries (mcc_entry_hits) and stores their hit bits, one word per
+// 32 entries.  Apart from the collision code, the test needs few registers,
+// so twice as many warps per SM hide its dependent loads (the entry, its
+// node's gas density and field, the table bracket).
+__global__ void __launch_bounds__(256) k_mcc_test(MccDev M, const uint2 *__restrict__ keys,
+                                                  const float2 *__restrict__ E, int nn, int nx,
+                                                  const unsigned long long *__restrict__ d_step,
+                                                  const MccWork *__restrict__ work,
+                                                  const unsigned long long *__restrict__ nwork,
+                                                  unsigned long long cap_run, unsigned *__restrict__ hits) {
+  pdl_wait();
+  extern __shared__ float tab[];
+  const float *te = M.eps, *ts = M.sig;
+  if (M.staged) {
+    const int ntab = M.off[M.N];
+    for (int t = threadIdx.x; t < ntab; t += blockDim.x) {
+      tab[t] = M.eps[t];
+      tab[ntab + t] = M.sig[t];
+    }
+    __syncthreads();
+    te = tab;
+    ts = tab + ntab;
+  }
+  const unsigned long long step = *d_step;
+  const int r = blockIdx.y;
+  const long long nw = (long long)min(nwork[(size_t)r * kNworkStride], cap_run);
+  const MccWork *__restrict__ seg = work + (size_t)r * cap_run;
+  unsigned *__restrict__ hw = hits + (size_t)r * hit_words(cap_run);
+  const float2 *Er = E + (size_t)r * nn;
+  const uint2 key = keys ? keys[r] : make_uint2(M.key0, M.key1);
+  const float expl = __expf(-M.lam);
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  for (long long base = warp * 32; base < nw; base += nwarps * 32) {
+    const long long wt = base + lane;
+    const bool hit = wt < nw && mcc_entry_hits(seg[wt], M, te, ts, Er, nx, step, key, expl);
+    const unsigned hm = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) hw[base >> 5] = hm;
+  }
+}
+
 __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_collide(const SpeciesDev *__restrict__ src,
                                                      const SpeciesDev *__restrict__ prod, int has_prod, MccDev M,
                                                      const uint2 *__restrict__ keys, unsigned long long *counts_runs,
@@ -292,7 +337,8 @@ __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_colli
                                                      const unsigned long long *__restrict__ d_step,
                                                      const MccWork *__restrict__ work,
                                                      const unsigned long long *__restrict__ nwork,
-                                                     unsigned long long cap_run, int *err) {
+                                                     unsigned long long cap_run,
+                                                     const unsigned *__restrict__ hits, int *err) {
   pdl_wait();
   extern __shared__ float tab[];
   const unsigned FULL = 0xffffffffu;
@@ -327,8 +373,8 @@ __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_colli
   unsigned acc_k[kMaxProc];
 #pragma unroll
   for (int k = 0; k < kMaxProc; k++) acc_k[k] = 0u;
-  // Each warp tests 32 entries at a time (mcc_entry_hits) and queues the
-  // ~5 % that collide in its own shared-memory queue; whenever 32 are queued
+  // Each warp reads the hit bits of 32 entries at a time (k_mcc_test) and
+  // queues the ~5 % that collide in its own shared-memory queue; whenever 32 are queued
   // (and for the rest at the end) it runs the collision code on them densely,
   // instead of diverging into the kinematics for its one or two colliding
   // lanes of every 32.  Warps never wait for one another.
@@ -336,12 +382,13 @@ __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_colli
   const uint2 key = keys ? keys[r] : make_uint2(M.key0, M.key1);
   unsigned *q = wq[threadIdx.x >> 5];
   int qn = 0;  // queued entries (warp-uniform)
+  const unsigned *__restrict__ hw = hits + (size_t)r * hit_words(cap_run);
   for (long long base = warp * 32;; base += nwarps * 32) {
     const bool more = base < nw;  // warp-uniform
     if (more) {
       const long long wt = base + lane;
-      const bool hit = wt < nw && mcc_entry_hits(seg[wt], M, te, ts, Er, nx, step, key, expl);
-      const unsigned hm = __ballot_sync(FULL, hit);
+      const unsigned hm = hw[base >> 5];  // bits past nw are zero
+      const bool hit = (hm >> lane) & 1u;
       if (hit) q[qn + __popc(hm & ((1u << lane) - 1u))] = (unsigned)wt;
       qn += __popc(hm);
       __syncwarp();
@@ -580,8 +627,10 @@ static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const Speci
   Mcc *m = c->mccs[mid];
   const int ntab = m->off[m->N];
   const size_t smem = M.staged ? (size_t)2 * ntab * sizeof(float) : 0;
-  if (smem > 48 * 1024)  // tables of up to kMaxTable nodes
+  if (smem > 48 * 1024) {  // tables of up to kMaxTable nodes
+    ISKRA_CUDA(c, cudaFuncSetAttribute(k_mcc_test, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ISKRA_CUDA(c, cudaFuncSetAttribute(k_mcc_collide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
   const uint2 key1 = make_uint2(M.key0, M.key1);
   if (phases != kMccCollideOnly) {
     ISKRA_CUDA(c, launch_pdl(k_zero_u64, (R + 255) / 256, 256, 0, st, nwork, R, kNworkStride));
@@ -589,10 +638,14 @@ static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const Speci
                              phases == kMccSelectAhead ? 1 : 0, work, nwork, cap_work, err));
   }
   if (phases == kMccSelectAhead) return ISKRA_OK;
+  unsigned *hits = reinterpret_cast<unsigned *>(work + (size_t)R * cap_work);
+  ISKRA_CUDA(c, launch_pdl(k_mcc_test, dim3(R == 1 ? c->num_sms * 8 : select_blocks, R), 256, smem, st, M, keys,
+                           E, nn, c->nx, d_step, (const MccWork *)work, (const unsigned long long *)nwork, cap_work,
+                           hits));
   const int collide_blocks = R == 1 ? c->num_sms * 8 : std::max(1, select_blocks / ISKRA_MCC_COLLIDE_SPLIT);
   ISKRA_CUDA(c, launch_pdl(k_mcc_collide, dim3(collide_blocks, R), 256, smem, st, src, prod, (int)(m->prod >= 0), M,
                            keys, counts, E, nn, c->nx, d_step, (const MccWork *)work, (const unsigned long long *)nwork,
-                           cap_work, err));
+                           cap_work, (const unsigned *)hits, err));
   return ISKRA_OK;
 }
 
@@ -652,7 +705,7 @@ int mcc_push_select(Ctx *c, int mid, double dt, PushSelect *S) {
   return ISKRA_OK;
 }
 
-size_t mcc_work_entry_bytes() { return sizeof(MccWork); }
+size_t mcc_work_bytes(size_t R, size_t cap) { return R * cap * sizeof(MccWork) + R * hit_words(cap) * sizeof(unsigned); }
 
 // Work list sized for the largest species; called where no stream capture can
 // be active (MCC set and species creation).
@@ -665,7 +718,7 @@ int ensure_mcc_work(Ctx *c) {
   cudaFree(c->mcc_work);
   c->mcc_work = nullptr;
   c->mcc_work_cap = 0;
-  ISKRA_CUDA(c, cudaMalloc(&c->mcc_work, (size_t)cap * sizeof(MccWork)));
+  ISKRA_CUDA(c, cudaMalloc(&c->mcc_work, mcc_work_bytes(1, (size_t)cap)));
   if (!c->mcc_nwork) ISKRA_CUDA(c, cudaMalloc(&c->mcc_nwork, sizeof(unsigned long long)));
   c->mcc_work_cap = (unsigned long long)cap;
   return ISKRA_OK;

@@ -287,6 +287,15 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
 #ifndef ISKRA_MCC_COLLIDE_SPLIT
 #define ISKRA_MCC_COLLIDE_SPLIT 2
 #endif
+// Launch shape of k_mcc_test (electron pass of a 128-run ensemble, ncu):
+// test blocks per run = the push's x SCALE8 / 8 -- 2x: 99 us, 1x: 106, 4x:
+// 98, 0.5x: 132; UNROLL 2 (two words per warp and round): no change.
+#ifndef ISKRA_MCC_TEST_UNROLL
+#define ISKRA_MCC_TEST_UNROLL 1
+#endif
+#ifndef ISKRA_MCC_TEST_SCALE8
+#define ISKRA_MCC_TEST_SCALE8 16
+#endif
 // Phase 2a over the work-list segment of run r = blockIdx.y: each warp
 // tests 32 entries (mcc_entry_hits) and stores their hit bits, one word per
 // 32 entries.  Apart from the collision code, the test needs few registers,
@@ -322,11 +331,19 @@ __global__ void __launch_bounds__(256) k_mcc_test(MccDev M, const uint2 *__restr
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const int lane = threadIdx.x & 31;
-  for (long long base = warp * 32; base < nw; base += nwarps * 32) {
-    const long long wt = base + lane;
-    const bool hit = wt < nw && mcc_entry_hits(seg[wt], M, te, ts, Er, nx, step, key, expl);
-    const unsigned hm = __ballot_sync(0xffffffffu, hit);
-    if (lane == 0) hw[base >> 5] = hm;
+  constexpr int U = ISKRA_MCC_TEST_UNROLL;  // words of 32 entries per warp and round
+  for (long long base = warp * 32 * U; base < nw; base += nwarps * 32 * U) {
+    bool hit[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const long long wt = base + 32 * u + lane;
+      hit[u] = wt < nw && mcc_entry_hits(seg[wt], M, te, ts, Er, nx, step, key, expl);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned hm = __ballot_sync(0xffffffffu, hit[u]);
+      if (lane == 0 && base + 32 * u < nw) hw[(base >> 5) + u] = hm;
+    }
   }
 }
 
@@ -639,7 +656,7 @@ static int queue_mcc_phases(Ctx *c, int mid, const MccDev &M, int R, const Speci
   }
   if (phases == kMccSelectAhead) return ISKRA_OK;
   unsigned *hits = reinterpret_cast<unsigned *>(work + (size_t)R * cap_work);
-  ISKRA_CUDA(c, launch_pdl(k_mcc_test, dim3(R == 1 ? c->num_sms * 8 : select_blocks, R), 256, smem, st, M, keys,
+  ISKRA_CUDA(c, launch_pdl(k_mcc_test, dim3(R == 1 ? c->num_sms * 8 : std::max(1, select_blocks * ISKRA_MCC_TEST_SCALE8 / 8), R), 256, smem, st, M, keys,
                            E, nn, c->nx, d_step, (const MccWork *)work, (const unsigned long long *)nwork, cap_work,
                            hits));
   const int collide_blocks = R == 1 ? c->num_sms * 8 : std::max(1, select_blocks / ISKRA_MCC_COLLIDE_SPLIT);

@@ -97,15 +97,30 @@ __global__ void k_runs_state(SpeciesState *st, int R, long long cap, int op) {
   }
 }
 
-__global__ void k_ens_step_begin(unsigned long long *d_step) {
+// Several of the step's per-run bookkeeping operations in one launch (each a
+// few bytes per run; as separate launches they cost more than their work):
+// the step counter, state transitions of up to kRunsOpsMax species states in
+// order, and zeroed work-list counters.
+constexpr int kRunsOpsMax = 8, kRunsZeroMax = 4;
+struct RunsOps {
+  unsigned long long *d_step;  // incremented when not null
+  int n, nzero;
+  SpeciesState *st[kRunsOpsMax];
+  long long cap[kRunsOpsMax];
+  int op[kRunsOpsMax];
+  unsigned long long *zero[kRunsZeroMax];  // R counters, kNworkStride apart
+};
+__global__ void k_runs_ops(RunsOps O, int R) {
   pdl_wait();
-  *d_step += 1ull;
-}
-
-__global__ void k_zero_u64_runs(unsigned long long *p, int n) {
-  pdl_wait();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[(size_t)i * kNworkStride] = 0ull;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (O.d_step && r == 0) *O.d_step += 1ull;
+  if (r >= R) return;
+  for (int i = 0; i < O.n; i++) {
+    SpeciesState &s = O.st[i][r];
+    if (O.op[i] == kRunsAppendBegin) s.np_new = s.np;
+    else if (O.op[i] == kRunsAppendEnd) s.np = s.np_new > O.cap[i] ? O.cap[i] : s.np_new;
+  }
+  for (int z = 0; z < O.nzero; z++) O.zero[z][(size_t)r * kNworkStride] = 0ull;
 }
 
 // Drop discarded particles of every run: live particles move to the other
@@ -166,23 +181,52 @@ static int ens_queue_step(Ens *e, double dt) {
   cudaStream_t st = c->stream;
   const int R = e->R, bpr = ens_blocks_per_run(e);
   const int rb = (R + 127) / 128;
-  ENS_CUDA(e, launch_pdl(k_ens_step_begin, 1, 1, 0, st, e->d_step));
+  // bookkeeping gathered into one k_runs_ops launch before each MCC set and
+  // before the pushes
+  RunsOps O{};
+  O.d_step = e->d_step;
+  auto op = [&](int sp, int kind) -> int {
+    if (O.n == kRunsOpsMax) {
+      ENS_CUDA(e, launch_pdl(k_runs_ops, rb, 128, 0, st, O, R));
+      O = RunsOps{};
+    }
+    O.st[O.n] = e->sp[sp].st;
+    O.cap[O.n] = e->sp[sp].cap;
+    O.op[O.n++] = kind;
+    return ISKRA_OK;
+  };
+  auto flush = [&]() -> int {
+    if (O.d_step || O.n || O.nzero) ENS_CUDA(e, launch_pdl(k_runs_ops, rb, 128, 0, st, O, R));
+    O = RunsOps{};
+    return ISKRA_OK;
+  };
   for (int m = 0; m < (int)e->mcc.size(); m++) {
     const int src = mcc_src(c, m), prod = mcc_prod(c, m);
-    ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[src].st, R, e->sp[src].cap, (int)kRunsAppendBegin));
-    if (prod >= 0)
-      ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[prod].st, R, e->sp[prod].cap, (int)kRunsAppendBegin));
-    int rc = launch_mcc_runs(c, m, dt, R, e->sp[src].views, prod >= 0 ? e->sp[prod].views : e->sp[src].views,
+    int rc = op(src, kRunsAppendBegin);
+    if (!rc && prod >= 0) rc = op(prod, kRunsAppendBegin);
+    if (!rc) rc = flush();
+    if (rc) return rc;
+    rc = launch_mcc_runs(c, m, dt, R, e->sp[src].views, prod >= 0 ? e->sp[prod].views : e->sp[src].views,
                              e->mcc[m].keys, e->mcc[m].counts, e->E32, e->nn, bpr, e->mcc[m].work, e->mcc[m].nwork,
                              e->work_cap, e->d_step, e->d_err, st, e->mcc[m].folded ? kMccCollideOnly : kMccBoth);
     if (rc) return ens_err(e, rc, c->err);
-    ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[src].st, R, e->sp[src].cap, (int)kRunsAppendEnd));
-    if (prod >= 0)
-      ENS_CUDA(e, launch_pdl(k_runs_state, rb, 128, 0, st, e->sp[prod].st, R, e->sp[prod].cap, (int)kRunsAppendEnd));
+    rc = op(src, kRunsAppendEnd);
+    if (!rc && prod >= 0) rc = op(prod, kRunsAppendEnd);
+    if (rc) return rc;
   }
   // the pushes make the folded sets' lists for the next step
-  for (int m = 0; m < (int)e->mcc.size(); m++)
-    if (e->mcc[m].folded) ENS_CUDA(e, launch_pdl(k_zero_u64_runs, rb, 128, 0, st, e->mcc[m].nwork, R));
+  for (int m = 0; m < (int)e->mcc.size(); m++) {
+    if (!e->mcc[m].folded) continue;
+    if (O.nzero == kRunsZeroMax) {
+      const int rc = flush();
+      if (rc) return rc;
+    }
+    O.zero[O.nzero++] = e->mcc[m].nwork;
+  }
+  {
+    const int rc = flush();
+    if (rc) return rc;
+  }
   for (int s = 0; s < (int)e->sp.size(); s++) {
     PushSelect S{};
     bool sel = false;

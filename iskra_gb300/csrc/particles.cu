@@ -631,19 +631,17 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
                                                                           const float2 *__restrict__ E2, int nnode,
                                                                           PushParams P, int *err, PushSelect S) {
   pdl_wait();
-  __shared__ PushShared sh;
+  extern __shared__ __align__(16) unsigned char push_runs_smem[];
+  PushShared &sh = *reinterpret_cast<PushShared *>(push_runs_smem);
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
   const int r = blockIdx.y;
   const SpeciesDev s = runs[r];
   const int nx = P.nx, cx = P.nx - 1, cy = P.ny - 1;
   E2 += (size_t)r * nnode;
-  for (int t = threadIdx.x; t < cx * cy; t += blockDim.x) {
-    const int i = t % cx, j = t / cx;
-    const int n0 = i + nx * j;
-    cell_record(E2, n0, nx, sh.e[2 * t], sh.e[2 * t + 1]);
-    window_clear(sh, t);
-  }
+  // the window is the run's whole grid: its nodes are the grid's
+  for (int t = threadIdx.x; t < nnode; t += blockDim.x) sh.ne[t] = __ldg(E2 + t);
+  for (int t = threadIdx.x; t < cx * cy; t += blockDim.x) window_clear(sh, t);
   __syncthreads();
   const long long np = s.st->np;
   const int cur = s.st->cur;
@@ -657,37 +655,44 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   const float expl = __expf(-S.lam);  // as k_mcc_select and k_mcc_collide form it
   MccWork *__restrict__ seg = SEL ? S.work + (size_t)r * S.cap_run : nullptr;
   const long long warp = (long long)blockIdx.x * nwb + wib, nwarps = (long long)gridDim.x * nwb;
-  // the next iteration's records are loaded before this one is pushed (two
-  // iterations in flight per warp: the loop was bound by the load latency)
-  float4 an = make_float4(0.f, 0.f, 0.f, 0.f);
-  float2 bn = make_float2(0.f, 0.f);
-  uint32_t idn = 0;  // the identifier, which the selection draw needs
+  // The records stream through the warp's ring of kEnsStages shared-memory
+  // stages filled by cp.async: two later iterations' records are in flight
+  // while one is pushed (the loop is bound by the load latency); each lane
+  // reads back only its own copies.  The identifier (for the selection draw)
+  // is loaded one iteration ahead.  Slots of later iterations are no slots
+  // this iteration's push writes.
+  const long long stride = nwarps * 32;
+#pragma unroll
+  for (int d = 0; d < kEnsStages - 1; d++) {
+    const long long q = warp * 32 + d * stride + lane;
+    if (q < np) cp_async_record(&sh.ra[wib][d][lane], &sh.rb[wib][d][lane], xv + q, zc + q);
+    cp_async_commit();
+  }
+  uint32_t idn = 0;
+  if (SEL && warp * 32 + lane < np) idn = ids[warp * 32 + lane];
   // A warp's selected entries gather in its shared-memory buffer and go to
   // the run's list 32 at a time: one reservation (an atomic on the run's
   // counter, which every warp of the run shares) per 32 entries instead of
   // one per iteration, and 1 KB contiguous stores.  nbuf: entries buffered
   // (warp-uniform, < 32 between iterations).
-  __shared__ MccWork wbuf[8][64];
+  MccWork(&wbuf)[8][64] = sh.wbuf;
   int nbuf = 0;
-  if (warp * 32 + lane < np) {
-    an = ld_stream(xv + warp * 32 + lane);
-    bn = ld_stream(zc + warp * 32 + lane);
-    if (SEL) idn = ids[warp * 32 + lane];
-  }
-  for (long long base = warp * 32; base < np; base += nwarps * 32) {
+  int st = 0;  // ring stage of the current iteration
+  for (long long base = warp * 32; base < np; base += stride) {
     const long long p = base + lane;
     const bool v = p < np;
-    const float4 a = an;
-    const float2 b = bn;
-    const uint32_t idc = idn;
     {
-      const long long pn = p + nwarps * 32;  // a slot no push of this iteration writes
-      if (pn < np) {
-        an = ld_stream(xv + pn);
-        bn = ld_stream(zc + pn);
-        if (SEL) idn = ids[pn];
-      }
+      const long long q = p + (kEnsStages - 1) * stride;
+      const int sn = st == 0 ? kEnsStages - 1 : st - 1;  // the stage read one iteration ago
+      if (q < np) cp_async_record(&sh.ra[wib][sn][lane], &sh.rb[wib][sn][lane], xv + q, zc + q);
+      cp_async_commit();
     }
+    cp_async_wait<kEnsStages - 1>();  // this lane's copies of the current stage have landed
+    const float4 a = sh.ra[wib][st][lane];
+    const float2 b = sh.rb[wib][st][lane];
+    st = st + 1 == kEnsStages ? 0 : st + 1;
+    const uint32_t idc = idn;
+    if (SEL && p + stride < np) idn = ids[p + stride];
     float4 na;
     float2 nb;
     push_warp<true, MX, MY, true>(s, xv, zc, p, v, a, b, E2, sh, 0, 0, cx, cy, P, ab, flags, SEL ? &na : nullptr,
@@ -711,6 +716,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
     }
   }
   if (SEL && nbuf) flush_entries(wbuf[wib], nbuf, S.nwork + (size_t)r * kNworkStride, seg, S.cap_run, flags);
+  cp_async_wait<0>();  // no copy is in flight when the block leaves the ring
   __syncthreads();
   const int wn = cx + 1;
   for (int t = threadIdx.x; t < (cx + 1) * (cy + 1); t += blockDim.x) {
@@ -764,7 +770,8 @@ int launch_push_runs(Ctx *c, int sid, const SpeciesDev *runs, int R, const float
     auto kern = sel ? k_push_runs<MX, MY, true> : k_push_runs<MX, MY, false>;                                   \
     cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,                                  \
                          (int)cudaSharedmemCarveoutMaxShared);                                                  \
-    ISKRA_CUDA(c, launch_pdl(kern, grid, 256, 0, st, runs, E2, nnode, P, err, S));                             \
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PushShared));          \
+    ISKRA_CUDA(c, launch_pdl(kern, grid, 256, sizeof(PushShared), st, runs, E2, nnode, P, err, S));            \
     return ISKRA_OK;                                                                                            \
   }
   ISKRA_PUSH_RUNS_CASE(0, 0) ISKRA_PUSH_RUNS_CASE(0, 1) ISKRA_PUSH_RUNS_CASE(0, 2)

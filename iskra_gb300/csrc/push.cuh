@@ -230,10 +230,19 @@ constexpr int kEnsWinCells = kEnsWin * kEnsWin;
 enum { kMomN, kMomU1, kMomU0, kMomV1, kMomV0, kMomQ2, kMomQ1, kMomQ0, kMoms };
 
 // Shared memory of an ensemble-run block: E records of the run's cells.
+// Dynamic shared memory of an ensemble push block (53 KB: 4 blocks per SM):
+// per warp a ring of kEnsStages record stages filled by cp.async (two warp
+// iterations in flight while the third is pushed), the selection buffer,
+// E at the window's nodes, the deposit moments.
+constexpr int kEnsStages = 3;
+constexpr int kEnsWinNodes = 2 * kEnsWinCells + 2;  // most nodes of a window of at most kEnsWinCells cells
 struct PushShared {
   static constexpr int kWinCells = kEnsWinCells;
-  float4 e[2 * kWinCells];        // E records of the window cells
-  unsigned mom[kMoms][kWinCells];  // deposit moments of the window cells
+  float4 ra[8][kEnsStages][32];     // staged records {hx, hy, vx, vy}
+  float2 rb[8][kEnsStages][32];     // staged records {vz, cell}
+  MccWork wbuf[8][64];              // selected work-list entries, per warp
+  float2 ne[kEnsWinNodes];          // E at the window's nodes (row stride: cells per row + 1)
+  unsigned mom[kMoms][kWinCells];   // deposit moments of the window cells
 };
 
 // Shared memory of a tile block: the warps' record rings, E at the window's
@@ -348,9 +357,10 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 
 // E records (corner fields) of window cell (la, lb)
 __device__ __forceinline__ void win_record(const PushShared &sh, int la, int lb, int ww, float4 &r0, float4 &r1) {
-  const int w = la + ww * lb;
-  r0 = sh.e[2 * w];
-  r1 = sh.e[2 * w + 1];
+  const int n = la + (ww + 1) * lb;
+  const float2 a = sh.ne[n], b = sh.ne[n + 1], c = sh.ne[n + ww + 1], d = sh.ne[n + ww + 2];
+  r0 = make_float4(a.x, a.y, b.x, b.y);
+  r1 = make_float4(c.x, c.y, d.x, d.y);
 }
 // track! flag of window cell w (ensemble blocks run without a tracker)
 __device__ __forceinline__ bool win_tracked(const PushShared &, int) { return false; }

@@ -111,23 +111,29 @@ constexpr int kMgBx = 32, kMgBy = 8;
 
 __device__ __forceinline__ int wrap_idx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+// (A x)_k with x(m) the iterate at node m
+template <bool FIVE, class X>
+__device__ __forceinline__ float apply9x(const float *__restrict__ coef, X x, int k, int i, int j, int nx, int ny,
+                                         int n) {
+  const int iw = wrap_idx(i - 1, nx), ie = wrap_idx(i + 1, nx);
+  const int rs = nx * wrap_idx(j - 1, ny), rc = nx * j, rn = nx * wrap_idx(j + 1, ny);
+  float a = coef[(size_t)4 * n + k] * x(k);
+  a = fmaf(coef[(size_t)1 * n + k], x(i + rs), a);
+  a = fmaf(coef[(size_t)3 * n + k], x(iw + rc), a);
+  a = fmaf(coef[(size_t)5 * n + k], x(ie + rc), a);
+  a = fmaf(coef[(size_t)7 * n + k], x(i + rn), a);
+  if (!FIVE) {
+    a = fmaf(coef[(size_t)0 * n + k], x(iw + rs), a);
+    a = fmaf(coef[(size_t)2 * n + k], x(ie + rs), a);
+    a = fmaf(coef[(size_t)6 * n + k], x(iw + rn), a);
+    a = fmaf(coef[(size_t)8 * n + k], x(ie + rn), a);
+  }
+  return a;
+}
 template <bool FIVE>
 __device__ __forceinline__ float apply9(const float *__restrict__ coef, const float *__restrict__ x, int k, int i,
                                         int j, int nx, int ny, int n) {
-  const int iw = wrap_idx(i - 1, nx), ie = wrap_idx(i + 1, nx);
-  const int rs = nx * wrap_idx(j - 1, ny), rc = nx * j, rn = nx * wrap_idx(j + 1, ny);
-  float a = coef[(size_t)4 * n + k] * x[k];
-  a = fmaf(coef[(size_t)1 * n + k], x[i + rs], a);
-  a = fmaf(coef[(size_t)3 * n + k], x[iw + rc], a);
-  a = fmaf(coef[(size_t)5 * n + k], x[ie + rc], a);
-  a = fmaf(coef[(size_t)7 * n + k], x[i + rn], a);
-  if (!FIVE) {
-    a = fmaf(coef[(size_t)0 * n + k], x[iw + rs], a);
-    a = fmaf(coef[(size_t)2 * n + k], x[ie + rs], a);
-    a = fmaf(coef[(size_t)6 * n + k], x[iw + rn], a);
-    a = fmaf(coef[(size_t)8 * n + k], x[ie + rn], a);
-  }
-  return a;
+  return apply9x<FIVE>(coef, [&](int m) { return x[m]; }, k, i, j, nx, ny, n);
 }
 
 // One damped-Jacobi sweep at node (i, j): xo = xi + dinv (b - A xi).
@@ -157,6 +163,23 @@ __device__ __forceinline__ void smooth_node(const float *__restrict__ coef, cons
   const float v = dk != 0.f ? xi[k] + dk * (b[k] - ax) : 0.f;
   if (z64) z64[k] = (double)v;
   else xo[k] = v;
+}
+
+// The first two sweeps at node (i, j): the first from x = 0 is pointwise
+// (x0 = dinv b), so the second forms x0 at the stencil's nodes itself --
+// the same products as two sweeps, without the first one's launch and its
+// pass over x.  r64 given: level 0, b = (float) r64 (also stored in b).
+template <bool FIVE>
+__device__ __forceinline__ void smooth01_node(const float *__restrict__ coef, const float *__restrict__ dinv,
+                                              float *__restrict__ xo, float *__restrict__ b, int nx, int ny, int i,
+                                              int j, const double *__restrict__ r64) {
+  const int n = nx * ny, k = i + nx * j;
+  auto bval = [&](int m) { return r64 ? (float)r64[m] : b[m]; };
+  auto x0 = [&](int m) { return __fmul_rn(dinv[m], bval(m)); };  // as the first sweep stores it
+  const float dk = dinv[k], bk = bval(k);
+  if (r64) b[k] = bk;
+  const float ax = apply9x<FIVE>(coef, x0, k, i, j, nx, ny, n);
+  xo[k] = dk != 0.f ? fmaf(dk, bk - ax, __fmul_rn(dk, bk)) : 0.f;
 }
 
 // r = b - A x at node (i, j) of the correction's nodes
@@ -250,6 +273,17 @@ __global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_smooth(const float *__rest
   if (*skip) return;
   const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
   if (i < nx && j < ny) smooth_node<FIVE>(coef, dinv, xi, xo, b, nx, ny, i, j, r64, z64);
+}
+
+template <bool FIVE>
+__global__ void __launch_bounds__(kMgBx * kMgBy) k_mg_smooth01(const float *__restrict__ coef,
+                                                               const float *__restrict__ dinv, float *__restrict__ xo,
+                                                               float *__restrict__ b, int nx, int ny, const int *skip,
+                                                               const double *__restrict__ r64) {
+  pdl_wait();
+  if (*skip) return;
+  const int i = blockIdx.x * kMgBx + threadIdx.x, j = blockIdx.y * kMgBy + threadIdx.y;
+  if (i < nx && j < ny) smooth01_node<FIVE>(coef, dinv, xo, b, nx, ny, i, j, r64);
 }
 
 template <bool FIVE>
@@ -603,10 +637,18 @@ int mg_queue_cycle(Ctx *c, Mg *m, const double *r, double *z, const int *skip) {
   const int lb = m->bottom ? m->bottom : L - 1;  // first level not run by per-level kernels
   for (int l = 0; l < lb; l++) {
     MgLevel &D = m->lv[l];
-    for (int s = 0; s < kMgSweeps; s++) {
-      const float *src = s == 0 ? nullptr : ((s & 1) ? D.x2 : D.x);
+    // the first two sweeps in one launch (into x), then the rest alternating
+    const double *r64 = l == 0 ? r : nullptr;
+    if (D.five)
+      ISKRA_CUDA(c, launch_pdl(k_mg_smooth01<true>, mg_grid2(D.nx, D.ny), t, 0, st, (const float *)D.coef,
+                               (const float *)D.dinv, D.x, D.b, D.nx, D.ny, skip, r64));
+    else
+      ISKRA_CUDA(c, launch_pdl(k_mg_smooth01<false>, mg_grid2(D.nx, D.ny), t, 0, st, (const float *)D.coef,
+                               (const float *)D.dinv, D.x, D.b, D.nx, D.ny, skip, r64));
+    for (int s = 2; s < kMgSweeps; s++) {
+      const float *src = (s & 1) ? D.x2 : D.x;
       float *dst = (s & 1) ? D.x : D.x2;
-      const int rc = mg_smooth(c, D, src, dst, skip, (l == 0 && s == 0) ? r : nullptr, nullptr);
+      const int rc = mg_smooth(c, D, src, dst, skip, nullptr, nullptr);
       if (rc) return rc;
     }
     if (D.five)

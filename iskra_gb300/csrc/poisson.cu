@@ -2557,6 +2557,8 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
     __syncthreads();
   }
   // inverse DFT (Hermitian spectrum) and update of the free rows
+  const bool pow2N = (N & (N - 1)) == 0;
+  const double invN = 1.0 / N;
   for (int k = threadIdx.x; k < nn; k += blockDim.x) {
     if (op.cls[k] & kFixedBit) continue;
     const int j = k / nx, i = k - j * nx;
@@ -2568,7 +2570,7 @@ __global__ void __launch_bounds__(256) k_field_runs(OpView op, FieldRuns F) {
       const int q = (j * m) % N;
       v += re * twc[q] - im * tws[q];
     }
-    xs[k] += v / N;
+    xs[k] += pow2N ? v * invN : v / N;  // 1/N exact for a power of two
   }
   __syncthreads();
   // ϕ and E = -∇ϕ

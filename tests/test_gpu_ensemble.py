@@ -33,9 +33,10 @@ def initial_state(seed, n0):
     return maxwellian(n0, 4.0, ME), maxwellian(n0, 0.03, M_AR)
 
 
-def configure(lib, n0, amp, w):
+def configure(lib, n0, amp, w, mcc=True):
     """A single-run context set up like problem/11_rf_discharge.jl (driven
-    Dirichlet electrode, grounded electrode, e- and Ar+ MCC)."""
+    Dirichlet electrode, grounded electrode, e- and Ar+ MCC unless mcc is
+    False)."""
     from iskra_gb300.device import Context
     ctx = Context(NX, NY, DX, DX)
     se = ctx.species_create(-QE, ME, w, 4 * n0)
@@ -52,6 +53,8 @@ def configure(lib, n0, amp, w):
     ctx.apply_dirichlet(right, 0.0)
     ctx.drive_dirichlet(left, amp, FREQ)
     assert ctx.set_method(0) == 0
+    if not mcc:
+        return ctx, se, si, None, None
     eps, el, ex, iz, cx = argon_tables()
     gas_n = np.full((NX, NY), 3.0 / (KB * 300.0))
     me_, _ = ctx.mcc_create(se, [(lib.MCC_ELASTIC_ISOTROPIC, 0.0, eps, el), (lib.MCC_EXCITATION, 11.5, eps, ex),
@@ -80,10 +83,10 @@ def eedf_compatible(ve_a, ve_b):
     return chi2_contingency(np.array([mg, mo]))[1]
 
 
-def make_ensemble(lib, R, n0, amps):
+def make_ensemble(lib, R, n0, amps, mcc=True):
     from iskra_gb300.device import Ensemble
     w = 1e15 * GAP * DX / n0
-    tmpl, se, si, me_, mi_ = configure(lib, n0, amps[0], w)
+    tmpl, se, si, me_, mi_ = configure(lib, n0, amps[0], w, mcc)
     ens = Ensemble(tmpl, R, 4 * n0)
     ens.set_seeds([1000 + r for r in range(R)])
     ens.set_drive_amplitude(0, np.asarray(amps, float))
@@ -94,8 +97,8 @@ def make_ensemble(lib, R, n0, amps):
     return tmpl, ens, states, (se, si, me_, mi_), w
 
 
-def single_run(lib, n0, amp, w, state, seed, steps):
-    ctx, se, si, me_, mi_ = configure(lib, n0, amp, w)
+def single_run(lib, n0, amp, w, state, seed, steps, mcc=True):
+    ctx, se, si, me_, mi_ = configure(lib, n0, amp, w, mcc)
     (xe, ve), (xi, vi) = state
     ctx.upload(se, xe, ve)
     ctx.upload(si, xi, vi)
@@ -142,6 +145,42 @@ def test_ensemble_first_steps_match_single_runs(lib):
         assert np.array_equal(ids_s[ks][o_s], ids_e[ke][o_e])
         assert np.allclose(xs[ks][o_s], xe[ke][o_e], rtol=0, atol=1e-6 * GAP)
         assert np.allclose(vs[ks][o_s], ve[ke][o_e], rtol=1e-5, atol=1.0)
+        ctx.close()
+    ens.close()
+    tmpl.close()
+
+
+def test_ensemble_without_mcc_matches_single_runs(lib):
+    """A collisionless ensemble (the push without the folded MCC selection):
+    after one step ρ and every particle equal the single run's bit for bit;
+    after three steps (the pushes read E from the two solvers' ϕ) positions
+    and velocities agree to FP32 rounding."""
+    R, n0 = 3, 4000
+    amps = [120.0, 260.0, 480.0]
+    tmpl, ens, states, (se, si, _, _), w = make_ensemble(lib, R, n0, amps, mcc=False)
+    ens.step(DT, 1)
+    ens.sync()
+    for r in range(R):
+        ctx, _ = single_run(lib, n0, amps[r], w, states[r], 1000 + r, 1, mcc=False)
+        assert np.array_equal(ctx.field(lib.FIELD_RHO), ens.field(r, lib.FIELD_RHO)), f"run {r}: ρ differs"
+        for s in (se, si):
+            xs, vs, ids_s = ctx.download(s)
+            xe, ve, ids_e = ens.download(r, s)
+            o_s, o_e = np.argsort(ids_s), np.argsort(ids_e)
+            assert np.array_equal(ids_s[o_s], ids_e[o_e])
+            assert np.array_equal(xs[o_s], xe[o_e]) and np.array_equal(vs[o_s], ve[o_e])
+        ctx.close()
+    ens.step(DT, 2)
+    ens.sync()
+    for r in range(R):
+        ctx, _ = single_run(lib, n0, amps[r], w, states[r], 1000 + r, 3, mcc=False)
+        for s in (se, si):
+            xs, vs, ids_s = ctx.download(s)
+            xe, ve, ids_e = ens.download(r, s)
+            o_s, o_e = np.argsort(ids_s), np.argsort(ids_e)
+            assert np.array_equal(ids_s[o_s], ids_e[o_e])
+            assert np.allclose(xs[o_s], xe[o_e], rtol=0, atol=1e-6 * GAP)
+            assert np.allclose(vs[o_s], ve[o_e], rtol=1e-5, atol=1.0)
         ctx.close()
     ens.close()
     tmpl.close()

@@ -284,3 +284,70 @@ def test_ensemble_runs_match_oracle(orc, lib):
         assert abs(ph[0, 0] - po.phi[0, 0]) <= 1e-9 * amps[r]  # the driven electrode, V((n-2)Δt)
     ens.close()
     tmpl.close()
+
+
+def test_ensemble_field_solve_with_complex_modes(lib):
+    """The ensemble's direct field solve (DFT along y + cyclic reduction per
+    Fourier mode) on a 41 x 8 grid, y periodic (N = 8: modes 0..4, three of
+    them complex): after one step ρ equals the single run's bit for bit and
+    ϕ agrees to 1e-9 of its range, run by run."""
+    from iskra_gb300.device import Context, Ensemble
+    nx, ny, gap = 41, 8, 0.01
+    dx = gap / (nx - 1)
+    n0, R = 3000, 2
+    amps = [150.0, 400.0]
+    w = 1e15 * gap * dx * (ny - 1) / n0
+
+    def context(amp):
+        ctx = Context(nx, ny, dx, dx)
+        se = ctx.species_create(-QE, ME, w, 4 * n0)
+        si = ctx.species_create(QE, M_AR, w, 4 * n0)
+        for s in (se, si):
+            ctx.set_boundary(s, lib.BND_DISCARD, lib.BND_WRAP)
+        ctx.poisson_create(EPS0)
+        ctx.apply_periodic(1)
+        left = np.zeros((nx, ny), bool)
+        left[0, :] = True
+        right = np.zeros((nx, ny), bool)
+        right[-1, :] = True
+        ctx.apply_dirichlet(left, 0.0)
+        ctx.apply_dirichlet(right, 0.0)
+        ctx.drive_dirichlet(left, amp, FREQ)
+        assert ctx.set_method(0) == 0
+        return ctx, se, si
+
+    rng = np.random.default_rng(8)
+    states = []
+    for r in range(R):
+        st = []
+        for T, m in ((4.0, ME), (0.03, M_AR)):
+            x = np.asfortranarray(np.column_stack([rng.uniform(0, gap, n0), rng.uniform(0, (ny - 1) * dx, n0)]))
+            v = np.asfortranarray(rng.standard_normal((n0, 3)) * np.sqrt(2 * T * QE / m))
+            st.append((x, v))
+        states.append(st)
+    tmpl, se, si = context(amps[0])
+    ens = Ensemble(tmpl, R, 4 * n0)
+    ens.set_drive_amplitude(0, np.asarray(amps, float))
+    for r in range(R):
+        for s, (x, v) in zip((se, si), states[r]):
+            ens.upload(r, s, x, v)
+    ens.step(DT, 1)
+    ens.sync()
+    for r in range(R):
+        ctx, se1, si1 = context(amps[r])
+        for s, (x, v) in zip((se1, si1), states[r]):
+            ctx.upload(s, x, v)
+        ctx.step(DT, 1, seed=1, rtol=1e-12)
+        ctx.sync()
+        assert np.array_equal(ctx.field(lib.FIELD_RHO), ens.field(r, lib.FIELD_RHO)), f"run {r}: ρ differs"
+        ps, pe = ctx.field(lib.FIELD_PHI), ens.field(r, lib.FIELD_PHI)
+        assert np.max(np.abs(ps - pe)) <= 1e-9 * max(1.0, np.max(np.abs(ps))), f"run {r}: ϕ differs"
+        for s in (se1, si1):
+            xs, vs, ids_s = ctx.download(s)
+            xe, ve, ids_e = ens.download(r, s)
+            o_s, o_e = np.argsort(ids_s), np.argsort(ids_e)
+            assert np.array_equal(ids_s[o_s], ids_e[o_e])
+            assert np.array_equal(xs[o_s], xe[o_e]) and np.array_equal(vs[o_s], ve[o_e])
+        ctx.close()
+    ens.close()
+    tmpl.close()

@@ -596,20 +596,6 @@ int launch_sort(Ctx *c, int sid) {
   return ISKRA_OK;
 }
 
-// ---------------------------------------------------------------------------
-// ensemble push: run r = blockIdx.y; every block of a run stages the run's
-// whole E grid (cx*cy <= kEnsWinCells cells), pushes a grid-stride share of the
-// run's particles (any order), deposits into shared memory and adds the
-// node sums to the run's accumulator.
-// ---------------------------------------------------------------------------
-//
-// SEL: the species is the source of an MCC set, and the push also makes the
-// set's work list for the next step -- each pushed particle that stays draws
-// its selection count for step + 1 from its own stream (the draw
-// k_mcc_select would make at the start of that step: nothing changes the
-// particle in between) and, when selected, its new record goes to the run's
-// list.  The next step's collision pass then starts without a selection pass
-// over all particles.
 // Appends a warp's n <= 32 buffered work-list entries to its run's list
 // (counter cnt, segment seg of cap entries).
 __device__ __forceinline__ void flush_entries(const MccWork *buf, int n, unsigned long long *cnt,
@@ -626,6 +612,20 @@ __device__ __forceinline__ void flush_entries(const MccWork *buf, int n, unsigne
   __syncwarp();  // buf may be written again
 }
 
+// ---------------------------------------------------------------------------
+// ensemble push: run r = blockIdx.y; every block of a run stages the run's
+// whole E grid (cx*cy <= kEnsWinCells cells), pushes a grid-stride share of the
+// run's particles (any order), deposits into shared memory and adds the
+// node sums to the run's accumulator.
+// ---------------------------------------------------------------------------
+//
+// SEL: the species is the source of an MCC set, and the push also makes the
+// set's work list for the next step -- each pushed particle that stays draws
+// its selection count for step + 1 from the hash of (set key, step + 1, id)
+// (the draw k_mcc_select would make at the start of that step: nothing
+// changes the particle in between) and, when selected, its new record goes
+// to the run's list.  The next step's collision pass then starts without a selection pass
+// over all particles.
 template <int MX, int MY, bool SEL>
 __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(const SpeciesDev *__restrict__ runs,
                                                                           const float2 *__restrict__ E2, int nnode,
@@ -657,7 +657,7 @@ __global__ void __launch_bounds__(256, ISKRA_PUSH_RUNS_MIN_BLOCKS) k_push_runs(c
   const long long warp = (long long)blockIdx.x * nwb + wib, nwarps = (long long)gridDim.x * nwb;
   // The records stream through the warp's ring of kEnsStages shared-memory
   // stages filled by cp.async: two later iterations' records are in flight
-  // while one is pushed (the loop is bound by the load latency); each lane
+  // while one is pushed (the loop was bound by the load latency); each lane
   // reads back only its own copies.  The identifier (for the selection draw)
   // is loaded one iteration ahead.  Slots of later iterations are no slots
   // this iteration's push writes.

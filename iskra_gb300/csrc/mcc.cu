@@ -272,18 +272,18 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
 // Phase 2 over the work list segment of run r = blockIdx.y: the run's stores
 // src[r] / prod[r], node field E + r nn, key keys[r] (or M's key for a single
 // context), counters counts_runs + r N (or M.counts).
-// Blocks of 256 threads per SM asked of the register allocator: 3 (80
-// registers, a few bytes spilled) against 2 (102 registers): 245 against
-// 283 us per electron pass of a 128-run ensemble, which waits on the
-// dependent loads of each entry (its node's gas density and field).
+// Blocks of 256 threads per SM asked of the register allocator for the
+// collision kernel: 3 (80 registers) against 2 (102 registers) -- measured
+// when the kernel also tested every entry: 245 against 283 us per electron
+// pass of a 128-run ensemble.
 #ifndef ISKRA_MCC_COLLIDE_MIN_BLOCKS
 #define ISKRA_MCC_COLLIDE_MIN_BLOCKS 3
 #endif
-// Ensembles: collision-pass blocks per run = the push's blocks per run / this.
-// A block's setup (run views, step, key) is a chain of dependent loads, and
-// with the push's count each warp ran only ~4 rounds of 32 entries: 2 gives
-// 218 against 241 us per electron pass of a 128-run ensemble (4: 252, 8: 389,
-// the largest runs' blocks then set the pass's length).
+// Ensembles: collision-kernel blocks per run = the push's blocks per run /
+// this.  A block's setup (run views, step, key) is a chain of dependent
+// loads: with the testing still in this kernel, 2 gave 218 against 241 us
+// per electron pass of a 128-run ensemble (4: 252, 8: 389, the largest runs'
+// blocks then set the pass's length); after the split, 4 and 8 gave no gain.
 #ifndef ISKRA_MCC_COLLIDE_SPLIT
 #define ISKRA_MCC_COLLIDE_SPLIT 2
 #endif

@@ -168,6 +168,24 @@ struct Stream {
     float rad = sqrtf(-2.0f * logf(a));
     return rad * cospif(2.0f * b);
   }
+  __device__ void normal2(float &n0, float &n1) {  // Box-Muller, both of the pair
+    float a = next();
+    const float b = next();
+    a = fmaxf(a, 1.0e-12f);
+    const float rad = sqrtf(-2.0f * logf(a));
+    float s, c;
+    sincospif(2.0f * b, &s, &c);
+    n0 = rad * c;
+    n1 = rad * s;
+  }
+  // three independent normal draws (a Box-Muller pair and one of a second)
+  __device__ void normal3(float v[3], float scale) {
+    normal2(v[0], v[1]);
+    v[2] = normal();
+    v[0] *= scale;
+    v[1] *= scale;
+    v[2] *= scale;
+  }
 };
 
 // The MCC random stream of one particle in one step (mcc.cu): Philox keyed by

@@ -473,7 +473,8 @@ __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_colli
         if (M.nu && !keys) atomicAdd(M.nu + (size_t)node * M.N + k, 1u);
         const int type = M.types[k];
         if (type <= ISKRA_MCC_INELASTIC_BACKWARD) {
-          float tv[3] = {R.normal() * M.vth_t, R.normal() * M.vth_t, R.normal() * M.vth_t};
+          float tv[3];
+          R.normal3(tv, M.vth_t);
           float vr[3], wv[3], dir[3];
           for (int c = 0; c < 3; c++) {
             vr[c] = v[c] - tv[c];
@@ -514,7 +515,7 @@ __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_colli
           u2 = R.next();
           diffuse_reflection(v, u1, u2, dir);
           for (int c = 0; c < 3; c++) cv[c] = v2 * dir[c];
-          for (int c = 0; c < 3; c++) tv_ion[c] = R.normal() * M.vth_t;
+          R.normal3(tv_ion, M.vth_t);
           ion_child = true;
         }
       }

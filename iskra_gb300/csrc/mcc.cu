@@ -53,6 +53,7 @@ struct MccDev {
   int logu[kMaxProc];    // table energies log-uniform: O(1) bracket guess
   float log_e0[kMaxProc], inv_dlog[kMaxProc];
   int staged;            // some table is not log-uniform: the collision pass stages the tables in shared memory
+  float kthr[kMaxProc];  // (k + 1) / N in FP32: the first term of process k's acceptance threshold
 };
 
 struct Mcc {
@@ -264,7 +265,7 @@ __device__ __forceinline__ bool mcc_entry_hits(const MccWork &e, const MccDev &M
     float Pk = -expm1f(-n * sg * M.dt);
     Pk *= M.inv_nmaxpt;
     if (Pk > 1.0f) return true;
-    if (U > (float)(k + 1) / M.N - Pk) return true;
+    if (U > M.kthr[k] - Pk) return true;
   }
   return false;
 }
@@ -468,7 +469,7 @@ __global__ void __launch_bounds__(256, ISKRA_MCC_COLLIDE_MIN_BLOCKS) k_mcc_colli
           flags |= DERR_PROB;
           break;
         }
-        if (!(U > (float)(k + 1) / M.N - Pk)) continue;
+        if (!(U > M.kthr[k] - Pk)) continue;
         acc_k[k]++;
         if (M.nu && !keys) atomicAdd(M.nu + (size_t)node * M.N + k, 1u);
         const int type = M.types[k];
@@ -627,6 +628,7 @@ static int mcc_params(Ctx *c, int mid, double dt, uint64_t seed, MccDev &M) {
   mcc_key(seed, m->set_index, M.key0, M.key1);
   M.staged = 0;
   for (int k = 0; k < m->N; k++) {
+    M.kthr[k] = (float)(k + 1) / (float)m->N;  // IEEE division: the bits the device's division gave
     M.logu[k] = m->logu[k];
     M.log_e0[k] = m->log_e0[k];
     M.inv_dlog[k] = m->inv_dlog[k];
